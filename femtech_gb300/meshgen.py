@@ -1,0 +1,194 @@
+"""Seeded synthetic meshes and load cases in FemTech's array layout.
+
+The reference reads LS-DYNA/Abaqus decks into ``coordinates[3*nNodes]``,
+``eptr``/``connectivity`` (CSR), ``ElementType`` and ``pid``
+(src/io/input/ReadLsDyna.cpp, ReadAbaqus.cpp).  The benchmark workloads here
+are synthetic, so these helpers build the same arrays directly:
+
+* ``hex_block``      structured C3D8 block, optional seeded node jitter;
+* ``tet_ellipsoid``  C3D4 ellipsoid from a jittered lattice + Delaunay;
+* ``Loads``          per-DOF boundary-condition table (fixed / ramp / sine /
+                     rigid rotation) in the form the C ABI takes.
+
+Node order of a C3D8 element follows the reference's convention (bottom face
+counter-clockwise, then top face; ShapeFunction_C3D8.cpp:26-33).
+"""
+import numpy as np
+
+C3D8, C3D4 = 0, 1
+BC_FREE, BC_HOLD = -1, -2
+BCK_FIXED, BCK_RAMP, BCK_SINE, BCK_ROT = 0, 1, 2, 3
+
+
+def hex_block(nx, ny, nz, lx, ly, lz, jitter=0.0, seed=0, origin=(0.0, 0.0, 0.0)):
+    """Structured nx*ny*nz C3D8 block of size lx*ly*lz.
+
+    ``jitter`` is the uniform node perturbation as a fraction of the local edge
+    length.  Interior nodes move in all directions; nodes on a face move only
+    tangentially, so the six faces stay planar and coordinate-selected
+    boundary sets are unchanged.
+    """
+    hx, hy, hz = lx / nx, ly / ny, lz / nz
+    i = np.arange(nx + 1)
+    j = np.arange(ny + 1)
+    k = np.arange(nz + 1)
+    K, J, I = np.meshgrid(k, j, i, indexing="ij")
+    X = np.stack([origin[0] + I * hx, origin[1] + J * hy, origin[2] + K * hz], -1).reshape(-1, 3)
+    if jitter > 0.0:
+        rng = np.random.default_rng(seed)
+        d = rng.uniform(-jitter, jitter, size=X.shape) * np.array([hx, hy, hz])
+        Ii, Jj, Kk = I.ravel(), J.ravel(), K.ravel()
+        d[(Ii == 0) | (Ii == nx), 0] = 0.0
+        d[(Jj == 0) | (Jj == ny), 1] = 0.0
+        d[(Kk == 0) | (Kk == nz), 2] = 0.0
+        X = X + d
+    # element ordering: i fastest, then j, then k
+    kk, jj, ii = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    ii, jj, kk = ii.ravel(), jj.ravel(), kk.ravel()
+
+    def nid(a, b, c):
+        return a + (nx + 1) * (b + (ny + 1) * c)
+
+    conn = np.stack([nid(ii, jj, kk), nid(ii + 1, jj, kk), nid(ii + 1, jj + 1, kk),
+                     nid(ii, jj + 1, kk), nid(ii, jj, kk + 1), nid(ii + 1, jj, kk + 1),
+                     nid(ii + 1, jj + 1, kk + 1), nid(ii, jj + 1, kk + 1)], -1)
+    E = conn.shape[0]
+    return dict(coordinates=np.ascontiguousarray(X, np.float64),
+                eptr=np.arange(0, 8 * E + 1, 8, dtype=np.int32),
+                connectivity=conn.astype(np.int32).ravel(),
+                etype=np.full(E, C3D8, np.int32), pid=np.zeros(E, np.int32),
+                shape=(nx, ny, nz), h=(hx, hy, hz))
+
+
+def tet_ellipsoid(a, b, c, h, jitter=0.1, seed=0):
+    """C3D4 mesh of the ellipsoid x^2/a^2 + y^2/b^2 + z^2/c^2 <= 1.
+
+    Lattice points of spacing h, jittered by +-jitter*h (seeded), plus points on
+    the surface; Delaunay tetrahedralisation (scipy/qhull); tets whose centroid
+    lies outside, or whose volume is tiny, are dropped.  Node order is made
+    right-handed (positive signed volume).
+    """
+    from scipy.spatial import Delaunay
+
+    rng = np.random.default_rng(seed)
+    xs = np.arange(-a, a + 1e-12, h)
+    ys = np.arange(-b, b + 1e-12, h)
+    zs = np.arange(-c, c + 1e-12, h)
+    P = np.stack(np.meshgrid(xs, ys, zs, indexing="ij"), -1).reshape(-1, 3)
+    P = P + rng.uniform(-jitter, jitter, P.shape) * h
+    r = (P[:, 0] / a) ** 2 + (P[:, 1] / b) ** 2 + (P[:, 2] / c) ** 2
+    P = P[r < (1.0 - 0.5 * h / min(a, b, c)) ** 2]
+    # surface points: Fibonacci sphere mapped onto the ellipsoid, density ~ 1/h^2
+    area = 4.0 * np.pi * ((a * b) ** 1.6 + (a * c) ** 1.6 + (b * c) ** 1.6) ** (1 / 1.6) / 3 ** (1 / 1.6)
+    ns = int(area / (h * h) * 1.15)
+    idx = np.arange(ns) + 0.5
+    phi = np.arccos(1 - 2 * idx / ns)
+    th = np.pi * (1 + 5 ** 0.5) * idx
+    S = np.stack([a * np.cos(th) * np.sin(phi), b * np.sin(th) * np.sin(phi), c * np.cos(phi)], -1)
+    X = np.concatenate([P, S], 0)
+    tri = Delaunay(X)
+    T = tri.simplices.astype(np.int64)
+    cen = X[T].mean(1)
+    inside = (cen[:, 0] / a) ** 2 + (cen[:, 1] / b) ** 2 + (cen[:, 2] / c) ** 2 < 1.0
+    v = np.einsum("ij,ij->i", np.cross(X[T[:, 1]] - X[T[:, 3]], X[T[:, 2]] - X[T[:, 3]]),
+                  X[T[:, 0]] - X[T[:, 3]]) / 6.0
+    keep = inside & (np.abs(v) > 1e-3 * h ** 3)
+    T, v = T[keep], v[keep]
+    neg = v < 0
+    T[neg, 0], T[neg, 1] = T[neg, 1].copy(), T[neg, 0].copy()
+    used = np.unique(T)
+    remap = -np.ones(len(X), np.int64)
+    remap[used] = np.arange(len(used))
+    T = remap[T]
+    X = X[used]
+    E = len(T)
+    return dict(coordinates=np.ascontiguousarray(X, np.float64),
+                eptr=np.arange(0, 4 * E + 1, 4, dtype=np.int32),
+                connectivity=T.astype(np.int32).ravel(), etype=np.full(E, C3D4, np.int32),
+                pid=np.zeros(E, np.int32))
+
+
+def materials(parts):
+    """parts: list of (materialID, [props...]) -> dict(materialID, properties[9*nPID])."""
+    mid = np.array([p[0] for p in parts], np.int32)
+    pr = np.zeros((len(parts), 9))
+    for i, (_, props) in enumerate(parts):
+        pr[i, : len(props)] = props
+    return dict(materialID=mid, properties=pr.ravel())
+
+
+class Loads:
+    """Per-DOF boundary functions: -1 free, -2 hold, >= 0 index into ``fns``."""
+
+    def __init__(self, nNodes):
+        self.dof_fn = np.full(3 * nNodes, BC_FREE, np.int32)
+        self.fns = []
+
+    def add_fn(self, kind, params):
+        self.fns.append((int(kind), [float(p) for p in params]))
+        return len(self.fns) - 1
+
+    def fix(self, nodes, dofs=(0, 1, 2), value=0.0):
+        f = self.add_fn(BCK_FIXED, [value])
+        for d in dofs:
+            self.dof_fn[3 * np.asarray(nodes) + d] = f
+        return f
+
+    def ramp(self, nodes, dof, rate):
+        f = self.add_fn(BCK_RAMP, [rate])
+        self.dof_fn[3 * np.asarray(nodes) + dof] = f
+        return f
+
+    def sine(self, nodes, dof, amplitude, omega):
+        f = self.add_fn(BCK_SINE, [amplitude, omega])
+        self.dof_fn[3 * np.asarray(nodes) + dof] = f
+        return f
+
+    def rotation(self, nodes, axis, center, alpha_peak, duration):
+        ax = np.asarray(axis, np.float64)
+        ax = ax / np.linalg.norm(ax)
+        f = self.add_fn(BCK_ROT, list(ax) + list(center) + [alpha_peak, duration])
+        for d in range(3):
+            self.dof_fn[3 * np.asarray(nodes) + d] = f
+        return f
+
+    def hold(self, nodes, dofs=(0, 1, 2)):
+        for d in dofs:
+            self.dof_fn[3 * np.asarray(nodes) + d] = BC_HOLD
+
+    @property
+    def boundary(self):
+        return (self.dof_fn != BC_FREE).astype(np.int32)
+
+
+def cube_tension_case(n=10, size=0.01, rho=1000.0, mu=3400.0, K=2.0e6, strain=0.1,
+                      t_ramp=0.01):
+    """Unit-cube tension: n^3 C3D8 cube, z=0 face fixed, top face pulled in z,
+    displacement ramped linearly to ``strain`` over ``t_ramp`` (the plain,
+    CPU-runnable configuration: 10x10x10, 0.01 m, Neo-Hookean)."""
+    mesh = hex_block(n, n, n, size, size, size)
+    lam = K - 2.0 * mu / 3.0
+    mats = materials([(1, [rho, mu, lam])])
+    X = mesh["coordinates"]
+    tol = 1e-9
+    loads = Loads(len(X))
+    loads.fix(np.where(np.abs(X[:, 2]) < tol)[0])
+    loads.ramp(np.where(np.abs(X[:, 2] - size) < tol)[0], 2, strain * size / t_ramp)
+    return mesh, mats, loads
+
+
+def ogden_block_case(nx=200, ny=200, nz=100, lx=0.2, ly=0.2, lz=0.1, jitter=0.1, seed=0,
+                     mu=1.5e3, alpha=5.0, K=20e6, rho=1040.0, amp=1e-3, freq=50.0):
+    """Jittered C3D8 block under top-face sinusoidal shear, 1-term Ogden
+    (the 200x200x100, 4.0M-element scale configuration by default)."""
+    mesh = hex_block(nx, ny, nz, lx, ly, lz, jitter=jitter, seed=seed)
+    lam = K - 2.0 * mu / 3.0
+    mats = materials([(6, [rho, mu, lam, alpha])])
+    X = mesh["coordinates"]
+    tol = 1e-9
+    loads = Loads(len(X))
+    loads.fix(np.where(np.abs(X[:, 2]) < tol)[0])
+    top = np.where(np.abs(X[:, 2] - lz) < tol)[0]
+    loads.sine(top, 0, amp, 2.0 * np.pi * freq)
+    loads.fix(top, dofs=(1, 2))
+    return mesh, mats, loads

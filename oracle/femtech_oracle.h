@@ -1,0 +1,87 @@
+/*
+ * femtech_oracle.h -- FP64 CPU restatement of FemTech's explicit-dynamics hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the checker that the CUDA path is compared
+ * against; it is never linked into, imported by or called from the product
+ * library (femtech_gb300/).  Only tests/, __graft_entry__.smoke() and the
+ * cpu_baseline / reference legs of bench.py use it.
+ *
+ * Parity is pinned: tests/golden/ holds vectors produced by the reference's own
+ * sources (compiled unmodified by oracle/Makefile into oracle/_ref/), and the
+ * CPU test-suite checks this restatement against them.  The Ogden (6) and
+ * anisotropic GOH + Prony (7) laws have no reference implementation; they are
+ * pinned through special cases that reduce to reference laws (Ogden alpha=2 ==
+ * HGOIsotropic with k1=0, GOH kappa=1/3 == HGOIsotropicViscoelastic with
+ * g2=0) plus energy finite-difference checks.
+ *
+ * Layout follows the reference (include/GlobalVariables.h): AoS nodal arrays
+ * [node*3+dim], CSR connectivity (eptr), per-part properties[pid*9+k].
+ */
+#ifndef FEMTECH_ORACLE_H
+#define FEMTECH_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OR_MAXMATPARAMS 9
+#define OR_C3D8 0
+#define OR_C3D4 1
+
+/* boundary-condition function kinds (per constrained DOF) */
+#define OR_BC_FREE (-1)
+#define OR_BC_HOLD (-2)
+#define OR_BCK_FIXED 0 /* u = p0, v = 0                                     */
+#define OR_BCK_RAMP 1  /* u = p0 * t, v = p0  (examples/ex9/ex9.cpp:227-244) */
+#define OR_BCK_SINE 2  /* u = p0 * sin(p1 t), v = p0 p1 cos(p1 t)           */
+#define OR_BCK_ROT 3   /* rigid rotation: axis p0..2, centre p3..5,
+                          half-sine angular acceleration peak p6 over p7 s  */
+
+typedef struct or_bc_fn {
+  int kind;
+  int pad;
+  double p[8];
+} or_bc_fn;
+
+typedef struct or_model {
+  /* inputs, reference layout; owned by the caller */
+  int nNodes, nelements, nPID;
+  const double *coordinates; /* 3*nNodes                              */
+  const int *eptr;           /* nelements+1                           */
+  const int *connectivity;   /* eptr[nelements]                       */
+  const int *etype;          /* OR_C3D8 / OR_C3D4 per element         */
+  const int *pid;            /* part id per element                   */
+  const int *materialID;     /* per part                              */
+  const double *properties;  /* 9 per part                            */
+  const double *fiber;       /* 3 per element (material 7) or NULL    */
+  /* derived (owned by the oracle) */
+  int *nGP, *nShp, *gpPtr, *dsptr, *gptr, *fptr, *pk2ptr;
+  double *shp, *dshp, *detJ, *gw;
+  double *F, *detF, *pk2;
+  double *hist; /* 27 doubles per Gauss point: H1[9], H2[9], S0n[9] */
+  double *mass; /* 3*nNodes                                          */
+  double *fe;   /* scratch: 24 doubles per element                   */
+  double *ce;   /* dilatational wave speed per part                  */
+  int nthreads;
+} or_model;
+
+int or_setup(or_model *m);
+void or_free(or_model *m);
+int or_get_force(or_model *m, const double *u, double dt, double *fi);
+double or_stable_time_step(const or_model *m, const double *u, const int *boundary);
+int or_material_stress(int matID, const double *props, const double *F, double J,
+                       const double *a0, double dt, double *hist27, double *S6);
+int or_explicit_run(or_model *m, const int *dof_fn, const or_bc_fn *fns, int nfn,
+                    double t0, double tMax, double reduction, double failure_dt,
+                    int max_steps, int out_every, double *u, double *v, double *a,
+                    double *u_out, double *t_out, int max_out, int *n_out,
+                    int *steps_done, double *time_out, double *dt_out);
+void or_apply_bc(const or_model *m, const int *dof_fn, const or_bc_fn *fns,
+                 double t, double *u, double *v, double *a);
+void or_set_threads(or_model *m, int n);
+int or_max_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

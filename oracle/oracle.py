@@ -1,0 +1,299 @@
+"""ctypes front-end of the FP64 oracle (test infrastructure only).
+
+Two checkers live here:
+
+* ``Oracle``     -- the C restatement in ``femtech_oracle.c`` (``liboracle.so``),
+  built on every machine by ``__graft_entry__.build()``;
+* ``RefBuild``   -- the reference's own hot-path sources compiled unmodified
+  into ``_ref/libfemtech_ref.so`` (only where the reference tree exists).
+
+Only tests/, ``__graft_entry__.smoke()`` and the CPU legs of ``bench.py`` use
+this module; the product package never imports it.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+REFLIB = os.path.join(HERE, "_ref", "libfemtech_ref.so")
+
+BC_FREE, BC_HOLD = -1, -2
+BCK_FIXED, BCK_RAMP, BCK_SINE, BCK_ROT = 0, 1, 2, 3
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+
+
+class BcFn(C.Structure):
+    _fields_ = [("kind", C.c_int), ("pad", C.c_int), ("p", C.c_double * 8)]
+
+
+class _Model(C.Structure):
+    _fields_ = [
+        ("nNodes", C.c_int), ("nelements", C.c_int), ("nPID", C.c_int),
+        ("coordinates", C.c_void_p), ("eptr", C.c_void_p), ("connectivity", C.c_void_p),
+        ("etype", C.c_void_p), ("pid", C.c_void_p), ("materialID", C.c_void_p),
+        ("properties", C.c_void_p), ("fiber", C.c_void_p),
+        ("nGP", C.c_void_p), ("nShp", C.c_void_p), ("gpPtr", C.c_void_p),
+        ("dsptr", C.c_void_p), ("gptr", C.c_void_p), ("fptr", C.c_void_p),
+        ("pk2ptr", C.c_void_p),
+        ("shp", C.c_void_p), ("dshp", C.c_void_p), ("detJ", C.c_void_p), ("gw", C.c_void_p),
+        ("F", C.c_void_p), ("detF", C.c_void_p), ("pk2", C.c_void_p),
+        ("hist", C.c_void_p), ("mass", C.c_void_p), ("fe", C.c_void_p), ("ce", C.c_void_p),
+        ("nthreads", C.c_int),
+    ]
+
+
+def build(quiet=True):
+    """Compile liboracle.so (always) and the reference build (if the tree exists)."""
+    out = subprocess.run(["make", "-C", HERE, "liboracle.so"], capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
+    ref = os.environ.get("FEMTECH_REFERENCE", "/root/reference")
+    if os.path.isdir(os.path.join(ref, "src")):
+        out = subprocess.run(["make", "-C", HERE, "-j8", "ref", "REF=" + ref],
+                             capture_output=True, text=True)
+        if out.returncode != 0:
+            raise RuntimeError("reference build failed:\n" + out.stdout + out.stderr)
+
+
+def bc_table(fns):
+    """fns: list of (kind, params) -> ctypes array of BcFn."""
+    arr = (BcFn * max(1, len(fns)))()
+    for i, (kind, params) in enumerate(fns):
+        arr[i].kind = kind
+        for j, v in enumerate(params):
+            arr[i].p[j] = float(v)
+    return arr
+
+
+class Oracle:
+    """FP64 restatement of ShapeFunctions/AssembleLumpedMass/GetForce/StableTimeStep."""
+
+    _lib = None
+
+    @classmethod
+    def lib(cls):
+        if cls._lib is None:
+            if not os.path.exists(LIB):
+                build()
+            L = C.CDLL(LIB)
+            M = C.POINTER(_Model)
+            L.or_setup.argtypes = [M]
+            L.or_free.argtypes = [M]
+            L.or_get_force.argtypes = [M, _dp, C.c_double, _dp]
+            L.or_stable_time_step.argtypes = [M, _dp, _ip]
+            L.or_stable_time_step.restype = C.c_double
+            L.or_material_stress.argtypes = [C.c_int, _dp, _dp, C.c_double, C.c_void_p,
+                                             C.c_double, _dp, _dp]
+            L.or_explicit_run.argtypes = [M, _ip, C.c_void_p, C.c_int, C.c_double, C.c_double,
+                                          C.c_double, C.c_double, C.c_int, C.c_int, _dp, _dp,
+                                          _dp, _dp, _dp, C.c_int, C.POINTER(C.c_int),
+                                          C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                          C.POINTER(C.c_double)]
+            L.or_set_threads.argtypes = [M, C.c_int]
+            L.or_max_threads.restype = C.c_int
+            cls._lib = L
+        return cls._lib
+
+    def __init__(self, mesh, mats, threads=1):
+        L = self.lib()
+        self.mesh = mesh
+        self._keep = {
+            "coordinates": np.ascontiguousarray(mesh["coordinates"], dtype=np.float64).ravel(),
+            "eptr": np.ascontiguousarray(mesh["eptr"], dtype=np.int32),
+            "connectivity": np.ascontiguousarray(mesh["connectivity"], dtype=np.int32),
+            "etype": np.ascontiguousarray(mesh["etype"], dtype=np.int32),
+            "pid": np.ascontiguousarray(mesh["pid"], dtype=np.int32),
+            "materialID": np.ascontiguousarray(mats["materialID"], dtype=np.int32),
+            "properties": np.ascontiguousarray(mats["properties"], dtype=np.float64).ravel(),
+        }
+        fib = mesh.get("fiber")
+        if fib is not None:
+            self._keep["fiber"] = np.ascontiguousarray(fib, dtype=np.float64).ravel()
+        m = _Model()
+        m.nNodes = len(self._keep["coordinates"]) // 3
+        m.nelements = len(self._keep["eptr"]) - 1
+        m.nPID = len(self._keep["materialID"])
+        for k, v in self._keep.items():
+            setattr(m, k, v.ctypes.data)
+        m.nthreads = threads
+        self.m = m
+        self.nNodes, self.nE = m.nNodes, m.nelements
+        rc = L.or_setup(C.byref(m))
+        if rc != 0:
+            raise RuntimeError("or_setup failed %d" % rc)
+        ngp = np.ctypeslib.as_array(C.cast(m.gpPtr, C.POINTER(C.c_int)), (m.nelements + 1,))
+        self.ngp_total = int(ngp[-1])
+
+    def set_threads(self, n):
+        self.lib().or_set_threads(C.byref(self.m), int(n))
+
+    def __del__(self):
+        try:
+            self.lib().or_free(C.byref(self.m))
+        except Exception:
+            pass
+
+    def _arr(self, name, n, ctype=C.c_double):
+        return np.ctypeslib.as_array(C.cast(getattr(self.m, name), C.POINTER(ctype)), (n,)).copy()
+
+    @property
+    def mass(self):
+        return self._arr("mass", 3 * self.nNodes)
+
+    def gp_arrays(self):
+        n = self.ngp_total
+        return (self._arr("F", 9 * n).reshape(n, 9), self._arr("detF", n),
+                self._arr("pk2", 6 * n).reshape(n, 6))
+
+    def shape_arrays(self):
+        ds = np.ctypeslib.as_array(C.cast(self.m.dsptr, C.POINTER(C.c_int)), (self.nE + 1,))
+        return self._arr("dshp", int(ds[-1])), self._arr("detJ", self.ngp_total)
+
+    def get_force(self, u, dt):
+        fi = np.zeros(3 * self.nNodes)
+        rc = self.lib().or_get_force(C.byref(self.m), np.ascontiguousarray(u, np.float64).ravel(),
+                                     float(dt), fi)
+        if rc:
+            raise RuntimeError("or_get_force failed %d" % rc)
+        return fi
+
+    def stable_time_step(self, u, boundary):
+        return self.lib().or_stable_time_step(C.byref(self.m),
+                                              np.ascontiguousarray(u, np.float64).ravel(),
+                                              np.ascontiguousarray(boundary, np.int32).ravel())
+
+    def explicit_run(self, dof_fn, fns, tmax, reduction, max_steps, out_every, t0=0.0,
+                     failure_dt=0.0, u=None, v=None, a=None, max_out=None):
+        n = 3 * self.nNodes
+        u = np.zeros(n) if u is None else np.array(u, np.float64).ravel()
+        v = np.zeros(n) if v is None else np.array(v, np.float64).ravel()
+        a = np.zeros(n) if a is None else np.array(a, np.float64).ravel()
+        if max_out is None:
+            max_out = max(1, max_steps // max(out_every, 1) + 1)
+        uo = np.zeros(max_out * n)
+        to = np.zeros(max_out)
+        nout, steps = C.c_int(), C.c_int()
+        tt, dd = C.c_double(), C.c_double()
+        tab = bc_table(fns)
+        rc = self.lib().or_explicit_run(
+            C.byref(self.m), np.ascontiguousarray(dof_fn, np.int32).ravel(), C.cast(tab, C.c_void_p),
+            len(fns), t0, tmax, reduction, failure_dt, max_steps, out_every, u, v, a, uo, to,
+            max_out, C.byref(nout), C.byref(steps), C.byref(tt), C.byref(dd))
+        k = nout.value
+        return dict(rc=rc, u=u, v=v, a=a, u_out=uo[: k * n].reshape(k, n), t_out=to[:k],
+                    steps=steps.value, time=tt.value, dt=dd.value)
+
+
+def material_stress(mat, props, F, J=None, a0=None, dt=0.0, hist=None):
+    """Single-point PK2 stress (Voigt 11,22,33,23,13,12) of the oracle's laws."""
+    L = Oracle.lib()
+    F = np.ascontiguousarray(F, np.float64).reshape(9)
+    if J is None:
+        J = float(np.linalg.det(F.reshape(3, 3, order="F")))
+    h = np.zeros(27) if hist is None else hist
+    S = np.zeros(6)
+    a0p = None
+    if a0 is not None:
+        a0 = np.ascontiguousarray(a0, np.float64)
+        a0p = a0.ctypes.data
+    pr = np.zeros(9)
+    pr[: len(props)] = props
+    rc = L.or_material_stress(int(mat), pr, F, float(J), a0p, float(dt), h, S)
+    if rc:
+        raise RuntimeError("unknown material")
+    return S
+
+
+class RefBuild:
+    """The reference's own sources (one rank), as a checker for the oracle."""
+
+    _lib = None
+
+    @classmethod
+    def available(cls):
+        return os.path.exists(REFLIB)
+
+    @classmethod
+    def lib(cls):
+        if cls._lib is None:
+            L = C.CDLL(REFLIB)
+            L.ref_setup.argtypes = [C.c_int, C.c_int, _dp, _ip, _ip, _ip, _ip, C.c_int, _ip, _dp,
+                                    C.c_void_p]
+            L.ref_get_mass.argtypes = [_dp]
+            L.ref_num_gp.restype = C.c_int
+            L.ref_get_gp.argtypes = [_dp, _dp, _dp]
+            L.ref_get_shape.argtypes = [_dp, _dp]
+            L.ref_get_force.argtypes = [_dp, C.c_double, _dp, _dp]
+            L.ref_stable_time_step.argtypes = [_dp, _ip]
+            L.ref_stable_time_step.restype = C.c_double
+            L.ref_explicit_run.argtypes = [_ip, C.c_void_p, C.c_int, C.c_double, C.c_double,
+                                           C.c_double, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp,
+                                           C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                           C.POINTER(C.c_double), C.POINTER(C.c_double)]
+            cls._lib = L
+        return cls._lib
+
+    def __init__(self, mesh, mats):
+        L = self.lib()
+        self.X = np.ascontiguousarray(mesh["coordinates"], np.float64).ravel()
+        self.nNodes = len(self.X) // 3
+        eptr = np.ascontiguousarray(mesh["eptr"], np.int32)
+        self.nE = len(eptr) - 1
+        fib = mesh.get("fiber")
+        self._fib = None if fib is None else np.ascontiguousarray(fib, np.float64).ravel()
+        rc = L.ref_setup(self.nNodes, self.nE, self.X, eptr,
+                         np.ascontiguousarray(mesh["connectivity"], np.int32),
+                         np.ascontiguousarray(mesh["etype"], np.int32),
+                         np.ascontiguousarray(mesh["pid"], np.int32), len(mats["materialID"]),
+                         np.ascontiguousarray(mats["materialID"], np.int32),
+                         np.ascontiguousarray(mats["properties"], np.float64).ravel(),
+                         None if self._fib is None else self._fib.ctypes.data)
+        if rc:
+            raise RuntimeError("ref_setup failed %d" % rc)
+        self.ngp = L.ref_num_gp()
+
+    @property
+    def mass(self):
+        m = np.zeros(3 * self.nNodes)
+        self.lib().ref_get_mass(m)
+        return m
+
+    def gp_arrays(self):
+        n = self.ngp
+        F, d, p = np.zeros(9 * n), np.zeros(n), np.zeros(6 * n)
+        self.lib().ref_get_gp(F, d, p)
+        return F.reshape(n, 9), d, p.reshape(n, 6)
+
+    def get_force(self, u, dt):
+        fi, fn = np.zeros(3 * self.nNodes), np.zeros(3 * self.nNodes)
+        rc = self.lib().ref_get_force(np.ascontiguousarray(u, np.float64).ravel(), float(dt), fi, fn)
+        if rc:
+            raise RuntimeError("ref_get_force failed %d" % rc)
+        return fi
+
+    def stable_time_step(self, u, boundary):
+        return self.lib().ref_stable_time_step(np.ascontiguousarray(u, np.float64).ravel(),
+                                               np.ascontiguousarray(boundary, np.int32).ravel())
+
+    def explicit_run(self, dof_fn, fns, tmax, reduction, max_steps, out_every, t0=0.0,
+                     max_out=None):
+        n = 3 * self.nNodes
+        u, v, a = np.zeros(n), np.zeros(n), np.zeros(n)
+        if max_out is None:
+            max_out = max(1, max_steps // max(out_every, 1) + 1)
+        uo, to = np.zeros(max_out * n), np.zeros(max_out)
+        nout, steps = C.c_int(), C.c_int()
+        tt, dd = C.c_double(), C.c_double()
+        tab = bc_table(fns)
+        rc = self.lib().ref_explicit_run(np.ascontiguousarray(dof_fn, np.int32).ravel(),
+                                         C.cast(tab, C.c_void_p), len(fns), t0, tmax, reduction,
+                                         max_steps, out_every, u, v, a, uo, to, max_out,
+                                         C.byref(nout), C.byref(steps), C.byref(tt), C.byref(dd))
+        k = nout.value
+        return dict(rc=rc, u=u, v=v, a=a, u_out=uo[: k * n].reshape(k, n), t_out=to[:k],
+                    steps=steps.value, time=tt.value, dt=dd.value)

@@ -1,0 +1,349 @@
+/*
+ * refshim.cpp -- glue that lets FemTech's own hot-path sources (compiled
+ * unmodified from the reference tree by oracle/Makefile) run as a single-rank
+ * library, plus an extern "C" driver API used to produce golden vectors.
+ *
+ * TEST INFRASTRUCTURE ONLY: the output (oracle/_ref/libfemtech_ref.so) is a
+ * checker; it is never linked into the product.
+ *
+ * What is project-written here (the reference's own versions need MPI,
+ * ParMETIS, BLAS or the mesh readers):
+ *   - one-rank MPI bodies (collectives are copies),
+ *   - plain triple-loop dgemm_/dgemv_ (include/blas.h:14-26 signatures),
+ *   - definitions of the globals normally defined by the readers
+ *     (src/io/input/ReadInputFile.cpp:6-19, ReadMaterials.cpp:5-6), by
+ *     InitFinalizeFemTech.cpp:9-11 and by PartitionMesh.cpp (halo pattern,
+ *     empty on one rank) and by the example drivers (ex9.cpp:9-17),
+ *   - StressUpdate: forwards material IDs 0-5 to the reference routines (as
+ *     src/fem/SolidMechanics/StressUpdate.cpp:7-27 does) and 6/7 to the FP64
+ *     restatements of the new laws in oracle/femtech_oracle.c,
+ *   - a driver loop in the shape of examples/ex9/ex9.cpp:79-175.
+ */
+#include "FemTech.h"
+#include "blas.h"
+
+#include <stdarg.h>
+#include <stdexcept>
+#include <string>
+
+extern "C" {
+#include "femtech_oracle.h"
+}
+
+/* ---------------- one-rank MPI ---------------- */
+static size_t dtsize(MPI_Datatype t) { return (size_t)t; }
+int MPI_Init(int *, char ***) { return 0; }
+int MPI_Finalize(void) { return 0; }
+int MPI_Comm_size(MPI_Comm, int *s) { *s = 1; return 0; }
+int MPI_Comm_rank(MPI_Comm, int *r) { *r = 0; return 0; }
+int MPI_Abort(MPI_Comm, int code) { throw std::runtime_error("MPI_Abort " + std::to_string(code)); }
+int MPI_Barrier(MPI_Comm) { return 0; }
+int MPI_Allreduce(const void *s, void *r, int n, MPI_Datatype t, MPI_Op, MPI_Comm) {
+  if (s != MPI_IN_PLACE) memcpy(r, s, n * dtsize(t));
+  return 0;
+}
+int MPI_Reduce(const void *s, void *r, int n, MPI_Datatype t, MPI_Op, int, MPI_Comm) {
+  if (s != MPI_IN_PLACE) memcpy(r, s, n * dtsize(t));
+  return 0;
+}
+int MPI_Bcast(void *, int, MPI_Datatype, int, MPI_Comm) { return 0; }
+int MPI_Gather(const void *s, int n, MPI_Datatype t, void *r, int, MPI_Datatype, int, MPI_Comm) {
+  if (s != MPI_IN_PLACE) memcpy(r, s, n * dtsize(t));
+  return 0;
+}
+int MPI_Gatherv(const void *s, int n, MPI_Datatype t, void *r, const int *, const int *displs,
+                MPI_Datatype, int, MPI_Comm) {
+  memcpy((char *)r + displs[0] * dtsize(t), s, n * dtsize(t));
+  return 0;
+}
+int MPI_Scatterv(const void *s, const int *counts, const int *displs, MPI_Datatype t, void *r,
+                 int, MPI_Datatype, int, MPI_Comm) {
+  memcpy(r, (const char *)s + displs[0] * dtsize(t), counts[0] * dtsize(t));
+  return 0;
+}
+int MPI_Isend(const void *, int, MPI_Datatype, int, int, MPI_Comm, MPI_Request *) { return 0; }
+int MPI_Irecv(void *, int, MPI_Datatype, int, int, MPI_Comm, MPI_Request *) { return 0; }
+int MPI_Wait(MPI_Request *, MPI_Status *) { return 0; }
+
+/* ---------------- plain BLAS (column-major) ---------------- */
+extern "C" void dgemm_(char *ta, char *tb, int *m, int *n, int *k, double *alpha, double *a,
+                       int *lda, double *b, int *ldb, double *beta, double *c, int *ldc) {
+  bool tA = (*ta == 'T' || *ta == 't'), tB = (*tb == 'T' || *tb == 't');
+  for (int j = 0; j < *n; ++j)
+    for (int i = 0; i < *m; ++i) {
+      double s = 0.0;
+      for (int l = 0; l < *k; ++l) {
+        double x = tA ? a[l + *lda * i] : a[i + *lda * l];
+        double y = tB ? b[j + *ldb * l] : b[l + *ldb * j];
+        s += x * y;
+      }
+      double *cij = c + i + *ldc * j;
+      *cij = (*beta == 0.0) ? *alpha * s : *alpha * s + *beta * *cij;
+    }
+}
+extern "C" void dgemv_(char *tr, int *m, int *n, double *alpha, double *a, int *lda, double *x,
+                       int *incx, double *beta, double *y, int *incy) {
+  bool t = (*tr == 'T' || *tr == 't');
+  int ny = t ? *n : *m, nx = t ? *m : *n;
+  for (int j = 0; j < ny; ++j) {
+    double s = 0.0;
+    for (int i = 0; i < nx; ++i) {
+      double aij = t ? a[i + *lda * j] : a[j + *lda * i];
+      s += aij * x[i * *incx];
+    }
+    double *yj = y + j * *incy;
+    *yj = (*beta == 0.0) ? *alpha * s : *alpha * s + *beta * *yj;
+  }
+}
+extern "C" void dgesv_(int *, int *, double *, int *, int *, double *, int *, int *info) { *info = -1; }
+extern "C" void dgetrf_(int *, int *, double *, int *, int *, int *info) { *info = -1; }
+extern "C" void dgetrs_(char *, int *, int *, double *, int *, int *, double *, int *, int *info) { *info = -1; }
+
+/* ---------------- logging: errors and warnings to stderr ---------------- */
+static void vlog(enum logLevel level, const char *fmt, va_list ap) {
+  if (level > WARNING) return;
+  vfprintf(stderr, fmt, ap);
+  fputc('\n', stderr);
+}
+#define LOGFN(name)                                   \
+  void name(enum logLevel level, const char *fmt, ...) { \
+    va_list ap;                                       \
+    va_start(ap, fmt);                                \
+    vlog(level, fmt, ap);                             \
+    va_end(ap);                                       \
+  }
+LOGFN(fileLog)
+LOGFN(fileLogMaster)
+LOGFN(fileLogSingle)
+void fileLogMatrix(enum logLevel, const double *, const int, const int, const char *, ...) {}
+void fileLogMatrixRM(enum logLevel, const double *, const int, const int, const char *, ...) {}
+void fileLogMatrixSingle(enum logLevel, const double *, const int, const int, const char *, ...) {}
+void fileLogMatrixRMSingle(enum logLevel, const double *, const int, const int, const char *, ...) {}
+void fileLogArray(enum logLevel, const double *, const int, const char *, ...) {}
+void fileLogArrayMaster(enum logLevel, const double *, const int, const char *, ...) {}
+void fileLogArraySingle(enum logLevel, const double *, const int, const char *, ...) {}
+void fileLogArrayInt(enum logLevel, const int *, const int, const char *, ...) {}
+void fileLogArrayIntMaster(enum logLevel, const int *, const int, const char *, ...) {}
+void fileLogArrayIntSingle(enum logLevel, const int *, const int, const char *, ...) {}
+
+struct RefTerminate {
+  int code;
+};
+void TerminateFemTech(int errorCode) { throw RefTerminate{errorCode}; }
+void FreeArrays() {}
+
+/* ---------------- globals defined outside the compiled hot-path files ---------------- */
+int nparts = 0, nelements = 0, nallelements = 0, nNodes = 0, ndim = 0, nDOF = 0;
+double *coordinates;
+double *mass, *stiffness, *rhs; /* src/fem/Assembly.cpp:3-4 */
+int *connectivity, *eptr, *pid, *global_eid;
+char **ElementType;
+int nPIDglobal = 0, nPID = 0;
+int *materialID;
+double *properties;
+int world_rank = 0, world_size = 1;
+std::string uid = "oracle";
+int *globalNodeID;
+int sendProcessCount = 0;
+int *sendProcessID, *sendNeighbourCount, *sendNeighbourCountCum, *sendNodeIndex;
+double *sendNodeDisplacement, *recvNodeDisplacement;
+double Time, dt;
+double ExplicitTimeStepReduction = 0.8;
+double FailureTimeStep = 0.0;
+bool ImplicitStatic = false, ImplicitDynamic = false, ExplicitDynamic = true;
+
+/* history and fibre arrays of the new materials 6/7 */
+static double *g_hist = nullptr;
+static double *g_fiber = nullptr;
+
+/* StressUpdate: material switch of src/fem/SolidMechanics/StressUpdate.cpp:7-27 */
+void StressUpdate(int e, int gp) {
+  int mat = materialID[pid[e]];
+  switch (mat) {
+    case 0: break;
+    case 1: CompressibleNeoHookean(e, gp); break;
+    case 2: StVenantKirchhoff(e, gp); break;
+    case 3: LinearElastic(e, gp); break;
+    case 4: HGOIsotropic(e, gp); break;
+    case 5: HGOIsotropicViscoelastic(e, gp); break;
+    case 6:
+    case 7: {
+      int gi = gpPtr[e] + gp;
+      or_material_stress(mat, &properties[MAXMATPARAMS * pid[e]], &F[fptr[e] + 9 * gp],
+                         detF[detFptr[e] + gp], g_fiber ? g_fiber + 3 * e : nullptr, dt,
+                         g_hist + 27 * (size_t)gi, &pk2[pk2ptr[e] + 6 * gp]);
+      break;
+    }
+    default: TerminateFemTech(1);
+  }
+}
+
+/* ---------------- extern "C" driver API ---------------- */
+extern "C" {
+
+int ref_setup(int nN, int nE, const double *coords, const int *ep, const int *conn,
+              const int *etype, const int *pidIn, int nP, const int *matID, const double *props,
+              const double *fiber) {
+  try {
+    ndim = 3;
+    nNodes = nN;
+    nelements = nallelements = nE;
+    nDOF = 3 * nN;
+    nPID = nPIDglobal = nP;
+    coordinates = (double *)malloc(sizeof(double) * 3 * nN);
+    memcpy(coordinates, coords, sizeof(double) * 3 * nN);
+    eptr = (int *)malloc(sizeof(int) * (nE + 1));
+    memcpy(eptr, ep, sizeof(int) * (nE + 1));
+    connectivity = (int *)malloc(sizeof(int) * ep[nE]);
+    memcpy(connectivity, conn, sizeof(int) * ep[nE]);
+    pid = (int *)malloc(sizeof(int) * nE);
+    memcpy(pid, pidIn, sizeof(int) * nE);
+    global_eid = (int *)malloc(sizeof(int) * nE);
+    ElementType = (char **)malloc(sizeof(char *) * nE);
+    static char hex[] = "C3D8", tet[] = "C3D4";
+    for (int e = 0; e < nE; ++e) {
+      global_eid[e] = e;
+      ElementType[e] = etype[e] == 0 ? hex : tet;
+    }
+    materialID = (int *)malloc(sizeof(int) * nP);
+    memcpy(materialID, matID, sizeof(int) * nP);
+    properties = (double *)malloc(sizeof(double) * MAXMATPARAMS * nP);
+    memcpy(properties, props, sizeof(double) * MAXMATPARAMS * nP);
+    sendProcessCount = 0;
+    sendNeighbourCountCum = (int *)calloc(1, sizeof(int));
+    ExplicitDynamic = true;
+    AllocateArrays();
+    if (energyFile) {
+      fclose(energyFile);
+      energyFile = nullptr;
+      remove(("energy_" + uid + ".dat").c_str());
+    }
+    ShapeFunctions();
+    AssembleLumpedMass();
+    free(g_hist);
+    g_hist = (double *)calloc(27 * (size_t)gpPtr[nE], sizeof(double));
+    free(g_fiber);
+    g_fiber = nullptr;
+    if (fiber) {
+      g_fiber = (double *)malloc(sizeof(double) * 3 * nE);
+      memcpy(g_fiber, fiber, sizeof(double) * 3 * nE);
+    }
+    Time = 0.0;
+    dt = 0.0;
+    return 0;
+  } catch (RefTerminate &t) {
+    return -t.code;
+  }
+}
+
+int ref_get_mass(double *m) {
+  memcpy(m, mass, sizeof(double) * nDOF);
+  return 0;
+}
+
+int ref_num_gp(void) { return gpPtr[nelements]; }
+
+int ref_get_gp(double *Fout, double *detFout, double *pk2out) {
+  int ng = gpPtr[nelements];
+  if (Fout) memcpy(Fout, F, sizeof(double) * 9 * ng);
+  if (detFout) memcpy(detFout, detF, sizeof(double) * ng);
+  if (pk2out) memcpy(pk2out, pk2, sizeof(double) * 6 * ng);
+  return 0;
+}
+
+int ref_get_shape(double *dshpOut, double *detJOut) {
+  if (dshpOut) memcpy(dshpOut, dshp, sizeof(double) * dsptr[nelements]);
+  if (detJOut) memcpy(detJOut, detJacobian, sizeof(double) * gpPtr[nelements]);
+  return 0;
+}
+
+/* GetForce() on the given displacements with the given global dt. */
+int ref_get_force(const double *u, double dtIn, double *fiOut, double *fnetOut) {
+  try {
+    memcpy(displacements, u, sizeof(double) * nDOF);
+    dt = dtIn;
+    GetForce();
+    if (fiOut) memcpy(fiOut, fi, sizeof(double) * nDOF);
+    if (fnetOut) memcpy(fnetOut, f_net, sizeof(double) * nDOF);
+    return 0;
+  } catch (RefTerminate &t) {
+    return -t.code;
+  }
+}
+
+double ref_stable_time_step(const double *u, const int *bnd) {
+  try {
+    memcpy(displacements, u, sizeof(double) * nDOF);
+    memcpy(boundary, bnd, sizeof(int) * nDOF);
+    FailureTimeStep = 0.0;
+    return StableTimeStep();
+  } catch (RefTerminate &t) {
+    return -(double)t.code;
+  }
+}
+
+/* The explicit loop of examples/ex9/ex9.cpp:79-175 with driver-side
+ * boundary conditions given as per-DOF function indices (see or_apply_bc). */
+int ref_explicit_run(const int *dof_fn, const or_bc_fn *fns, int nfn, double t0, double tMax,
+                     double reduction, int max_steps, int out_every, double *uInOut,
+                     double *vInOut, double *aInOut, double *u_out, double *t_out, int max_out,
+                     int *n_out, int *steps_done, double *time_out, double *dt_out) {
+  (void)nfn;
+  try {
+    or_model bcm;
+    memset(&bcm, 0, sizeof(bcm));
+    bcm.nNodes = nNodes;
+    bcm.coordinates = coordinates;
+    memcpy(displacements, uInOut, sizeof(double) * nDOF);
+    memcpy(velocities, vInOut, sizeof(double) * nDOF);
+    memcpy(accelerations, aInOut, sizeof(double) * nDOF);
+    for (int i = 0; i < nDOF; ++i) boundary[i] = dof_fn[i] != OR_BC_FREE;
+    ExplicitTimeStepReduction = reduction;
+    FailureTimeStep = 0.0;
+    Time = t0;
+    *n_out = 0;
+    or_apply_bc(&bcm, dof_fn, fns, Time, displacements, velocities, accelerations);
+    dt = ExplicitTimeStepReduction * StableTimeStep();
+    GetForce();
+    CalculateAccelerations();
+    int step = 0;
+    while (Time < tMax && step < max_steps) {
+      double t_n = Time;
+      double t_np1 = Time + dt;
+      Time = t_np1;
+      double dt_nphalf = dt;
+      double t_nphalf = 0.5 * (t_np1 + t_n);
+      for (int i = 0; i < nDOF; i++) {
+        if (boundary[i])
+          velocities_half[i] = velocities[i];
+        else
+          velocities_half[i] = velocities[i] + (t_nphalf - t_n) * accelerations[i];
+      }
+      for (int i = 0; i < nDOF; i++)
+        if (!boundary[i]) displacements[i] = displacements[i] + dt_nphalf * velocities_half[i];
+      or_apply_bc(&bcm, dof_fn, fns, Time, displacements, velocities, accelerations);
+      GetForce();
+      CalculateAccelerations();
+      for (int i = 0; i < nDOF; i++)
+        if (!boundary[i]) velocities[i] = velocities_half[i] + (t_np1 - t_nphalf) * accelerations[i];
+      ++step;
+      if (out_every > 0 && step % out_every == 0 && *n_out < max_out) {
+        memcpy(u_out + (size_t)(*n_out) * nDOF, displacements, sizeof(double) * nDOF);
+        t_out[*n_out] = Time;
+        ++*n_out;
+      }
+      dt = ExplicitTimeStepReduction * StableTimeStep();
+    }
+    *steps_done = step;
+    *time_out = Time;
+    *dt_out = dt;
+    memcpy(uInOut, displacements, sizeof(double) * nDOF);
+    memcpy(vInOut, velocities, sizeof(double) * nDOF);
+    memcpy(aInOut, accelerations, sizeof(double) * nDOF);
+    return 0;
+  } catch (RefTerminate &t) {
+    return -t.code;
+  }
+}
+
+}  // extern "C"
