@@ -1,0 +1,224 @@
+"""femtech_gb300 -- GB300 (sm_103a) engine for FemTech's explicit-dynamics hot path.
+
+The compute lives in ``libftgpu.so`` (CUDA kernels behind the C ABI of
+``include/ftgpu.h``).  This module is a thin ctypes front-end whose methods
+carry the names of the reference functions they replace:
+
+    ShapeFunctions()+AssembleLumpedMass()  -> Model.setup(), Model.mass
+    GetForce()                              -> Model.GetForce(u, dt)
+    StableTimeStep()                        -> Model.StableTimeStep(u)
+    the driver's explicit loop (ex9.cpp)    -> Model.init_explicit(), Model.run()
+
+There is no CPU fallback: if the library is missing or no GPU is present the
+calls raise.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import meshgen  # noqa: F401
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libftgpu.so")
+
+FP64, MIXED = 0, 1
+C3D8, C3D4 = 0, 1
+OK = 0
+ERR_MATERIAL, ERR_INPUT, ERR_ALLOC, ERR_DT, ERR_INVERTED = -1, -3, -12, -19, -20
+ERR_CUDA, ERR_STATE, ERR_NODEVICE = -30, -31, -32
+
+
+class FtgpuError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("ftgpu status %d: %s" % (status, msg))
+        self.status = status
+
+
+class BcFn(C.Structure):
+    _fields_ = [("kind", C.c_int), ("pad", C.c_int), ("p", C.c_double * 8)]
+
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_lib = None
+
+
+def lib():
+    """Load libftgpu.so (built by femtech_gb300.build / __graft_entry__.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("libftgpu.so is not built; run femtech_gb300.build.build() first")
+    L = C.CDLL(LIB_PATH)
+    vp = C.c_void_p
+    L.ftgpu_create.argtypes = [C.POINTER(vp), C.c_int, C.c_int]
+    L.ftgpu_destroy.argtypes = [vp]
+    L.ftgpu_status_string.restype = C.c_char_p
+    L.ftgpu_status_string.argtypes = [C.c_int]
+    L.ftgpu_last_error.restype = C.c_char_p
+    L.ftgpu_set_mesh.argtypes = [vp, C.c_int, C.c_int, _dp, _ip, _ip, _ip, _ip]
+    L.ftgpu_set_materials.argtypes = [vp, C.c_int, _ip, _dp]
+    L.ftgpu_set_fibers.argtypes = [vp, _dp]
+    L.ftgpu_set_bc.argtypes = [vp, _ip, C.c_int, vp]
+    L.ftgpu_set_instances.argtypes = [vp, C.c_int, _ip, _dp, _dp, _dp]
+    L.ftgpu_set_patch_size.argtypes = [vp, C.c_int]
+    L.ftgpu_setup.argtypes = [vp]
+    L.ftgpu_get_mass.argtypes = [vp, _dp]
+    L.ftgpu_get_force.argtypes = [vp, _dp, C.c_double, vp, vp]
+    L.ftgpu_stable_time_step.argtypes = [vp, _dp, C.POINTER(C.c_double)]
+    L.ftgpu_get_gauss_points.argtypes = [vp, vp, vp, vp]
+    L.ftgpu_num_gauss_points.argtypes = [vp]
+    L.ftgpu_set_state.argtypes = [vp, vp, vp, vp, C.c_double]
+    L.ftgpu_init_explicit.argtypes = [vp, C.c_double, C.c_double, C.c_double]
+    L.ftgpu_run.argtypes = [vp, C.c_int, C.POINTER(C.c_int)]
+    L.ftgpu_get_state.argtypes = [vp, vp, vp, vp, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                  C.POINTER(C.c_longlong)]
+    L.ftgpu_get_instance_clock.argtypes = [vp, vp, vp, vp, vp]
+    L.ftgpu_launches_per_step.argtypes = [vp]
+    L.ftgpu_check.argtypes = [vp]
+    _lib = L
+    return L
+
+
+def _check(status):
+    if status != OK:
+        L = lib()
+        raise FtgpuError(status, "%s (%s)" % (L.ftgpu_status_string(status).decode(),
+                                              L.ftgpu_last_error().decode()))
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def bc_table(fns):
+    arr = (BcFn * max(1, len(fns)))()
+    for i, (kind, params) in enumerate(fns):
+        arr[i].kind = int(kind)
+        for j, v in enumerate(params):
+            arr[i].p[j] = float(v)
+    return arr
+
+
+class Model:
+    """One engine model (mesh + materials + loads) on one GPU."""
+
+    def __init__(self, mesh, mats, precision=MIXED, device=0, fiber=None, loads=None,
+                 patch_size=0, instances=None, setup=True):
+        L = lib()
+        h = C.c_void_p()
+        _check(L.ftgpu_create(C.byref(h), int(device), int(precision)))
+        self.h = h
+        self.precision = precision
+        X = np.ascontiguousarray(mesh["coordinates"], np.float64).ravel()
+        self.nNodes = len(X) // 3
+        eptr = np.ascontiguousarray(mesh["eptr"], np.int32)
+        self.nE = len(eptr) - 1
+        _check(L.ftgpu_set_mesh(h, self.nNodes, self.nE, X, eptr,
+                                np.ascontiguousarray(mesh["connectivity"], np.int32),
+                                np.ascontiguousarray(mesh["etype"], np.int32),
+                                np.ascontiguousarray(mesh["pid"], np.int32)))
+        mid = np.ascontiguousarray(mats["materialID"], np.int32)
+        _check(L.ftgpu_set_materials(h, len(mid), mid,
+                                     np.ascontiguousarray(mats["properties"], np.float64).ravel()))
+        fib = fiber if fiber is not None else mesh.get("fiber")
+        if fib is not None:
+            _check(L.ftgpu_set_fibers(h, np.ascontiguousarray(fib, np.float64).ravel()))
+        if loads is not None:
+            self.set_bc(loads.dof_fn, loads.fns)
+        if patch_size:
+            _check(L.ftgpu_set_patch_size(h, int(patch_size)))
+        if instances is not None:
+            off = np.ascontiguousarray(instances["node_offset"], np.int32)
+            n = len(off) - 1
+            _check(L.ftgpu_set_instances(
+                h, n, off, np.ascontiguousarray(instances["tmax"], np.float64),
+                np.ascontiguousarray(instances["reduction"], np.float64),
+                np.ascontiguousarray(instances.get("failure_dt", np.zeros(n)), np.float64)))
+        self.ninst = 1 if instances is None else len(instances["node_offset"]) - 1
+        if setup:
+            self.setup()
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ftgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- set-up ----
+    def set_bc(self, dof_fn, fns):
+        self._fns = bc_table(fns)
+        _check(lib().ftgpu_set_bc(self.h, np.ascontiguousarray(dof_fn, np.int32).ravel(),
+                                  len(fns), C.cast(self._fns, C.c_void_p)))
+
+    def setup(self):
+        """ShapeFunctions() + AssembleLumpedMass() on the device."""
+        _check(lib().ftgpu_setup(self.h))
+
+    @property
+    def mass(self):
+        m = np.zeros(3 * self.nNodes)
+        _check(lib().ftgpu_get_mass(self.h, m))
+        return m
+
+    # ---- symbol-compatible primitives ----
+    def GetForce(self, u, dt=0.0):
+        """Internal force fi (and f_net = -fi) on displacements u, like GetForce()."""
+        fi = np.zeros(3 * self.nNodes)
+        _check(lib().ftgpu_get_force(self.h, np.ascontiguousarray(u, np.float64).ravel(),
+                                     float(dt), fi.ctypes.data, None))
+        return fi
+
+    def StableTimeStep(self, u):
+        d = C.c_double()
+        _check(lib().ftgpu_stable_time_step(self.h, np.ascontiguousarray(u, np.float64).ravel(),
+                                            C.byref(d)))
+        return d.value
+
+    def gauss_points(self):
+        n = lib().ftgpu_num_gauss_points(self.h)
+        F, J, S = np.zeros(9 * n), np.zeros(n), np.zeros(6 * n)
+        _check(lib().ftgpu_get_gauss_points(self.h, F.ctypes.data, J.ctypes.data, S.ctypes.data))
+        return F.reshape(n, 9), J, S.reshape(n, 6)
+
+    # ---- device-resident explicit loop ----
+    def set_state(self, u=None, v=None, a=None, time=0.0):
+        arrs = [None if x is None else np.ascontiguousarray(x, np.float64).ravel() for x in (u, v, a)]
+        _check(lib().ftgpu_set_state(self.h, *[_ptr(x) for x in arrs], float(time)))
+
+    def init_explicit(self, reduction=0.9, failure_dt=0.0, tmax=1e300):
+        _check(lib().ftgpu_init_explicit(self.h, float(reduction), float(failure_dt), float(tmax)))
+
+    def run(self, max_steps):
+        s = C.c_int()
+        _check(lib().ftgpu_run(self.h, int(max_steps), C.byref(s)))
+        return s.value
+
+    def state(self):
+        n = 3 * self.nNodes
+        u, v, a = np.zeros(n), np.zeros(n), np.zeros(n)
+        t, dt, st = C.c_double(), C.c_double(), C.c_longlong()
+        _check(lib().ftgpu_get_state(self.h, u.ctypes.data, v.ctypes.data, a.ctypes.data,
+                                     C.byref(t), C.byref(dt), C.byref(st)))
+        return dict(u=u, v=v, a=a, time=t.value, dt=dt.value, step=st.value)
+
+    def instance_clocks(self):
+        n = self.ninst
+        t, dt = np.zeros(n), np.zeros(n)
+        st, dn = np.zeros(n, np.int64), np.zeros(n, np.int32)
+        _check(lib().ftgpu_get_instance_clock(self.h, t.ctypes.data, dt.ctypes.data,
+                                              st.ctypes.data, dn.ctypes.data))
+        return dict(time=t, dt=dt, step=st, done=dn)
+
+    def launches_per_step(self):
+        return lib().ftgpu_launches_per_step(self.h)
+
+    def check(self):
+        _check(lib().ftgpu_check(self.h))

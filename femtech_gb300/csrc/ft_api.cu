@@ -1,0 +1,998 @@
+// ft_api.cu -- the C ABI of include/ftgpu.h: device memory, one-time setup,
+// symbol-compatible primitives and the graph-captured explicit loop.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "ft_common.h"
+#include "ft_launch.h"
+#include "ft_node.cuh"
+#include "ft_patches.h"
+#include "ftgpu.h"
+
+namespace ftgpu {
+
+static thread_local std::string g_last_error;
+
+static int fail(int code, const std::string &msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define CK(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return fail(FTGPU_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));    \
+  } while (0)
+#define CKI(expr)                                                                         \
+  do {                                                                                    \
+    int r_ = (expr);                                                                      \
+    if (r_ != 0)                                                                          \
+      return r_ > 0 ? fail(FTGPU_ERR_CUDA, std::string(#expr) + ": " +                    \
+                                               cudaGetErrorString((cudaError_t)r_))       \
+                    : r_;                                                                 \
+  } while (0)
+
+// Owning device buffer.
+struct DBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  DBuf() = default;
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  ~DBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  int alloc(size_t b) {
+    release();
+    if (b == 0) b = 16;
+    if (cudaMalloc(&p, b) != cudaSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+      return fail(FTGPU_ERR_ALLOC, "cudaMalloc of " + std::to_string(b) + " bytes failed");
+    }
+    bytes = b;
+    return 0;
+  }
+  template <class T>
+  int upload(const T *h, size_t n) {
+    int r = alloc(n * sizeof(T));
+    if (r) return r;
+    if (n && cudaMemcpy(p, h, n * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess)
+      return fail(FTGPU_ERR_CUDA, "upload failed");
+    return 0;
+  }
+  template <class T>
+  T *as() const {
+    return reinterpret_cast<T *>(p);
+  }
+};
+
+// Mass of one element's corners: m_a = rho * sum_gp w detJ N_a
+// (Mass3D.cpp:5-67 row-sum lumping with sum_b N_b = 1), FP64.
+template <int ET>
+__global__ void k_mass(const int *patch_elem_off, const int *patch_node_off,
+                       const int *patch_ent_off, const uint16_t *lptr, const uint16_t *lent,
+                       const uint16_t *lconn, const int *epid, const int *slot_node,
+                       const double *X, long long N, const MatP<double> *mats, int patch_begin,
+                       int elem_begin, double *sM) {
+  constexpr int NC = ET == 0 ? 8 : 4;
+  __shared__ double shM[NC][kMaxPatchElems];
+  const int p = patch_begin + blockIdx.x;
+  const int e0 = patch_elem_off[p], ne = patch_elem_off[p + 1] - e0;
+  const int s0 = patch_node_off[p], ns = patch_node_off[p + 1] - s0;
+  const int t = threadIdx.x;
+  if (t < ne) {
+    const int e = e0 + t;
+    double x[NC][3];
+    for (int a = 0; a < NC; ++a) {
+      const int n = slot_node[s0 + lconn[NC * (long long)(e - elem_begin) + a]];
+      for (int d = 0; d < 3; ++d) x[a][d] = X[d * N + n];
+    }
+    const double rho = mats[epid[e] & 0x7fffffff].p[0];
+    double m[NC];
+    for (int a = 0; a < NC; ++a) m[a] = 0.0;
+    if (ET == 0) {
+      const int sgn[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
+                             {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
+      const int sg[8][3] = {{-1, -1, 1}, {1, -1, 1}, {1, 1, 1}, {-1, 1, 1},
+                            {-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1}};
+      const double G = 0.577350269189626;
+      for (int g = 0; g < 8; ++g) {
+        const double xi = sg[g][0] * G, et = sg[g][1] * G, ze = sg[g][2] * G;
+        double A[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        double N[8];
+        for (int a = 0; a < 8; ++a) {
+          const double sx = sgn[a][0], sy = sgn[a][1], sz = sgn[a][2];
+          N[a] = (1 + sx * xi) * (1 + sy * et) * (1 + sz * ze) / 8;
+          const double dx = sx * (1 + sy * et) * (1 + sz * ze) / 8;
+          const double dy = sy * (1 + sx * xi) * (1 + sz * ze) / 8;
+          const double dz = sz * (1 + sx * xi) * (1 + sy * et) / 8;
+          for (int d = 0; d < 3; ++d) {
+            A[0][d] += dx * x[a][d];
+            A[1][d] += dy * x[a][d];
+            A[2][d] += dz * x[a][d];
+          }
+        }
+        const double det = A[0][0] * (A[1][1] * A[2][2] - A[1][2] * A[2][1]) -
+                           A[0][1] * (A[1][0] * A[2][2] - A[1][2] * A[2][0]) +
+                           A[0][2] * (A[1][0] * A[2][1] - A[1][1] * A[2][0]);
+        for (int a = 0; a < 8; ++a) m[a] += det * N[a];
+      }
+    } else {
+      double A[3][3];
+      for (int r = 0; r < 3; ++r)
+        for (int d = 0; d < 3; ++d) A[r][d] = x[r][d] - x[3][d];
+      const double det = A[0][0] * (A[1][1] * A[2][2] - A[1][2] * A[2][1]) -
+                         A[0][1] * (A[1][0] * A[2][2] - A[1][2] * A[2][0]) +
+                         A[0][2] * (A[1][0] * A[2][1] - A[1][1] * A[2][0]);
+      for (int a = 0; a < 4; ++a) m[a] = fabs(det) / 6.0 * 0.25;
+    }
+    for (int a = 0; a < NC; ++a) shM[a][t] = rho * m[a];
+  }
+  __syncthreads();
+  const uint16_t *lp = lptr + s0 + p;
+  const uint16_t *le = lent + patch_ent_off[p];
+  for (int i = t; i < ns; i += blockDim.x) {
+    double s = 0.0;
+    for (int k = lp[i]; k < lp[i + 1]; ++k) {
+      const int ent = le[k];
+      s += shM[ent % NC][ent / NC];
+    }
+    sM[s0 + i] = s;
+  }
+}
+
+__global__ void k_gather_mass(const int *slot_off, const int *slots, const double *sM,
+                              long long N, double *mass) {
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  double s = 0.0;
+  for (int k = slot_off[n]; k < slot_off[n + 1]; ++k) s += sM[slots[k]];
+  mass[n] = s;
+}
+
+__global__ void k_fill_u64(unsigned long long *p, unsigned long long v, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = v;
+}
+
+// ------------------------------------------------------------------------
+struct EngineBase {
+  virtual ~EngineBase() = default;
+};
+
+}  // namespace ftgpu
+
+using namespace ftgpu;
+
+struct ftgpu_model {
+  int device = 0;
+  int precision = FTGPU_MIXED;
+  cudaStream_t stream = nullptr;
+  // host inputs (reference layout)
+  int nNodes = 0, nE = 0, nPID = 0;
+  std::vector<double> X;
+  std::vector<int> eptr, conn, etype, pid, materialID;
+  std::vector<double> props, fiber;
+  std::vector<int> dof_fn;
+  std::vector<BcFn> fns;
+  int ninst = 1;
+  std::vector<int> node_off;
+  std::vector<InstParams> inst;
+  bool inst_set = false;
+  int patch_elems = 0;
+  bool setup_done = false, init_done = false;
+  PatchSet ps;
+  std::vector<int> gp_off;  // reference Gauss-point offset of each element
+  long long ngp_total = 0;
+  long long S = 0;
+  std::vector<double> mass_host;
+  std::vector<double> t0_state;  // pending initial state
+  double t0 = 0.0;
+  // device buffers
+  DBuf patch_elem_off, patch_node_off, patch_inst, patch_ent_off, lptr, lent, lconn, epid, fib;
+  DBuf sX, sU, sF, mats;
+  std::vector<std::unique_ptr<DBuf>> hist;
+  DBuf clock, dtmin, err, instp;
+  DBuf slot_off, slots, node_inst, nbc, fnsbuf;
+  DBuf dX, u, v, a, vh, mass, minv, fi;
+  DBuf gpF, gpJ, gpS;
+  // graph of one chunk of steps
+  cudaGraphExec_t chunk_exec = nullptr;
+  int chunk_steps = 0;
+  Clock *h_clock = nullptr;  // pinned
+  int *h_err = nullptr;
+  ~ftgpu_model() {
+    if (chunk_exec) cudaGraphExecDestroy(chunk_exec);
+    if (h_clock) cudaFreeHost(h_clock);
+    if (h_err) cudaFreeHost(h_err);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace {
+
+bool is_fp64(const ftgpu_model *m) { return m->precision == FTGPU_FP64; }
+
+int max_patch(const ftgpu_model *m) {
+  int pe = m->patch_elems > 0 ? m->patch_elems : 128;
+  if (is_fp64(m)) pe = std::min(pe, 128);
+  return std::max(32, std::min(pe, kMaxPatchElems));
+}
+
+template <class R>
+ElemArgs<R> elem_args(ftgpu_model *m, const PatchGroup &g, int gi) {
+  ElemArgs<R> A;
+  memset(&A, 0, sizeof(A));
+  A.patch_elem_off = m->patch_elem_off.as<int>();
+  A.patch_node_off = m->patch_node_off.as<int>();
+  A.patch_inst = m->patch_inst.as<int>();
+  A.patch_ent_off = m->patch_ent_off.as<int>();
+  A.lptr = m->lptr.as<uint16_t>();
+  A.lent = m->lent.as<uint16_t>();
+  A.lconn = m->lconn.as<uint16_t>() + m->ps.group_lconn_off[gi];
+  A.epid = m->epid.as<int>();
+  A.fib = m->fib.as<R>();
+  A.sX = m->sX.as<R>();
+  A.sU = m->sU.as<R>();
+  A.sF = m->sF.as<R>();
+  A.hist = m->hist[gi] ? m->hist[gi]->as<R>() : nullptr;
+  A.mats = m->mats.as<MatP<R>>();
+  A.clock = m->clock.as<Clock>();
+  A.dtmin = m->dtmin.as<unsigned long long>();
+  A.err = m->err.as<int>();
+  A.gpF = m->gpF.as<double>();
+  A.gpJ = m->gpJ.as<double>();
+  A.gpS = m->gpS.as<double>();
+  A.S = m->S;
+  A.E = m->nE;
+  A.ninst = m->ninst;
+  A.parity = 0;
+  A.patch_begin = g.patch_begin;
+  A.npatch = g.npatch;
+  A.elem_begin = g.elem_begin;
+  A.nelem = g.nelem;
+  A.use_clock = 1;
+  A.dt_direct = 0.0;
+  long long gpb = 0;
+  for (int k = 0; k < gi; ++k) gpb += (long long)m->ps.groups[k].nelem * (m->ps.groups[k].etype == 0 ? 8 : 1);
+  A.gpbase = gpb;
+  return A;
+}
+
+NodeArgs node_args(ftgpu_model *m, int mode, int parity) {
+  NodeArgs A;
+  memset(&A, 0, sizeof(A));
+  A.slot_off = m->slot_off.as<int>();
+  A.slots = m->slots.as<int>();
+  A.node_inst = m->ninst > 1 ? m->node_inst.as<int>() : nullptr;
+  A.nbc = m->nbc.as<int16_t>();
+  A.fns = m->fnsbuf.as<BcFn>();
+  A.X = m->dX.as<double>();
+  A.u = m->u.as<double>();
+  A.v = m->v.as<double>();
+  A.a = m->a.as<double>();
+  A.vh = m->vh.as<double>();
+  A.mass = m->mass.as<double>();
+  A.minv = m->minv.as<double>();
+  A.sF = m->sF.p;
+  A.sU = m->sU.p;
+  A.clock = m->clock.as<Clock>();
+  A.dtmin = m->dtmin.as<unsigned long long>();
+  A.inst = m->instp.as<InstParams>();
+  A.err = m->err.as<int>();
+  A.fi_out = m->fi.as<double>();
+  A.N = m->nNodes;
+  A.S = m->S;
+  A.ninst = m->ninst;
+  A.parity = parity;
+  A.mode = mode;
+  A.fp64 = is_fp64(m) ? 1 : 0;
+  return A;
+}
+
+int launch_node(ftgpu_model *m, int mode, int parity) {
+  NodeArgs A = node_args(m, mode, parity);
+  const int th = 256;
+  const long long nb = (m->nNodes + th - 1) / th;
+  if (is_fp64(m))
+    k_node<double><<<(unsigned)nb, th, 0, m->stream>>>(A);
+  else
+    k_node<float><<<(unsigned)nb, th, 0, m->stream>>>(A);
+  return (int)cudaGetLastError();
+}
+
+template <class R>
+int launch_groups_t(ftgpu_model *m, int parity, int use_clock, double dt_direct, int gp,
+                    int dt_only) {
+  const int PE = max_patch(m);
+  for (size_t gi = 0; gi < m->ps.groups.size(); ++gi) {
+    const PatchGroup &g = m->ps.groups[gi];
+    ElemArgs<R> A = elem_args<R>(m, g, (int)gi);
+    A.parity = parity;
+    A.use_clock = use_clock;
+    A.dt_direct = dt_direct;
+    const size_t smem = elem_smem_bytes_host<R>(g.etype, PE);
+    int r = launch_elem<R>(g.etype, g.mat, gp, g.npatch, PE, smem, m->stream, A, dt_only);
+    if (r) return r;
+  }
+  return 0;
+}
+
+int launch_groups(ftgpu_model *m, int parity, int use_clock, double dt_direct, int gp,
+                  int dt_only) {
+  return is_fp64(m) ? launch_groups_t<double>(m, parity, use_clock, dt_direct, gp, dt_only)
+                    : launch_groups_t<float>(m, parity, use_clock, dt_direct, gp, dt_only);
+}
+
+int fill_dtmin(ftgpu_model *m) {
+  k_fill_u64<<<(2 * m->ninst + 255) / 256, 256, 0, m->stream>>>(
+      m->dtmin.as<unsigned long long>(), kDtHugeBits, 2 * m->ninst);
+  return (int)cudaGetLastError();
+}
+
+// AoS [3N] host -> SoA [3][N] device
+int upload_aos(ftgpu_model *m, const double *h, DBuf &d) {
+  const long long N = m->nNodes;
+  std::vector<double> t(3 * N);
+  for (long long n = 0; n < N; ++n)
+    for (int k = 0; k < 3; ++k) t[k * N + n] = h ? h[3 * n + k] : 0.0;
+  CK(cudaMemcpyAsync(d.p, t.data(), 3 * N * sizeof(double), cudaMemcpyHostToDevice, m->stream));
+  CK(cudaStreamSynchronize(m->stream));
+  return 0;
+}
+
+int download_aos(ftgpu_model *m, const DBuf &d, double *h) {
+  if (!h) return 0;
+  const long long N = m->nNodes;
+  std::vector<double> t(3 * N);
+  CK(cudaMemcpyAsync(t.data(), d.p, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+  CK(cudaStreamSynchronize(m->stream));
+  for (long long n = 0; n < N; ++n)
+    for (int k = 0; k < 3; ++k) h[3 * n + k] = t[k * N + n];
+  return 0;
+}
+
+int check_err(ftgpu_model *m) {
+  CK(cudaMemcpyAsync(m->h_err, m->err.p, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
+  CK(cudaStreamSynchronize(m->stream));
+  int e = *m->h_err;
+  if (e & kErrInverted) return fail(FTGPU_ERR_INVERTED, "non-positive or non-finite Jacobian");
+  if (e & kErrIndex) return fail(FTGPU_ERR_INPUT, "local node index out of range");
+  return 0;
+}
+
+// Per-element part word: part | (1 << 31) when every node of the element has
+// all three DOFs constrained (skipped by StableTimeStep.cpp:13-19).
+int upload_epid(ftgpu_model *m) {
+  std::vector<int> w(m->nE);
+  for (int ge = 0; ge < m->nE; ++ge) {
+    const int e = m->ps.elem_order[ge];
+    bool active = false;
+    for (int k = m->eptr[e]; k < m->eptr[e + 1]; ++k) {
+      const int n = m->conn[k];
+      bool all = true;
+      for (int d = 0; d < 3; ++d)
+        if (m->dof_fn.empty() || m->dof_fn[3 * n + d] == FTGPU_BC_FREE) all = false;
+      if (!all) {
+        active = true;
+        break;
+      }
+    }
+    w[ge] = m->pid[e] | (active ? 0 : (int)0x80000000u);
+  }
+  return m->epid.upload(w.data(), w.size());
+}
+
+int upload_bc(ftgpu_model *m) {
+  const long long N = m->nNodes;
+  std::vector<int16_t> nb(3 * N, (int16_t)FTGPU_BC_FREE);
+  if (!m->dof_fn.empty())
+    for (long long n = 0; n < N; ++n)
+      for (int d = 0; d < 3; ++d) nb[d * N + n] = (int16_t)m->dof_fn[3 * n + d];
+  int r = m->nbc.upload(nb.data(), nb.size());
+  if (r) return r;
+  std::vector<BcFn> f = m->fns;
+  if (f.empty()) f.resize(1);
+  return m->fnsbuf.upload(f.data(), f.size());
+}
+
+template <class R>
+int upload_materials(ftgpu_model *m) {
+  std::vector<MatP<R>> t(m->nPID);
+  for (int p = 0; p < m->nPID; ++p) {
+    const double *pr = &m->props[FTGPU_MAXMATPARAMS * p];
+    MatP<R> q;
+    memset(&q, 0, sizeof(q));
+    for (int k = 0; k < 9; ++k) q.p[k] = R(pr[k]);
+    const double mu = pr[1], lambda = pr[2], rho = pr[0];
+    q.K = R(lambda + 2.0 * mu / 3.0);
+    // CalculateTimeStep.cpp:16-18
+    const double nu = 0.5 * lambda / (lambda + mu);
+    const double ce = std::sqrt(lambda * (1.0 / nu - 1.0) / rho);
+    q.ce = ce;
+    q.inv_ce = R(1.0 / ce);
+    q.mat = m->materialID[p];
+    t[p] = q;
+  }
+  return m->mats.upload(t.data(), t.size());
+}
+
+template <class R>
+int setup_t(ftgpu_model *m) {
+  const long long N = m->nNodes;
+  const int E = m->nE;
+  // element material / instance for grouping
+  std::vector<int> emat(E), einst(E, 0), ninst_of(N, 0);
+  if (m->ninst > 1)
+    for (int i = 0; i < m->ninst; ++i)
+      for (int n = m->node_off[i]; n < m->node_off[i + 1]; ++n) ninst_of[n] = i;
+  for (int e = 0; e < E; ++e) {
+    if (m->pid[e] < 0 || m->pid[e] >= m->nPID) return fail(FTGPU_ERR_INPUT, "pid out of range");
+    const int mt = m->materialID[m->pid[e]];
+    if (mt < 0 || mt > 7) return fail(FTGPU_ERR_MATERIAL, "unknown material ID");
+    emat[e] = mt;
+    einst[e] = ninst_of[m->conn[m->eptr[e]]];
+    for (int k = m->eptr[e]; k < m->eptr[e + 1]; ++k)
+      if (ninst_of[m->conn[k]] != einst[e]) return fail(FTGPU_ERR_INPUT, "element spans instances");
+  }
+  const int PE = max_patch(m);
+  int rc = build_patches((int)N, E, m->X.data(), m->eptr.data(), m->conn.data(), m->etype.data(),
+                         emat.data(), einst.data(), PE, kMaxLocalNodes, m->ps);
+  if (rc) return fail(FTGPU_ERR_INPUT, "invalid mesh (element type / node count / node index)");
+  PatchSet &ps = m->ps;
+  const int P = (int)ps.patch_inst.size();
+  m->S = (long long)ps.slot_node.size();
+  const long long S = m->S;
+  CKI(m->patch_elem_off.upload(ps.patch_elem_off.data(), P + 1));
+  CKI(m->patch_node_off.upload(ps.patch_node_off.data(), P + 1));
+  CKI(m->patch_inst.upload(ps.patch_inst.data(), P));
+  CKI(m->patch_ent_off.upload(ps.patch_ent_off.data(), P + 1));
+  CKI(m->lptr.upload(ps.lptr.data(), ps.lptr.size()));
+  CKI(m->lent.upload(ps.lent.data(), ps.lent.size()));
+  CKI(m->lconn.upload(ps.lconn.data(), ps.lconn.size()));
+  CKI(m->slot_off.upload(ps.node_slot_off.data(), N + 1));
+  CKI(m->slots.upload(ps.node_slots.data(), ps.node_slots.size()));
+  CKI(upload_epid(m));
+  CKI(upload_materials<R>(m));
+  // reference coordinates per slot: absolute in FP64 mode, relative to the
+  // patch's first node in mixed mode (keeps FP32 digits for element geometry)
+  {
+    std::vector<R> sx(3 * S);
+    for (int p = 0; p < P; ++p) {
+      const int s0 = ps.patch_node_off[p], s1 = ps.patch_node_off[p + 1];
+      double anc[3] = {0, 0, 0};
+      if (!is_fp64(m))
+        for (int d = 0; d < 3; ++d) anc[d] = m->X[3 * ps.slot_node[s0] + d];
+      for (int s = s0; s < s1; ++s)
+        for (int d = 0; d < 3; ++d) sx[d * S + s] = R(m->X[3 * ps.slot_node[s] + d] - anc[d]);
+    }
+    CKI(m->sX.upload(sx.data(), sx.size()));
+  }
+  CKI(m->sU.alloc(3 * S * sizeof(R)));
+  CK(cudaMemset(m->sU.p, 0, 3 * S * sizeof(R)));
+  CKI(m->sF.alloc(3 * S * sizeof(R)));
+  CK(cudaMemset(m->sF.p, 0, 3 * S * sizeof(R)));
+  // fibres (material 7), group order, SoA
+  bool any7 = false;
+  for (auto &g : ps.groups) any7 |= g.mat == 7;
+  if (any7) {
+    std::vector<R> fb(3 * (size_t)E, R(0));
+    for (int ge = 0; ge < E; ++ge) {
+      const int e = ps.elem_order[ge];
+      double a0[3] = {1, 0, 0};
+      if (!m->fiber.empty()) {
+        for (int d = 0; d < 3; ++d) a0[d] = m->fiber[3 * e + d];
+        double nrm = std::sqrt(a0[0] * a0[0] + a0[1] * a0[1] + a0[2] * a0[2]);
+        if (nrm > 0)
+          for (int d = 0; d < 3; ++d) a0[d] /= nrm;
+      }
+      for (int d = 0; d < 3; ++d) fb[d * (size_t)E + ge] = R(a0[d]);
+    }
+    CKI(m->fib.upload(fb.data(), fb.size()));
+  }
+  // viscoelastic history per group: [ncomp][NGP][nelem], zero
+  m->hist.clear();
+  for (auto &g : ps.groups) {
+    int nc = g.mat == 5 ? 18 : (g.mat == 7 ? 12 : 0);
+    if (nc == 0) {
+      m->hist.emplace_back(nullptr);
+      continue;
+    }
+    const size_t n = (size_t)nc * (g.etype == 0 ? 8 : 1) * g.nelem;
+    auto b = std::make_unique<DBuf>();
+    CKI(b->alloc(n * sizeof(R)));
+    CK(cudaMemset(b->p, 0, n * sizeof(R)));
+    m->hist.push_back(std::move(b));
+  }
+  // reference Gauss-point offsets (gpPtr of ShapeFunctions.cpp:64-165)
+  m->gp_off.assign(E + 1, 0);
+  for (int e = 0; e < E; ++e) m->gp_off[e + 1] = m->gp_off[e] + (m->etype[e] == 0 ? 8 : 1);
+  m->ngp_total = m->gp_off[E];
+  // nodal state
+  {
+    std::vector<double> xs(3 * N);
+    for (long long n = 0; n < N; ++n)
+      for (int d = 0; d < 3; ++d) xs[d * N + n] = m->X[3 * n + d];
+    CKI(m->dX.upload(xs.data(), xs.size()));
+  }
+  for (DBuf *b : {&m->u, &m->v, &m->a, &m->vh, &m->fi}) {
+    CKI(b->alloc(3 * N * sizeof(double)));
+    CK(cudaMemset(b->p, 0, 3 * N * sizeof(double)));
+  }
+  CKI(upload_bc(m));
+  // instances
+  if (!m->inst_set) {
+    m->ninst = 1;
+    m->node_off = {0, (int)N};
+    m->inst.assign(1, InstParams{1e300, 0.9, 0.0, 0, 0, 0});
+  }
+  if (m->ninst > 1) {
+    std::vector<int> ni(N);
+    for (int i = 0; i < m->ninst; ++i)
+      for (int n = m->node_off[i]; n < m->node_off[i + 1]; ++n) ni[n] = i;
+    CKI(m->node_inst.upload(ni.data(), N));
+  }
+  for (int i = 0; i < m->ninst; ++i) m->inst[i].node_begin = m->node_off[i];
+  CKI(m->instp.upload(m->inst.data(), m->ninst));
+  std::vector<Clock> ck(2 * m->ninst);
+  for (auto &c : ck) c = Clock{0.0, 0.0, 0, 0, 0};
+  CKI(m->clock.upload(ck.data(), ck.size()));
+  CKI(m->dtmin.alloc(2 * m->ninst * sizeof(unsigned long long)));
+  CKI(m->err.alloc(sizeof(int)));
+  CK(cudaMemset(m->err.p, 0, sizeof(int)));
+  CKI(fill_dtmin(m));
+  // lumped mass on the device (FP64), replaces AssembleLumpedMass()
+  {
+    DBuf sM, snode, mpd;
+    CKI(sM.alloc(S * sizeof(double)));
+    CKI(snode.upload(ps.slot_node.data(), ps.slot_node.size()));
+    std::vector<MatP<double>> md(m->nPID);
+    for (int p = 0; p < m->nPID; ++p) {
+      memset(&md[p], 0, sizeof(md[p]));
+      for (int k = 0; k < 9; ++k) md[p].p[k] = m->props[9 * p + k];
+    }
+    CKI(mpd.upload(md.data(), md.size()));
+    for (size_t gi = 0; gi < ps.groups.size(); ++gi) {
+      const PatchGroup &g = ps.groups[gi];
+      const uint16_t *lc = m->lconn.as<uint16_t>() + ps.group_lconn_off[gi];
+      if (g.npatch == 0) continue;
+      if (g.etype == 0)
+        k_mass<0><<<g.npatch, PE, 0, m->stream>>>(
+            m->patch_elem_off.as<int>(), m->patch_node_off.as<int>(), m->patch_ent_off.as<int>(),
+            m->lptr.as<uint16_t>(), m->lent.as<uint16_t>(), lc, m->epid.as<int>(),
+            snode.as<int>(), m->dX.as<double>(), N, mpd.as<MatP<double>>(), g.patch_begin,
+            g.elem_begin, sM.as<double>());
+      else
+        k_mass<1><<<g.npatch, PE, 0, m->stream>>>(
+            m->patch_elem_off.as<int>(), m->patch_node_off.as<int>(), m->patch_ent_off.as<int>(),
+            m->lptr.as<uint16_t>(), m->lent.as<uint16_t>(), lc, m->epid.as<int>(),
+            snode.as<int>(), m->dX.as<double>(), N, mpd.as<MatP<double>>(), g.patch_begin,
+            g.elem_begin, sM.as<double>());
+      CK(cudaGetLastError());
+    }
+    CKI(m->mass.alloc(N * sizeof(double)));
+    k_gather_mass<<<(unsigned)((N + 255) / 256), 256, 0, m->stream>>>(
+        m->slot_off.as<int>(), m->slots.as<int>(), sM.as<double>(), N, m->mass.as<double>());
+    CK(cudaGetLastError());
+    m->mass_host.resize(N);
+    CK(cudaMemcpyAsync(m->mass_host.data(), m->mass.p, N * sizeof(double), cudaMemcpyDeviceToHost,
+                       m->stream));
+    CK(cudaStreamSynchronize(m->stream));
+    std::vector<double> mi(N);
+    for (long long n = 0; n < N; ++n) mi[n] = 1.0 / m->mass_host[n];
+    CKI(m->minv.upload(mi.data(), N));
+  }
+  if (!m->h_clock) CK(cudaMallocHost((void **)&m->h_clock, sizeof(Clock) * std::max(2 * m->ninst, 2)));
+  if (!m->h_err) CK(cudaMallocHost((void **)&m->h_err, sizeof(int)));
+  m->setup_done = true;
+  m->init_done = false;
+  if (m->chunk_exec) {
+    cudaGraphExecDestroy(m->chunk_exec);
+    m->chunk_exec = nullptr;
+  }
+  return 0;
+}
+
+int ensure_gp(ftgpu_model *m) {
+  const size_t n = (size_t)m->ngp_total;
+  if (m->gpJ.bytes >= n * sizeof(double)) return 0;
+  CKI(m->gpF.alloc(9 * n * sizeof(double)));
+  CKI(m->gpJ.alloc(n * sizeof(double)));
+  CKI(m->gpS.alloc(6 * n * sizeof(double)));
+  return 0;
+}
+
+// One chunk: BEGIN, K x (element groups, node), the last node pass FINISH.
+int capture_chunk(ftgpu_model *m, int K) {
+  if (m->chunk_exec && m->chunk_steps == K) return 0;
+  if (m->chunk_exec) cudaGraphExecDestroy(m->chunk_exec);
+  m->chunk_exec = nullptr;
+  cudaGraph_t g;
+  CK(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
+  int r = launch_node(m, kNodeBegin, 0);
+  for (int k = 0; k < K && !r; ++k) {
+    r = launch_groups(m, k & 1, 1, 0.0, 0, 0);
+    if (!r) r = launch_node(m, k == K - 1 ? kNodeFinish : kNodeFused, k & 1);
+  }
+  cudaError_t ce = cudaStreamEndCapture(m->stream, &g);
+  if (r) return fail(FTGPU_ERR_CUDA, std::string("capture launch: ") + cudaGetErrorString((cudaError_t)r));
+  if (ce != cudaSuccess) return fail(FTGPU_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(ce));
+  ce = cudaGraphInstantiate(&m->chunk_exec, g, 0);
+  cudaGraphDestroy(g);
+  if (ce != cudaSuccess) return fail(FTGPU_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(ce));
+  m->chunk_steps = K;
+  return 0;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------
+extern "C" {
+
+const char *ftgpu_status_string(int s) {
+  switch (s) {
+    case FTGPU_OK: return "ok";
+    case FTGPU_ERR_MATERIAL: return "unknown material";
+    case FTGPU_ERR_INPUT: return "bad input";
+    case FTGPU_ERR_ALLOC: return "device allocation failed";
+    case FTGPU_ERR_DT: return "time step below FailureTimeStep";
+    case FTGPU_ERR_INVERTED: return "inverted or non-finite element";
+    case FTGPU_ERR_CUDA: return "CUDA error";
+    case FTGPU_ERR_STATE: return "call out of order";
+    case FTGPU_ERR_NODEVICE: return "no CUDA device";
+    default: return "unknown status";
+  }
+}
+
+const char *ftgpu_last_error(void) { return g_last_error.c_str(); }
+
+int ftgpu_create(ftgpu_model **out, int device, int precision) {
+  if (!out) return fail(FTGPU_ERR_INPUT, "null output pointer");
+  *out = nullptr;
+  if (precision != FTGPU_FP64 && precision != FTGPU_MIXED) return fail(FTGPU_ERR_INPUT, "precision");
+  int nd = 0;
+  if (cudaGetDeviceCount(&nd) != cudaSuccess || nd <= device || device < 0) {
+    cudaGetLastError();
+    return fail(FTGPU_ERR_NODEVICE, "no CUDA device available");
+  }
+  CK(cudaSetDevice(device));
+  auto m = std::make_unique<ftgpu_model>();
+  m->device = device;
+  m->precision = precision;
+  CK(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
+  *out = m.release();
+  return FTGPU_OK;
+}
+
+int ftgpu_destroy(ftgpu_model *m) {
+  if (!m) return FTGPU_OK;
+  cudaSetDevice(m->device);
+  if (m->stream) cudaStreamSynchronize(m->stream);
+  delete m;
+  return FTGPU_OK;
+}
+
+int ftgpu_set_mesh(ftgpu_model *m, int nNodes, int nelements, const double *coordinates,
+                   const int *eptr, const int *connectivity, const int *etype, const int *pid) {
+  if (!m || nNodes <= 0 || nelements <= 0 || !coordinates || !eptr || !connectivity || !etype ||
+      !pid)
+    return fail(FTGPU_ERR_INPUT, "set_mesh: bad arguments");
+  m->nNodes = nNodes;
+  m->nE = nelements;
+  m->X.assign(coordinates, coordinates + 3 * (size_t)nNodes);
+  m->eptr.assign(eptr, eptr + nelements + 1);
+  const int nc = eptr[nelements];
+  if (nc <= 0) return fail(FTGPU_ERR_INPUT, "set_mesh: empty connectivity");
+  m->conn.assign(connectivity, connectivity + nc);
+  m->etype.assign(etype, etype + nelements);
+  m->pid.assign(pid, pid + nelements);
+  for (int e = 0; e < nelements; ++e) {
+    if (etype[e] != FTGPU_C3D8 && etype[e] != FTGPU_C3D4)
+      return fail(FTGPU_ERR_INPUT, "set_mesh: element type must be C3D8 or C3D4");
+    if (eptr[e + 1] - eptr[e] != (etype[e] == FTGPU_C3D8 ? 8 : 4))
+      return fail(FTGPU_ERR_INPUT, "set_mesh: node count does not match element type");
+  }
+  for (int k = 0; k < nc; ++k)
+    if (connectivity[k] < 0 || connectivity[k] >= nNodes)
+      return fail(FTGPU_ERR_INPUT, "set_mesh: node index out of range");
+  m->setup_done = m->init_done = false;
+  return FTGPU_OK;
+}
+
+int ftgpu_set_materials(ftgpu_model *m, int nPID, const int *materialID, const double *props) {
+  if (!m || nPID <= 0 || !materialID || !props) return fail(FTGPU_ERR_INPUT, "set_materials");
+  for (int p = 0; p < nPID; ++p)
+    if (materialID[p] < 0 || materialID[p] > 7)
+      return fail(FTGPU_ERR_MATERIAL, "unknown material ID (StressUpdate.cpp:25)");
+  m->nPID = nPID;
+  m->materialID.assign(materialID, materialID + nPID);
+  m->props.assign(props, props + FTGPU_MAXMATPARAMS * (size_t)nPID);
+  if (m->setup_done) {
+    int r = is_fp64(m) ? upload_materials<double>(m) : upload_materials<float>(m);
+    if (r) return r;
+  }
+  return FTGPU_OK;
+}
+
+int ftgpu_set_fibers(ftgpu_model *m, const double *fiber) {
+  if (!m || !fiber || m->nE <= 0) return fail(FTGPU_ERR_INPUT, "set_fibers");
+  m->fiber.assign(fiber, fiber + 3 * (size_t)m->nE);
+  m->setup_done = false;
+  return FTGPU_OK;
+}
+
+int ftgpu_set_bc(ftgpu_model *m, const int *dof_fn, int nfn, const ftgpu_bc_fn *fns) {
+  if (!m || m->nNodes <= 0 || !dof_fn || nfn < 0) return fail(FTGPU_ERR_INPUT, "set_bc");
+  m->dof_fn.assign(dof_fn, dof_fn + 3 * (size_t)m->nNodes);
+  for (int v : m->dof_fn)
+    if (v < FTGPU_BC_HOLD || v >= nfn) return fail(FTGPU_ERR_INPUT, "set_bc: function index");
+  m->fns.resize(nfn);
+  for (int i = 0; i < nfn; ++i) {
+    m->fns[i].kind = fns[i].kind;
+    m->fns[i].pad = 0;
+    for (int k = 0; k < 8; ++k) m->fns[i].p[k] = fns[i].p[k];
+    if (fns[i].kind < 0 || fns[i].kind > 3) return fail(FTGPU_ERR_INPUT, "set_bc: kind");
+  }
+  if (m->setup_done) {
+    CKI(upload_bc(m));
+    CKI(upload_epid(m));
+    if (m->chunk_exec) {
+      cudaGraphExecDestroy(m->chunk_exec);
+      m->chunk_exec = nullptr;
+    }
+  }
+  return FTGPU_OK;
+}
+
+int ftgpu_set_instances(ftgpu_model *m, int ninst, const int *node_offset, const double *tmax,
+                        const double *reduction, const double *failure_dt) {
+  if (!m || ninst <= 0 || !node_offset || node_offset[0] != 0 || node_offset[ninst] != m->nNodes)
+    return fail(FTGPU_ERR_INPUT, "set_instances");
+  m->ninst = ninst;
+  m->node_off.assign(node_offset, node_offset + ninst + 1);
+  m->inst.resize(ninst);
+  for (int i = 0; i < ninst; ++i) {
+    if (node_offset[i + 1] <= node_offset[i]) return fail(FTGPU_ERR_INPUT, "empty instance");
+    m->inst[i] = InstParams{tmax ? tmax[i] : 1e300, reduction ? reduction[i] : 0.9,
+                            failure_dt ? failure_dt[i] : 0.0, 0, node_offset[i], 0};
+  }
+  m->inst_set = true;
+  m->setup_done = false;
+  return FTGPU_OK;
+}
+
+int ftgpu_set_patch_size(ftgpu_model *m, int pe) {
+  if (!m || pe < 0 || pe > kMaxPatchElems) return fail(FTGPU_ERR_INPUT, "set_patch_size");
+  m->patch_elems = pe;
+  m->setup_done = false;
+  return FTGPU_OK;
+}
+
+int ftgpu_setup(ftgpu_model *m) {
+  if (!m || m->nNodes <= 0 || m->nPID <= 0) return fail(FTGPU_ERR_STATE, "setup before mesh/materials");
+  CK(cudaSetDevice(m->device));
+  return is_fp64(m) ? setup_t<double>(m) : setup_t<float>(m);
+}
+
+int ftgpu_get_mass(ftgpu_model *m, double *mass) {
+  if (!m || !m->setup_done) return fail(FTGPU_ERR_STATE, "get_mass before setup");
+  for (int n = 0; n < m->nNodes; ++n)
+    for (int d = 0; d < 3; ++d) mass[3 * n + d] = m->mass_host[n];
+  return FTGPU_OK;
+}
+
+int ftgpu_num_gauss_points(ftgpu_model *m) {
+  if (!m || !m->setup_done) return 0;
+  return (int)m->ngp_total;
+}
+
+int ftgpu_get_force(ftgpu_model *m, const double *u, double dt, double *fi, double *f_net) {
+  if (!m || !m->setup_done) return fail(FTGPU_ERR_STATE, "get_force before setup");
+  CK(cudaSetDevice(m->device));
+  CKI(upload_aos(m, u, m->u));
+  CKI(launch_node(m, kNodeScatterU, 0));
+  CKI(ensure_gp(m));
+  CKI(fill_dtmin(m));
+  CKI(launch_groups(m, 0, 0, dt, 1, 0));
+  CKI(launch_node(m, kNodeGather, 0));
+  CKI(check_err(m));
+  std::vector<double> h(3 * (size_t)m->nNodes);
+  CKI(download_aos(m, m->fi, h.data()));
+  if (fi) memcpy(fi, h.data(), h.size() * sizeof(double));
+  if (f_net)
+    for (size_t i = 0; i < h.size(); ++i) f_net[i] = -h[i];
+  return FTGPU_OK;
+}
+
+int ftgpu_stable_time_step(ftgpu_model *m, const double *u, double *dt_min) {
+  if (!m || !m->setup_done || !dt_min) return fail(FTGPU_ERR_STATE, "stable_time_step before setup");
+  CK(cudaSetDevice(m->device));
+  CKI(upload_aos(m, u, m->u));
+  CKI(launch_node(m, kNodeScatterU, 0));
+  CKI(fill_dtmin(m));
+  CKI(launch_groups(m, 0, 0, 0.0, 0, 1));
+  std::vector<unsigned long long> h(2 * m->ninst);
+  CK(cudaMemcpyAsync(h.data(), m->dtmin.p, h.size() * 8, cudaMemcpyDeviceToHost, m->stream));
+  CK(cudaStreamSynchronize(m->stream));
+  double mn = 1e20;  // "huge" of GlobalVariables.h:15
+  for (int i = 0; i < m->ninst; ++i) {
+    double v;
+    memcpy(&v, &h[i], 8);
+    mn = std::min(mn, v);
+  }
+  *dt_min = mn;
+  CKI(fill_dtmin(m));
+  return check_err(m);
+}
+
+int ftgpu_get_gauss_points(ftgpu_model *m, double *F, double *detF, double *pk2) {
+  if (!m || !m->setup_done || m->gpJ.bytes == 0) return fail(FTGPU_ERR_STATE, "no recorded Gauss points");
+  const size_t n = (size_t)m->ngp_total;
+  std::vector<double> f(9 * n), j(n), s(6 * n);
+  CK(cudaMemcpy(f.data(), m->gpF.p, f.size() * 8, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(j.data(), m->gpJ.p, j.size() * 8, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(s.data(), m->gpS.p, s.size() * 8, cudaMemcpyDeviceToHost));
+  // group order -> reference element order
+  long long q = 0;
+  for (const PatchGroup &g : m->ps.groups) {
+    const int ng = g.etype == 0 ? 8 : 1;
+    for (int k = 0; k < g.nelem; ++k) {
+      const int e = m->ps.elem_order[g.elem_begin + k];
+      for (int gp = 0; gp < ng; ++gp, ++q) {
+        const long long r = m->gp_off[e] + gp;
+        if (F) memcpy(F + 9 * r, &f[9 * q], 9 * sizeof(double));
+        if (detF) detF[r] = j[q];
+        if (pk2) memcpy(pk2 + 6 * r, &s[6 * q], 6 * sizeof(double));
+      }
+    }
+  }
+  return FTGPU_OK;
+}
+
+int ftgpu_set_state(ftgpu_model *m, const double *u, const double *v, const double *a,
+                    double time) {
+  if (!m || !m->setup_done) return fail(FTGPU_ERR_STATE, "set_state before setup");
+  CK(cudaSetDevice(m->device));
+  CKI(upload_aos(m, u, m->u));
+  CKI(upload_aos(m, v, m->v));
+  CKI(upload_aos(m, a, m->a));
+  m->t0 = time;
+  m->init_done = false;
+  return FTGPU_OK;
+}
+
+int ftgpu_init_explicit(ftgpu_model *m, double reduction, double failure_dt, double tmax) {
+  if (!m || !m->setup_done) return fail(FTGPU_ERR_STATE, "init_explicit before setup");
+  CK(cudaSetDevice(m->device));
+  if (!m->inst_set) {
+    m->inst[0].tmax = tmax;
+    m->inst[0].reduction = reduction;
+    m->inst[0].failure_dt = failure_dt;
+  }
+  for (int i = 0; i < m->ninst; ++i) m->inst[i].step_limit = 0x7fffffffffffffffll;
+  CK(cudaMemcpyAsync(m->instp.p, m->inst.data(), m->ninst * sizeof(InstParams),
+                     cudaMemcpyHostToDevice, m->stream));
+  CK(cudaMemsetAsync(m->err.p, 0, sizeof(int), m->stream));
+  NodeArgs A = node_args(m, kNodeBegin, 0);
+  k_apply_bc<<<(unsigned)((m->nNodes + 255) / 256), 256, 0, m->stream>>>(A, m->t0);
+  CK(cudaGetLastError());
+  CKI(launch_node(m, kNodeScatterU, 0));
+  CKI(fill_dtmin(m));
+  CKI(launch_groups(m, 0, 0, 0.0, 0, 1));
+  k_clock_init<<<(m->ninst + 127) / 128, 128, 0, m->stream>>>(
+      m->clock.as<Clock>(), m->dtmin.as<unsigned long long>(), m->instp.as<InstParams>(),
+      m->ninst, m->t0);
+  CK(cudaGetLastError());
+  CKI(launch_groups(m, 0, 1, 0.0, 0, 0));
+  CKI(launch_node(m, kNodeInit, 0));
+  CKI(check_err(m));
+  CK(cudaMemcpyAsync(m->h_clock, m->clock.p, sizeof(Clock) * m->ninst, cudaMemcpyDeviceToHost,
+                     m->stream));
+  CK(cudaStreamSynchronize(m->stream));
+  for (int i = 0; i < m->ninst; ++i)
+    if (m->h_clock[i].done & 4) return fail(FTGPU_ERR_DT, "initial dt below FailureTimeStep");
+  m->init_done = true;
+  return FTGPU_OK;
+}
+
+int ftgpu_run(ftgpu_model *m, int max_steps, int *steps_done) {
+  if (!m || !m->init_done) return fail(FTGPU_ERR_STATE, "run before init_explicit");
+  if (max_steps <= 0) {
+    if (steps_done) *steps_done = 0;
+    return FTGPU_OK;
+  }
+  CK(cudaSetDevice(m->device));
+  const int ni = m->ninst;
+  CK(cudaMemcpyAsync(m->h_clock, m->clock.p, sizeof(Clock) * ni, cudaMemcpyDeviceToHost, m->stream));
+  CK(cudaStreamSynchronize(m->stream));
+  const long long start0 = m->h_clock[0].step;
+  for (int i = 0; i < ni; ++i) {
+    m->h_clock[i].done &= ~2;  // a new run lifts the previous step limit
+    m->inst[i].step_limit = m->h_clock[i].step + max_steps;
+  }
+  CK(cudaMemcpyAsync(m->clock.p, m->h_clock, sizeof(Clock) * ni, cudaMemcpyHostToDevice, m->stream));
+  CK(cudaMemcpyAsync(m->instp.p, m->inst.data(), ni * sizeof(InstParams), cudaMemcpyHostToDevice,
+                     m->stream));
+  const int K = 16;
+  CKI(capture_chunk(m, K));
+  const long long max_chunks = (max_steps + K - 1) / K + 1;
+  int rc = FTGPU_OK;
+  for (long long c = 0; c < max_chunks; ++c) {
+    CK(cudaGraphLaunch(m->chunk_exec, m->stream));
+    CK(cudaMemcpyAsync(m->h_clock, m->clock.p, sizeof(Clock) * ni, cudaMemcpyDeviceToHost,
+                       m->stream));
+    CK(cudaMemcpyAsync(m->h_err, m->err.p, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
+    CK(cudaStreamSynchronize(m->stream));
+    if (*m->h_err & kErrInverted) {
+      rc = fail(FTGPU_ERR_INVERTED, "non-positive or non-finite Jacobian");
+      break;
+    }
+    bool all = true, dterr = false;
+    for (int i = 0; i < ni; ++i) {
+      all &= m->h_clock[i].done != 0;
+      dterr |= (m->h_clock[i].done & 4) != 0;
+    }
+    if (dterr) {
+      rc = fail(FTGPU_ERR_DT, "time step below FailureTimeStep");
+      break;
+    }
+    if (all) break;
+  }
+  if (steps_done) *steps_done = (int)(m->h_clock[0].step - start0);
+  return rc;
+}
+
+int ftgpu_get_state(ftgpu_model *m, double *u, double *v, double *a, double *time, double *dt,
+                    long long *step) {
+  if (!m || !m->setup_done) return fail(FTGPU_ERR_STATE, "get_state before setup");
+  CK(cudaSetDevice(m->device));
+  CKI(download_aos(m, m->u, u));
+  CKI(download_aos(m, m->v, v));
+  CKI(download_aos(m, m->a, a));
+  Clock c;
+  CK(cudaMemcpy(&c, m->clock.p, sizeof(Clock), cudaMemcpyDeviceToHost));
+  if (time) *time = c.time;
+  if (dt) *dt = c.dt;
+  if (step) *step = c.step;
+  return FTGPU_OK;
+}
+
+int ftgpu_get_instance_clock(ftgpu_model *m, double *time, double *dt, long long *step, int *done) {
+  if (!m || !m->setup_done) return fail(FTGPU_ERR_STATE, "get_instance_clock before setup");
+  std::vector<Clock> c(m->ninst);
+  CK(cudaMemcpy(c.data(), m->clock.p, sizeof(Clock) * m->ninst, cudaMemcpyDeviceToHost));
+  for (int i = 0; i < m->ninst; ++i) {
+    if (time) time[i] = c[i].time;
+    if (dt) dt[i] = c[i].dt;
+    if (step) step[i] = c[i].step;
+    if (done) done[i] = c[i].done;
+  }
+  return FTGPU_OK;
+}
+
+int ftgpu_launches_per_step(ftgpu_model *m) {
+  if (!m || !m->setup_done) return 0;
+  int g = 0;
+  for (auto &x : m->ps.groups) g += x.npatch > 0;
+  return g + 1;
+}
+
+int ftgpu_check(ftgpu_model *m) {
+  if (!m || !m->setup_done) return fail(FTGPU_ERR_STATE, "check before setup");
+  CK(cudaSetDevice(m->device));
+  return check_err(m);
+}
+
+}  // extern "C"

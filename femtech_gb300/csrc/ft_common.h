@@ -1,0 +1,111 @@
+// ft_common.h -- device data structures shared by the kernels and the host
+// orchestration of the explicit hot path.
+#pragma once
+
+#include <cstdint>
+
+#include "ft_materials.cuh"
+
+namespace ftgpu {
+
+constexpr int kMaxPatchElems = 256;   // elements per patch (thread block) upper bound
+constexpr int kMaxLocalNodes = 320;   // local nodes per patch (shared memory bound)
+constexpr int kElemThreads = 128;     // threads per element block
+
+// Per-instance clock, double-buffered by step parity.  Between steps it holds
+// the state the reference keeps in the globals Time and dt (ex9.cpp:9).
+struct Clock {
+  double time;     // t_n
+  double dt;       // dt_n (the next step's increment)
+  long long step;  // steps completed
+  int done;        // bit0 tMax reached, bit1 step limit, bit2 error
+  int err;
+};
+
+struct InstParams {
+  double tmax;
+  double reduction;   // ExplicitTimeStepReduction
+  double failure_dt;  // FailureTimeStep
+  long long step_limit;
+  int node_begin;     // first node: its thread advances the clock
+  int pad;
+};
+
+struct BcFn {
+  int kind;
+  int pad;
+  double p[8];
+};
+
+// Start value of the stable-dt minimum: the reference's "huge" = 1e20
+// (include/GlobalVariables.h:15, StableTimeStep.cpp:6), as FP64 bits.
+constexpr unsigned long long kDtHugeBits = 0x4415af1d78b58c40ull;
+
+enum { kBcFree = -1, kBcHold = -2 };
+enum { kBckFixed = 0, kBckRamp = 1, kBckSine = 2, kBckRot = 3 };
+enum { kErrInverted = 1, kErrDt = 2, kErrIndex = 4 };
+
+template <class Real>
+struct ElemArgs {
+  // patches
+  const int *patch_elem_off;  // [P+1] (element index in group order)
+  const int *patch_node_off;  // [P+1] (slot index)
+  const int *patch_inst;      // [P]
+  const int *patch_ent_off;   // [P+1] into lent
+  const uint16_t *lptr;       // per patch: n_local+1 offsets (block at patch_node_off[p]+p)
+  const uint16_t *lent;       // local CSR entries: e_local * NC + corner
+  // elements (group order)
+  const uint16_t *lconn;      // this group's [nelem*NC] local node of each corner
+  const int *epid;            // [E] part | (skip-dt << 31)
+  const Real *fib;            // [3][E] unit fibre (material 7) or null
+  // slots
+  const Real *sX;             // [3][S] reference coordinates (patch-relative in mixed mode)
+  const Real *sU;             // [3][S] displacement replicas
+  Real *sF;                   // [3][S] patch-partial internal forces
+  // material state
+  Real *hist;                 // [ncomp][NGP][nelem] of this group
+  const MatP<Real> *mats;
+  // clock
+  Clock *clock;               // [2][ninst]
+  unsigned long long *dtmin;  // [2][ninst] (FP64 bit patterns)
+  int *err;
+  // optional Gauss-point outputs, [gpbase + e*NGP + g]
+  double *gpF;
+  double *gpJ;
+  double *gpS;
+  long long S, E;             // SoA strides
+  int ninst, parity;
+  int patch_begin, npatch, elem_begin, nelem;
+  int use_clock;              // 1: dt and done flags from the clock; 0: dt_direct
+  double dt_direct;
+  long long gpbase;
+};
+
+struct NodeArgs {
+  const int *slot_off;        // [N+1]
+  const int *slots;           // node -> slots
+  const int *node_inst;       // [N] or null (one instance)
+  const int16_t *nbc;         // [3N] per-DOF function (-1 free, -2 hold, >= 0 fn)
+  const uint8_t *nbcflag;     // [N] bit0 any constrained DOF
+  const BcFn *fns;
+  const double *X;            // [3][N] FP64 reference coordinates
+  double *u, *v, *a, *vh;     // [3][N]
+  const double *mass;         // [N] lumped mass (FP64)
+  const double *minv;         // [N] 1 / mass
+  const void *sF;             // [3][S] partial forces (Real)
+  void *sU;                   // [3][S] displacement replicas (Real)
+  Clock *clock;
+  unsigned long long *dtmin;
+  const InstParams *inst;
+  int *err;
+  double *fi_out;             // optional [3][N] assembled internal force
+  long long N, S;
+  int ninst, parity;
+  int mode;                   // kNodeBegin / kNodeFused / kNodeFinish / kNodeInit
+  int fp64;                   // slot arrays are double
+};
+
+enum { kNodeBegin = 0, kNodeFused = 1, kNodeFinish = 2, kNodeInit = 3, kNodeGather = 4,
+       kNodeScatterU = 5 };
+
+}  // namespace ftgpu

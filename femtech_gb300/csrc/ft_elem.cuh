@@ -1,0 +1,531 @@
+// ft_elem.cuh -- element kernels: internal force, stress update, stable-dt
+// contribution and in-block deterministic assembly, one thread block per mesh
+// patch.
+//
+// Reference path replaced (per element, per Gauss point):
+//   CalculateDeformationGradient.cpp:4-30, DeterminateF.cpp:38-57,
+//   StressUpdate.cpp:7-27 + materials/*, InternalForceUpdate.cpp:4-28 with
+//   StrainDisplacementMatrix.cpp:25-77, the element scatter of
+//   GetForce_3D.cpp:39-44, and the per-element part of StableTimeStep.cpp:4-40
+//   (CalculateTimeStep.cpp:7-21, CalculateCharacteristicLength_C3D8/C3D4).
+//
+// GB300 layout: a patch is a spatially compact set of <= 256 elements whose
+// <= 320 distinct nodes are replicated contiguously ("slots"), so the block
+// stages node data with coalesced loads into shared memory, every thread
+// computes one element, corner forces land in shared memory and are summed per
+// local node in a fixed order (local CSR), and one partial force per slot goes
+// back to HBM.  The node kernel adds the (1-8) partials of each node in slot
+// order: no floating-point atomics anywhere, so runs are bitwise reproducible.
+//
+// C3D8 kinematics use the tensor-product structure of the trilinear element:
+// the 8 nodal vectors are Hadamard-transformed once, after which every
+// Jacobian column at a Gauss point costs 3 FMAs, and the B0^T S contraction is
+// accumulated as 7 moment vectors that one inverse transform turns into the 8
+// nodal forces.  Mathematically this is the reference's
+//   F = sum_a x_a (x) dN_a/dX,  f_a = sum_gp w detJ B0_a^T S.
+#pragma once
+
+#include "ft_common.h"
+
+namespace ftgpu {
+
+template <class R> __device__ __forceinline__ R r_inf();
+template <> __device__ __forceinline__ float r_inf<float>() { return __int_as_float(0x7f800000); }
+template <> __device__ __forceinline__ double r_inf<double>() {
+  return __longlong_as_double(0x7ff0000000000000ll);
+}
+
+// Hadamard transform of the 8 corner vectors of a C3D8 (node signs of
+// ShapeFunction_C3D8.cpp:26-33), scaled by 1/8:
+// h = [xi, eta, zeta, xi.eta, xi.zeta, eta.zeta, xi.eta.zeta]
+template <class R>
+__device__ __forceinline__ void hex_hadamard(const R (&x)[8][3], R (&h)[7][3]) {
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    R d0 = x[1][d] - x[0][d], d1 = x[2][d] - x[3][d], d2 = x[5][d] - x[4][d], d3 = x[6][d] - x[7][d];
+    R s0 = x[1][d] + x[0][d], s1 = x[2][d] + x[3][d], s2 = x[5][d] + x[4][d], s3 = x[6][d] + x[7][d];
+    const R q = R(0.125);
+    h[0][d] = q * ((d0 + d1) + (d2 + d3));
+    h[3][d] = q * ((d1 - d0) + (d3 - d2));
+    h[4][d] = q * ((d2 + d3) - (d0 + d1));
+    h[6][d] = q * ((d0 - d1) + (d3 - d2));
+    h[1][d] = q * ((s1 - s0) + (s3 - s2));
+    h[2][d] = q * ((s2 + s3) - (s0 + s1));
+    h[5][d] = q * ((s0 - s1) + (s3 - s2));
+  }
+}
+
+template <class R>
+__device__ __forceinline__ void adj3(const R (&A)[3][3], R (&J)[3][3], R &det) {
+  J[0][0] = A[1][1] * A[2][2] - A[1][2] * A[2][1];
+  J[0][1] = A[0][2] * A[2][1] - A[0][1] * A[2][2];
+  J[0][2] = A[0][1] * A[1][2] - A[0][2] * A[1][1];
+  J[1][0] = A[1][2] * A[2][0] - A[1][0] * A[2][2];
+  J[1][1] = A[0][0] * A[2][2] - A[0][2] * A[2][0];
+  J[1][2] = A[0][2] * A[1][0] - A[0][0] * A[1][2];
+  J[2][0] = A[1][0] * A[2][1] - A[1][1] * A[2][0];
+  J[2][1] = A[0][1] * A[2][0] - A[0][0] * A[2][1];
+  J[2][2] = A[0][0] * A[1][1] - A[0][1] * A[1][0];
+  det = A[0][0] * J[0][0] + A[0][1] * J[1][0] + A[0][2] * J[2][0];
+}
+
+// Per-Gauss-point material update on the displacement gradient D = F - I.
+// hist points at this element's first history component (stride hs per
+// component, gstride per Gauss point).
+template <class R, int MAT>
+__device__ __forceinline__ Sym6<R> stress_at(const MatP<R> &mp, const R (&D)[3][3], R Jm1,
+                                             const R (&a0)[3], R *hist, long long hs,
+                                             const R (&pc)[4]) {
+  Sym6<R> S;
+  if (MAT == 0) {
+    S = Sym6<R>{0, 0, 0, 0, 0, 0};
+  } else if (MAT == 1) {
+    S = mat_neohookean(mp, D, Jm1);
+  } else if (MAT == 2) {
+    S = mat_svk(mp, D);
+  } else if (MAT == 3) {
+    S = mat_linear(mp, D, Jm1);
+  } else if (MAT == 4) {
+    Sym6<R> Si, Sv;
+    mat_hgo_parts<R, false>(mp, D, Jm1, a0, Si, Sv);
+    S = Sym6<R>{Si.xx + Sv.xx, Si.yy + Sv.yy, Si.zz + Sv.zz, Si.yz + Sv.yz, Si.xz + Sv.xz,
+                Si.xy + Sv.xy};
+  } else if (MAT == 6) {
+    S = mat_ogden(mp, D, Jm1);
+  } else {  // 5 / 7: HGO family + Prony series (HGOIsotropicViscoelastic.cpp:98-159)
+    Sym6<R> Si, Sv;
+    mat_hgo_parts<R, MAT == 7>(mp, D, Jm1, a0, Si, Sv);
+    R sd[6] = {Si.xx, Si.yy, Si.zz, Si.yz, Si.xz, Si.xy};
+    R sv[6] = {Sv.xx, Sv.yy, Sv.zz, Sv.yz, Sv.xz, Sv.xy};
+    constexpr int NT = MAT == 5 ? 2 : 1;
+    R out[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      R s0 = hist[(NT * 6 + c) * hs];
+      R dS = sd[c] - s0;
+      R h1 = pc[0] * hist[c * hs] + pc[1] * dS;
+      hist[c * hs] = h1;
+      R acc = sd[c] + sv[c] + h1;
+      if (NT == 2) {
+        R h2 = pc[2] * hist[(6 + c) * hs] + pc[3] * dS;
+        hist[(6 + c) * hs] = h2;
+        acc += h2;
+      }
+      hist[(NT * 6 + c) * hs] = sd[c];
+      out[c] = acc;
+    }
+    S = Sym6<R>{out[0], out[1], out[2], out[3], out[4], out[5]};
+  }
+  return S;
+}
+
+// Prony constants c1 = exp(-dt/tau), c2 = g (1 - c1) / (dt/tau) per term
+// (HGOIsotropicViscoelastic.cpp:122-131), with 1 - c1 taken as -expm1 so that
+// dt << tau keeps its digits in FP32.
+template <class R, int MAT>
+__device__ __forceinline__ void prony_consts(const MatP<R> &mp, R dt, R (&pc)[4]) {
+  pc[0] = pc[1] = pc[2] = pc[3] = 0;
+  if (MAT == 5 || MAT == 7) {
+    R rt1 = dt / mp.p[6];
+    pc[0] = d_exp(-rt1);
+    pc[1] = mp.p[5] * (-d_expm1(-rt1)) / rt1;
+    if (MAT == 5) {
+      R rt2 = dt / mp.p[8];
+      pc[2] = d_exp(-rt2);
+      pc[3] = mp.p[7] * (-d_expm1(-rt2)) / rt2;
+    }
+  }
+}
+
+template <class R>
+__device__ __forceinline__ R norm3(R x, R y, R z) {
+  return d_sqrt(x * x + y * y + z * z);
+}
+
+// areaHexahedronFace, src/math/Geometry.cpp:29-64 (signed tolerance test kept;
+// the 2x2 quadrature uses (q cD + c1) x (q' cD + c2) = c1 x c2 + q cD x c2 + q' c1 x cD).
+template <class R>
+__device__ __forceinline__ R hex_face_area(const R (&xc)[8][3], int i1, int i2, int i3, int i4) {
+  R cD[3], c1[3], c2[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    R p1 = xc[i1][k], p2 = xc[i2][k], p3 = xc[i3][k], p4 = xc[i4][k];
+    cD[k] = R(0.25) * (p1 - p2 + p3 - p4);
+    c1[k] = R(0.25) * (-p1 + p2 + p3 - p4);
+    c2[k] = R(0.25) * (-p1 - p2 + p3 + p4);
+  }
+  R n0x = c1[1] * c2[2] - c1[2] * c2[1], n0y = c1[2] * c2[0] - c1[0] * c2[2],
+    n0z = c1[0] * c2[1] - c1[1] * c2[0];
+  const R tol = R(1e-6);
+  if (cD[0] < tol && cD[1] < tol && cD[2] < tol) return 4 * norm3(n0x, n0y, n0z);
+  R n1x = cD[1] * c2[2] - cD[2] * c2[1], n1y = cD[2] * c2[0] - cD[0] * c2[2],
+    n1z = cD[0] * c2[1] - cD[1] * c2[0];
+  R n2x = c1[1] * cD[2] - c1[2] * cD[1], n2y = c1[2] * cD[0] - c1[0] * cD[2],
+    n2z = c1[0] * cD[1] - c1[1] * cD[0];
+  const R t = R(0.57735026918962576451);
+  R area = 0;
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      R qj = j ? t : -t, qi = i ? t : -t;
+      area += norm3(n0x + qj * n1x + qi * n2x, n0y + qj * n1y + qi * n2y,
+                    n0z + qj * n1z + qi * n2z);
+    }
+  return area;
+}
+
+template <class R, int MAT, bool GP>
+__device__ __forceinline__ void hex_element(const R (&x)[8][3], const R (&u)[8][3],
+                                            const MatP<R> &mp, const R (&pc)[4],
+                                            const R (&a0)[3], R *hist, long long hs,
+                                            long long gs, bool dt_only, R (&f)[8][3], R &le,
+                                            int &bad, const ElemArgs<R> &A, long long gpo) {
+  R hu[7][3];
+  R vol = 0;
+  R m[7][3];
+#pragma unroll
+  for (int i = 0; i < 7; ++i) m[i][0] = m[i][1] = m[i][2] = 0;
+  if (!dt_only) {
+    R hx[7][3];
+    hex_hadamard(x, hx);
+    hex_hadamard(u, hu);
+    // Gauss point order of GaussQuadrature3D.cpp:17-58, literal as there
+    constexpr int sg[8][3] = {{-1, -1, 1}, {1, -1, 1}, {1, 1, 1}, {-1, 1, 1},
+                              {-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1}};
+    const R G = R(0.577350269189626);
+#pragma unroll
+    for (int g = 0; g < 8; ++g) {
+      const R xi = sg[g][0] * G, et = sg[g][1] * G, ze = sg[g][2] * G;
+      const R ez = et * ze, xz = xi * ze, xe = xi * et;
+      R Am[3][3], H[3][3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        Am[0][d] = hx[0][d] + et * hx[3][d] + ze * hx[4][d] + ez * hx[6][d];
+        Am[1][d] = hx[1][d] + xi * hx[3][d] + ze * hx[5][d] + xz * hx[6][d];
+        Am[2][d] = hx[2][d] + xi * hx[4][d] + et * hx[5][d] + xe * hx[6][d];
+        H[d][0] = hu[0][d] + et * hu[3][d] + ze * hu[4][d] + ez * hu[6][d];
+        H[d][1] = hu[1][d] + xi * hu[3][d] + ze * hu[5][d] + xz * hu[6][d];
+        H[d][2] = hu[2][d] + xi * hu[4][d] + et * hu[5][d] + xe * hu[6][d];
+      }
+      R Ad[3][3], detA;
+      adj3(Am, Ad, detA);
+      const R idet = 1 / detA;
+      R D[3][3];  // D = H A^{-T} = H adj(A)^T / det A
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+          D[i][j] = idet * (H[i][0] * Ad[j][0] + H[i][1] * Ad[j][1] + H[i][2] * Ad[j][2]);
+      const R Jm1 = jm1_of(D);
+      if (!(Jm1 > R(-1)) || !(detA != 0)) bad = 1;
+      vol += (1 + Jm1) * detA;
+      Sym6<R> S = stress_at<R, MAT>(mp, D, Jm1, a0, hist + g * gs, hs, pc);
+      if (GP) {
+        long long q = gpo + g;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) A.gpF[9 * q + i + 3 * j] = double((i == j ? R(1) : R(0)) + D[i][j]);
+        A.gpJ[q] = double(1 + Jm1);
+        A.gpS[6 * q + 0] = S.xx;
+        A.gpS[6 * q + 1] = S.yy;
+        A.gpS[6 * q + 2] = S.zz;
+        A.gpS[6 * q + 3] = S.yz;
+        A.gpS[6 * q + 4] = S.xz;
+        A.gpS[6 * q + 5] = S.xy;
+      }
+      // P = F S = S + D S ; Gm = P adj(A)  (w = 1; det A cancels A^{-1})
+      const R s[3][3] = {{S.xx, S.xy, S.xz}, {S.xy, S.yy, S.yz}, {S.xz, S.yz, S.zz}};
+      R P[3][3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+          P[i][j] = s[i][j] + D[i][0] * s[0][j] + D[i][1] * s[1][j] + D[i][2] * s[2][j];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        R g0 = P[i][0] * Ad[0][0] + P[i][1] * Ad[1][0] + P[i][2] * Ad[2][0];
+        R g1 = P[i][0] * Ad[0][1] + P[i][1] * Ad[1][1] + P[i][2] * Ad[2][1];
+        R g2 = P[i][0] * Ad[0][2] + P[i][1] * Ad[1][2] + P[i][2] * Ad[2][2];
+        m[0][i] += g0;
+        m[1][i] += g1;
+        m[2][i] += g2;
+        m[3][i] += et * g0 + xi * g1;
+        m[4][i] += ze * g0 + xi * g2;
+        m[5][i] += ze * g1 + et * g2;
+        m[6][i] += ez * g0 + xz * g1 + xe * g2;
+      }
+    }
+    // inverse transform: f_a = 1/8 sum_k sign_k(a) m_k
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const R q = R(0.125);
+      R t1 = m[0][i] + m[6][i], t2 = m[0][i] - m[6][i], t3 = m[3][i] + m[4][i],
+        t4 = m[3][i] - m[4][i];
+      R Pmm = t1 - t3, Ppp = t1 + t3, Ppm = t2 + t4, Pmp = t2 - t4;
+      R r1 = m[1][i] + m[2][i], r2 = m[1][i] - m[2][i];
+      R Qmm = m[5][i] - r1, Qpp = m[5][i] + r1, Qpm = r2 - m[5][i], Qmp = -r2 - m[5][i];
+      f[0][i] = q * (Qmm - Pmm);
+      f[1][i] = q * (Qmm + Pmm);
+      f[2][i] = q * (Qpm + Ppm);
+      f[3][i] = q * (Qpm - Ppm);
+      f[4][i] = q * (Qmp - Pmp);
+      f[5][i] = q * (Qmp + Pmp);
+      f[6][i] = q * (Qpp + Ppp);
+      f[7][i] = q * (Qpp - Ppp);
+    }
+  }
+  // characteristic length on the current geometry: volume / max face area
+  // (CalculateCharacteristicLength_C3D8.cpp:6-29); the 2x2x2 Gauss sum of
+  // det(dx/dxi) is the exact volume of the trilinear hexahedron.
+  R xc[8][3];
+#pragma unroll
+  for (int a = 0; a < 8; ++a)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) xc[a][d] = x[a][d] + u[a][d];
+  if (dt_only) {
+    R hc[7][3];
+    hex_hadamard(xc, hc);
+    constexpr int sg[8][3] = {{-1, -1, 1}, {1, -1, 1}, {1, 1, 1}, {-1, 1, 1},
+                              {-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1}};
+    const R G = R(0.577350269189626);
+#pragma unroll
+    for (int g = 0; g < 8; ++g) {
+      const R xi = sg[g][0] * G, et = sg[g][1] * G, ze = sg[g][2] * G;
+      R Am[3][3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        Am[0][d] = hc[0][d] + et * hc[3][d] + ze * hc[4][d] + et * ze * hc[6][d];
+        Am[1][d] = hc[1][d] + xi * hc[3][d] + ze * hc[5][d] + xi * ze * hc[6][d];
+        Am[2][d] = hc[2][d] + xi * hc[4][d] + et * hc[5][d] + xi * et * hc[6][d];
+      }
+      R Ad[3][3], det;
+      adj3(Am, Ad, det);
+      vol += det;
+    }
+  }
+  R amax = hex_face_area(xc, 0, 1, 2, 3);
+  amax = fmax(amax, hex_face_area(xc, 4, 5, 6, 7));
+  amax = fmax(amax, hex_face_area(xc, 0, 3, 7, 4));
+  amax = fmax(amax, hex_face_area(xc, 1, 2, 6, 5));
+  amax = fmax(amax, hex_face_area(xc, 0, 1, 5, 4));
+  amax = fmax(amax, hex_face_area(xc, 3, 2, 6, 7));
+  le = vol / amax;
+}
+
+// C3D4: one Gauss point at (1/4,1/4,1/4), weight 1/6, |det J|
+// (ShapeFunction_C3D4.cpp:59-73, GaussQuadrature3D.cpp:60-69).
+template <class R, int MAT, bool GP>
+__device__ __forceinline__ void tet_element(const R (&x)[4][3], const R (&u)[4][3],
+                                            const MatP<R> &mp, const R (&pc)[4],
+                                            const R (&a0)[3], R *hist, long long hs,
+                                            bool dt_only, R (&f)[4][3], R &le, int &bad,
+                                            const ElemArgs<R> &A, long long gpo) {
+  R Am[3][3], H[3][3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      Am[r][d] = x[r][d] - x[3][d];
+      H[d][r] = u[r][d] - u[3][d];
+    }
+  R Ad[3][3], detA;
+  adj3(Am, Ad, detA);
+  const R idet = 1 / detA;
+  R D[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      D[i][j] = idet * (H[i][0] * Ad[j][0] + H[i][1] * Ad[j][1] + H[i][2] * Ad[j][2]);
+  const R Jm1 = jm1_of(D);
+  if (!(Jm1 > R(-1)) || !(detA != 0)) bad = 1;
+  if (!dt_only) {
+    Sym6<R> S = stress_at<R, MAT>(mp, D, Jm1, a0, hist, hs, pc);
+    if (GP) {
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) A.gpF[9 * gpo + i + 3 * j] = double((i == j ? R(1) : R(0)) + D[i][j]);
+      A.gpJ[gpo] = double(1 + Jm1);
+      A.gpS[6 * gpo + 0] = S.xx;
+      A.gpS[6 * gpo + 1] = S.yy;
+      A.gpS[6 * gpo + 2] = S.zz;
+      A.gpS[6 * gpo + 3] = S.yz;
+      A.gpS[6 * gpo + 4] = S.xz;
+      A.gpS[6 * gpo + 5] = S.xy;
+    }
+    const R s[3][3] = {{S.xx, S.xy, S.xz}, {S.xy, S.yy, S.yz}, {S.xz, S.yz, S.zz}};
+    R P[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        P[i][j] = s[i][j] + D[i][0] * s[0][j] + D[i][1] * s[1][j] + D[i][2] * s[2][j];
+    // G = (|det A| / 6) P A^{-1} = sign(det A)/6 * P adj(A)
+    const R w = (detA >= 0 ? R(1) : R(-1)) * R(1.0 / 6.0);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      R g0 = w * (P[i][0] * Ad[0][0] + P[i][1] * Ad[1][0] + P[i][2] * Ad[2][0]);
+      R g1 = w * (P[i][0] * Ad[0][1] + P[i][1] * Ad[1][1] + P[i][2] * Ad[2][1]);
+      R g2 = w * (P[i][0] * Ad[0][2] + P[i][1] * Ad[1][2] + P[i][2] * Ad[2][2]);
+      f[0][i] = g0;
+      f[1][i] = g1;
+      f[2][i] = g2;
+      f[3][i] = -(g0 + g1 + g2);
+    }
+  }
+  // min altitude (CalculateCharacteristicLength_C3D4.cpp:5-46): 6V / max |n_face|
+  R xc[4][3];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) xc[a][d] = x[a][d] + u[a][d];
+  R six_v = fabs((1 + Jm1) * detA);
+  constexpr int fc[4][3] = {{1, 2, 3}, {2, 3, 0}, {3, 0, 1}, {0, 1, 2}};
+  R nmax = 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int p1 = fc[k][0], p2 = fc[k][1], p3 = fc[k][2];
+    R v1x = xc[p2][0] - xc[p1][0], v1y = xc[p2][1] - xc[p1][1], v1z = xc[p2][2] - xc[p1][2];
+    R v2x = xc[p3][0] - xc[p1][0], v2y = xc[p3][1] - xc[p1][1], v2z = xc[p3][2] - xc[p1][2];
+    R n = norm3(v1y * v2z - v1z * v2y, v1z * v2x - v1x * v2z, v1x * v2y - v1y * v2x);
+    nmax = fmax(nmax, n);
+  }
+  le = six_v / nmax;
+}
+
+template <class R>
+__device__ __forceinline__ double dt_of(R le, const MatP<R> &mp);
+template <>
+__device__ __forceinline__ double dt_of<float>(float le, const MatP<float> &mp) {
+  return double(le * mp.inv_ce);
+}
+template <>
+__device__ __forceinline__ double dt_of<double>(double le, const MatP<double> &mp) {
+  return le / mp.ce;  // CalculateTimeStep.cpp:19
+}
+
+template <class R, int ET, int MAT, bool GP>
+__global__ void __launch_bounds__(kElemThreads) k_elem(const ElemArgs<R> A, int dt_only) {
+  constexpr int NC = ET == 0 ? 8 : 4;
+  constexpr int NGP = ET == 0 ? 8 : 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  R *shX = reinterpret_cast<R *>(smem_raw);
+  R *shU = shX + 3 * kMaxLocalNodes;
+  R *shF = shU + 3 * kMaxLocalNodes;  // [NC*3][blockDim]
+  const int PE = blockDim.x;
+  const int t = threadIdx.x;
+  const int p = A.patch_begin + blockIdx.x;
+  const int inst = A.patch_inst[p];
+  const Clock *ck = A.clock + A.parity * A.ninst + inst;
+  if (A.use_clock && ck->done) return;
+  const R dt = A.use_clock ? R(ck->dt) : R(A.dt_direct);
+  const int e0 = A.patch_elem_off[p], ne = A.patch_elem_off[p + 1] - e0;
+  const int s0 = A.patch_node_off[p], ns = A.patch_node_off[p + 1] - s0;
+  for (int i = t; i < ns; i += PE) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      shX[d * kMaxLocalNodes + i] = A.sX[d * A.S + s0 + i];
+      shU[d * kMaxLocalNodes + i] = A.sU[d * A.S + s0 + i];
+    }
+  }
+  __syncthreads();
+  double dte = r_inf<double>();
+  int bad = 0;
+  if (t < ne) {
+    const int e = e0 + t;
+    int lc[NC];
+    if (NC == 8) {
+      uint4 v = *reinterpret_cast<const uint4 *>(A.lconn + 8ll * (e - A.elem_begin));
+      lc[0] = v.x & 0xffff; lc[1] = v.x >> 16; lc[2] = v.y & 0xffff; lc[3] = v.y >> 16;
+      lc[4] = v.z & 0xffff; lc[5] = v.z >> 16; lc[6] = v.w & 0xffff; lc[7] = v.w >> 16;
+    } else {
+      uint2 v = *reinterpret_cast<const uint2 *>(A.lconn + 4ll * (e - A.elem_begin));
+      lc[0] = v.x & 0xffff; lc[1] = v.x >> 16; lc[2] = v.y & 0xffff; lc[3] = v.y >> 16;
+    }
+    R x[NC][3], u[NC][3];
+#pragma unroll
+    for (int a = 0; a < NC; ++a) {
+      int l = lc[a] < ns ? lc[a] : 0;
+      if (lc[a] >= ns) bad |= 2;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        x[a][d] = shX[d * kMaxLocalNodes + l];
+        u[a][d] = shU[d * kMaxLocalNodes + l];
+      }
+    }
+    const int pw = A.epid[e];
+    const bool skip = pw < 0;
+    const MatP<R> mp = A.mats[pw & 0x7fffffff];
+    R a0[3] = {R(1), R(0), R(0)};
+    if (MAT == 7) {
+      a0[0] = A.fib[e];
+      a0[1] = A.fib[A.E + e];
+      a0[2] = A.fib[2 * A.E + e];
+    }
+    R pc[4];
+    prony_consts<R, MAT>(mp, dt, pc);
+    const long long el = e - A.elem_begin;
+    R *hist = A.hist ? A.hist + el : nullptr;
+    const long long gs = A.nelem, hs = (long long)NGP * A.nelem;
+    R f[NC][3];
+    R le;
+    const long long gpo = A.gpbase + el * NGP;
+    if (ET == 0)
+      hex_element<R, MAT, GP>(reinterpret_cast<const R(&)[8][3]>(x),
+                              reinterpret_cast<const R(&)[8][3]>(u), mp, pc, a0, hist, hs, gs,
+                              dt_only != 0, reinterpret_cast<R(&)[8][3]>(f), le, bad, A, gpo);
+    else
+      tet_element<R, MAT, GP>(reinterpret_cast<const R(&)[4][3]>(x),
+                              reinterpret_cast<const R(&)[4][3]>(u), mp, pc, a0, hist, hs,
+                              dt_only != 0, reinterpret_cast<R(&)[4][3]>(f), le, bad, A, gpo);
+    if (!dt_only) {
+#pragma unroll
+      for (int a = 0; a < NC; ++a)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) shF[(a * 3 + d) * PE + t] = f[a][d];
+    }
+    if (!skip) dte = dt_of<R>(le, mp);
+  }
+  if (bad) atomicOr(A.err, (bad & 1 ? kErrInverted : 0) | (bad & 2 ? kErrIndex : 0));
+  // block minimum of the element time steps -> one FP64 atomicMin per block
+  // (positive doubles order like their bit patterns)
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) dte = fmin(dte, __shfl_xor_sync(0xffffffffu, dte, o));
+  __shared__ double wmin[kElemThreads / 32];
+  if ((t & 31) == 0) wmin[t >> 5] = dte;
+  __syncthreads();
+  if (t == 0) {
+    double mn = wmin[0];
+    for (int w = 1; w < (PE + 31) / 32; ++w) mn = fmin(mn, wmin[w]);
+    atomicMin(A.dtmin + A.parity * A.ninst + inst, (unsigned long long)__double_as_longlong(mn));
+  }
+  if (dt_only) return;
+  // in-block assembly: local node i sums its corners in (element, corner) order
+  const uint16_t *lp = A.lptr + s0 + p;
+  const uint16_t *le = A.lent + A.patch_ent_off[p];
+  for (int i = t; i < ns; i += PE) {
+    const int b = lp[i], en = lp[i + 1];
+    R f0 = 0, f1 = 0, f2 = 0;
+    for (int k = b; k < en; ++k) {
+      const int ent = le[k];
+      const int el = ent / NC, a = ent - el * NC;
+      f0 += shF[(a * 3 + 0) * PE + el];
+      f1 += shF[(a * 3 + 1) * PE + el];
+      f2 += shF[(a * 3 + 2) * PE + el];
+    }
+    A.sF[s0 + i] = f0;
+    A.sF[A.S + s0 + i] = f1;
+    A.sF[2 * A.S + s0 + i] = f2;
+  }
+}
+
+template <class R>
+size_t elem_smem_bytes(int ET, int PE) {
+  const int NC = ET == 0 ? 8 : 4;
+  return sizeof(R) * (6 * (size_t)kMaxLocalNodes + (size_t)NC * 3 * PE);
+}
+
+}  // namespace ftgpu

@@ -1,0 +1,41 @@
+// ft_launch.h -- host launchers of the element kernels (one translation unit per precision).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "ft_common.h"
+
+namespace ftgpu {
+
+// Launch the element kernel of (etype, material) over `nblocks` patches.
+// gp = 1 records per-Gauss-point F/detF/PK2; dt_only = 1 computes only the
+// stable-time-step contribution.  Returns a cudaError_t value.
+int launch_elem_f32(int etype, int mat, int gp, int nblocks, int threads, size_t smem,
+                    cudaStream_t s, const ElemArgs<float> &A, int dt_only);
+int launch_elem_f64(int etype, int mat, int gp, int nblocks, int threads, size_t smem,
+                    cudaStream_t s, const ElemArgs<double> &A, int dt_only);
+
+// Dynamic shared memory of one element block: node X and u for
+// kMaxLocalNodes slots plus NC*3 corner forces per element.
+template <class R>
+inline size_t elem_smem_bytes_host(int etype, int PE) {
+  const int NC = etype == 0 ? 8 : 4;
+  return sizeof(R) * (6 * (size_t)kMaxLocalNodes + (size_t)NC * 3 * PE);
+}
+
+template <class R>
+inline int launch_elem(int etype, int mat, int gp, int nblocks, int threads, size_t smem,
+                       cudaStream_t s, const ElemArgs<R> &A, int dt_only);
+template <>
+inline int launch_elem<float>(int etype, int mat, int gp, int nblocks, int threads, size_t smem,
+                              cudaStream_t s, const ElemArgs<float> &A, int dt_only) {
+  return launch_elem_f32(etype, mat, gp, nblocks, threads, smem, s, A, dt_only);
+}
+template <>
+inline int launch_elem<double>(int etype, int mat, int gp, int nblocks, int threads,
+                               size_t smem, cudaStream_t s, const ElemArgs<double> &A,
+                               int dt_only) {
+  return launch_elem_f64(etype, mat, gp, nblocks, threads, smem, s, A, dt_only);
+}
+
+}  // namespace ftgpu

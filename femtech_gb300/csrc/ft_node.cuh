@@ -1,0 +1,228 @@
+// ft_node.cuh -- nodal kernels: deterministic force gather fused with the
+// central-difference update, boundary conditions and the clock advance.
+//
+// Reference path replaced, per step (examples/ex9/ex9.cpp:107-175):
+//   f_net = fe - fi (GetForce_3D.cpp:49-51), a = f_net / m for free DOFs
+//   (CalculateAcclerations.cpp:7-11), v = v_half + (t_{n+1} - t_half) a,
+//   then -- once the stable dt of the new geometry is known -- the next
+//   step's v_half = v + (t_half' - t_{n+1}) a, u += dt v_half and the driver's
+//   ApplyBoundaryConditions at the new time, and Time/dt bookkeeping.
+// Nodal state is FP64 SoA [3][N]; the per-slot partial forces are summed in
+// slot order, so the result does not depend on scheduling.
+#pragma once
+
+#include "ft_common.h"
+
+namespace ftgpu {
+
+__device__ __forceinline__ void rot_angle(const double *p, double t, double &th, double &om) {
+  const double a0 = p[6], T = p[7], pi = 3.14159265358979323846;
+  if (t <= T) {
+    om = a0 * T / pi * (1.0 - cos(pi * t / T));
+    th = a0 * T / pi * (t - T / pi * sin(pi * t / T));
+  } else {
+    const double wT = 2.0 * a0 * T / pi, thT = a0 * T * T / pi;
+    om = wT;
+    th = thT + wT * (t - T);
+  }
+}
+
+// Prescribed displacement / velocity of DOF d of node n at time t.  Only the
+// rigid rotation reads the node's reference position (SoA X, stride N).
+__device__ __forceinline__ void bc_value(const BcFn &b, int d, double t, const double *X,
+                                         long long N, long long n, double &u, double &v) {
+  switch (b.kind) {
+    case kBckFixed: u = b.p[0]; v = 0.0; break;
+    case kBckRamp: u = t * b.p[0]; v = b.p[0]; break;
+    case kBckSine: u = b.p[0] * sin(b.p[1] * t); v = b.p[0] * b.p[1] * cos(b.p[1] * t); break;
+    default: {  // rigid rotation about a fixed axis
+      double th, om;
+      rot_angle(b.p, t, th, om);
+      const double k0 = b.p[0], k1 = b.p[1], k2 = b.p[2];
+      const double r0 = X[n] - b.p[3], r1 = X[N + n] - b.p[4], r2 = X[2 * N + n] - b.p[5];
+      const double c = cos(th), s = sin(th), kr = k0 * r0 + k1 * r1 + k2 * r2;
+      const double R0 = r0 * c + (k1 * r2 - k2 * r1) * s + k0 * kr * (1.0 - c);
+      const double R1 = r1 * c + (k2 * r0 - k0 * r2) * s + k1 * kr * (1.0 - c);
+      const double R2 = r2 * c + (k0 * r1 - k1 * r0) * s + k2 * kr * (1.0 - c);
+      const double w0 = om * (k1 * R2 - k2 * R1), w1 = om * (k2 * R0 - k0 * R2),
+                   w2 = om * (k0 * R1 - k1 * R0);
+      u = d == 0 ? R0 - r0 : (d == 1 ? R1 - r1 : R2 - r2);
+      v = d == 0 ? w0 : (d == 1 ? w1 : w2);
+    }
+  }
+}
+
+template <class R>
+__global__ void __launch_bounds__(256) k_node(const NodeArgs A) {
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= A.N) return;
+  const int inst = A.node_inst ? A.node_inst[n] : 0;
+  const InstParams &ip = A.inst[inst];
+  const bool leader = (n == ip.node_begin);
+  const R *sF = reinterpret_cast<const R *>(A.sF);
+  R *sU = reinterpret_cast<R *>(A.sU);
+  const int sb = A.slot_off[n], se = A.slot_off[n + 1];
+  const long long N = A.N, S = A.S;
+
+  if (A.mode == kNodeScatterU) {  // replicate u into the patch slots
+    for (int k = sb; k < se; ++k) {
+      const int s = A.slots[k];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) sU[d * S + s] = R(A.u[d * N + n]);
+    }
+    return;
+  }
+  if (A.mode == kNodeGather) {  // assembled internal force fi = sum of partials
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      double f = 0.0;
+      for (int k = sb; k < se; ++k) f += double(sF[d * S + A.slots[k]]);
+      A.fi_out[d * N + n] = f;
+    }
+    return;
+  }
+
+  const Clock ck = A.clock[A.parity * A.ninst + inst];
+  if (A.mode == kNodeBegin) {
+    // first half of a step: v_half, u update, BCs at t_{n+1} (ex9.cpp:109-138)
+    if (ck.done) return;
+    const double t_n = ck.time, dt = ck.dt, t_np1 = t_n + dt, t_half = 0.5 * (t_np1 + t_n);
+    double un[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const int fn = A.nbc[d * N + n];
+      double u = A.u[d * N + n];
+      if (fn == kBcFree) {
+        const double vh = A.v[d * N + n] + (t_half - t_n) * A.a[d * N + n];
+        u = u + dt * vh;
+        A.vh[d * N + n] = vh;
+        A.u[d * N + n] = u;
+      } else if (fn >= 0) {
+        double vb;
+        bc_value(A.fns[fn], d, t_np1, A.X, N, n, u, vb);
+        A.u[d * N + n] = u;
+        A.v[d * N + n] = vb;
+        A.a[d * N + n] = 0.0;
+      }
+      un[d] = u;
+    }
+    for (int k = sb; k < se; ++k) {
+      const int s = A.slots[k];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) sU[d * S + s] = R(un[d]);
+    }
+    return;
+  }
+  if (A.mode == kNodeInit) {
+    // accelerations after the pre-loop GetForce (ex9.cpp:90-93)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      if (A.nbc[d * N + n] != kBcFree) continue;
+      double f = 0.0;
+      for (int k = sb; k < se; ++k) f += double(sF[d * S + A.slots[k]]);
+      A.a[d * N + n] = A.fp64 ? -f / A.mass[n] : -f * A.minv[n];
+    }
+    if (leader) A.dtmin[A.parity * A.ninst + inst] = kDtHugeBits;
+    return;
+  }
+
+  // kNodeFused / kNodeFinish: end of step n (+ start of step n+1 when fused)
+  Clock *nxt = A.clock + (A.parity ^ 1) * A.ninst + inst;
+  if (ck.done) {
+    if (leader) *nxt = ck;
+    return;
+  }
+  const double t_n = ck.time, dt = ck.dt, t_np1 = t_n + dt, t_half = 0.5 * (t_np1 + t_n);
+  const double raw = __longlong_as_double((long long)A.dtmin[A.parity * A.ninst + inst]);
+  const double ndt = ip.reduction * raw;
+  int done = 0;
+  if (!(t_np1 < ip.tmax)) done |= 1;
+  if (ck.step + 1 >= ip.step_limit) done |= 2;
+  if (raw < ip.failure_dt) done |= 4;
+  const bool advance = (A.mode == kNodeFused) && !done;
+  const double t_np2 = t_np1 + ndt, t_half2 = 0.5 * (t_np2 + t_np1);
+  double un[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const int fn = A.nbc[d * N + n];
+    double u = A.u[d * N + n];
+    if (fn == kBcFree) {
+      double f = 0.0;
+      for (int k = sb; k < se; ++k) f += double(sF[d * S + A.slots[k]]);
+      const double acc = A.fp64 ? -f / A.mass[n] : -f * A.minv[n];
+      const double vel = A.vh[d * N + n] + (t_np1 - t_half) * acc;
+      if (advance) {
+        const double vh2 = vel + (t_half2 - t_np1) * acc;
+        u = u + ndt * vh2;
+        A.vh[d * N + n] = vh2;
+        A.u[d * N + n] = u;
+      } else {
+        A.v[d * N + n] = vel;
+        A.a[d * N + n] = acc;
+      }
+    } else if (fn >= 0 && advance) {
+      double vb;
+      bc_value(A.fns[fn], d, t_np2, A.X, N, n, u, vb);
+      A.u[d * N + n] = u;
+      A.v[d * N + n] = vb;
+      A.a[d * N + n] = 0.0;
+    }
+    un[d] = u;
+  }
+  if (advance) {
+    for (int k = sb; k < se; ++k) {
+      const int s = A.slots[k];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) sU[d * S + s] = R(un[d]);
+    }
+  }
+  if (leader) {
+    Clock c;
+    c.time = t_np1;
+    c.dt = ndt;
+    c.step = ck.step + 1;
+    c.done = done;
+    c.err = (done & 4) ? kErrDt : 0;
+    *nxt = c;
+    A.dtmin[(A.parity ^ 1) * A.ninst + inst] = kDtHugeBits;
+  }
+}
+
+// Pre-loop clock: dt = reduction * StableTimeStep() at t0 (ex9.cpp:87).
+__global__ void k_clock_init(Clock *clock, unsigned long long *dtmin, const InstParams *ip,
+                             int ninst, double t0) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ninst) return;
+  const double raw = __longlong_as_double((long long)dtmin[i]);
+  Clock c;
+  c.time = t0;
+  c.dt = ip[i].reduction * raw;
+  c.step = 0;
+  c.done = 0;
+  if (raw < ip[i].failure_dt) c.done |= 4;
+  if (!(t0 < ip[i].tmax)) c.done |= 1;
+  c.err = (c.done & 4) ? kErrDt : 0;
+  clock[i] = c;
+  clock[ninst + i] = c;
+  dtmin[i] = kDtHugeBits;
+  dtmin[ninst + i] = kDtHugeBits;
+}
+
+// Apply the boundary functions at time t (pre-loop BC call, ex9.cpp:84).
+__global__ void k_apply_bc(const NodeArgs A, double t) {
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= A.N) return;
+  const long long N = A.N;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const int fn = A.nbc[d * N + n];
+    if (fn < 0) continue;
+    double u, v;
+    bc_value(A.fns[fn], d, t, A.X, N, n, u, v);
+    A.u[d * N + n] = u;
+    A.v[d * N + n] = v;
+    A.a[d * N + n] = 0.0;
+  }
+}
+
+}  // namespace ftgpu

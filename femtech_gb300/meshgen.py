@@ -63,37 +63,41 @@ def hex_block(nx, ny, nz, lx, ly, lz, jitter=0.0, seed=0, origin=(0.0, 0.0, 0.0)
 def tet_ellipsoid(a, b, c, h, jitter=0.1, seed=0):
     """C3D4 mesh of the ellipsoid x^2/a^2 + y^2/b^2 + z^2/c^2 <= 1.
 
-    Lattice points of spacing h, jittered by +-jitter*h (seeded), plus points on
-    the surface; Delaunay tetrahedralisation (scipy/qhull); tets whose centroid
-    lies outside, or whose volume is tiny, are dropped.  Node order is made
-    right-handed (positive signed volume).
+    Lattice of spacing h; every lattice cube whose centre lies inside is split
+    into the 6 tetrahedra of its Kuhn (Freudenthal) subdivision -- the
+    Delaunay triangulation of the lattice with a consistent diagonal, so the
+    mesh is conforming and free of slivers -- then all nodes are jittered by
+    +-jitter*h (seeded).  The surface is the resulting staircase.  Node order
+    is made right-handed (positive signed volume).
     """
-    from scipy.spatial import Delaunay
-
     rng = np.random.default_rng(seed)
-    xs = np.arange(-a, a + 1e-12, h)
-    ys = np.arange(-b, b + 1e-12, h)
-    zs = np.arange(-c, c + 1e-12, h)
-    P = np.stack(np.meshgrid(xs, ys, zs, indexing="ij"), -1).reshape(-1, 3)
-    P = P + rng.uniform(-jitter, jitter, P.shape) * h
-    r = (P[:, 0] / a) ** 2 + (P[:, 1] / b) ** 2 + (P[:, 2] / c) ** 2
-    P = P[r < (1.0 - 0.5 * h / min(a, b, c)) ** 2]
-    # surface points: Fibonacci sphere mapped onto the ellipsoid, density ~ 1/h^2
-    area = 4.0 * np.pi * ((a * b) ** 1.6 + (a * c) ** 1.6 + (b * c) ** 1.6) ** (1 / 1.6) / 3 ** (1 / 1.6)
-    ns = int(area / (h * h) * 1.15)
-    idx = np.arange(ns) + 0.5
-    phi = np.arccos(1 - 2 * idx / ns)
-    th = np.pi * (1 + 5 ** 0.5) * idx
-    S = np.stack([a * np.cos(th) * np.sin(phi), b * np.sin(th) * np.sin(phi), c * np.cos(phi)], -1)
-    X = np.concatenate([P, S], 0)
-    tri = Delaunay(X)
-    T = tri.simplices.astype(np.int64)
-    cen = X[T].mean(1)
-    inside = (cen[:, 0] / a) ** 2 + (cen[:, 1] / b) ** 2 + (cen[:, 2] / c) ** 2 < 1.0
-    v = np.einsum("ij,ij->i", np.cross(X[T[:, 1]] - X[T[:, 3]], X[T[:, 2]] - X[T[:, 3]]),
-                  X[T[:, 0]] - X[T[:, 3]]) / 6.0
-    keep = inside & (np.abs(v) > 1e-3 * h ** 3)
-    T, v = T[keep], v[keep]
+    nx, ny, nz = (int(np.ceil(2 * s / h)) + 1 for s in (a, b, c))
+    o = np.array([-a, -b, -c]) - 0.5 * (np.array([nx, ny, nz]) * h - 2 * np.array([a, b, c]))
+    ci, cj, ck = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    cen = o + (np.stack([ci, cj, ck], -1).reshape(-1, 3) + 0.5) * h
+    ins = (cen[:, 0] / a) ** 2 + (cen[:, 1] / b) ** 2 + (cen[:, 2] / c) ** 2 < 1.0
+    cubes = np.stack([ci.ravel(), cj.ravel(), ck.ravel()], -1)[ins]
+
+    def nid(i, j, k):
+        return i + (nx + 1) * (j + (ny + 1) * k)
+
+    perms = [(0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0)]
+    tets = []
+    for p in perms:
+        path = [np.zeros(3, np.int64)]
+        for ax in p:
+            step = path[-1].copy()
+            step[ax] += 1
+            path.append(step)
+        tets.append(np.stack([nid(cubes[:, 0] + q[0], cubes[:, 1] + q[1], cubes[:, 2] + q[2])
+                              for q in path], -1))
+    T = np.concatenate(tets, 0)
+    gi, gj, gk = np.meshgrid(np.arange(nx + 1), np.arange(ny + 1), np.arange(nz + 1), indexing="ij")
+    X = o + np.stack([gi.transpose(2, 1, 0).ravel(), gj.transpose(2, 1, 0).ravel(),
+                      gk.transpose(2, 1, 0).ravel()], -1) * h
+    X = X + rng.uniform(-jitter, jitter, X.shape) * h
+    v = np.einsum("ij,ij->i", np.cross(X[T[:, 0]] - X[T[:, 3]], X[T[:, 1]] - X[T[:, 3]]),
+                  X[T[:, 2]] - X[T[:, 3]])
     neg = v < 0
     T[neg, 0], T[neg, 1] = T[neg, 1].copy(), T[neg, 0].copy()
     used = np.unique(T)

@@ -1,0 +1,175 @@
+/*
+ * ftgpu.h -- C ABI of the GB300 (sm_103a) explicit-dynamics engine.
+ *
+ * The engine replaces FemTech's per-step hot path: the internal force of every
+ * element (GetForce / GetForce_3D with CalculateDeformationGradient,
+ * DeterminateF, StressUpdate, InternalForceUpdate), the nodal assembly, the
+ * accelerations, the central-difference velocity/displacement update of the
+ * example drivers and the stable-time-step reduction.  Arrays cross the ABI in
+ * the reference's own layout (include/GlobalVariables.h): AoS nodal arrays
+ * indexed [node*3+dim], CSR connectivity eptr/connectivity, per-part
+ * materialID[] and properties[pid*MAXMATPARAMS+k] as filled by ReadMaterials().
+ *
+ * Plain C types only.  Every call returns FTGPU_OK (0) or a negative status;
+ * the library never aborts the process (the reference calls
+ * TerminateFemTech(code) -> MPI_Abort; callers map the negative codes back).
+ * One model is driven from one host thread (the reference is non-reentrant
+ * too: its scratch arrays mat1..mat4, B and fintGQ are globals).
+ */
+#ifndef FTGPU_H
+#define FTGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (mirroring TerminateFemTech's codes where one exists) ---- */
+#define FTGPU_OK 0
+#define FTGPU_ERR_MATERIAL (-1)    /* unknown material ID: StressUpdate.cpp:25-26 (code 1)   */
+#define FTGPU_ERR_INPUT (-3)       /* bad mesh / argument: TerminateFemTech(3)               */
+#define FTGPU_ERR_ALLOC (-12)      /* device allocation failed: AllocateArrays.cpp (code 12) */
+#define FTGPU_ERR_DT (-19)         /* dt below FailureTimeStep: StableTimeStep.cpp:35-38     */
+#define FTGPU_ERR_INVERTED (-20)   /* J <= 0 or non-finite at a Gauss point                  */
+#define FTGPU_ERR_CUDA (-30)       /* CUDA runtime error                                     */
+#define FTGPU_ERR_STATE (-31)      /* call out of order (e.g. step before setup)             */
+#define FTGPU_ERR_NODEVICE (-32)   /* no CUDA device / extension not usable                  */
+
+/* ---- precision modes ---- */
+#define FTGPU_FP64 0  /* element kinematics, stress and nodal state in FP64       */
+#define FTGPU_MIXED 1 /* FP32 element kinematics/stress, FP64 nodal state and dt   */
+
+/* ---- element types (ElementType strings "C3D8"/"C3D4" of the reference) ---- */
+#define FTGPU_C3D8 0
+#define FTGPU_C3D4 1
+
+/* ---- material IDs (StressUpdate.cpp:7-27, plus two new laws) ----
+ * 0 rigid, 1 compressible Neo-Hookean [rho,mu,lambda], 2 St.Venant-Kirchhoff
+ * [rho,mu,lambda], 3 linear elastic [rho,mu,lambda], 4 HGO isotropic
+ * [rho,mu,lambda,k1,k2], 5 HGO isotropic + 2-term Prony
+ * [rho,mu,lambda,k1,k2,g1,t1,g2,t2], 6 one-term Ogden [rho,mu,lambda,alpha],
+ * 7 anisotropic GOH (fibre per element, dispersion kappa) + 1-term Prony
+ * [rho,mu,lambda,k1,k2,g1,t1,kappa]. */
+#define FTGPU_MAXMATPARAMS 9
+
+/* ---- boundary-condition functions (driver-side BCs of examples/exN) ----
+ * Each DOF is FTGPU_BC_FREE, FTGPU_BC_HOLD (constrained, values untouched: the
+ * reference's boundary[] flag alone) or the index of a function below.
+ * A constrained DOF gets u(t), v(t) and a = 0 after every displacement update,
+ * as ApplyBoundaryConditions does in examples/ex9/ex9.cpp:187-248. */
+#define FTGPU_BC_FREE (-1)
+#define FTGPU_BC_HOLD (-2)
+#define FTGPU_BCK_FIXED 0 /* u = p0, v = 0                                         */
+#define FTGPU_BCK_RAMP 1  /* u = p0 * t, v = p0                                    */
+#define FTGPU_BCK_SINE 2  /* u = p0 sin(p1 t), v = p0 p1 cos(p1 t)                 */
+#define FTGPU_BCK_ROT 3   /* rigid rotation about unit axis p0..2 through p3..5 with
+                             angular acceleration p6 sin(pi t / p7) for t <= p7     */
+
+typedef struct ftgpu_bc_fn {
+  int kind;
+  int pad;
+  double p[8];
+} ftgpu_bc_fn;
+
+typedef struct ftgpu_model ftgpu_model;
+
+/* Create / destroy a model on a CUDA device.  precision: FTGPU_FP64 / MIXED. */
+int ftgpu_create(ftgpu_model **out, int device, int precision);
+int ftgpu_destroy(ftgpu_model *m);
+const char *ftgpu_status_string(int status);
+const char *ftgpu_last_error(void);
+
+/* Mesh in the reference's arrays (ReadInputFile + PartitionMesh leave these in
+ * coordinates, eptr, connectivity, ElementType, pid: GlobalVariables.h:34-48).
+ * etype[e] is FTGPU_C3D8 or FTGPU_C3D4.  Arrays are copied. */
+int ftgpu_set_mesh(ftgpu_model *m, int nNodes, int nelements, const double *coordinates,
+                   const int *eptr, const int *connectivity, const int *etype, const int *pid);
+
+/* Materials as ReadMaterials() leaves them (ReadMaterials.cpp:8-138):
+ * materialID[nPID], properties[nPID*FTGPU_MAXMATPARAMS]. */
+int ftgpu_set_materials(ftgpu_model *m, int nPID, const int *materialID,
+                        const double *properties);
+
+/* Unit fibre direction per element (3*nelements), used by material 7. */
+int ftgpu_set_fibers(ftgpu_model *m, const double *fiber);
+
+/* Boundary conditions: dof_fn[3*nNodes] (FREE, HOLD or function index) and the
+ * function table.  Replaces the boundary[] array plus the driver's
+ * ApplyBoundaryConditions() (ex9.cpp:187-248). */
+int ftgpu_set_bc(ftgpu_model *m, const int *dof_fn, int nfn, const ftgpu_bc_fn *fns);
+
+/* Several independent instances in one model (batched ensemble).  Nodes of
+ * instance i are [node_offset[i], node_offset[i+1]); no element may span two
+ * instances.  Per-instance end time, dt reduction factor and failure dt.
+ * Without this call the model is one instance. */
+int ftgpu_set_instances(ftgpu_model *m, int ninst, const int *node_offset, const double *tmax,
+                        const double *reduction, const double *failure_dt);
+
+/* Patch size (elements per thread block) used when setup() builds its
+ * element patches: 0 = default.  Exposed for the autotuner. */
+int ftgpu_set_patch_size(ftgpu_model *m, int elements_per_patch);
+
+/* One-time setup on the device: element patches, reference shape-function
+ * data and the lumped mass.  Replaces ShapeFunctions() (ShapeFunctions.cpp:32)
+ * and AssembleLumpedMass() (Mass3D.cpp:127). */
+int ftgpu_setup(ftgpu_model *m);
+
+/* Lumped mass per DOF, as AssembleLumpedMass() leaves mass[nDOF]. */
+int ftgpu_get_mass(ftgpu_model *m, double *mass);
+
+/* ---- symbol-compatible primitives (one call = one reference function) ---- */
+
+/* GetForce() (GetForce.cpp:12-25 -> GetForce_3D.cpp:5-53) on displacements
+ * u[nDOF] with the global dt used by the viscoelastic update: writes
+ * fi[nDOF] (internal force) and, if non-NULL, f_net = -fi.  Viscoelastic
+ * history advances exactly as one reference GetForce() call does. */
+int ftgpu_get_force(ftgpu_model *m, const double *u, double dt, double *fi, double *f_net);
+
+/* StableTimeStep() (StableTimeStep.cpp:4-40) on displacements u[nDOF]:
+ * min over elements (elements whose nodes are all fully constrained are
+ * skipped) of characteristic length / dilatational wave speed. */
+int ftgpu_stable_time_step(ftgpu_model *m, const double *u, double *dt_min);
+
+/* Per-Gauss-point F (column-major 9), detF and PK2 (Voigt 11,22,33,23,13,12)
+ * of the last ftgpu_get_force call, in the reference's element order and
+ * Gauss-point order (fptr/detFptr/pk2ptr layout of ShapeFunctions.cpp). */
+int ftgpu_get_gauss_points(ftgpu_model *m, double *F, double *detF, double *pk2);
+
+/* Number of Gauss points (8 per C3D8, 1 per C3D4). */
+int ftgpu_num_gauss_points(ftgpu_model *m);
+
+/* ---- device-resident explicit loop (fast mode) ---- */
+
+/* Initial state (AoS [nDOF], any may be NULL = zero) and start time. */
+int ftgpu_set_state(ftgpu_model *m, const double *u, const double *v, const double *a,
+                    double time);
+
+/* The pre-loop sequence of examples/ex9/ex9.cpp:81-93: apply BCs at t0,
+ * dt = reduction * StableTimeStep(), GetForce(), CalculateAccelerations().
+ * reduction / failure_dt / tmax apply to every instance not configured by
+ * ftgpu_set_instances. */
+int ftgpu_init_explicit(ftgpu_model *m, double reduction, double failure_dt, double tmax);
+
+/* Advance every instance by up to max_steps central-difference steps
+ * (ex9.cpp:107-175) or until Time >= tMax; the loop runs on the device as
+ * CUDA-graph chunks.  *steps_done = steps taken by instance 0. */
+int ftgpu_run(ftgpu_model *m, int max_steps, int *steps_done);
+
+/* State after the last completed step, AoS [nDOF] (any pointer may be NULL),
+ * plus the instance-0 time, next dt and step count. */
+int ftgpu_get_state(ftgpu_model *m, double *u, double *v, double *a, double *time, double *dt,
+                    long long *step);
+
+/* Per-instance time / next dt / steps / done flag (arrays of ninst). */
+int ftgpu_get_instance_clock(ftgpu_model *m, double *time, double *dt, long long *step,
+                             int *done);
+
+/* Number of kernel launches one step issues (element groups + nodal update). */
+int ftgpu_launches_per_step(ftgpu_model *m);
+
+/* Synchronise and return the device error word (0 = none). */
+int ftgpu_check(ftgpu_model *m);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,149 @@
+"""Generate the golden fixtures in tests/golden/ from the reference itself.
+
+Run in a checkout where the reference tree exists (default /root/reference,
+override with FEMTECH_REFERENCE): it builds the reference's own hot-path
+sources into oracle/_ref/libfemtech_ref.so (oracle/Makefile) and records their
+outputs on small seeded inputs.  The fixtures are committed; tests never need
+the reference tree.
+
+Fixtures:
+  ref_force.npz   GetForce / mass / StableTimeStep / Gauss-point pk2 of the
+                  reference on jittered C3D8 and C3D4 meshes, materials 1-5,
+                  including three consecutive viscoelastic calls (material 5).
+  ref_ex9.npz     examples/ex9 (one C3D8, Neo-Hookean, ramped tension, 0.8
+                  dt factor, t = 0..1 s) run by the reference loop, plus the
+                  last row of examples/ex9/abaqus/abaqus.rpt (the CI target of
+                  examples/ex9/compareResults.py).
+  ref_cube.npz    the CPU-runnable configuration: 10x10x10 C3D8 cube 0.01 m,
+                  Neo-Hookean rho 1000, mu 3.4 kPa, K 2 MPa, z=0 fixed, top
+                  face ramped to 10 % strain over 10 ms, 0.9 dt factor, all
+                  displacements every 100 steps.
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from femtech_gb300 import meshgen as mg  # noqa: E402
+from oracle import oracle as orc  # noqa: E402
+
+REF = os.environ.get("FEMTECH_REFERENCE", "/root/reference")
+
+MATS = {
+    1: [1000.0, 3400.0, 2.0e6],
+    2: [1000.0, 3400.0, 2.0e6],
+    3: [1000.0, 3400.0, 2.0e6],
+    4: [1040.0, 1.0e3, 2.0e6, 5.0e3, 10.0],
+    5: [1040.0, 1.0e3, 2.0e6, 5.0e3, 10.0, 0.6, 6.0e-3, 0.2, 2.0e-3],
+}
+
+
+def small_meshes():
+    hexm = mg.hex_block(3, 2, 2, 0.003, 0.002, 0.002, jitter=0.15, seed=11)
+    tetm = mg.tet_ellipsoid(0.004, 0.003, 0.0025, 0.0012, jitter=0.1, seed=5)
+    return hexm, tetm
+
+
+def force_cases():
+    out = {}
+    hexm, tetm = small_meshes()
+    rng = np.random.default_rng(1234)
+    for name, mesh in (("hex", hexm), ("tet", tetm)):
+        n = len(mesh["coordinates"])
+        # three displacement states, small against the thinnest element
+        amp = 3.0e-5 if name == "hex" else 2.0e-6
+        u = rng.normal(0.0, amp, (3, 3 * n))
+        out[name + "_X"] = mesh["coordinates"]
+        out[name + "_conn"] = mesh["connectivity"]
+        out[name + "_etype"] = mesh["etype"]
+        out[name + "_u"] = u
+        for mid, props in MATS.items():
+            mats = mg.materials([(mid, props)])
+            r = orc.RefBuild(mesh, mats)
+            fis, pk2s = [], []
+            for k in range(3):
+                fis.append(r.get_force(u[k], 1.0e-6))
+                pk2s.append(r.gp_arrays()[2])
+                assert np.all(np.isfinite(fis[-1])), (name, mid, k)
+            out["%s_m%d_fi" % (name, mid)] = np.array(fis)
+            out["%s_m%d_pk2" % (name, mid)] = np.array(pk2s)
+            out["%s_m%d_mass" % (name, mid)] = r.mass
+            b = np.zeros(3 * n, np.int32)
+            out["%s_m%d_dt" % (name, mid)] = np.array([r.stable_time_step(u[k], b) for k in range(3)])
+    return out
+
+
+def abaqus_last_row(path):
+    rows = []
+    with open(path) as f:
+        for line in f:
+            parts = line.split()
+            try:
+                vals = [float(p) for p in parts]
+            except ValueError:
+                continue
+            if len(vals) >= 13:
+                rows.append(vals)
+    return np.array(rows[-1])
+
+
+def ex9_case():
+    # examples/ex9/1-elt-cube.k: one C3D8, element nodes 1 2 4 3 5 6 8 7
+    X = np.array([[0, 0, 0], [0.005, 0, 0], [0, 0.005, 0], [0.005, 0.005, 0],
+                  [0, 0, 0.005], [0.005, 0, 0.005], [0, 0.005, 0.005], [0.005, 0.005, 0.005]],
+                 np.float64)
+    conn = np.array([0, 1, 3, 2, 4, 5, 7, 6], np.int32)
+    mesh = dict(coordinates=X, eptr=np.array([0, 8], np.int32), connectivity=conn,
+                etype=np.array([0], np.int32), pid=np.array([0], np.int32))
+    mats = mg.materials([(1, [1040.0, 100.0, 100.0])])  # examples/ex9/materials.dat
+    loads = ex9_loads(X)
+    r = orc.RefBuild(mesh, mats)
+    res = r.explicit_run(loads.dof_fn, loads.fns, tmax=1.0, reduction=0.8, max_steps=100000,
+                         out_every=1)
+    abq = abaqus_last_row(os.path.join(REF, "examples/ex9/abaqus/abaqus.rpt"))
+    return dict(X=X, conn=conn, u_out=res["u_out"], t_out=res["t_out"], steps=res["steps"],
+                time=res["time"], u=res["u"], v=res["v"], a=res["a"],
+                abaqus_last=abq[[0, 10, 11, 12]])
+
+
+def ex9_loads(X):
+    """ApplyBoundaryConditions of examples/ex9/ex9.cpp:187-248 (dMax 7 mm, tMax 1 s)."""
+    tol = 1e-5
+    loads = mg.Loads(len(X))
+    fx = np.where(np.abs(X[:, 0]) < tol)[0]
+    fy = np.where(np.abs(X[:, 1]) < tol)[0]
+    fz = np.where(np.abs(X[:, 2]) < tol)[0]
+    top = np.where(np.abs(X[:, 1] - 0.005) < tol)[0]
+    loads.fix(fx, dofs=(0,))
+    loads.fix(fy, dofs=(1,))
+    loads.fix(fz, dofs=(2,))
+    loads.ramp(top, 1, 0.007 / 1.0)
+    return loads
+
+
+def cube_case():
+    mesh, mats, loads = mg.cube_tension_case(n=10)
+    r = orc.RefBuild(mesh, mats)
+    res = r.explicit_run(loads.dof_fn, loads.fns, tmax=0.01, reduction=0.9, max_steps=100000,
+                         out_every=100)
+    return dict(u_out=res["u_out"], t_out=res["t_out"], steps=res["steps"], time=res["time"],
+                u=res["u"], v=res["v"], a=res["a"])
+
+
+def main():
+    orc.build()
+    if not orc.RefBuild.available():
+        raise SystemExit("reference build missing")
+    np.savez_compressed(os.path.join(HERE, "ref_force.npz"), **force_cases())
+    np.savez_compressed(os.path.join(HERE, "ref_ex9.npz"), **ex9_case())
+    np.savez_compressed(os.path.join(HERE, "ref_cube.npz"), **cube_case())
+    for f in ("ref_force.npz", "ref_ex9.npz", "ref_cube.npz"):
+        print(f, os.path.getsize(os.path.join(HERE, f)))
+
+
+if __name__ == "__main__":
+    main()

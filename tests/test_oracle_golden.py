@@ -1,0 +1,53 @@
+"""Pin the FP64 oracle to the reference's own outputs (tests/golden, produced by
+the reference sources compiled unmodified; see tests/golden/make_golden.py)."""
+import numpy as np
+import pytest
+
+from helpers import MATS, ex9_mesh_loads, golden_mesh, rel
+from femtech_gb300 import meshgen as mg
+
+
+@pytest.mark.parametrize("name", ["hex", "tet"])
+@pytest.mark.parametrize("mid", [1, 2, 3, 4, 5])
+def test_force_mass_dt_pk2_match_reference(oracle_lib, golden, name, mid):
+    f = golden["ref_force"]
+    mesh = golden_mesh(golden, name)
+    o = oracle_lib.Oracle(mesh, mg.materials([(mid, MATS[mid])]))
+    np.testing.assert_allclose(o.mass, f["%s_m%d_mass" % (name, mid)], rtol=1e-14, atol=0)
+    u = f[name + "_u"]
+    b = np.zeros(3 * o.nNodes, np.int32)
+    for k in range(3):  # consecutive calls: viscoelastic history must advance identically
+        fi = o.get_force(u[k], 1.0e-6)
+        ref = f["%s_m%d_fi" % (name, mid)][k]
+        assert rel(fi, ref) < 1e-13
+        pk2 = o.gp_arrays()[2]
+        assert rel(pk2, f["%s_m%d_pk2" % (name, mid)][k]) < 1e-13
+        assert o.stable_time_step(u[k], b) == pytest.approx(f["%s_m%d_dt" % (name, mid)][k],
+                                                            rel=1e-14)
+
+
+def test_ex9_loop_matches_reference_and_abaqus(oracle_lib, golden):
+    g = golden["ref_ex9"]
+    mesh, mats, loads = ex9_mesh_loads()
+    o = oracle_lib.Oracle(mesh, mats)
+    res = o.explicit_run(loads.dof_fn, loads.fns, tmax=1.0, reduction=0.8, max_steps=100000,
+                         out_every=1)
+    assert res["steps"] == int(g["steps"])
+    assert rel(res["u_out"], g["u_out"]) < 1e-12
+    # the reference CI check (examples/ex9/compareResults.py:14-25): node
+    # (0.005,0.005,0.005) within 5 % of Abaqus, final time within 1 %
+    abq = g["abaqus_last"]
+    assert abs(res["time"] - abq[0]) / abq[0] < 0.01
+    u8 = res["u"][21:24]
+    assert np.max(np.abs((u8 - abq[1:]) / abq[1:])) < 0.05
+
+
+def test_cube_tension_matches_reference(oracle_lib, golden):
+    g = golden["ref_cube"]
+    mesh, mats, loads = mg.cube_tension_case(n=10)
+    o = oracle_lib.Oracle(mesh, mats, threads=4)
+    res = o.explicit_run(loads.dof_fn, loads.fns, tmax=0.01, reduction=0.9, max_steps=100000,
+                         out_every=100)
+    assert res["steps"] == int(g["steps"])
+    np.testing.assert_allclose(res["t_out"], g["t_out"], rtol=1e-14)
+    assert rel(res["u_out"], g["u_out"]) < 1e-12
