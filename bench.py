@@ -1,0 +1,377 @@
+#!/usr/bin/env python
+"""Element-updates/s of FemTech's explicit hot path on GB300.
+
+Default workload (the headline configuration that fits one GPU): the
+200x200x100 C3D8 block (4,000,000 elements, 4,080,501 nodes, 0.2x0.2x0.1 m),
+nodes jittered +-10 % of the edge length (seeded; faces kept planar), 1-term
+Ogden (mu 1.5 kPa, alpha 5, K 20 MPa, rho 1040), base fixed, top face
+sinusoidal shear 1 mm at 50 Hz, dt = 0.9 x stable dt; FP32 element kernels,
+FP64 nodal state and dt.  One step = one central-difference step of every
+element (force, stress, stable dt, assembly, nodal update), i.e. one
+element-update per element.  Inputs are synthetic (seeded), generated in the
+run.
+
+Reported (one JSON line from rank 0):
+  value       element-updates/s, device time of the timed steps (CUDA events
+              on the engine's stream, device synchronised on both sides)
+  e2e         the same metric through the public C ABI with host buffers:
+              initial state uploaded from host, displacements read back every
+              100 steps, setup of the loop included
+  roofline    dominant kernel (element pass) against measured HBM bandwidth,
+              with its FP32-pipe use against the nominal FP32 rate
+  cpu_baseline the FP64 oracle (OpenMP port of the reference algorithm) on
+              the host cores, on a bounded sub-block of the same workload
+
+--impl reference times the reference algorithm on the host CPU (the oracle
+port on all host threads; the reference's own sources where they were
+compiled in this checkout) on the same metric.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+# Workload
+NX, NY, NZ = 200, 200, 100
+LX, LY, LZ = 0.2, 0.2, 0.1
+WORKLOAD = "ogden_hex8_block_200x200x100_jitter10_sine50Hz"
+
+# Algorithmic traffic model of one element-update (compulsory bytes at the
+# stated precisions; intermediate patch buffers are overhead, not counted):
+#   element pass: connectivity 8 x 4 B, per node X f32 12 B + u f32 12 B read
+#   and internal force f32 12 B written, x (nodes / elements)
+#   nodal pass:   per node u f64 24 + v_half f64 24 + mass f64 8 read,
+#                 u 24 + v_half 24 written + force f32 12 read
+ELEM_BYTES_PER_EL = 32.0
+ELEM_BYTES_PER_NODE = 36.0
+NODE_BYTES_PER_NODE = 116.0
+# FP32 operations of one C3D8 Ogden element-update in this formulation,
+# counted from the kernel source (ft_elem.cuh / ft_materials.cuh), FMA = 2:
+#   Hadamard transforms 2 x 72 adds; per Gauss point: Jacobian and
+#   displacement-gradient columns 2 x 54, adj(A) 45, D = H adj^T / det 63,
+#   J - 1 30, 2E 39, Jacobi eigen (4 sweeps x 3 rotations x 58) 696,
+#   principal functions 45, S 60, P = S + D S 54, P adj(A) 45, moments 48
+#   -> 1233 per Gauss point; 8 points 9864; inverse transform 84; face areas
+#   and volume 550.
+FLOP_PER_EL_OGDEN = 144 + 9864 + 84 + 550
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(mx)) if mx else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def reduce_max_sum(vals, world, backend_device=None):
+    """Max of times and sum of work over ranks (torch.distributed when world > 1)."""
+    if world == 1:
+        return vals
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor(vals, dtype=torch.float64, device=backend_device or "cpu")
+    mx = t.clone()
+    dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+    return mx.tolist()
+
+
+def build_workload(nx=NX, ny=NY, nz=NZ, lx=LX, ly=LY, lz=LZ):
+    from femtech_gb300 import meshgen as mg
+    return mg.ogden_block_case(nx=nx, ny=ny, nz=nz, lx=lx, ly=ly, lz=lz, jitter=0.1, seed=0)
+
+
+def cpu_reference_rate(threads, target_s=12.0, kind="port"):
+    """Element-updates/s of the FP64 reference algorithm on host cores, on a
+    bounded sub-block (40x40x20 of the same spacing, jitter, law and loads)."""
+    from oracle import oracle as orc
+    sub = (40, 40, 20)
+    mesh, mats, loads = build_workload(sub[0], sub[1], sub[2], LX * sub[0] / NX, LY * sub[1] / NY,
+                                       LZ * sub[2] / NZ)
+    E = len(mesh["etype"])
+    if kind == "reference" and orc.RefBuild.available():
+        runner = orc.RefBuild(mesh, mats)
+        threads = 1
+    else:
+        kind = "port"
+        runner = orc.Oracle(mesh, mats, threads=threads)
+    t = time.perf_counter()
+    runner.explicit_run(loads.dof_fn, loads.fns, tmax=1.0, reduction=0.9, max_steps=2, out_every=0)
+    per = (time.perf_counter() - t) / 3.0
+    steps = max(2, int(target_s / max(per, 1e-6)))
+    t = time.perf_counter()
+    res = runner.explicit_run(loads.dof_fn, loads.fns, tmax=1.0, reduction=0.9, max_steps=steps,
+                              out_every=0)
+    dt = time.perf_counter() - t
+    rate = E * res["steps"] / dt
+    return dict(value=rate, unit="element-updates/s", cores=threads, kind=kind,
+                sample="%dx%dx%d sub-block (%d C3D8, same spacing/jitter/law/loads), FP64, %d steps "
+                       "incl. initial force and dt, %.1f s" % (sub + (E, res["steps"], dt)))
+
+
+def run_reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    from oracle import oracle as orc
+    if not os.path.exists(orc.LIB):
+        orc.build()
+    kind = "reference" if orc.RefBuild.available() else "port"
+    # W + K bounded samples; the value is the rate of the timed ones
+    rates = []
+    for i in range(max(args.warmup, 0) + max(1, min(args.steps, 3))):
+        r = cpu_reference_rate(threads, target_s=8.0 if i >= args.warmup else 2.0, kind=kind)
+        if i >= args.warmup:
+            rates.append(r)
+    v = float(np.mean([r["value"] for r in rates]))
+    base = rates[-1]
+    base["value"] = v
+    line = {"metric": "element-updates/s", "value": v, "unit": "element-updates/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "impl": "reference", "dtype": "f64",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "sample": base["sample"]},
+            "cpu_baseline": base,
+            "e2e": {"value": v, "unit": "element-updates/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--size", default=None, help="nx,ny,nz override (smaller cases for profiling)")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return run_reference_arm(args, rank, world)
+    if args.warmup < 3:
+        raise SystemExit("at least 3 warm-up steps are required")
+
+    import torch
+    import femtech_gb300 as ft
+
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = local
+    nx, ny, nz = NX, NY, NZ
+    if args.size:
+        nx, ny, nz = (int(x) for x in args.size.split(","))
+    lx, ly, lz = LX * nx / NX, LY * ny / NY, LZ * nz / NZ
+    t0 = time.perf_counter()
+    mesh, mats, loads = build_workload(nx, ny, nz, lx, ly, lz)
+    E = len(mesh["etype"])
+    N = len(mesh["coordinates"])
+    model = ft.Model(mesh, mats, precision=ft.MIXED, device=dev, loads=loads)
+    log("setup %.1f s (%d elements, %d nodes)" % (time.perf_counter() - t0, E, N))
+    model.init_explicit(reduction=0.9, failure_dt=0.0, tmax=1e300)
+    model.run(args.warmup)
+    torch.cuda.synchronize(dev)
+
+    # ---- timed region: device time of K steps ----
+    sampler = ClockSampler(dev)
+    sampler.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    steps, dev_ms = timed_run(model, args.steps)
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = sampler.stop()
+    ms = reduce_max_sum([dev_ms], world, "cuda:%d" % dev)[0]
+    value = E * steps * world / (ms / 1000.0)
+    launches = model.launches_per_step() * steps + math.ceil(steps / 16)
+
+    # ---- per-kernel times (events around every pass) for the roofline ----
+    kp = min(args.steps, 400)
+    pk = ft.lib()
+    import ctypes as C
+    sd, em, nm = C.c_int(), C.c_double(), C.c_double()
+    ft._check(pk.ftgpu_run_profiled(model.h, kp, C.byref(sd), C.byref(em), C.byref(nm)))
+    elem_ms = em.value / max(sd.value, 1)
+    node_ms = nm.value / max(sd.value, 1)
+    hbm, peak_kind = peaks()
+    elem_bytes = E * ELEM_BYTES_PER_EL + N * ELEM_BYTES_PER_NODE
+    node_bytes = N * NODE_BYTES_PER_NODE
+    if elem_ms >= node_ms:
+        dom, dom_ms, dom_bytes = "k_elem<float,C3D8,Ogden> (all patches of one step)", elem_ms, elem_bytes
+    else:
+        dom, dom_ms, dom_bytes = "k_node<float> fused update", node_ms, node_bytes
+    achieved = dom_bytes / (dom_ms / 1e3) / 1e9
+    traffic = load_traffic(E)
+    sm_mhz = clocks.get("sm_mhz") or 2070.0
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    fp32_ach = FLOP_PER_EL_OGDEN * E / (elem_ms / 1e3) / 1e12
+
+    # ---- end to end through the C ABI with host buffers ----
+    e2e = end_to_end(ft, mesh, mats, loads, dev, args.steps, E, N)
+
+    line = {
+        "metric": "element-updates/s", "value": value, "unit": "element-updates/s",
+        "n_gpus": world, "steps": steps, "warmup": args.warmup,
+        "ms_per_step": ms / max(steps, 1), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 element kernels / f64 nodal state",
+        "data": "synthetic (seeded jittered block, generated in-run)",
+        "config": {"workload": WORKLOAD if not args.size else "ogden_hex8_block_%dx%dx%d" % (nx, ny, nz),
+                   "elements": E, "nodes": N, "material": "ogden mu=1.5e3 alpha=5 K=2e7 rho=1040",
+                   "precision": "mixed", "l2": "inputs larger than L2 (%.2f GB resident)" %
+                   ((E * 48 + N * 140) / 1e9),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
+                     "unit": "GB/s", "frac": achieved / hbm, "peak_source": peak_kind,
+                     "traffic": None if traffic is None else traffic * (1.0 if dom.startswith("k_elem") else 0.0) or None,
+                     "algorithmic_bytes_per_launch": dom_bytes,
+                     "launch_ms": dom_ms, "elem_pass_ms": elem_ms, "node_pass_ms": node_ms,
+                     "fp32": {"achieved": fp32_ach, "peak": fp32_peak, "unit": "TFLOP/s",
+                              "frac": fp32_ach / fp32_peak, "peak_source": "nominal 152 SM x 128 lanes x 2 x median SM clock",
+                              "flop_per_element": FLOP_PER_EL_OGDEN}},
+        "e2e": e2e,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_reference_rate(os.cpu_count() or 1)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    model.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def timed_run(model, steps):
+    import ctypes as C
+    import femtech_gb300 as ft
+    sd, ms = C.c_int(), C.c_double()
+    ft._check(ft.lib().ftgpu_run_timed(model.h, int(steps), C.byref(sd), C.byref(ms)))
+    return sd.value, ms.value
+
+
+def end_to_end(ft, mesh, mats, loads, dev, steps, E, N):
+    """Public-API run with host buffers: upload the initial state from host
+    memory, run the loop, read all displacements back every 100 steps."""
+    import torch
+    model = ft.Model(mesh, mats, precision=ft.MIXED, device=dev, loads=loads)
+    u0 = torch.zeros(3 * N, dtype=torch.float64).pin_memory().numpy()
+    v0 = torch.zeros(3 * N, dtype=torch.float64).pin_memory().numpy()
+    a0 = torch.zeros(3 * N, dtype=torch.float64).pin_memory().numpy()
+    every = 100
+    outs = 0
+    torch.cuda.synchronize(dev)
+    t = time.perf_counter()
+    model.set_state(u0, v0, a0, 0.0)
+    model.init_explicit(reduction=0.9, failure_dt=0.0, tmax=1e300)
+    done = 0
+    while done < steps:
+        k = model.run(min(every, steps - done))
+        done += k
+        u = model.state()["u"]
+        outs += 1
+        if k == 0:
+            break
+    torch.cuda.synchronize(dev)
+    el = time.perf_counter() - t
+    model.close()
+    del u
+    h2d = 3 * 3 * N * 8
+    d2h = outs * 3 * 3 * N * 8
+    return {"value": E * done / el, "unit": "element-updates/s",
+            "h2d_bytes_per_step": h2d / max(done, 1), "d2h_bytes_per_step": d2h / max(done, 1),
+            "what": "set_state from pinned host arrays + init_explicit + run, full u/v/a read "
+                    "back every %d steps" % every}
+
+
+def load_traffic(E):
+    """DRAM bytes per element pass from the committed ncu summary, scaled by
+    element count (traffic grows in proportion to the elements processed)."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    b = d.get("elem_pass_dram_bytes_per_element")
+    return None if b is None else b * E
+
+
+if __name__ == "__main__":
+    main()

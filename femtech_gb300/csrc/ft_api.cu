@@ -208,13 +208,18 @@ struct ftgpu_model {
   DBuf slot_off, slots, node_inst, nbc, fnsbuf;
   DBuf dX, u, v, a, vh, mass, minv, fi;
   DBuf gpF, gpJ, gpS;
-  // graph of one chunk of steps
+  // graph of one chunk of steps (plain, and with timing events)
   cudaGraphExec_t chunk_exec = nullptr;
   int chunk_steps = 0;
+  cudaGraphExec_t prof_exec = nullptr;
+  int prof_steps = 0;
+  std::vector<cudaEvent_t> prof_ev;
   Clock *h_clock = nullptr;  // pinned
   int *h_err = nullptr;
   ~ftgpu_model() {
     if (chunk_exec) cudaGraphExecDestroy(chunk_exec);
+    if (prof_exec) cudaGraphExecDestroy(prof_exec);
+    for (cudaEvent_t e : prof_ev) cudaEventDestroy(e);
     if (h_clock) cudaFreeHost(h_clock);
     if (h_err) cudaFreeHost(h_err);
     if (stream) cudaStreamDestroy(stream);
@@ -224,6 +229,14 @@ struct ftgpu_model {
 namespace {
 
 bool is_fp64(const ftgpu_model *m) { return m->precision == FTGPU_FP64; }
+
+// Captured graphs bake in buffer pointers and BC tables: drop them whenever those change.
+void drop_graphs(ftgpu_model *m) {
+  if (m->chunk_exec) cudaGraphExecDestroy(m->chunk_exec);
+  if (m->prof_exec) cudaGraphExecDestroy(m->prof_exec);
+  m->chunk_exec = m->prof_exec = nullptr;
+  m->chunk_steps = m->prof_steps = 0;
+}
 
 int max_patch(const ftgpu_model *m) {
   int pe = m->patch_elems > 0 ? m->patch_elems : 128;
@@ -594,14 +607,13 @@ int setup_t(ftgpu_model *m) {
     for (long long n = 0; n < N; ++n) mi[n] = 1.0 / m->mass_host[n];
     CKI(m->minv.upload(mi.data(), N));
   }
-  if (!m->h_clock) CK(cudaMallocHost((void **)&m->h_clock, sizeof(Clock) * std::max(2 * m->ninst, 2)));
+  if (m->h_clock) cudaFreeHost(m->h_clock);
+  m->h_clock = nullptr;
+  CK(cudaMallocHost((void **)&m->h_clock, sizeof(Clock) * std::max(2 * m->ninst, 2)));
   if (!m->h_err) CK(cudaMallocHost((void **)&m->h_err, sizeof(int)));
   m->setup_done = true;
   m->init_done = false;
-  if (m->chunk_exec) {
-    cudaGraphExecDestroy(m->chunk_exec);
-    m->chunk_exec = nullptr;
-  }
+  drop_graphs(m);
   return 0;
 }
 
@@ -615,25 +627,116 @@ int ensure_gp(ftgpu_model *m) {
 }
 
 // One chunk: BEGIN, K x (element groups, node), the last node pass FINISH.
-int capture_chunk(ftgpu_model *m, int K) {
-  if (m->chunk_exec && m->chunk_steps == K) return 0;
-  if (m->chunk_exec) cudaGraphExecDestroy(m->chunk_exec);
-  m->chunk_exec = nullptr;
+// With prof, event-record nodes bracket every element pass and node pass
+// (events 2k / 2k+1 / 2k+2 around step k).
+int capture_chunk(ftgpu_model *m, int K, bool prof) {
+  cudaGraphExec_t &exec = prof ? m->prof_exec : m->chunk_exec;
+  int &steps = prof ? m->prof_steps : m->chunk_steps;
+  if (exec && steps == K) return 0;
+  if (exec) cudaGraphExecDestroy(exec);
+  exec = nullptr;
+  if (prof) {
+    for (cudaEvent_t e : m->prof_ev) cudaEventDestroy(e);
+    m->prof_ev.assign(2 * K + 1, nullptr);
+    for (auto &e : m->prof_ev) CK(cudaEventCreate(&e));
+  }
   cudaGraph_t g;
   CK(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
   int r = launch_node(m, kNodeBegin, 0);
   for (int k = 0; k < K && !r; ++k) {
-    r = launch_groups(m, k & 1, 1, 0.0, 0, 0);
+    if (prof) r = (int)cudaEventRecordWithFlags(m->prof_ev[2 * k], m->stream, cudaEventRecordExternal);
+    if (!r) r = launch_groups(m, k & 1, 1, 0.0, 0, 0);
+    if (prof && !r)
+      r = (int)cudaEventRecordWithFlags(m->prof_ev[2 * k + 1], m->stream, cudaEventRecordExternal);
     if (!r) r = launch_node(m, k == K - 1 ? kNodeFinish : kNodeFused, k & 1);
   }
+  if (prof && !r) r = (int)cudaEventRecordWithFlags(m->prof_ev[2 * K], m->stream, cudaEventRecordExternal);
   cudaError_t ce = cudaStreamEndCapture(m->stream, &g);
   if (r) return fail(FTGPU_ERR_CUDA, std::string("capture launch: ") + cudaGetErrorString((cudaError_t)r));
   if (ce != cudaSuccess) return fail(FTGPU_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(ce));
-  ce = cudaGraphInstantiate(&m->chunk_exec, g, 0);
+  ce = cudaGraphInstantiate(&exec, g, 0);
   cudaGraphDestroy(g);
   if (ce != cudaSuccess) return fail(FTGPU_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(ce));
-  m->chunk_steps = K;
+  steps = K;
   return 0;
+}
+
+// The host side of the explicit loop: launch chunk graphs until every
+// instance is done (tMax, step limit) or an error shows up.
+int run_impl(ftgpu_model *m, int max_steps, int *steps_done, bool prof, double *elem_ms,
+             double *node_ms, double *device_ms) {
+  if (!m || !m->init_done) return fail(FTGPU_ERR_STATE, "run before init_explicit");
+  if (steps_done) *steps_done = 0;
+  if (elem_ms) *elem_ms = 0.0;
+  if (node_ms) *node_ms = 0.0;
+  if (device_ms) *device_ms = 0.0;
+  if (max_steps <= 0) return FTGPU_OK;
+  CK(cudaSetDevice(m->device));
+  const int ni = m->ninst;
+  CK(cudaMemcpyAsync(m->h_clock, m->clock.p, sizeof(Clock) * ni, cudaMemcpyDeviceToHost, m->stream));
+  CK(cudaStreamSynchronize(m->stream));
+  const long long start0 = m->h_clock[0].step;
+  for (int i = 0; i < ni; ++i) {
+    m->h_clock[i].done &= ~2;  // a new run lifts the previous step limit
+    m->inst[i].step_limit = m->h_clock[i].step + max_steps;
+  }
+  CK(cudaMemcpyAsync(m->clock.p, m->h_clock, sizeof(Clock) * ni, cudaMemcpyHostToDevice, m->stream));
+  CK(cudaMemcpyAsync(m->instp.p, m->inst.data(), ni * sizeof(InstParams), cudaMemcpyHostToDevice,
+                     m->stream));
+  const int K = 16;
+  CKI(capture_chunk(m, K, prof));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (device_ms) {
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaEventRecord(e0, m->stream));
+  }
+  const long long max_chunks = (max_steps + K - 1) / K + 1;
+  int rc = FTGPU_OK;
+  long long prev = start0;
+  for (long long c = 0; c < max_chunks; ++c) {
+    CK(cudaGraphLaunch(prof ? m->prof_exec : m->chunk_exec, m->stream));
+    CK(cudaMemcpyAsync(m->h_clock, m->clock.p, sizeof(Clock) * ni, cudaMemcpyDeviceToHost,
+                       m->stream));
+    CK(cudaMemcpyAsync(m->h_err, m->err.p, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
+    CK(cudaStreamSynchronize(m->stream));
+    if (prof) {
+      const long long taken = m->h_clock[0].step - prev;
+      for (long long k = 0; k < std::min<long long>(taken, K); ++k) {
+        float a = 0.f, b = 0.f;
+        CK(cudaEventElapsedTime(&a, m->prof_ev[2 * k], m->prof_ev[2 * k + 1]));
+        CK(cudaEventElapsedTime(&b, m->prof_ev[2 * k + 1], m->prof_ev[2 * k + 2]));
+        if (elem_ms) *elem_ms += a;
+        if (node_ms) *node_ms += b;
+      }
+    }
+    prev = m->h_clock[0].step;
+    if (*m->h_err & kErrInverted) {
+      rc = fail(FTGPU_ERR_INVERTED, "non-positive or non-finite Jacobian");
+      break;
+    }
+    bool all = true, dterr = false;
+    for (int i = 0; i < ni; ++i) {
+      all &= m->h_clock[i].done != 0;
+      dterr |= (m->h_clock[i].done & 4) != 0;
+    }
+    if (dterr) {
+      rc = fail(FTGPU_ERR_DT, "time step below FailureTimeStep");
+      break;
+    }
+    if (all) break;
+  }
+  if (device_ms) {
+    CK(cudaEventRecord(e1, m->stream));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    *device_ms = ms;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+  }
+  if (steps_done) *steps_done = (int)(m->h_clock[0].step - start0);
+  return rc;
 }
 
 }  // namespace
@@ -722,6 +825,7 @@ int ftgpu_set_materials(ftgpu_model *m, int nPID, const int *materialID, const d
   if (m->setup_done) {
     int r = is_fp64(m) ? upload_materials<double>(m) : upload_materials<float>(m);
     if (r) return r;
+    drop_graphs(m);
   }
   return FTGPU_OK;
 }
@@ -748,10 +852,7 @@ int ftgpu_set_bc(ftgpu_model *m, const int *dof_fn, int nfn, const ftgpu_bc_fn *
   if (m->setup_done) {
     CKI(upload_bc(m));
     CKI(upload_epid(m));
-    if (m->chunk_exec) {
-      cudaGraphExecDestroy(m->chunk_exec);
-      m->chunk_exec = nullptr;
-    }
+    drop_graphs(m);
   }
   return FTGPU_OK;
 }
@@ -908,50 +1009,24 @@ int ftgpu_init_explicit(ftgpu_model *m, double reduction, double failure_dt, dou
 }
 
 int ftgpu_run(ftgpu_model *m, int max_steps, int *steps_done) {
-  if (!m || !m->init_done) return fail(FTGPU_ERR_STATE, "run before init_explicit");
-  if (max_steps <= 0) {
-    if (steps_done) *steps_done = 0;
-    return FTGPU_OK;
-  }
-  CK(cudaSetDevice(m->device));
-  const int ni = m->ninst;
-  CK(cudaMemcpyAsync(m->h_clock, m->clock.p, sizeof(Clock) * ni, cudaMemcpyDeviceToHost, m->stream));
-  CK(cudaStreamSynchronize(m->stream));
-  const long long start0 = m->h_clock[0].step;
-  for (int i = 0; i < ni; ++i) {
-    m->h_clock[i].done &= ~2;  // a new run lifts the previous step limit
-    m->inst[i].step_limit = m->h_clock[i].step + max_steps;
-  }
-  CK(cudaMemcpyAsync(m->clock.p, m->h_clock, sizeof(Clock) * ni, cudaMemcpyHostToDevice, m->stream));
-  CK(cudaMemcpyAsync(m->instp.p, m->inst.data(), ni * sizeof(InstParams), cudaMemcpyHostToDevice,
-                     m->stream));
-  const int K = 16;
-  CKI(capture_chunk(m, K));
-  const long long max_chunks = (max_steps + K - 1) / K + 1;
-  int rc = FTGPU_OK;
-  for (long long c = 0; c < max_chunks; ++c) {
-    CK(cudaGraphLaunch(m->chunk_exec, m->stream));
-    CK(cudaMemcpyAsync(m->h_clock, m->clock.p, sizeof(Clock) * ni, cudaMemcpyDeviceToHost,
-                       m->stream));
-    CK(cudaMemcpyAsync(m->h_err, m->err.p, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
-    CK(cudaStreamSynchronize(m->stream));
-    if (*m->h_err & kErrInverted) {
-      rc = fail(FTGPU_ERR_INVERTED, "non-positive or non-finite Jacobian");
-      break;
-    }
-    bool all = true, dterr = false;
-    for (int i = 0; i < ni; ++i) {
-      all &= m->h_clock[i].done != 0;
-      dterr |= (m->h_clock[i].done & 4) != 0;
-    }
-    if (dterr) {
-      rc = fail(FTGPU_ERR_DT, "time step below FailureTimeStep");
-      break;
-    }
-    if (all) break;
-  }
-  if (steps_done) *steps_done = (int)(m->h_clock[0].step - start0);
-  return rc;
+  return run_impl(m, max_steps, steps_done, false, nullptr, nullptr, nullptr);
+}
+
+int ftgpu_run_timed(ftgpu_model *m, int max_steps, int *steps_done, double *device_ms) {
+  return run_impl(m, max_steps, steps_done, false, nullptr, nullptr, device_ms);
+}
+
+int ftgpu_run_profiled(ftgpu_model *m, int max_steps, int *steps_done, double *elem_ms,
+                       double *node_ms) {
+  return run_impl(m, max_steps, steps_done, true, elem_ms, node_ms, nullptr);
+}
+
+int ftgpu_layout_info(ftgpu_model *m, long long *npatch, long long *nslots, int *ngroups) {
+  if (!m || !m->setup_done) return fail(FTGPU_ERR_STATE, "layout_info before setup");
+  if (npatch) *npatch = (long long)m->ps.patch_inst.size();
+  if (nslots) *nslots = m->S;
+  if (ngroups) *ngroups = (int)m->ps.groups.size();
+  return FTGPU_OK;
 }
 
 int ftgpu_get_state(ftgpu_model *m, double *u, double *v, double *a, double *time, double *dt,

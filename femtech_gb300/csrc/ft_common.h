@@ -10,7 +10,7 @@ namespace ftgpu {
 
 constexpr int kMaxPatchElems = 256;   // elements per patch (thread block) upper bound
 constexpr int kMaxLocalNodes = 320;   // local nodes per patch (shared memory bound)
-constexpr int kElemThreads = 128;     // threads per element block
+constexpr int kElemThreads = 256;     // upper bound of threads per element block
 
 // Per-instance clock, double-buffered by step parity.  Between steps it holds
 // the state the reference keeps in the globals Time and dt (ex9.cpp:9).

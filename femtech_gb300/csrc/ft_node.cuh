@@ -129,7 +129,11 @@ __global__ void __launch_bounds__(256) k_node(const NodeArgs A) {
   // kNodeFused / kNodeFinish: end of step n (+ start of step n+1 when fused)
   Clock *nxt = A.clock + (A.parity ^ 1) * A.ninst + inst;
   if (ck.done) {
-    if (leader) *nxt = ck;
+    // keep both clock slots and the next dt-min slot valid for the next run
+    if (leader) {
+      *nxt = ck;
+      A.dtmin[(A.parity ^ 1) * A.ninst + inst] = kDtHugeBits;
+    }
     return;
   }
   const double t_n = ck.time, dt = ck.dt, t_np1 = t_n + dt, t_half = 0.5 * (t_np1 + t_n);

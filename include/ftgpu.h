@@ -154,6 +154,20 @@ int ftgpu_init_explicit(ftgpu_model *m, double reduction, double failure_dt, dou
  * CUDA-graph chunks.  *steps_done = steps taken by instance 0. */
 int ftgpu_run(ftgpu_model *m, int max_steps, int *steps_done);
 
+/* ftgpu_run with CUDA events recorded on the model's stream around the whole
+ * run: *device_ms is the device time of the steps taken. */
+int ftgpu_run_timed(ftgpu_model *m, int max_steps, int *steps_done, double *device_ms);
+
+/* ftgpu_run with an event before and after every element pass and nodal pass
+ * of every step: *elem_ms / *node_ms are the summed device times of the
+ * element kernels (all groups) and of the nodal kernel. */
+int ftgpu_run_profiled(ftgpu_model *m, int max_steps, int *steps_done, double *elem_ms,
+                       double *node_ms);
+
+/* Number of element patches (thread blocks of one element pass) and of node
+ * slots (patch-local node replicas): the sizes the traffic model uses. */
+int ftgpu_layout_info(ftgpu_model *m, long long *npatch, long long *nslots, int *ngroups);
+
 /* State after the last completed step, AoS [nDOF] (any pointer may be NULL),
  * plus the instance-0 time, next dt and step count. */
 int ftgpu_get_state(ftgpu_model *m, double *u, double *v, double *a, double *time, double *dt,
