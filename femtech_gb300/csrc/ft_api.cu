@@ -319,10 +319,18 @@ int launch_node(ftgpu_model *m, int mode, int parity) {
   NodeArgs A = node_args(m, mode, parity);
   const int th = 256;
   const long long nb = (m->nNodes + th - 1) / th;
-  if (is_fp64(m))
-    k_node<double><<<(unsigned)nb, th, 0, m->stream>>>(A);
-  else
-    k_node<float><<<(unsigned)nb, th, 0, m->stream>>>(A);
+  const bool step = mode == kNodeFused || mode == kNodeFinish;
+  if (is_fp64(m)) {
+    if (step)
+      k_node_step<double><<<(unsigned)nb, th, 0, m->stream>>>(A);
+    else
+      k_node<double><<<(unsigned)nb, th, 0, m->stream>>>(A);
+  } else {
+    if (step)
+      k_node_step<float><<<(unsigned)nb, th, 0, m->stream>>>(A);
+    else
+      k_node<float><<<(unsigned)nb, th, 0, m->stream>>>(A);
+  }
   return (int)cudaGetLastError();
 }
 
@@ -437,6 +445,19 @@ int upload_materials(ftgpu_model *m) {
     q.ce = ce;
     q.inv_ce = R(1.0 / ce);
     q.mat = m->materialID[p];
+    if (q.mat == 6) {
+      // binomial coefficients of (1+x)^(alpha/2-1) and (1+x)^(alpha/2), powers 1..n
+      const double a = pr[3];
+      double ba = 1.0, bb = 1.0;
+      for (int k = 0; k < kOgdenSeries; ++k) {
+        ba *= (a / 2.0 - 1.0 - k) / (k + 1.0);
+        bb *= (a / 2.0 - k) / (k + 1.0);
+        q.ser_a[k] = R(ba);
+        q.ser_b[k] = R(bb);
+      }
+      // FP32 path: series while |2E|_F < 0.04; FP64 mode keeps the eigen path
+      q.ser_thr2 = sizeof(R) == 4 ? R(0.04 * 0.04) : R(0);
+    }
     t[p] = q;
   }
   return m->mats.upload(t.data(), t.size());

@@ -181,82 +181,111 @@ __device__ __forceinline__ void hex_element(const R (&x)[8][3], const R (&u)[8][
                                             const R (&a0)[3], R *hist, long long hs,
                                             long long gs, bool dt_only, R (&f)[8][3], R &le,
                                             int &bad, const ElemArgs<R> &A, long long gpo) {
-  R hu[7][3];
+  // characteristic length on the current geometry first (volume / max face
+  // area, CalculateCharacteristicLength_C3D8.cpp:6-29) so that the nodal
+  // values are dead before the Gauss loop; the 2x2x2 Gauss sum of
+  // det(dx/dxi) below is the exact volume of the trilinear hexahedron.
+  R amax;
+  {
+    R xc[8][3];
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) xc[a][d] = x[a][d] + u[a][d];
+    amax = hex_face_area(xc, 0, 1, 2, 3);
+    amax = fmax(amax, hex_face_area(xc, 4, 5, 6, 7));
+    amax = fmax(amax, hex_face_area(xc, 0, 3, 7, 4));
+    amax = fmax(amax, hex_face_area(xc, 1, 2, 6, 5));
+    amax = fmax(amax, hex_face_area(xc, 0, 1, 5, 4));
+    amax = fmax(amax, hex_face_area(xc, 3, 2, 6, 7));
+  }
+  R hx[7][3], hu[7][3];
+  hex_hadamard(x, hx);
+  hex_hadamard(u, hu);
   R vol = 0;
   R m[7][3];
 #pragma unroll
   for (int i = 0; i < 7; ++i) m[i][0] = m[i][1] = m[i][2] = 0;
-  if (!dt_only) {
-    R hx[7][3];
-    hex_hadamard(x, hx);
-    hex_hadamard(u, hu);
-    // Gauss point order of GaussQuadrature3D.cpp:17-58, literal as there
-    constexpr int sg[8][3] = {{-1, -1, 1}, {1, -1, 1}, {1, 1, 1}, {-1, 1, 1},
-                              {-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1}};
-    const R G = R(0.577350269189626);
+  const R G = R(0.577350269189626);
+  // Gauss points in the order of GaussQuadrature3D.cpp:17-58 (literal as
+  // there): xi > 0 for g in {1,2,5,6}, eta > 0 for {2,3,6,7}, zeta > 0 for g < 4.
+  // The loop is not unrolled: one Gauss point's code stays in the
+  // instruction cache and its temporaries are the only ones live.
+#pragma unroll 1
+  for (int g = 0; g < 8; ++g) {
+    const R xi = ((g + 1) & 2) ? G : -G, et = (g & 2) ? G : -G, ze = g < 4 ? G : -G;
+    const R ez = et * ze, xz = xi * ze, xe = xi * et;
+    R Am[3][3], H[3][3];
 #pragma unroll
-    for (int g = 0; g < 8; ++g) {
-      const R xi = sg[g][0] * G, et = sg[g][1] * G, ze = sg[g][2] * G;
-      const R ez = et * ze, xz = xi * ze, xe = xi * et;
-      R Am[3][3], H[3][3];
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        Am[0][d] = hx[0][d] + et * hx[3][d] + ze * hx[4][d] + ez * hx[6][d];
-        Am[1][d] = hx[1][d] + xi * hx[3][d] + ze * hx[5][d] + xz * hx[6][d];
-        Am[2][d] = hx[2][d] + xi * hx[4][d] + et * hx[5][d] + xe * hx[6][d];
-        H[d][0] = hu[0][d] + et * hu[3][d] + ze * hu[4][d] + ez * hu[6][d];
-        H[d][1] = hu[1][d] + xi * hu[3][d] + ze * hu[5][d] + xz * hu[6][d];
-        H[d][2] = hu[2][d] + xi * hu[4][d] + et * hu[5][d] + xe * hu[6][d];
-      }
-      R Ad[3][3], detA;
-      adj3(Am, Ad, detA);
-      const R idet = 1 / detA;
-      R D[3][3];  // D = H A^{-T} = H adj(A)^T / det A
-#pragma unroll
-      for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j)
-          D[i][j] = idet * (H[i][0] * Ad[j][0] + H[i][1] * Ad[j][1] + H[i][2] * Ad[j][2]);
-      const R Jm1 = jm1_of(D);
-      if (!(Jm1 > R(-1)) || !(detA != 0)) bad = 1;
-      vol += (1 + Jm1) * detA;
-      Sym6<R> S = stress_at<R, MAT>(mp, D, Jm1, a0, hist + g * gs, hs, pc);
-      if (GP) {
-        long long q = gpo + g;
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-          for (int j = 0; j < 3; ++j) A.gpF[9 * q + i + 3 * j] = double((i == j ? R(1) : R(0)) + D[i][j]);
-        A.gpJ[q] = double(1 + Jm1);
-        A.gpS[6 * q + 0] = S.xx;
-        A.gpS[6 * q + 1] = S.yy;
-        A.gpS[6 * q + 2] = S.zz;
-        A.gpS[6 * q + 3] = S.yz;
-        A.gpS[6 * q + 4] = S.xz;
-        A.gpS[6 * q + 5] = S.xy;
-      }
-      // P = F S = S + D S ; Gm = P adj(A)  (w = 1; det A cancels A^{-1})
-      const R s[3][3] = {{S.xx, S.xy, S.xz}, {S.xy, S.yy, S.yz}, {S.xz, S.yz, S.zz}};
-      R P[3][3];
-#pragma unroll
-      for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j)
-          P[i][j] = s[i][j] + D[i][0] * s[0][j] + D[i][1] * s[1][j] + D[i][2] * s[2][j];
-#pragma unroll
-      for (int i = 0; i < 3; ++i) {
-        R g0 = P[i][0] * Ad[0][0] + P[i][1] * Ad[1][0] + P[i][2] * Ad[2][0];
-        R g1 = P[i][0] * Ad[0][1] + P[i][1] * Ad[1][1] + P[i][2] * Ad[2][1];
-        R g2 = P[i][0] * Ad[0][2] + P[i][1] * Ad[1][2] + P[i][2] * Ad[2][2];
-        m[0][i] += g0;
-        m[1][i] += g1;
-        m[2][i] += g2;
-        m[3][i] += et * g0 + xi * g1;
-        m[4][i] += ze * g0 + xi * g2;
-        m[5][i] += ze * g1 + et * g2;
-        m[6][i] += ez * g0 + xz * g1 + xe * g2;
-      }
+    for (int d = 0; d < 3; ++d) {
+      Am[0][d] = hx[0][d] + et * hx[3][d] + ze * hx[4][d] + ez * hx[6][d];
+      Am[1][d] = hx[1][d] + xi * hx[3][d] + ze * hx[5][d] + xz * hx[6][d];
+      Am[2][d] = hx[2][d] + xi * hx[4][d] + et * hx[5][d] + xe * hx[6][d];
+      H[d][0] = hu[0][d] + et * hu[3][d] + ze * hu[4][d] + ez * hu[6][d];
+      H[d][1] = hu[1][d] + xi * hu[3][d] + ze * hu[5][d] + xz * hu[6][d];
+      H[d][2] = hu[2][d] + xi * hu[4][d] + et * hu[5][d] + xe * hu[6][d];
     }
+    R Ad[3][3], detA;
+    adj3(Am, Ad, detA);
+    if (dt_only) {
+      // current Jacobian = reference Jacobian + displacement derivatives
+      R Ac[3][3], Adc[3][3], detc;
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) Ac[i][d] = Am[i][d] + H[d][i];
+      adj3(Ac, Adc, detc);
+      vol += detc;
+      continue;
+    }
+    const R idet = 1 / detA;
+    R D[3][3];  // D = H A^{-T} = H adj(A)^T / det A
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        D[i][j] = idet * (H[i][0] * Ad[j][0] + H[i][1] * Ad[j][1] + H[i][2] * Ad[j][2]);
+    const R Jm1 = jm1_of(D);
+    if (!(Jm1 > R(-1)) || !(detA != 0)) bad = 1;
+    vol += (1 + Jm1) * detA;
+    Sym6<R> S = stress_at<R, MAT>(mp, D, Jm1, a0, hist + g * gs, hs, pc);
+    if (GP) {
+      long long q = gpo + g;
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) A.gpF[9 * q + i + 3 * j] = double((i == j ? R(1) : R(0)) + D[i][j]);
+      A.gpJ[q] = double(1 + Jm1);
+      A.gpS[6 * q + 0] = S.xx;
+      A.gpS[6 * q + 1] = S.yy;
+      A.gpS[6 * q + 2] = S.zz;
+      A.gpS[6 * q + 3] = S.yz;
+      A.gpS[6 * q + 4] = S.xz;
+      A.gpS[6 * q + 5] = S.xy;
+    }
+    // P = F S = S + D S ; Gm = P adj(A)  (w = 1; det A cancels A^{-1})
+    const R s[3][3] = {{S.xx, S.xy, S.xz}, {S.xy, S.yy, S.yz}, {S.xz, S.yz, S.zz}};
+    R P[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        P[i][j] = s[i][j] + D[i][0] * s[0][j] + D[i][1] * s[1][j] + D[i][2] * s[2][j];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      R g0 = P[i][0] * Ad[0][0] + P[i][1] * Ad[1][0] + P[i][2] * Ad[2][0];
+      R g1 = P[i][0] * Ad[0][1] + P[i][1] * Ad[1][1] + P[i][2] * Ad[2][1];
+      R g2 = P[i][0] * Ad[0][2] + P[i][1] * Ad[1][2] + P[i][2] * Ad[2][2];
+      m[0][i] += g0;
+      m[1][i] += g1;
+      m[2][i] += g2;
+      m[3][i] += et * g0 + xi * g1;
+      m[4][i] += ze * g0 + xi * g2;
+      m[5][i] += ze * g1 + et * g2;
+      m[6][i] += ez * g0 + xz * g1 + xe * g2;
+    }
+  }
+  if (!dt_only) {
     // inverse transform: f_a = 1/8 sum_k sign_k(a) m_k
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
@@ -276,41 +305,6 @@ __device__ __forceinline__ void hex_element(const R (&x)[8][3], const R (&u)[8][
       f[7][i] = q * (Qpp - Ppp);
     }
   }
-  // characteristic length on the current geometry: volume / max face area
-  // (CalculateCharacteristicLength_C3D8.cpp:6-29); the 2x2x2 Gauss sum of
-  // det(dx/dxi) is the exact volume of the trilinear hexahedron.
-  R xc[8][3];
-#pragma unroll
-  for (int a = 0; a < 8; ++a)
-#pragma unroll
-    for (int d = 0; d < 3; ++d) xc[a][d] = x[a][d] + u[a][d];
-  if (dt_only) {
-    R hc[7][3];
-    hex_hadamard(xc, hc);
-    constexpr int sg[8][3] = {{-1, -1, 1}, {1, -1, 1}, {1, 1, 1}, {-1, 1, 1},
-                              {-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1}};
-    const R G = R(0.577350269189626);
-#pragma unroll
-    for (int g = 0; g < 8; ++g) {
-      const R xi = sg[g][0] * G, et = sg[g][1] * G, ze = sg[g][2] * G;
-      R Am[3][3];
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        Am[0][d] = hc[0][d] + et * hc[3][d] + ze * hc[4][d] + et * ze * hc[6][d];
-        Am[1][d] = hc[1][d] + xi * hc[3][d] + ze * hc[5][d] + xi * ze * hc[6][d];
-        Am[2][d] = hc[2][d] + xi * hc[4][d] + et * hc[5][d] + xi * et * hc[6][d];
-      }
-      R Ad[3][3], det;
-      adj3(Am, Ad, det);
-      vol += det;
-    }
-  }
-  R amax = hex_face_area(xc, 0, 1, 2, 3);
-  amax = fmax(amax, hex_face_area(xc, 4, 5, 6, 7));
-  amax = fmax(amax, hex_face_area(xc, 0, 3, 7, 4));
-  amax = fmax(amax, hex_face_area(xc, 1, 2, 6, 5));
-  amax = fmax(amax, hex_face_area(xc, 0, 1, 5, 4));
-  amax = fmax(amax, hex_face_area(xc, 3, 2, 6, 7));
   le = vol / amax;
 }
 
@@ -408,7 +402,10 @@ __device__ __forceinline__ double dt_of<double>(double le, const MatP<double> &m
 }
 
 template <class R, int ET, int MAT, bool GP>
-__global__ void __launch_bounds__(kElemThreads) k_elem(const ElemArgs<R> A, int dt_only) {
+// At most 128 registers per thread (two 256-thread or four 128-thread blocks
+// per SM); only the rarely taken eigen-decomposition fallback of the Ogden law
+// needs more and spills there.
+__global__ void __launch_bounds__(kElemThreads, 2) k_elem(const ElemArgs<R> A, int dt_only) {
   constexpr int NC = ET == 0 ? 8 : 4;
   constexpr int NGP = ET == 0 ? 8 : 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];

@@ -22,6 +22,8 @@ struct Sym6 {
   R xx, yy, zz, yz, xz, xy;
 };
 
+constexpr int kOgdenSeries = 6;  // terms of the small-strain Ogden series
+
 template <class R>
 struct MatP {  // per-part material parameters, precomputed on the host
   R p[9];      // properties[pid*9 + k] converted to R
@@ -30,6 +32,12 @@ struct MatP {  // per-part material parameters, precomputed on the host
   double ce;   // dilatational wave speed in FP64
   int mat;     // material ID
   int pad;
+  // Ogden: binomial coefficients binom(alpha/2 - 1, k) and binom(alpha/2, k),
+  // k = 1..kOgdenSeries, and the squared Frobenius bound on 2E below which
+  // the series is used (0 = always the eigen-decomposition)
+  R ser_a[kOgdenSeries];
+  R ser_b[kOgdenSeries];
+  R ser_thr2;
 };
 
 template <class R> __device__ __forceinline__ R d_log1p(R x);
@@ -331,32 +339,78 @@ __device__ __forceinline__ void jacobi_sym3(Sym6<R> A, R (&w)[3], R (&V)[3][3]) 
     for (int j = 0; j < 3; ++j) V[i][j] = v[i][j];
 }
 
+// symmetric product of two commuting symmetric matrices (powers of one matrix)
+template <class R>
+__device__ __forceinline__ Sym6<R> sym_mul(const Sym6<R> &a, const Sym6<R> &b) {
+  Sym6<R> r;
+  r.xx = a.xx * b.xx + a.xy * b.xy + a.xz * b.xz;
+  r.yy = a.xy * b.xy + a.yy * b.yy + a.yz * b.yz;
+  r.zz = a.xz * b.xz + a.yz * b.yz + a.zz * b.zz;
+  r.yz = a.xy * b.xz + a.yy * b.yz + a.yz * b.zz;
+  r.xz = a.xx * b.xz + a.xy * b.yz + a.xz * b.zz;
+  r.xy = a.xx * b.xy + a.xy * b.yy + a.xz * b.yz;
+  return r;
+}
+
 template <class R>
 __device__ __forceinline__ Sym6<R> mat_ogden(const MatP<R> &m, const R (&D)[3][3], R Jm1) {
   R mu = m.p[1], alpha = m.p[3];
   Sym6<R> e = two_E(D);
-  R w[3], V[3][3];
-  jacobi_sym3<R, sizeof(R) == 4 ? 4 : 6>(e, w, V);
   R lnJ = d_log1p(Jm1);
-  R em[3], mean = 0;
-#pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    R y = R(0.5) * alpha * (d_log1p(w[i]) - R(2.0 / 3.0) * lnJ);  // (alpha/2) ln lbar_i^2
-    em[i] = d_expm1(y);
-    mean += em[i];
-  }
-  mean *= R(1.0 / 3.0);
-  R c = 2 * mu / alpha;
-  R f[3];
-#pragma unroll
-  for (int i = 0; i < 3; ++i) f[i] = c * (em[i] - mean) / (1 + w[i]);
   Sym6<R> S;
-  S.xx = f[0] * V[0][0] * V[0][0] + f[1] * V[0][1] * V[0][1] + f[2] * V[0][2] * V[0][2];
-  S.yy = f[0] * V[1][0] * V[1][0] + f[1] * V[1][1] * V[1][1] + f[2] * V[1][2] * V[1][2];
-  S.zz = f[0] * V[2][0] * V[2][0] + f[1] * V[2][1] * V[2][1] + f[2] * V[2][2] * V[2][2];
-  S.yz = f[0] * V[1][0] * V[2][0] + f[1] * V[1][1] * V[2][1] + f[2] * V[1][2] * V[2][2];
-  S.xz = f[0] * V[0][0] * V[2][0] + f[1] * V[0][1] * V[2][1] + f[2] * V[0][2] * V[2][2];
-  S.xy = f[0] * V[0][0] * V[1][0] + f[1] * V[0][1] * V[1][1] + f[2] * V[0][2] * V[1][2];
+  const R n2 = e.xx * e.xx + e.yy * e.yy + e.zz * e.zz +
+               2 * (e.yz * e.yz + e.xz * e.xz + e.xy * e.xy);
+  if (n2 < m.ser_thr2) {
+    // Small strain: with M = 2E = C - I the isochoric stress is
+    //   S_iso = (2 mu/alpha) J^{-alpha/3} [C^{alpha/2-1} - tr(C^{alpha/2})/3 C^{-1}]
+    //         = c [A - Ci - tr(B)/3 (I + Ci)],
+    // A = (I+M)^{alpha/2-1} - I, B = (I+M)^{alpha/2} - I, Ci = (I+M)^{-1} - I,
+    // each a binomial series in powers of M (exact to FP32 rounding while
+    // |M|_F < 0.04, no eigenvectors, no cancellation of O(1) terms).
+    Sym6<R> P = e;
+    Sym6<R> A = sym_scale(e, m.ser_a[0]);
+    Sym6<R> Ci = sym_scale(e, R(-1));
+    R trB = m.ser_b[0] * (e.xx + e.yy + e.zz);
+#pragma unroll
+    for (int k = 1; k < kOgdenSeries; ++k) {
+      P = sym_mul(P, e);
+      const R sa = m.ser_a[k], sc = (k & 1) ? R(1) : R(-1);
+      A = Sym6<R>{A.xx + sa * P.xx, A.yy + sa * P.yy, A.zz + sa * P.zz, A.yz + sa * P.yz,
+                  A.xz + sa * P.xz, A.xy + sa * P.xy};
+      Ci = Sym6<R>{Ci.xx + sc * P.xx, Ci.yy + sc * P.yy, Ci.zz + sc * P.zz, Ci.yz + sc * P.yz,
+                   Ci.xz + sc * P.xz, Ci.xy + sc * P.xy};
+      trB += m.ser_b[k] * (P.xx + P.yy + P.zz);
+    }
+    const R c = 2 * mu / alpha * d_exp(-alpha * R(1.0 / 3.0) * lnJ);
+    const R t = trB * R(1.0 / 3.0);
+    S.xx = c * (A.xx - Ci.xx - t * (1 + Ci.xx));
+    S.yy = c * (A.yy - Ci.yy - t * (1 + Ci.yy));
+    S.zz = c * (A.zz - Ci.zz - t * (1 + Ci.zz));
+    S.yz = c * (A.yz - Ci.yz - t * Ci.yz);
+    S.xz = c * (A.xz - Ci.xz - t * Ci.xz);
+    S.xy = c * (A.xy - Ci.xy - t * Ci.xy);
+  } else {
+    R w[3], V[3][3];
+    jacobi_sym3<R, sizeof(R) == 4 ? 4 : 6>(e, w, V);
+    R em[3], mean = 0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      R y = R(0.5) * alpha * (d_log1p(w[i]) - R(2.0 / 3.0) * lnJ);  // (alpha/2) ln lbar_i^2
+      em[i] = d_expm1(y);
+      mean += em[i];
+    }
+    mean *= R(1.0 / 3.0);
+    R c = 2 * mu / alpha;
+    R f[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) f[i] = c * (em[i] - mean) / (1 + w[i]);
+    S.xx = f[0] * V[0][0] * V[0][0] + f[1] * V[0][1] * V[0][1] + f[2] * V[0][2] * V[0][2];
+    S.yy = f[0] * V[1][0] * V[1][0] + f[1] * V[1][1] * V[1][1] + f[2] * V[1][2] * V[1][2];
+    S.zz = f[0] * V[2][0] * V[2][0] + f[1] * V[2][1] * V[2][1] + f[2] * V[2][2] * V[2][2];
+    S.yz = f[0] * V[1][0] * V[2][0] + f[1] * V[1][1] * V[2][1] + f[2] * V[1][2] * V[2][2];
+    S.xz = f[0] * V[0][0] * V[2][0] + f[1] * V[0][1] * V[2][1] + f[2] * V[0][2] * V[2][2];
+    S.xy = f[0] * V[0][0] * V[1][0] + f[1] * V[0][1] * V[1][1] + f[2] * V[0][2] * V[1][2];
+  }
   Sym6<R> ac = adj_I_plus(e);
   R J = 1 + Jm1;
   R Jp = R(0.5) * m.K * Jm1 * (2 + Jm1) / (J * J);

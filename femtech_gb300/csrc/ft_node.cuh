@@ -52,6 +52,40 @@ __device__ __forceinline__ void bc_value(const BcFn &b, int d, double t, const d
   }
 }
 
+// Time bookkeeping of one step, as the driver does it on the host
+// (ex9.cpp:107-113,172): t_{n+1} = t_n + dt, t_half = (t_{n+1} + t_n) / 2, the
+// next dt = ExplicitTimeStepReduction * StableTimeStep(), and the stop tests.
+struct StepScalars {
+  double t_np1, t_np2, ndt;
+  double c1;   // t_{n+1} - t_half         (full-step velocity)
+  double c2;   // t_half' - t_{n+1}        (next half-step velocity)
+  double c12;  // t_half' - t_half         (both at once)
+  int done;
+  bool advance;
+};
+
+__device__ __forceinline__ StepScalars step_scalars(const Clock &ck, const InstParams &ip,
+                                                    unsigned long long dtbits, int mode) {
+  StepScalars s;
+  const double t_n = ck.time, dt = ck.dt;
+  s.t_np1 = t_n + dt;
+  const double t_half = 0.5 * (s.t_np1 + t_n);
+  const double raw = __longlong_as_double((long long)dtbits);
+  s.ndt = ip.reduction * raw;
+  int done = 0;
+  if (!(s.t_np1 < ip.tmax)) done |= 1;
+  if (ck.step + 1 >= ip.step_limit) done |= 2;
+  if (raw < ip.failure_dt) done |= 4;
+  s.done = done;
+  s.advance = (mode == kNodeFused) && !done;
+  s.t_np2 = s.t_np1 + s.ndt;
+  const double t_half2 = 0.5 * (s.t_np2 + s.t_np1);
+  s.c1 = s.t_np1 - t_half;
+  s.c2 = t_half2 - s.t_np1;
+  s.c12 = t_half2 - t_half;
+  return s;
+}
+
 template <class R>
 __global__ void __launch_bounds__(256) k_node(const NodeArgs A) {
   const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -126,6 +160,36 @@ __global__ void __launch_bounds__(256) k_node(const NodeArgs A) {
     return;
   }
 
+}
+
+// End of step n (mode kNodeFused also starts step n+1; kNodeFinish stops
+// there).  The step scalars are computed once per block by thread 0 for the
+// instance of the block's first node; nodes of another instance (blocks that
+// straddle two instances of a batch) compute their own.
+template <class R>
+__global__ void __launch_bounds__(256) k_node_step(const NodeArgs A) {
+  __shared__ StepScalars shs;
+  __shared__ Clock shck;
+  __shared__ int shinst;
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (threadIdx.x == 0) {
+    const long long n0 = (long long)blockIdx.x * blockDim.x;
+    const int i0 = A.node_inst ? A.node_inst[n0] : 0;
+    shck = A.clock[A.parity * A.ninst + i0];
+    shs = step_scalars(shck, A.inst[i0], A.dtmin[A.parity * A.ninst + i0], A.mode);
+    shinst = i0;
+  }
+  __syncthreads();
+  if (n >= A.N) return;
+  const int inst = A.node_inst ? A.node_inst[n] : 0;
+  const bool same = inst == shinst;
+  const InstParams &ip = A.inst[inst];
+  const bool leader = (n == ip.node_begin);
+  const R *sF = reinterpret_cast<const R *>(A.sF);
+  R *sU = reinterpret_cast<R *>(A.sU);
+  const int sb = A.slot_off[n], se = A.slot_off[n + 1];
+  const long long N = A.N, S = A.S;
+  const Clock ck = same ? shck : A.clock[A.parity * A.ninst + inst];
   // kNodeFused / kNodeFinish: end of step n (+ start of step n+1 when fused)
   Clock *nxt = A.clock + (A.parity ^ 1) * A.ninst + inst;
   if (ck.done) {
@@ -136,37 +200,46 @@ __global__ void __launch_bounds__(256) k_node(const NodeArgs A) {
     }
     return;
   }
-  const double t_n = ck.time, dt = ck.dt, t_np1 = t_n + dt, t_half = 0.5 * (t_np1 + t_n);
-  const double raw = __longlong_as_double((long long)A.dtmin[A.parity * A.ninst + inst]);
-  const double ndt = ip.reduction * raw;
-  int done = 0;
-  if (!(t_np1 < ip.tmax)) done |= 1;
-  if (ck.step + 1 >= ip.step_limit) done |= 2;
-  if (raw < ip.failure_dt) done |= 4;
-  const bool advance = (A.mode == kNodeFused) && !done;
-  const double t_np2 = t_np1 + ndt, t_half2 = 0.5 * (t_np2 + t_np1);
+  const StepScalars sc =
+      same ? shs : step_scalars(ck, ip, A.dtmin[A.parity * A.ninst + inst], A.mode);
+  const bool advance = sc.advance;
+  constexpr bool kF64 = sizeof(R) == 8;
+  // sum of the patch partials in slot order (in the element precision)
+  R fs0 = 0, fs1 = 0, fs2 = 0;
+  for (int k = sb; k < se; ++k) {
+    const int s = A.slots[k];
+    fs0 += sF[s];
+    fs1 += sF[S + s];
+    fs2 += sF[2 * S + s];
+  }
+  const double fsum[3] = {double(fs0), double(fs1), double(fs2)};
+  const double minv = kF64 ? 0.0 : A.minv[n];
   double un[3];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const int fn = A.nbc[d * N + n];
     double u = A.u[d * N + n];
     if (fn == kBcFree) {
-      double f = 0.0;
-      for (int k = sb; k < se; ++k) f += double(sF[d * S + A.slots[k]]);
-      const double acc = A.fp64 ? -f / A.mass[n] : -f * A.minv[n];
-      const double vel = A.vh[d * N + n] + (t_np1 - t_half) * acc;
+      const double acc = kF64 ? -fsum[d] / A.mass[n] : -fsum[d] * minv;
+      const double vh = A.vh[d * N + n];
       if (advance) {
-        const double vh2 = vel + (t_half2 - t_np1) * acc;
-        u = u + ndt * vh2;
+        double vh2;
+        if (kF64) {  // the two half-step updates of ex9.cpp:147-152 and :116-123
+          const double vel = vh + sc.c1 * acc;
+          vh2 = vel + sc.c2 * acc;
+        } else {  // one update with the combined coefficient t_half' - t_half
+          vh2 = vh + sc.c12 * acc;
+        }
+        u = u + sc.ndt * vh2;
         A.vh[d * N + n] = vh2;
         A.u[d * N + n] = u;
       } else {
-        A.v[d * N + n] = vel;
+        A.v[d * N + n] = vh + sc.c1 * acc;
         A.a[d * N + n] = acc;
       }
     } else if (fn >= 0 && advance) {
       double vb;
-      bc_value(A.fns[fn], d, t_np2, A.X, N, n, u, vb);
+      bc_value(A.fns[fn], d, sc.t_np2, A.X, N, n, u, vb);
       A.u[d * N + n] = u;
       A.v[d * N + n] = vb;
       A.a[d * N + n] = 0.0;
@@ -174,19 +247,21 @@ __global__ void __launch_bounds__(256) k_node(const NodeArgs A) {
     un[d] = u;
   }
   if (advance) {
+    const R r0 = R(un[0]), r1 = R(un[1]), r2 = R(un[2]);
     for (int k = sb; k < se; ++k) {
       const int s = A.slots[k];
-#pragma unroll
-      for (int d = 0; d < 3; ++d) sU[d * S + s] = R(un[d]);
+      sU[s] = r0;
+      sU[S + s] = r1;
+      sU[2 * S + s] = r2;
     }
   }
   if (leader) {
     Clock c;
-    c.time = t_np1;
-    c.dt = ndt;
+    c.time = sc.t_np1;
+    c.dt = sc.ndt;
     c.step = ck.step + 1;
-    c.done = done;
-    c.err = (done & 4) ? kErrDt : 0;
+    c.done = sc.done;
+    c.err = (sc.done & 4) ? kErrDt : 0;
     *nxt = c;
     A.dtmin[(A.parity ^ 1) * A.ninst + inst] = kDtHugeBits;
   }
