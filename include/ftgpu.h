@@ -183,6 +183,26 @@ int ftgpu_launches_per_step(ftgpu_model *m);
 /* Synchronise and return the device error word (0 = none). */
 int ftgpu_check(ftgpu_model *m);
 
+/* ---- allocation-free internal force (no counterpart in the reference) ----
+ * For callers that cannot let a library allocate device memory (they own all
+ * of it, e.g. through their own pool, or run under a fixed budget): the C3D8
+ * internal force fi of one material on caller-owned DEVICE arrays in the
+ * reference layout -- coordinates[3*nNodes], connectivity[8*nelements],
+ * u[3*nNodes], and the node -> element-corner map node_elem_ptr[nNodes+1] /
+ * node_elem_ent[8*nelements] (entries e*8+corner, summed in the given
+ * order) -- written to fi[3*nNodes] (device).  properties: 9 host doubles.
+ * Materials 0-4 and 6 (the viscoelastic laws need per-call state).  No
+ * cudaMalloc/cudaFree: the corner-force scratch is a static device array
+ * holding FTGPU_NOALLOC_MAX_ELEMENTS elements; larger meshes are rejected
+ * with FTGPU_ERR_INPUT.  The first call on a device looks up that array's
+ * address (make it before any stream capture).  All calls share the array,
+ * so calls that overlap on the GPU race; the call waits for its stream. */
+#define FTGPU_NOALLOC_MAX_ELEMENTS 32768
+int ftgpu_hex8_force_noalloc(int nNodes, int nelements, const double *coordinates,
+                             const int *connectivity, const int *node_elem_ptr,
+                             const int *node_elem_ent, const double *u, int materialID,
+                             const double *properties, double *fi, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
