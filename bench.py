@@ -54,15 +54,15 @@ WORKLOAD = "ogden_hex8_block_200x200x100_jitter10_sine50Hz"
 ELEM_BYTES_PER_EL = 32.0
 ELEM_BYTES_PER_NODE = 36.0
 NODE_BYTES_PER_NODE = 116.0
-# FP32 operations of one C3D8 Ogden element-update in this formulation,
-# counted from the kernel source (ft_elem.cuh / ft_materials.cuh), FMA = 2:
-#   Hadamard transforms 2 x 72 adds; per Gauss point: Jacobian and
-#   displacement-gradient columns 2 x 54, adj(A) 45, D = H adj^T / det 63,
-#   J - 1 30, 2E 39, Jacobi eigen (4 sweeps x 3 rotations x 58) 696,
-#   principal functions 45, S 60, P = S + D S 54, P adj(A) 45, moments 48
-#   -> 1233 per Gauss point; 8 points 9864; inverse transform 84; face areas
-#   and volume 550.
-FLOP_PER_EL_OGDEN = 144 + 9864 + 84 + 550
+# FP32 operations of one C3D8 Ogden element-update in this formulation
+# (small-strain series path), counted from the kernel source (ft_elem.cuh /
+# ft_materials.cuh), FMA = 2: per Gauss point Jacobian and displacement-
+# gradient columns 108, adj/det 32, D = H adj^T / det 63, J - 1 27, Ogden
+# series law 428 (2E 40, norm 11, five symmetric powers with the A / Ci / tr B
+# updates 290, J^-alpha/3 5, S 30, volumetric 37, start 15), P = S + D S 54,
+# P adj 45, moments 63 -> 820 per Gauss point, 6560 for 8; Hadamard
+# transforms 150, face areas 540, inverse transform 90.
+FLOP_PER_EL_OGDEN = 6560 + 150 + 540 + 90
 
 
 def log(*a):
