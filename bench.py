@@ -192,11 +192,13 @@ def run_reference_arm(args, rank, world):
     if not os.path.exists(orc.LIB):
         orc.build()
     kind = "reference" if orc.RefBuild.available() else "port"
-    # W + K bounded samples; the value is the rate of the timed ones
+    # bounded samples (each a few seconds of every host thread): up to two
+    # short warm-up samples, then up to three timed ones; value = their mean
+    warm = min(max(args.warmup, 0), 2)
     rates = []
-    for i in range(max(args.warmup, 0) + max(1, min(args.steps, 3))):
-        r = cpu_reference_rate(threads, target_s=8.0 if i >= args.warmup else 2.0, kind=kind)
-        if i >= args.warmup:
+    for i in range(warm + max(1, min(args.steps, 3))):
+        r = cpu_reference_rate(threads, target_s=8.0 if i >= warm else 2.0, kind=kind)
+        if i >= warm:
             rates.append(r)
     v = float(np.mean([r["value"] for r in rates]))
     base = rates[-1]
@@ -211,14 +213,57 @@ def run_reference_arm(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def make_workload(name, size=None):
+    """Mesh, materials, loads, instances and the traffic / flop model of one
+    benchmark configuration."""
+    from femtech_gb300 import meshgen as mg
+    if name == "block":
+        nx, ny, nz = NX, NY, NZ
+        if size:
+            nx, ny, nz = (int(x) for x in size.split(","))
+        mesh, mats, loads = build_workload(nx, ny, nz, LX * nx / NX, LY * ny / NY, LZ * nz / NZ)
+        E, N = len(mesh["etype"]), len(mesh["coordinates"])
+        return dict(mesh=mesh, mats=mats, loads=loads, instances=None,
+                    label=WORKLOAD if not size else "ogden_hex8_block_%dx%dx%d" % (nx, ny, nz),
+                    elem_bytes=E * ELEM_BYTES_PER_EL + N * ELEM_BYTES_PER_NODE,
+                    flop=FLOP_PER_EL_OGDEN * E, kernel="k_elem<float,C3D8,Ogden>",
+                    material="ogden mu=1.5e3 alpha=5 K=2e7 rho=1040")
+    if name == "head":
+        target = int(size) if size else 2_000_000
+        mesh, mats, loads = mg.head_case(target_elements=target)
+        E, N = len(mesh["etype"]), len(mesh["coordinates"])
+        inner = int((mesh["pid"] == 1).sum())
+        # C3D4: connectivity 16 B + part 4 B per element; interior fibre 12 B and
+        # Prony history (H, S0: 12 f32) read + written 96 B; nodes as above
+        eb = E * (16 + 4) + inner * (12 + 96) + N * ELEM_BYTES_PER_NODE
+        return dict(mesh=mesh, mats=mats, loads=loads, instances=None,
+                    label="head_tet4_ellipsoid_%dk_shell_NH_core_GOH_prony_rotation" % (E // 1000),
+                    elem_bytes=eb, flop=None, kernel="k_elem<float,C3D4,NH|GOH+Prony>",
+                    material="shell NH E=6GPa nu=0.3; core GOH mu=1kPa k1=5kPa k2=10 kappa=0.1 "
+                             "lambda=2.19e8 + Prony g1=0.6 tau1=6ms")
+    if name == "ensemble":
+        n = int(size) if size else 256
+        mesh, mats, loads, off = mg.ensemble_case(n_instances=n)
+        E, N = len(mesh["etype"]), len(mesh["coordinates"])
+        inst = dict(node_offset=off, tmax=np.full(n, 1e300), reduction=np.full(n, 0.9))
+        return dict(mesh=mesh, mats=mats, loads=loads, instances=inst,
+                    label="ensemble_%d_ogden_hex8_blocks_4k_250k" % n,
+                    elem_bytes=E * ELEM_BYTES_PER_EL + N * ELEM_BYTES_PER_NODE,
+                    flop=FLOP_PER_EL_OGDEN * E, kernel="k_elem<float,C3D8,Ogden> (all instances)",
+                    material="ogden per instance mu~U[0.5,5]kPa alpha~U[-5,8] K~U[2,50]MPa")
+    raise SystemExit("unknown workload " + name)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="block", choices=["block", "head", "ensemble"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--size", default=None, help="nx,ny,nz override (smaller cases for profiling)")
+    ap.add_argument("--size", default=None,
+                    help="block: nx,ny,nz; head: target elements; ensemble: instances")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
@@ -234,15 +279,13 @@ def main():
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
     dev = local
-    nx, ny, nz = NX, NY, NZ
-    if args.size:
-        nx, ny, nz = (int(x) for x in args.size.split(","))
-    lx, ly, lz = LX * nx / NX, LY * ny / NY, LZ * nz / NZ
     t0 = time.perf_counter()
-    mesh, mats, loads = build_workload(nx, ny, nz, lx, ly, lz)
+    wl = make_workload(args.workload, args.size)
+    mesh, mats, loads = wl["mesh"], wl["mats"], wl["loads"]
     E = len(mesh["etype"])
     N = len(mesh["coordinates"])
-    model = ft.Model(mesh, mats, precision=ft.MIXED, device=dev, loads=loads)
+    model = ft.Model(mesh, mats, precision=ft.MIXED, device=dev, loads=loads,
+                     instances=wl["instances"])
     log("setup %.1f s (%d elements, %d nodes)" % (time.perf_counter() - t0, E, N))
     model.init_explicit(reduction=0.9, failure_dt=0.0, tmax=1e300)
     model.run(args.warmup)
@@ -272,45 +315,48 @@ def main():
     elem_ms = em.value / max(sd.value, 1)
     node_ms = nm.value / max(sd.value, 1)
     hbm, peak_kind = peaks()
-    elem_bytes = E * ELEM_BYTES_PER_EL + N * ELEM_BYTES_PER_NODE
+    elem_bytes = wl["elem_bytes"]
     node_bytes = N * NODE_BYTES_PER_NODE
     if elem_ms >= node_ms:
-        dom, dom_ms, dom_bytes = "k_elem<float,C3D8,Ogden> (all patches of one step)", elem_ms, elem_bytes
+        dom, dom_ms, dom_bytes = wl["kernel"] + " (one element pass)", elem_ms, elem_bytes
     else:
-        dom, dom_ms, dom_bytes = "k_node<float> fused update", node_ms, node_bytes
+        dom, dom_ms, dom_bytes = "k_node_step<float> fused update", node_ms, node_bytes
     achieved = dom_bytes / (dom_ms / 1e3) / 1e9
-    traffic = load_traffic(E)
+    traffic = load_traffic(args.workload, E) if dom_ms == elem_ms else None
     sm_mhz = clocks.get("sm_mhz") or 2070.0
     fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
-    fp32_ach = FLOP_PER_EL_OGDEN * E / (elem_ms / 1e3) / 1e12
+    fp32 = None
+    if wl["flop"]:
+        fp32_ach = wl["flop"] / (elem_ms / 1e3) / 1e12
+        fp32 = {"achieved": fp32_ach, "peak": fp32_peak, "unit": "TFLOP/s",
+                "frac": fp32_ach / fp32_peak,
+                "peak_source": "nominal 152 SM x 128 lanes x 2 x median SM clock",
+                "flop_per_element": wl["flop"] / E}
 
     # ---- end to end through the C ABI with host buffers ----
-    e2e = end_to_end(ft, mesh, mats, loads, dev, args.steps, E, N)
+    e2e = end_to_end(ft, wl, dev, args.steps, E, N)
 
     line = {
         "metric": "element-updates/s", "value": value, "unit": "element-updates/s",
         "n_gpus": world, "steps": steps, "warmup": args.warmup,
         "ms_per_step": ms / max(steps, 1), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 element kernels / f64 nodal state",
-        "data": "synthetic (seeded jittered block, generated in-run)",
-        "config": {"workload": WORKLOAD if not args.size else "ogden_hex8_block_%dx%dx%d" % (nx, ny, nz),
-                   "elements": E, "nodes": N, "material": "ogden mu=1.5e3 alpha=5 K=2e7 rho=1040",
-                   "precision": "mixed", "l2": "inputs larger than L2 (%.2f GB resident)" %
-                   ((E * 48 + N * 140) / 1e9),
+        "data": "synthetic (seeded, generated in-run)",
+        "config": {"workload": wl["label"], "elements": E, "nodes": N,
+                   "material": wl["material"], "precision": "mixed",
+                   "l2": "inputs larger than L2 (%.2f GB resident)" % ((E * 48 + N * 140) / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "gpu_launches": launches,
         "clocks": clocks,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
                      "unit": "GB/s", "frac": achieved / hbm, "peak_source": peak_kind,
-                     "traffic": None if traffic is None else traffic * (1.0 if dom.startswith("k_elem") else 0.0) or None,
-                     "algorithmic_bytes_per_launch": dom_bytes,
+                     "traffic": traffic, "algorithmic_bytes_per_launch": dom_bytes,
                      "launch_ms": dom_ms, "elem_pass_ms": elem_ms, "node_pass_ms": node_ms,
-                     "fp32": {"achieved": fp32_ach, "peak": fp32_peak, "unit": "TFLOP/s",
-                              "frac": fp32_ach / fp32_peak, "peak_source": "nominal 152 SM x 128 lanes x 2 x median SM clock",
-                              "flop_per_element": FLOP_PER_EL_OGDEN}},
+                     "node_pass_algorithmic_gbs": node_bytes / (node_ms / 1e3) / 1e9,
+                     "fp32": fp32},
         "e2e": e2e,
     }
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and args.workload == "block":
         line["cpu_baseline"] = cpu_reference_rate(os.cpu_count() or 1)
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -327,11 +373,12 @@ def timed_run(model, steps):
     return sd.value, ms.value
 
 
-def end_to_end(ft, mesh, mats, loads, dev, steps, E, N):
+def end_to_end(ft, wl, dev, steps, E, N):
     """Public-API run with host buffers: upload the initial state from host
     memory, run the loop, read all displacements back every 100 steps."""
     import torch
-    model = ft.Model(mesh, mats, precision=ft.MIXED, device=dev, loads=loads)
+    model = ft.Model(wl["mesh"], wl["mats"], precision=ft.MIXED, device=dev, loads=wl["loads"],
+                     instances=wl["instances"])
     u0 = torch.zeros(3 * N, dtype=torch.float64).pin_memory().numpy()
     v0 = torch.zeros(3 * N, dtype=torch.float64).pin_memory().numpy()
     a0 = torch.zeros(3 * N, dtype=torch.float64).pin_memory().numpy()
@@ -361,15 +408,17 @@ def end_to_end(ft, mesh, mats, loads, dev, steps, E, N):
                     "back every %d steps" % every}
 
 
-def load_traffic(E):
-    """DRAM bytes per element pass from the committed ncu summary, scaled by
-    element count (traffic grows in proportion to the elements processed)."""
+def load_traffic(workload, E):
+    """DRAM bytes of one element pass from the committed ncu summary
+    (profiles/traffic.json, bytes per element of a smaller capture of the same
+    kernel), scaled by the element count: traffic grows in proportion to the
+    elements processed."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     if not os.path.exists(p):
         return None
     with open(p) as f:
         d = json.load(f)
-    b = d.get("elem_pass_dram_bytes_per_element")
+    b = d.get(workload, {}).get("elem_pass_dram_bytes_per_element")
     return None if b is None else b * E
 
 

@@ -192,6 +192,7 @@ struct ftgpu_model {
   std::vector<InstParams> inst;
   bool inst_set = false;
   int patch_elems = 0;
+  int node_threads = 256;
   bool setup_done = false, init_done = false;
   PatchSet ps;
   std::vector<int> gp_off;  // reference Gauss-point offset of each element
@@ -317,7 +318,7 @@ NodeArgs node_args(ftgpu_model *m, int mode, int parity) {
 
 int launch_node(ftgpu_model *m, int mode, int parity) {
   NodeArgs A = node_args(m, mode, parity);
-  const int th = 256;
+  const int th = m->node_threads;
   const long long nb = (m->nNodes + th - 1) / th;
   const bool step = mode == kNodeFused || mode == kNodeFinish;
   if (is_fp64(m)) {
@@ -899,6 +900,15 @@ int ftgpu_set_patch_size(ftgpu_model *m, int pe) {
   if (!m || pe < 0 || pe > kMaxPatchElems) return fail(FTGPU_ERR_INPUT, "set_patch_size");
   m->patch_elems = pe;
   m->setup_done = false;
+  return FTGPU_OK;
+}
+
+int ftgpu_set_node_threads(ftgpu_model *m, int threads) {
+  if (!m) return fail(FTGPU_ERR_INPUT, "set_node_threads");
+  if (threads == 0) threads = 256;
+  if (threads < 64 || threads > 512 || threads % 32) return fail(FTGPU_ERR_INPUT, "node threads");
+  m->node_threads = threads;
+  drop_graphs(m);
   return FTGPU_OK;
 }
 

@@ -87,7 +87,7 @@ __device__ __forceinline__ StepScalars step_scalars(const Clock &ck, const InstP
 }
 
 template <class R>
-__global__ void __launch_bounds__(256) k_node(const NodeArgs A) {
+__global__ void __launch_bounds__(512) k_node(const NodeArgs A) {
   const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= A.N) return;
   const int inst = A.node_inst ? A.node_inst[n] : 0;
@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(256) k_node(const NodeArgs A) {
 // instance of the block's first node; nodes of another instance (blocks that
 // straddle two instances of a batch) compute their own.
 template <class R>
-__global__ void __launch_bounds__(256) k_node_step(const NodeArgs A) {
+__global__ void __launch_bounds__(512) k_node_step(const NodeArgs A) {
   __shared__ StepScalars shs;
   __shared__ Clock shck;
   __shared__ int shinst;

@@ -181,6 +181,106 @@ def cube_tension_case(n=10, size=0.01, rho=1000.0, mu=3400.0, K=2.0e6, strain=0.
     return mesh, mats, loads
 
 
+def boundary_nodes_tet(conn):
+    """Nodes on the boundary of a C3D4 mesh (faces used by exactly one tet)."""
+    T = np.asarray(conn).reshape(-1, 4)
+    faces = np.concatenate([T[:, [1, 2, 3]], T[:, [0, 2, 3]], T[:, [0, 1, 3]], T[:, [0, 1, 2]]])
+    faces = np.sort(faces, axis=1)
+    uniq, cnt = np.unique(faces, axis=0, return_counts=True)
+    return np.unique(uniq[cnt == 1])
+
+
+def smooth_fibers(X, seed=0, modes=6, scale=0.05):
+    """Unit fibre directions from a seeded smooth random field: a sum of a few
+    random Fourier modes per component, normalised."""
+    rng = np.random.default_rng(seed)
+    a = np.zeros_like(X)
+    for _ in range(modes):
+        k = rng.normal(0.0, 1.0 / scale, 3)
+        ph = rng.uniform(0, 2 * np.pi, 3)
+        amp = rng.normal(0.0, 1.0, 3)
+        a += amp * np.sin(X @ k[:, None] + ph)
+    n = np.linalg.norm(a, axis=1, keepdims=True)
+    a[n[:, 0] < 1e-12] = [1.0, 0.0, 0.0]
+    return a / np.maximum(np.linalg.norm(a, axis=1, keepdims=True), 1e-12)
+
+
+def head_case(a=0.09, b=0.07, c=0.06, h=None, target_elements=2_000_000, shell=0.005, seed=0,
+              E_shell=6.0e9, nu_shell=0.3, rho_shell=2000.0, mu=1.0e3, k1=5.0e3, k2=10.0,
+              kappa=0.1, lam=2.19e8, rho=1040.0, g1=0.6, tau1=6.0e-3, alpha_peak=6.0e3,
+              pulse=0.01):
+    """Head-like C3D4 ellipsoid: outer `shell` layer Neo-Hookean (E, nu given),
+    interior anisotropic GOH (fibre field, dispersion kappa) + 1-term Prony;
+    boundary nodes follow a rigid rotation about a seeded random axis with
+    angular acceleration alpha_peak sin(pi t / pulse) for t <= pulse."""
+    if h is None:  # 6 tets per lattice cube inside the ellipsoid volume
+        vol = 4.0 / 3.0 * np.pi * a * b * c
+        h = (vol * 6.0 / target_elements) ** (1.0 / 3.0)
+    mesh = tet_ellipsoid(a, b, c, h, jitter=0.1, seed=seed)
+    X = mesh["coordinates"]
+    T = mesh["connectivity"].reshape(-1, 4)
+    cen = X[T].mean(1)
+    rho_s = np.sqrt((cen[:, 0] / a) ** 2 + (cen[:, 1] / b) ** 2 + (cen[:, 2] / c) ** 2)
+    depth = np.linalg.norm(cen, axis=1) * (1.0 / np.maximum(rho_s, 1e-9) - 1.0)
+    in_shell = depth < shell
+    mesh["pid"] = np.where(in_shell, 0, 1).astype(np.int32)
+    mesh["fiber"] = smooth_fibers(cen, seed=seed + 1)
+    mu_s = E_shell / (2 * (1 + nu_shell))
+    lam_s = E_shell * nu_shell / ((1 + nu_shell) * (1 - 2 * nu_shell))
+    mats = materials([(1, [rho_shell, mu_s, lam_s]),
+                      (7, [rho, mu, lam, k1, k2, g1, tau1, kappa])])
+    rng = np.random.default_rng(seed + 2)
+    axis = rng.normal(size=3)
+    axis /= np.linalg.norm(axis)
+    loads = Loads(len(X))
+    loads.rotation(boundary_nodes_tet(mesh["connectivity"]), axis, [0.0, 0.0, 0.0], alpha_peak,
+                   pulse)
+    return mesh, mats, loads
+
+
+def ensemble_case(n_instances=256, e_min=4_000, e_max=250_000, seed=0, h=1.0e-3, jitter=0.1):
+    """Batched ensemble of independent C3D8 Ogden blocks: element counts
+    log-uniform in [e_min, e_max], seeded aspect ratios, per-instance
+    mu ~ U[0.5, 5] kPa, alpha ~ U[-5, 8] (|alpha| >= 0.1), K ~ U[2, 50] MPa,
+    top-face shear amplitude ~ U[0.5, 3] mm at 50 Hz, base fixed.  Returns
+    the concatenated mesh, materials (one part per instance), loads and the
+    instance node offsets."""
+    rng = np.random.default_rng(seed)
+    Xs, conns, pids, dofs, fns, parts = [], [], [], [], [], []
+    node_off = [0]
+    for i in range(n_instances):
+        E = int(np.exp(rng.uniform(np.log(e_min), np.log(e_max))))
+        r = np.exp(rng.uniform(np.log(0.5), np.log(2.0), 2))  # aspect ratios x:z, y:z
+        nz = max(2, int(round((E / (r[0] * r[1])) ** (1.0 / 3.0))))
+        nx, ny = max(2, int(round(r[0] * nz))), max(2, int(round(r[1] * nz)))
+        mu = rng.uniform(0.5e3, 5.0e3)
+        alpha = rng.uniform(-5.0, 8.0)
+        while abs(alpha) < 0.1:
+            alpha = rng.uniform(-5.0, 8.0)
+        K = rng.uniform(2.0e6, 50.0e6)
+        amp = rng.uniform(0.5e-3, 3.0e-3)
+        m, mt, ld = ogden_block_case(nx=nx, ny=ny, nz=nz, lx=nx * h, ly=ny * h, lz=nz * h,
+                                     jitter=jitter, seed=seed * 1000 + i, mu=mu, alpha=alpha,
+                                     K=K, amp=amp)
+        Xs.append(m["coordinates"])
+        conns.append(m["connectivity"] + node_off[-1])
+        pids.append(np.full(len(m["etype"]), i, np.int32))
+        parts.append((6, list(mt["properties"][:4])))
+        d = ld.dof_fn.copy()
+        d[d >= 0] += len(fns)
+        dofs.append(d)
+        fns += ld.fns
+        node_off.append(node_off[-1] + len(m["coordinates"]))
+    E = sum(len(c) // 8 for c in conns)
+    mesh = dict(coordinates=np.concatenate(Xs), connectivity=np.concatenate(conns).astype(np.int32),
+                eptr=np.arange(0, 8 * E + 1, 8, dtype=np.int64).astype(np.int32),
+                etype=np.zeros(E, np.int32), pid=np.concatenate(pids))
+    loads = Loads(node_off[-1])
+    loads.dof_fn = np.concatenate(dofs)
+    loads.fns = fns
+    return mesh, materials(parts), loads, np.array(node_off, np.int32)
+
+
 def ogden_block_case(nx=200, ny=200, nz=100, lx=0.2, ly=0.2, lz=0.1, jitter=0.1, seed=0,
                      mu=1.5e3, alpha=5.0, K=20e6, rho=1040.0, amp=1e-3, freq=50.0):
     """Jittered C3D8 block under top-face sinusoidal shear, 1-term Ogden

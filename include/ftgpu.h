@@ -108,6 +108,10 @@ int ftgpu_set_instances(ftgpu_model *m, int ninst, const int *node_offset, const
  * element patches: 0 = default.  Exposed for the autotuner. */
 int ftgpu_set_patch_size(ftgpu_model *m, int elements_per_patch);
 
+/* Threads per block of the nodal kernels (64..512, multiple of 32; 0 =
+ * default 256).  Exposed for the autotuner. */
+int ftgpu_set_node_threads(ftgpu_model *m, int threads);
+
 /* One-time setup on the device: element patches, reference shape-function
  * data and the lumped mass.  Replaces ShapeFunctions() (ShapeFunctions.cpp:32)
  * and AssembleLumpedMass() (Mass3D.cpp:127). */
