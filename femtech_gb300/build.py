@@ -17,7 +17,8 @@ OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libftgpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["ft_elem_f32.cu", "ft_elem_f64.cu", "ft_api.cu", "ft_patches.cpp", "ft_noalloc.cu"]
+SOURCES = ["ft_elem_f32.cu", "ft_elem_f64.cu", "ft_api.cu", "ft_patches.cpp", "ft_noalloc.cu",
+           "ft_mlp.cu"]
 
 
 def nvcc():

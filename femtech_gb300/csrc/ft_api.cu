@@ -313,6 +313,9 @@ NodeArgs node_args(ftgpu_model *m, int mode, int parity) {
   A.parity = parity;
   A.mode = mode;
   A.fp64 = is_fp64(m) ? 1 : 0;
+  A.nrot = 0;
+  for (size_t i = 0; i < m->fns.size() && A.nrot < kMaxRotFns; ++i)
+    if (m->fns[i].kind == kBckRot) A.rot_ids[A.nrot++] = (int)i;
   return A;
 }
 
@@ -426,6 +429,8 @@ int upload_bc(ftgpu_model *m) {
   int r = m->nbc.upload(nb.data(), nb.size());
   if (r) return r;
   std::vector<BcFn> f = m->fns;
+  int slot = 0;
+  for (auto &b : f) b.pad = (b.kind == kBckRot && slot < kMaxRotFns) ? slot++ : -1;
   if (f.empty()) f.resize(1);
   return m->fnsbuf.upload(f.data(), f.size());
 }

@@ -41,6 +41,10 @@ struct BcFn {
 // (include/GlobalVariables.h:15, StableTimeStep.cpp:6), as FP64 bits.
 constexpr unsigned long long kDtHugeBits = 0x4415af1d78b58c40ull;
 
+// Rigid-rotation functions whose trigonometry the nodal step caches per block
+// (BcFn::pad holds a function's cache slot, -1 if none).
+constexpr int kMaxRotFns = 8;
+
 enum { kBcFree = -1, kBcHold = -2 };
 enum { kBckFixed = 0, kBckRamp = 1, kBckSine = 2, kBckRot = 3 };
 enum { kErrInverted = 1, kErrDt = 2, kErrIndex = 4 };
@@ -103,6 +107,8 @@ struct NodeArgs {
   int ninst, parity;
   int mode;                   // kNodeBegin / kNodeFused / kNodeFinish / kNodeInit
   int fp64;                   // slot arrays are double
+  int nrot;                   // rigid-rotation functions with a cache slot
+  int rot_ids[kMaxRotFns];    // their indices in fns
 };
 
 enum { kNodeBegin = 0, kNodeFused = 1, kNodeFinish = 2, kNodeInit = 3, kNodeGather = 4,

@@ -1,0 +1,689 @@
+// ft_mlp.cu -- BF16 tensor-core MLP for the constitutive surrogate: training
+// data from the plain GOH law, forward / backward GEMMs, Adam, prediction.
+//
+// GEMMs use the warp-level BF16 tensor-core MMA (m16n8k16, FP32 accumulate)
+// with fused epilogues (bias + SiLU, SiLU derivative); every reduction (bias
+// gradients, the batch dimension of weight gradients) runs in a fixed order,
+// so training is bitwise reproducible.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "ft_mlp.cuh"
+#include "ftgpu.h"
+
+namespace ftgpu {
+
+typedef __nv_bfloat16 bf16;
+
+// ---------------- counter-based random numbers ----------------
+__host__ __device__ inline uint64_t mix64(uint64_t z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+__device__ inline double urand(uint64_t seed, uint64_t i, int k) {
+  return (mix64(seed ^ mix64(i * 64 + k)) >> 11) * (1.0 / 9007199254740992.0);
+}
+__device__ inline double nrand(uint64_t seed, uint64_t i, int k) {  // Box-Muller
+  double u1 = urand(seed, i, 2 * k) + 1e-300, u2 = urand(seed, i, 2 * k + 1);
+  return sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
+}
+
+// Training sample i: a random rotation Q (unit quaternion), principal
+// stretches in [lo, hi], U = Q diag(l) Q^T, a random unit fibre; target = the
+// scaled residual of the plain law's isochoric PK2 over its linearisation.
+__global__ void k_mlp_gen(long long n, uint64_t seed, double lo, double hi, MatP<double> mp,
+                          SurrogateLaw law, bf16 *X, float *T) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double q[4], qn = 0;
+  for (int k = 0; k < 4; ++k) {
+    q[k] = nrand(seed, i, k);
+    qn += q[k] * q[k];
+  }
+  qn = 1.0 / sqrt(qn);
+  for (int k = 0; k < 4; ++k) q[k] *= qn;
+  const double w = q[0], x = q[1], y = q[2], z = q[3];
+  const double Q[3][3] = {{1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)},
+                          {2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)},
+                          {2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)}};
+  double l[3];
+  for (int k = 0; k < 3; ++k) l[k] = lo + (hi - lo) * urand(seed, i, 10 + k);
+  double a0[3], an = 0;
+  for (int k = 0; k < 3; ++k) {
+    a0[k] = nrand(seed, i, 20 + k);
+    an += a0[k] * a0[k];
+  }
+  an = 1.0 / sqrt(an);
+  for (int k = 0; k < 3; ++k) a0[k] *= an;
+  double D[3][3];
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) {
+      double s = 0;
+      for (int k = 0; k < 3; ++k) s += Q[r][k] * l[k] * Q[c][k];
+      D[r][c] = s - (r == c ? 1.0 : 0.0);
+    }
+  const double Jm1 = jm1_of(D);
+  Sym6<double> Si, Sv;
+  mat_hgo_parts<double, true>(mp, D, Jm1, a0, Si, Sv);
+  Sym6<double> e2 = two_E(D);
+  double E[6] = {0.5 * e2.xx, 0.5 * e2.yy, 0.5 * e2.zz, 0.5 * e2.yz, 0.5 * e2.xz, 0.5 * e2.xy};
+  float xf[kMlpUsedIn];
+  double Slin[6], scale;
+  surrogate_features(E, a0, law, xf, Slin, scale);
+  const double S[6] = {Si.xx, Si.yy, Si.zz, Si.yz, Si.xz, Si.xy};
+  for (int k = 0; k < kMlpIn; ++k) X[i * kMlpIn + k] = __float2bfloat16_rn(k < kMlpUsedIn ? xf[k] : 0.f);
+  for (int k = 0; k < kMlpOut; ++k) T[i * kMlpOut + k] = k < 6 ? float((S[k] - Slin[k]) / scale) : 0.f;
+}
+
+// ---------------- generic BF16 tensor-core GEMM ----------------
+// C(M x N) = A(M x K) B(K x N); element (i,k) of A at A[i*sam + k*sak], (k,j)
+// of B at B[k*sbk + j*sbn].  One warp computes a 16 x 32 tile with four
+// m16n8k16 MMAs per 16-wide K step; a block is 4 warps (64 x 32).
+enum { kEpiStore = 0, kEpiBiasSilu = 1, kEpiBias = 2, kEpiSiluGrad = 3 };
+
+__device__ inline uint32_t pack2(bf16 lo, bf16 hi) {
+  return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+}
+
+__device__ inline float silu(float z) { return z / (1.f + __expf(-z)); }
+__device__ inline float dsilu(float z) {
+  const float s = 1.f / (1.f + __expf(-z));
+  return s * (1.f + z * (1.f - s));
+}
+
+struct GemmArgs {
+  int M, N, K;
+  const bf16 *A;
+  long long sam, sak;
+  const bf16 *B;
+  long long sbk, sbn;
+  float *C;          // kEpiStore / kEpiBias: output (f32)
+  long long scm, scn;
+  const float *bias; // kEpiBiasSilu / kEpiBias
+  float *Z;          // kEpiBiasSilu: pre-activation out, [M][N]
+  bf16 *H;           // kEpiBiasSilu: activation out, [M][N]
+  const float *Zp;   // kEpiSiluGrad: pre-activation of the layer below, [M][N]
+  bf16 *dZ;          // kEpiSiluGrad: gradient out, [M][N]
+};
+
+template <int EPI>
+__global__ void __launch_bounds__(128) k_gemm(const GemmArgs g) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gq = lane >> 2, tq = lane & 3;
+  const long long m0 = (long long)blockIdx.x * 64 + warp * 16;
+  const int n0 = blockIdx.y * 32;
+  const bf16 zero = __float2bfloat16_rn(0.f);
+  auto Aat = [&](long long i, int k) -> bf16 {
+    return (i < g.M && k < g.K) ? g.A[i * g.sam + k * g.sak] : zero;
+  };
+  auto Bat = [&](int k, int j) -> bf16 {
+    return (k < g.K && j < g.N) ? g.B[(long long)k * g.sbk + (long long)j * g.sbn] : zero;
+  };
+  float acc[4][4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+  for (int k0 = 0; k0 < g.K; k0 += 16) {
+    const uint32_t a0 = pack2(Aat(m0 + gq, k0 + 2 * tq), Aat(m0 + gq, k0 + 2 * tq + 1));
+    const uint32_t a1 = pack2(Aat(m0 + gq + 8, k0 + 2 * tq), Aat(m0 + gq + 8, k0 + 2 * tq + 1));
+    const uint32_t a2 = pack2(Aat(m0 + gq, k0 + 2 * tq + 8), Aat(m0 + gq, k0 + 2 * tq + 9));
+    const uint32_t a3 = pack2(Aat(m0 + gq + 8, k0 + 2 * tq + 8), Aat(m0 + gq + 8, k0 + 2 * tq + 9));
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int nn = n0 + 8 * j + gq;
+      const uint32_t b0 = pack2(Bat(k0 + 2 * tq, nn), Bat(k0 + 2 * tq + 1, nn));
+      const uint32_t b1 = pack2(Bat(k0 + 2 * tq + 8, nn), Bat(k0 + 2 * tq + 9, nn));
+      asm volatile(
+          "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+          "{%8,%9}, {%0,%1,%2,%3};\n"
+          : "+f"(acc[j][0]), "+f"(acc[j][1]), "+f"(acc[j][2]), "+f"(acc[j][3])
+          : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+      const long long i = m0 + gq + (h >= 2 ? 8 : 0);
+      const int c = n0 + 8 * j + 2 * tq + (h & 1);
+      if (i >= g.M || c >= g.N) continue;
+      float v = acc[j][h];
+      if (EPI == kEpiStore) {
+        g.C[i * g.scm + (long long)c * g.scn] = v;
+      } else if (EPI == kEpiBias) {
+        g.C[i * g.scm + (long long)c * g.scn] = v + g.bias[c];
+      } else if (EPI == kEpiBiasSilu) {
+        v += g.bias[c];
+        g.Z[i * g.N + c] = v;
+        g.H[i * g.N + c] = __float2bfloat16_rn(silu(v));
+      } else {  // kEpiSiluGrad
+        g.dZ[i * g.N + c] = __float2bfloat16_rn(v * dsilu(g.Zp[i * g.N + c]));
+      }
+    }
+}
+
+// column sums of an [M][N] bf16 matrix (bias gradients), fixed-order tree
+__global__ void k_colsum(const bf16 *dZ, long long M, int N, float *out) {
+  __shared__ float red[256];
+  const int c = blockIdx.x;
+  float s = 0.f;
+  for (long long i = threadIdx.x; i < M; i += blockDim.x) s += __bfloat162float(dZ[i * N + c]);
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[c] = red[0];
+}
+
+// MSE over the used outputs: dY = 2 (Y - T) / (n_used * M), per-row loss partials
+__global__ void k_mse(const float *Y, const float *T, long long M, bf16 *dY, float *rowloss) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= M) return;
+  float l = 0.f;
+  const float sc = 2.f / (float(kMlpUsedOut) * float(M));
+  for (int k = 0; k < kMlpOut; ++k) {
+    const float d = k < kMlpUsedOut ? Y[i * kMlpOut + k] - T[i * kMlpOut + k] : 0.f;
+    l += d * d;
+    dY[i * kMlpOut + k] = __float2bfloat16_rn(sc * d);
+  }
+  rowloss[i] = l;
+}
+
+__global__ void k_sum(const float *v, long long n, float *out) {
+  __shared__ float red[256];
+  float s = 0.f;
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) s += v[i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = red[0];
+}
+
+// Adam on the FP32 master parameters, then the BF16 weight copies
+__global__ void k_adam(float *P, const float *G, float *Mo, float *V, int n, float lr, float b1,
+                       float b2, float eps, float c1, float c2, bf16 *Wb) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float g = G[i];
+  const float m = b1 * Mo[i] + (1.f - b1) * g;
+  const float v = b2 * V[i] + (1.f - b2) * g * g;
+  Mo[i] = m;
+  V[i] = v;
+  const float p = P[i] - lr * (m / c1) / (sqrtf(v / c2) + eps);
+  P[i] = p;
+  Wb[i] = __float2bfloat16_rn(p);
+}
+
+__global__ void k_to_bf16(const float *P, int n, bf16 *Wb) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) Wb[i] = __float2bfloat16_rn(P[i]);
+}
+
+// ---------------- fused inference ----------------
+// Persistent blocks of 8 warps; the weights are staged once per block in
+// shared memory with rows padded by 8 bf16 (row stride 68 words: the 8 x 4
+// lanes of a B-fragment load hit 32 distinct banks).  A warp owns 16 rows and
+// keeps them in registers through all four layers: the FP32 accumulator
+// fragments of one layer (pairs of n8 tiles) are exactly the BF16 A fragments
+// of the next layer's k16 chunks.
+constexpr int kLdW0 = kMlpIn + 8, kLdW = kMlpHid + 8;
+constexpr size_t kInferSmem =
+    sizeof(bf16) * ((size_t)kMlpHid * kLdW0 + 2 * (size_t)kMlpHid * kLdW + (size_t)kMlpOut * kLdW) +
+    sizeof(float) * (3 * kMlpHid + kMlpOut);
+
+__device__ inline void mma16816(float (&c)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ inline uint32_t pack_f2(float lo, float hi) {
+  return pack2(__float2bfloat16_rn(lo), __float2bfloat16_rn(hi));
+}
+
+// one hidden layer 128 -> 128: a (8 k-chunks) -> bias + SiLU -> next (8 k-chunks)
+__device__ inline void hidden_layer(const uint32_t (&a)[8][4], uint32_t (&nx)[8][4],
+                                    const bf16 *W, const float *b, int gq, int tq) {
+#pragma unroll
+  for (int kc = 0; kc < 8; ++kc) {  // output n-tiles 2kc and 2kc+1
+    float c0[4] = {0.f, 0.f, 0.f, 0.f}, c1[4] = {0.f, 0.f, 0.f, 0.f};
+    const bf16 *r0 = W + (16 * kc + gq) * kLdW + 2 * tq;
+    const bf16 *r1 = W + (16 * kc + 8 + gq) * kLdW + 2 * tq;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      mma16816(c0, a[k], *reinterpret_cast<const uint32_t *>(r0 + 16 * k),
+               *reinterpret_cast<const uint32_t *>(r0 + 16 * k + 8));
+      mma16816(c1, a[k], *reinterpret_cast<const uint32_t *>(r1 + 16 * k),
+               *reinterpret_cast<const uint32_t *>(r1 + 16 * k + 8));
+    }
+    const float bA0 = b[16 * kc + 2 * tq], bA1 = b[16 * kc + 2 * tq + 1];
+    const float bB0 = b[16 * kc + 8 + 2 * tq], bB1 = b[16 * kc + 8 + 2 * tq + 1];
+    nx[kc][0] = pack_f2(silu(c0[0] + bA0), silu(c0[1] + bA1));
+    nx[kc][1] = pack_f2(silu(c0[2] + bA0), silu(c0[3] + bA1));
+    nx[kc][2] = pack_f2(silu(c1[0] + bB0), silu(c1[1] + bB1));
+    nx[kc][3] = pack_f2(silu(c1[2] + bB0), silu(c1[3] + bB1));
+  }
+}
+
+__global__ void __launch_bounds__(256) k_mlp_infer(const bf16 *__restrict__ X, long long n,
+                                                   const bf16 *__restrict__ Wg,
+                                                   const float *__restrict__ P,
+                                                   float *__restrict__ Y) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  bf16 *W0 = reinterpret_cast<bf16 *>(sm);
+  bf16 *W1 = W0 + kMlpHid * kLdW0;
+  bf16 *W2 = W1 + kMlpHid * kLdW;
+  bf16 *W3 = W2 + kMlpHid * kLdW;
+  float *bs = reinterpret_cast<float *>(W3 + kMlpOut * kLdW);
+  for (int i = threadIdx.x; i < kMlpHid * kMlpIn; i += blockDim.x)
+    W0[(i / kMlpIn) * kLdW0 + i % kMlpIn] = Wg[kOffW0 + i];
+  for (int i = threadIdx.x; i < kMlpHid * kMlpHid; i += blockDim.x) {
+    W1[(i / kMlpHid) * kLdW + i % kMlpHid] = Wg[kOffW1 + i];
+    W2[(i / kMlpHid) * kLdW + i % kMlpHid] = Wg[kOffW2 + i];
+  }
+  for (int i = threadIdx.x; i < kMlpOut * kMlpHid; i += blockDim.x)
+    W3[(i / kMlpHid) * kLdW + i % kMlpHid] = Wg[kOffW3 + i];
+  for (int i = threadIdx.x; i < kMlpHid; i += blockDim.x) {
+    bs[i] = P[kOffB0 + i];
+    bs[kMlpHid + i] = P[kOffB1 + i];
+    bs[2 * kMlpHid + i] = P[kOffB2 + i];
+  }
+  if (threadIdx.x < kMlpOut) bs[3 * kMlpHid + threadIdx.x] = P[kOffB3 + threadIdx.x];
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gq = lane >> 2, tq = lane & 3;
+  const long long tiles = (n + 15) / 16;
+  for (long long tile = (long long)blockIdx.x * 8 + warp; tile < tiles;
+       tile += (long long)gridDim.x * 8) {
+    const long long r0 = tile * 16 + gq, r1 = r0 + 8;
+    // layer 0 (K = 16): A fragment straight from the input rows
+    uint32_t a0[4];
+    a0[0] = r0 < n ? *reinterpret_cast<const uint32_t *>(X + r0 * kMlpIn + 2 * tq) : 0u;
+    a0[1] = r1 < n ? *reinterpret_cast<const uint32_t *>(X + r1 * kMlpIn + 2 * tq) : 0u;
+    a0[2] = r0 < n ? *reinterpret_cast<const uint32_t *>(X + r0 * kMlpIn + 8 + 2 * tq) : 0u;
+    a0[3] = r1 < n ? *reinterpret_cast<const uint32_t *>(X + r1 * kMlpIn + 8 + 2 * tq) : 0u;
+    uint32_t h[8][4], g[8][4];
+#pragma unroll
+    for (int kc = 0; kc < 8; ++kc) {
+      float c0[4] = {0.f, 0.f, 0.f, 0.f}, c1[4] = {0.f, 0.f, 0.f, 0.f};
+      const bf16 *w0 = W0 + (16 * kc + gq) * kLdW0 + 2 * tq;
+      const bf16 *w1 = W0 + (16 * kc + 8 + gq) * kLdW0 + 2 * tq;
+      mma16816(c0, a0, *reinterpret_cast<const uint32_t *>(w0),
+               *reinterpret_cast<const uint32_t *>(w0 + 8));
+      mma16816(c1, a0, *reinterpret_cast<const uint32_t *>(w1),
+               *reinterpret_cast<const uint32_t *>(w1 + 8));
+      const float bA0 = bs[16 * kc + 2 * tq], bA1 = bs[16 * kc + 2 * tq + 1];
+      const float bB0 = bs[16 * kc + 8 + 2 * tq], bB1 = bs[16 * kc + 8 + 2 * tq + 1];
+      h[kc][0] = pack_f2(silu(c0[0] + bA0), silu(c0[1] + bA1));
+      h[kc][1] = pack_f2(silu(c0[2] + bA0), silu(c0[3] + bA1));
+      h[kc][2] = pack_f2(silu(c1[0] + bB0), silu(c1[1] + bB1));
+      h[kc][3] = pack_f2(silu(c1[2] + bB0), silu(c1[3] + bB1));
+    }
+    hidden_layer(h, g, W1, bs + kMlpHid, gq, tq);
+    hidden_layer(g, h, W2, bs + 2 * kMlpHid, gq, tq);
+    // output layer (N = 8)
+    float c[4] = {0.f, 0.f, 0.f, 0.f};
+    const bf16 *w3 = W3 + gq * kLdW + 2 * tq;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      mma16816(c, h[k], *reinterpret_cast<const uint32_t *>(w3 + 16 * k),
+               *reinterpret_cast<const uint32_t *>(w3 + 16 * k + 8));
+    const float b0 = bs[3 * kMlpHid + 2 * tq], b1 = bs[3 * kMlpHid + 2 * tq + 1];
+    if (r0 < n) {
+      Y[r0 * kMlpOut + 2 * tq] = c[0] + b0;
+      Y[r0 * kMlpOut + 2 * tq + 1] = c[1] + b1;
+    }
+    if (r1 < n) {
+      Y[r1 * kMlpOut + 2 * tq] = c[2] + b0;
+      Y[r1 * kMlpOut + 2 * tq + 1] = c[3] + b1;
+    }
+  }
+}
+
+}  // namespace ftgpu
+
+using namespace ftgpu;
+
+// ------------------------------------------------------------------------
+struct ftgpu_surrogate {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  SurrogateLaw law;
+  MatP<double> mp;
+  float *P = nullptr, *G = nullptr, *Mo = nullptr, *V = nullptr;  // FP32 master, grad, Adam
+  bf16 *Wb = nullptr;                                             // BF16 copy (same layout)
+  bf16 *X = nullptr;                                              // training inputs [n][16]
+  float *T = nullptr;                                             // targets [n][8]
+  long long nsamples = 0;
+  // activations of one batch
+  long long cap = 0;
+  float *Z1 = nullptr, *Z2 = nullptr, *Z3 = nullptr, *Y = nullptr, *rowloss = nullptr, *loss = nullptr;
+  bf16 *H1 = nullptr, *H2 = nullptr, *H3 = nullptr, *dY = nullptr, *dZ1 = nullptr, *dZ2 = nullptr,
+       *dZ3 = nullptr;
+  long long adam_t = 0;
+  std::string err;
+  ~ftgpu_surrogate() {
+    for (void *p : {(void *)P, (void *)G, (void *)Mo, (void *)V, (void *)Wb, (void *)X, (void *)T,
+                    (void *)Z1, (void *)Z2, (void *)Z3, (void *)Y, (void *)rowloss, (void *)loss,
+                    (void *)H1, (void *)H2, (void *)H3, (void *)dY, (void *)dZ1, (void *)dZ2,
+                    (void *)dZ3})
+      if (p) cudaFree(p);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace {
+
+int sfail(int code) { return code; }
+
+#define SCK(x)                                        \
+  do {                                                \
+    if ((x) != cudaSuccess) {                         \
+      cudaGetLastError();                             \
+      return sfail(FTGPU_ERR_CUDA);                   \
+    }                                                 \
+  } while (0)
+
+template <class T>
+int dalloc(T **p, size_t n) {
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  if (cudaMalloc((void **)p, n * sizeof(T) + 16) != cudaSuccess) {
+    cudaGetLastError();
+    return FTGPU_ERR_ALLOC;
+  }
+  return 0;
+}
+
+int ensure_batch(ftgpu_surrogate *s, long long B) {
+  if (B <= s->cap) return 0;
+  int r = 0;
+  r |= dalloc(&s->Z1, B * kMlpHid) | dalloc(&s->Z2, B * kMlpHid) | dalloc(&s->Z3, B * kMlpHid);
+  r |= dalloc(&s->H1, B * kMlpHid) | dalloc(&s->H2, B * kMlpHid) | dalloc(&s->H3, B * kMlpHid);
+  r |= dalloc(&s->dZ1, B * kMlpHid) | dalloc(&s->dZ2, B * kMlpHid) | dalloc(&s->dZ3, B * kMlpHid);
+  r |= dalloc(&s->Y, B * kMlpOut) | dalloc(&s->dY, B * kMlpOut) | dalloc(&s->rowloss, B);
+  r |= dalloc(&s->loss, 1);
+  if (r) return FTGPU_ERR_ALLOC;
+  s->cap = B;
+  return 0;
+}
+
+template <int EPI>
+int gemm(cudaStream_t st, const GemmArgs &g) {
+  dim3 grid((unsigned)((g.M + 63) / 64), (unsigned)((g.N + 31) / 32));
+  k_gemm<EPI><<<grid, 128, 0, st>>>(g);
+  return cudaGetLastError() == cudaSuccess ? 0 : FTGPU_ERR_CUDA;
+}
+
+GemmArgs ga(int M, int N, int K, const bf16 *A, long long sam, long long sak, const bf16 *B,
+            long long sbk, long long sbn) {
+  GemmArgs g;
+  memset(&g, 0, sizeof(g));
+  g.M = M; g.N = N; g.K = K; g.A = A; g.sam = sam; g.sak = sak; g.B = B; g.sbk = sbk; g.sbn = sbn;
+  return g;
+}
+
+// forward of B rows of X: Z1/H1, Z2/H2, Z3/H3 and Y
+int forward(ftgpu_surrogate *s, const bf16 *X, long long B) {
+  const bf16 *W = s->Wb;
+  const float *P = s->P;
+  GemmArgs g = ga((int)B, kMlpHid, kMlpIn, X, kMlpIn, 1, W + kOffW0, 1, kMlpIn);
+  g.bias = P + kOffB0; g.Z = s->Z1; g.H = s->H1;
+  int r = gemm<kEpiBiasSilu>(s->stream, g);
+  g = ga((int)B, kMlpHid, kMlpHid, s->H1, kMlpHid, 1, W + kOffW1, 1, kMlpHid);
+  g.bias = P + kOffB1; g.Z = s->Z2; g.H = s->H2;
+  r |= gemm<kEpiBiasSilu>(s->stream, g);
+  g = ga((int)B, kMlpHid, kMlpHid, s->H2, kMlpHid, 1, W + kOffW2, 1, kMlpHid);
+  g.bias = P + kOffB2; g.Z = s->Z3; g.H = s->H3;
+  r |= gemm<kEpiBiasSilu>(s->stream, g);
+  g = ga((int)B, kMlpOut, kMlpHid, s->H3, kMlpHid, 1, W + kOffW3, 1, kMlpHid);
+  g.bias = P + kOffB3; g.C = s->Y; g.scm = kMlpOut; g.scn = 1;
+  r |= gemm<kEpiBias>(s->stream, g);
+  return r;
+}
+
+// loss and all parameter gradients of one batch (X, T) into G
+int backward(ftgpu_surrogate *s, const bf16 *X, const float *T, long long B) {
+  const bf16 *W = s->Wb;
+  float *G = s->G;
+  cudaStream_t st = s->stream;
+  int r = 0;
+  k_mse<<<(unsigned)((B + 255) / 256), 256, 0, st>>>(s->Y, T, B, s->dY, s->rowloss);
+  k_sum<<<1, 256, 0, st>>>(s->rowloss, B, s->loss);
+  // layer 3: dW3 = dY^T H3, db3, dZ3 = (dY W3) * silu'(Z3)
+  GemmArgs g = ga(kMlpOut, kMlpHid, (int)B, s->dY, 1, kMlpOut, s->H3, kMlpHid, 1);
+  g.C = G + kOffW3; g.scm = kMlpHid; g.scn = 1;
+  r |= gemm<kEpiStore>(st, g);
+  k_colsum<<<kMlpOut, 256, 0, st>>>(s->dY, B, kMlpOut, G + kOffB3);
+  g = ga((int)B, kMlpHid, kMlpOut, s->dY, kMlpOut, 1, W + kOffW3, kMlpHid, 1);
+  g.Zp = s->Z3; g.dZ = s->dZ3;
+  r |= gemm<kEpiSiluGrad>(st, g);
+  // layer 2
+  g = ga(kMlpHid, kMlpHid, (int)B, s->dZ3, 1, kMlpHid, s->H2, kMlpHid, 1);
+  g.C = G + kOffW2; g.scm = kMlpHid; g.scn = 1;
+  r |= gemm<kEpiStore>(st, g);
+  k_colsum<<<kMlpHid, 256, 0, st>>>(s->dZ3, B, kMlpHid, G + kOffB2);
+  g = ga((int)B, kMlpHid, kMlpHid, s->dZ3, kMlpHid, 1, W + kOffW2, kMlpHid, 1);
+  g.Zp = s->Z2; g.dZ = s->dZ2;
+  r |= gemm<kEpiSiluGrad>(st, g);
+  // layer 1
+  g = ga(kMlpHid, kMlpHid, (int)B, s->dZ2, 1, kMlpHid, s->H1, kMlpHid, 1);
+  g.C = G + kOffW1; g.scm = kMlpHid; g.scn = 1;
+  r |= gemm<kEpiStore>(st, g);
+  k_colsum<<<kMlpHid, 256, 0, st>>>(s->dZ2, B, kMlpHid, G + kOffB1);
+  g = ga((int)B, kMlpHid, kMlpHid, s->dZ2, kMlpHid, 1, W + kOffW1, kMlpHid, 1);
+  g.Zp = s->Z1; g.dZ = s->dZ1;
+  r |= gemm<kEpiSiluGrad>(st, g);
+  // layer 0
+  g = ga(kMlpHid, kMlpIn, (int)B, s->dZ1, 1, kMlpHid, X, kMlpIn, 1);
+  g.C = G + kOffW0; g.scm = kMlpIn; g.scn = 1;
+  r |= gemm<kEpiStore>(st, g);
+  k_colsum<<<kMlpHid, 256, 0, st>>>(s->dZ1, B, kMlpHid, G + kOffB0);
+  if (cudaGetLastError() != cudaSuccess) return FTGPU_ERR_CUDA;
+  return r;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ftgpu_surrogate_create(ftgpu_surrogate **out, int device, const double *props,
+                           unsigned long long seed) {
+  if (!out || !props) return FTGPU_ERR_INPUT;
+  *out = nullptr;
+  int nd = 0;
+  if (cudaGetDeviceCount(&nd) != cudaSuccess || device < 0 || device >= nd) {
+    cudaGetLastError();
+    return FTGPU_ERR_NODEVICE;
+  }
+  SCK(cudaSetDevice(device));
+  auto s = std::make_unique<ftgpu_surrogate>();
+  s->device = device;
+  SCK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+  memset(&s->mp, 0, sizeof(s->mp));
+  for (int k = 0; k < 9; ++k) s->mp.p[k] = props[k];
+  s->mp.K = props[2] + 2.0 * props[1] / 3.0;
+  s->mp.mat = 7;
+  s->law.mu = props[1];
+  s->law.k1 = props[3];
+  s->law.k2 = props[4];
+  s->law.kappa = props[7];
+  s->law.s0 = props[1] + props[3];
+  s->law.out_scale = 1.0;
+  s->law.trust_e2 = 0.25;
+  int r = dalloc(&s->P, kMlpParams) | dalloc(&s->G, kMlpParams) | dalloc(&s->Mo, kMlpParams) |
+          dalloc(&s->V, kMlpParams) | dalloc(&s->Wb, kMlpParams);
+  if (r) return FTGPU_ERR_ALLOC;
+  // Kaiming-uniform-style init (fan-in scaled), seeded, on the host
+  std::vector<float> p(kMlpParams, 0.f);
+  auto init = [&](int off, int rows, int cols, int used_cols) {
+    const double b = sqrt(6.0 / used_cols) * 0.5;
+    for (int i = 0; i < rows; ++i)
+      for (int j = 0; j < cols; ++j) {
+        const double u = (mix64(seed ^ mix64((uint64_t)(off + i * cols + j))) >> 11) *
+                         (1.0 / 9007199254740992.0);
+        p[off + i * cols + j] = j < used_cols ? float((2 * u - 1) * b) : 0.f;
+      }
+  };
+  init(kOffW0, kMlpHid, kMlpIn, kMlpUsedIn);
+  init(kOffW1, kMlpHid, kMlpHid, kMlpHid);
+  init(kOffW2, kMlpHid, kMlpHid, kMlpHid);
+  init(kOffW3, kMlpOut, kMlpHid, kMlpHid);
+  for (int j = kMlpUsedOut; j < kMlpOut; ++j)
+    for (int i = 0; i < kMlpHid; ++i) p[kOffW3 + j * kMlpHid + i] = 0.f;
+  SCK(cudaMemcpy(s->P, p.data(), kMlpParams * 4, cudaMemcpyHostToDevice));
+  SCK(cudaMemset(s->Mo, 0, kMlpParams * 4));
+  SCK(cudaMemset(s->V, 0, kMlpParams * 4));
+  k_to_bf16<<<(kMlpParams + 255) / 256, 256, 0, s->stream>>>(s->P, kMlpParams, s->Wb);
+  SCK(cudaStreamSynchronize(s->stream));
+  *out = s.release();
+  return FTGPU_OK;
+}
+
+int ftgpu_surrogate_destroy(ftgpu_surrogate *s) {
+  if (s) {
+    cudaSetDevice(s->device);
+    cudaStreamSynchronize(s->stream);
+    delete s;
+  }
+  return FTGPU_OK;
+}
+
+int ftgpu_surrogate_generate(ftgpu_surrogate *s, long long n, unsigned long long seed,
+                             double stretch_lo, double stretch_hi) {
+  if (!s || n <= 0 || !(stretch_lo > 0) || !(stretch_hi > stretch_lo)) return FTGPU_ERR_INPUT;
+  SCK(cudaSetDevice(s->device));
+  int r = dalloc(&s->X, n * kMlpIn) | dalloc(&s->T, n * kMlpOut);
+  if (r) return FTGPU_ERR_ALLOC;
+  k_mlp_gen<<<(unsigned)((n + 127) / 128), 128, 0, s->stream>>>(n, seed, stretch_lo, stretch_hi,
+                                                                 s->mp, s->law, s->X, s->T);
+  SCK(cudaGetLastError());
+  SCK(cudaStreamSynchronize(s->stream));
+  s->nsamples = n;
+  return FTGPU_OK;
+}
+
+int ftgpu_surrogate_train(ftgpu_surrogate *s, int epochs, int batch, double lr,
+                          double *final_loss) {
+  if (!s || s->nsamples <= 0 || batch <= 0 || epochs <= 0) return FTGPU_ERR_STATE;
+  SCK(cudaSetDevice(s->device));
+  int r = ensure_batch(s, batch);
+  if (r) return r;
+  const long long nb = s->nsamples / batch;
+  double last = 0.0;
+  const long long total = nb * epochs;
+  for (int ep = 0; ep < epochs; ++ep) {
+    double acc = 0.0;
+    for (long long b = 0; b < nb; ++b) {
+      const bf16 *X = s->X + b * batch * kMlpIn;
+      const float *T = s->T + b * batch * kMlpOut;
+      r = forward(s, X, batch);
+      r |= backward(s, X, T, batch);
+      if (r) return r;
+      ++s->adam_t;
+      // cosine-decayed learning rate over the whole run
+      const double frac = double(s->adam_t) / double(total + 1);
+      const float lr_t = float(lr * 0.5 * (1.0 + cos(3.141592653589793 * std::min(frac, 1.0))));
+      const float b1 = 0.9f, b2 = 0.999f;
+      const float c1 = 1.f - powf(b1, (float)s->adam_t), c2 = 1.f - powf(b2, (float)s->adam_t);
+      k_adam<<<(kMlpParams + 255) / 256, 256, 0, s->stream>>>(s->P, s->G, s->Mo, s->V, kMlpParams,
+                                                              lr_t, b1, b2, 1e-8f, c1, c2, s->Wb);
+      if (b == nb - 1) {
+        float hl = 0.f;
+        SCK(cudaMemcpyAsync(&hl, s->loss, 4, cudaMemcpyDeviceToHost, s->stream));
+        SCK(cudaStreamSynchronize(s->stream));
+        acc = hl / (double(batch) * kMlpUsedOut);
+      }
+    }
+    last = acc;
+  }
+  SCK(cudaStreamSynchronize(s->stream));
+  if (final_loss) *final_loss = last;
+  return FTGPU_OK;
+}
+
+// raw network outputs for host features x[n][16] (float) -> y[n][8]
+int ftgpu_surrogate_forward(ftgpu_surrogate *s, long long n, const float *x, float *y) {
+  if (!s || n <= 0 || !x || !y) return FTGPU_ERR_INPUT;
+  SCK(cudaSetDevice(s->device));
+  int r = ensure_batch(s, n);
+  if (r) return r;
+  std::vector<bf16> xb(n * kMlpIn);
+  for (long long i = 0; i < n * kMlpIn; ++i) xb[i] = __float2bfloat16_rn(x[i]);
+  bf16 *dX = nullptr;
+  if (dalloc(&dX, n * kMlpIn)) return FTGPU_ERR_ALLOC;
+  SCK(cudaMemcpy(dX, xb.data(), n * kMlpIn * 2, cudaMemcpyHostToDevice));
+  r = forward(s, dX, n);
+  SCK(cudaStreamSynchronize(s->stream));
+  SCK(cudaMemcpy(y, s->Y, n * kMlpOut * 4, cudaMemcpyDeviceToHost));
+  cudaFree(dX);
+  return r;
+}
+
+// loss and parameter gradient of one batch given on the host (gradient checks)
+int ftgpu_surrogate_gradient(ftgpu_surrogate *s, long long n, const float *x, const float *t,
+                             float *grad, double *loss) {
+  if (!s || n <= 0 || !x || !t) return FTGPU_ERR_INPUT;
+  SCK(cudaSetDevice(s->device));
+  int r = ensure_batch(s, n);
+  if (r) return r;
+  std::vector<bf16> xb(n * kMlpIn);
+  for (long long i = 0; i < n * kMlpIn; ++i) xb[i] = __float2bfloat16_rn(x[i]);
+  bf16 *dX = nullptr;
+  float *dT = nullptr;
+  if (dalloc(&dX, n * kMlpIn) || dalloc(&dT, n * kMlpOut)) return FTGPU_ERR_ALLOC;
+  SCK(cudaMemcpy(dX, xb.data(), n * kMlpIn * 2, cudaMemcpyHostToDevice));
+  SCK(cudaMemcpy(dT, t, n * kMlpOut * 4, cudaMemcpyHostToDevice));
+  r = forward(s, dX, n);
+  r |= backward(s, dX, dT, n);
+  SCK(cudaStreamSynchronize(s->stream));
+  float hl = 0.f;
+  SCK(cudaMemcpy(&hl, s->loss, 4, cudaMemcpyDeviceToHost));
+  if (loss) *loss = hl / (double(n) * kMlpUsedOut);
+  if (grad) SCK(cudaMemcpy(grad, s->G, kMlpParams * 4, cudaMemcpyDeviceToHost));
+  cudaFree(dX);
+  cudaFree(dT);
+  return r;
+}
+
+int ftgpu_surrogate_params(ftgpu_surrogate *s, float *get, const float *set) {
+  if (!s) return FTGPU_ERR_INPUT;
+  SCK(cudaSetDevice(s->device));
+  if (set) {
+    SCK(cudaMemcpy(s->P, set, kMlpParams * 4, cudaMemcpyHostToDevice));
+    k_to_bf16<<<(kMlpParams + 255) / 256, 256, 0, s->stream>>>(s->P, kMlpParams, s->Wb);
+    SCK(cudaStreamSynchronize(s->stream));
+  }
+  if (get) SCK(cudaMemcpy(get, s->P, kMlpParams * 4, cudaMemcpyDeviceToHost));
+  return FTGPU_OK;
+}
+
+// training samples back to the host (first n): x[n][16] as float, t[n][8]
+int ftgpu_surrogate_samples(ftgpu_surrogate *s, long long n, float *x, float *t) {
+  if (!s || n <= 0 || n > s->nsamples) return FTGPU_ERR_INPUT;
+  std::vector<bf16> xb(n * kMlpIn);
+  SCK(cudaMemcpy(xb.data(), s->X, n * kMlpIn * 2, cudaMemcpyDeviceToHost));
+  if (x)
+    for (long long i = 0; i < n * kMlpIn; ++i) x[i] = __bfloat162float(xb[i]);
+  if (t) SCK(cudaMemcpy(t, s->T, n * kMlpOut * 4, cudaMemcpyDeviceToHost));
+  return FTGPU_OK;
+}
+
+int ftgpu_surrogate_num_params(void) { return kMlpParams; }
+
+}  // extern "C"

@@ -1,0 +1,75 @@
+// ft_mlp.cuh -- the learned constitutive surrogate: shapes, parameter layout and
+// the input features / output reconstruction shared by training and in-loop use.
+//
+// What is learned: the isochoric (deviatoric-response) PK2 stress S_iso(E, a0)
+// of the anisotropic GOH law (material 7), i.e. the costly nonlinear part of
+// the stress update (exponential fibre term, J^{-2/3}, adjugate products).  The
+// volumetric stress and the 1-term Prony recurrence are linear in S_iso and
+// stay exact.  The network predicts a residual over the law's small-strain
+// linearisation, scaled by |E|^2 (the residual is O(|E|^2)):
+//   S_iso = S_lin(E, a0) + s0 |E|^2 NN(x),  s0 = mu + k1,
+//   S_lin = 2 mu dev E + 2 k1 (1-3 kappa) max(Ea, 0) dev(a0 a0),
+//   Ea    = 2 (1-3 kappa) (a0.E.a0 - tr E / 3),
+// so small strains are carried by the exact linear part.  Inputs x: the six
+// Green-strain components (Voigt 11,22,33,23,13,12) / 0.5 and the fibre a0.
+// Network: 16 (9 used) -> 128 -> 128 -> 128 -> 8 (6 used), SiLU, BF16 weights
+// and activations, FP32 accumulation.
+#pragma once
+
+#include <cuda_bf16.h>
+
+#include "ft_materials.cuh"
+
+namespace ftgpu {
+
+constexpr int kMlpIn = 16, kMlpHid = 128, kMlpOut = 8;
+constexpr int kMlpUsedIn = 9, kMlpUsedOut = 6;
+// flat FP32 parameter vector: W0[128][16] b0 W1[128][128] b1 W2[128][128] b2 W3[8][128] b3
+constexpr int kOffW0 = 0;
+constexpr int kOffB0 = kOffW0 + kMlpHid * kMlpIn;
+constexpr int kOffW1 = kOffB0 + kMlpHid;
+constexpr int kOffB1 = kOffW1 + kMlpHid * kMlpHid;
+constexpr int kOffW2 = kOffB1 + kMlpHid;
+constexpr int kOffB2 = kOffW2 + kMlpHid * kMlpHid;
+constexpr int kOffW3 = kOffB2 + kMlpHid;
+constexpr int kOffB3 = kOffW3 + kMlpOut * kMlpHid;
+constexpr int kMlpParams = kOffB3 + kMlpOut;
+constexpr double kStrainScale = 0.5;
+constexpr double kE2Floor = 1e-14;
+
+struct SurrogateLaw {  // the GOH parameters the surrogate was trained for
+  double mu, k1, k2, kappa;
+  double s0;           // output scale mu + k1
+  double out_scale;    // extra normalisation of the residual (training std)
+  double trust_e2;     // |E|_F^2 above which the plain law is used
+};
+
+// features and linear part from the Green strain (symmetric, Voigt order) and a0
+template <class R>
+__host__ __device__ inline void surrogate_features(const R (&E)[6], const R (&a0)[3],
+                                                   const SurrogateLaw &law, float (&x)[kMlpUsedIn],
+                                                   R (&Slin)[6], R &scale) {
+  const R tr3 = (E[0] + E[1] + E[2]) / R(3);
+  const R aEa = a0[0] * a0[0] * E[0] + a0[1] * a0[1] * E[1] + a0[2] * a0[2] * E[2] +
+                R(2) * (a0[1] * a0[2] * E[3] + a0[0] * a0[2] * E[4] + a0[0] * a0[1] * E[5]);
+  const R c4 = R(1) - R(3) * R(law.kappa);
+  const R Ea = R(2) * c4 * (aEa - tr3);
+  const R f = Ea > R(0) ? R(2) * R(law.k1) * c4 * Ea : R(0);
+  const R mu2 = R(2) * R(law.mu);
+  const R third = R(1) / R(3);
+  Slin[0] = mu2 * (E[0] - tr3) + f * (a0[0] * a0[0] - third);
+  Slin[1] = mu2 * (E[1] - tr3) + f * (a0[1] * a0[1] - third);
+  Slin[2] = mu2 * (E[2] - tr3) + f * (a0[2] * a0[2] - third);
+  Slin[3] = mu2 * E[3] + f * a0[1] * a0[2];
+  Slin[4] = mu2 * E[4] + f * a0[0] * a0[2];
+  Slin[5] = mu2 * E[5] + f * a0[0] * a0[1];
+  R e2 = E[0] * E[0] + E[1] * E[1] + E[2] * E[2] + R(2) * (E[3] * E[3] + E[4] * E[4] + E[5] * E[5]);
+  if (e2 < R(kE2Floor)) e2 = R(kE2Floor);
+  scale = R(law.s0) * R(law.out_scale) * e2;
+  for (int k = 0; k < 6; ++k) x[k] = float(E[k] / R(kStrainScale));
+  x[6] = float(a0[0]);
+  x[7] = float(a0[1]);
+  x[8] = float(a0[2]);
+}
+
+}  // namespace ftgpu

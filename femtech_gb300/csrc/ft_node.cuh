@@ -27,6 +27,34 @@ __device__ __forceinline__ void rot_angle(const double *p, double t, double &th,
   }
 }
 
+// cos / sin of the rotation angle and the angular velocity of a rigid-rotation
+// function at time t (the only transcendental work of the rotation).
+__device__ __forceinline__ void rot_trig(const BcFn &b, double t, double &c, double &s,
+                                         double &om) {
+  double th;
+  rot_angle(b.p, t, th, om);
+  c = cos(th);
+  s = sin(th);
+}
+
+// Displacement and velocity of node n under a rigid rotation (Rodrigues).
+__device__ __forceinline__ void rot_apply(const BcFn &b, double c, double s, double om,
+                                          const double *X, long long N, long long n,
+                                          double (&ur)[3], double (&vr)[3]) {
+  const double k0 = b.p[0], k1 = b.p[1], k2 = b.p[2];
+  const double r0 = X[n] - b.p[3], r1 = X[N + n] - b.p[4], r2 = X[2 * N + n] - b.p[5];
+  const double kr = k0 * r0 + k1 * r1 + k2 * r2;
+  const double R0 = r0 * c + (k1 * r2 - k2 * r1) * s + k0 * kr * (1.0 - c);
+  const double R1 = r1 * c + (k2 * r0 - k0 * r2) * s + k1 * kr * (1.0 - c);
+  const double R2 = r2 * c + (k0 * r1 - k1 * r0) * s + k2 * kr * (1.0 - c);
+  ur[0] = R0 - r0;
+  ur[1] = R1 - r1;
+  ur[2] = R2 - r2;
+  vr[0] = om * (k1 * R2 - k2 * R1);
+  vr[1] = om * (k2 * R0 - k0 * R2);
+  vr[2] = om * (k0 * R1 - k1 * R0);
+}
+
 // Prescribed displacement / velocity of DOF d of node n at time t.  Only the
 // rigid rotation reads the node's reference position (SoA X, stride N).
 __device__ __forceinline__ void bc_value(const BcFn &b, int d, double t, const double *X,
@@ -166,11 +194,15 @@ __global__ void __launch_bounds__(512) k_node(const NodeArgs A) {
 // there).  The step scalars are computed once per block by thread 0 for the
 // instance of the block's first node; nodes of another instance (blocks that
 // straddle two instances of a batch) compute their own.
+// At most 64 registers: the kernel waits on memory, so resident warps matter.
+// The trigonometry of rigid-rotation functions (at the new time) is also
+// evaluated once per block, for up to kMaxRotFns functions.
 template <class R>
-__global__ void __launch_bounds__(512) k_node_step(const NodeArgs A) {
+__global__ void __launch_bounds__(512, 2) k_node_step(const NodeArgs A) {
   __shared__ StepScalars shs;
   __shared__ Clock shck;
   __shared__ int shinst;
+  __shared__ double shrot[kMaxRotFns][3];
   const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (threadIdx.x == 0) {
     const long long n0 = (long long)blockIdx.x * blockDim.x;
@@ -178,6 +210,9 @@ __global__ void __launch_bounds__(512) k_node_step(const NodeArgs A) {
     shck = A.clock[A.parity * A.ninst + i0];
     shs = step_scalars(shck, A.inst[i0], A.dtmin[A.parity * A.ninst + i0], A.mode);
     shinst = i0;
+    if (shs.advance)
+      for (int k = 0; k < A.nrot; ++k)
+        rot_trig(A.fns[A.rot_ids[k]], shs.t_np2, shrot[k][0], shrot[k][1], shrot[k][2]);
   }
   __syncthreads();
   if (n >= A.N) return;
@@ -215,6 +250,28 @@ __global__ void __launch_bounds__(512) k_node_step(const NodeArgs A) {
   const double fsum[3] = {double(fs0), double(fs1), double(fs2)};
   const double minv = kF64 ? 0.0 : A.minv[n];
   double un[3];
+  // a rigid rotation drives all its DOFs at once: evaluate it once per node
+  double ur[3] = {0.0, 0.0, 0.0}, vr[3] = {0.0, 0.0, 0.0};
+  int rot_fn = -1;
+  if (advance) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const int fn = A.nbc[d * N + n];
+      if (fn >= 0 && rot_fn < 0 && A.fns[fn].kind == kBckRot) rot_fn = fn;
+    }
+    if (rot_fn >= 0) {
+      const BcFn &b = A.fns[rot_fn];
+      double c, s, om;
+      if (same && b.pad >= 0 && b.pad < A.nrot) {
+        c = shrot[b.pad][0];
+        s = shrot[b.pad][1];
+        om = shrot[b.pad][2];
+      } else {
+        rot_trig(b, sc.t_np2, c, s, om);
+      }
+      rot_apply(b, c, s, om, A.X, N, n, ur, vr);
+    }
+  }
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const int fn = A.nbc[d * N + n];
@@ -239,7 +296,12 @@ __global__ void __launch_bounds__(512) k_node_step(const NodeArgs A) {
       }
     } else if (fn >= 0 && advance) {
       double vb;
-      bc_value(A.fns[fn], d, sc.t_np2, A.X, N, n, u, vb);
+      if (fn == rot_fn) {
+        u = ur[d];
+        vb = vr[d];
+      } else {
+        bc_value(A.fns[fn], d, sc.t_np2, A.X, N, n, u, vb);
+      }
       A.u[d * N + n] = u;
       A.v[d * N + n] = vb;
       A.a[d * N + n] = 0.0;

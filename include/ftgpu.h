@@ -187,6 +187,35 @@ int ftgpu_launches_per_step(ftgpu_model *m);
 /* Synchronise and return the device error word (0 = none). */
 int ftgpu_check(ftgpu_model *m);
 
+/* ---- learned constitutive surrogate for material 7 (no counterpart in the
+ * reference; it replaces the isochoric part of HGOIsotropicViscoelastic's
+ * stress, HGOIsotropicViscoelastic.cpp:53-97, generalised to fibres) ----
+ * An MLP 16(9 used)->128->128->128->8(6 used), SiLU, BF16 weights and
+ * activations, FP32 accumulation, trained on the GPU on samples of the plain
+ * law.  It predicts S_iso = S_lin + s0 |E|^2 NN(E, a0) (S_lin: the law's
+ * small-strain linearisation); the volumetric stress and the Prony recurrence
+ * stay exact.  properties: the 9 material-7 parameters. */
+typedef struct ftgpu_surrogate ftgpu_surrogate;
+int ftgpu_surrogate_create(ftgpu_surrogate **out, int device, const double *properties,
+                           unsigned long long seed);
+int ftgpu_surrogate_destroy(ftgpu_surrogate *s);
+/* nsamples states: random rotation, principal stretches in [lo, hi], random fibre */
+int ftgpu_surrogate_generate(ftgpu_surrogate *s, long long nsamples, unsigned long long seed,
+                             double stretch_lo, double stretch_hi);
+/* Adam (cosine-decayed lr) over the generated samples; *final_loss = last batch MSE */
+int ftgpu_surrogate_train(ftgpu_surrogate *s, int epochs, int batch, double lr,
+                          double *final_loss);
+/* raw network outputs y[n][8] for features x[n][16] (host arrays) */
+int ftgpu_surrogate_forward(ftgpu_surrogate *s, long long n, const float *x, float *y);
+/* MSE loss and its gradient w.r.t. the FP32 parameter vector for one batch */
+int ftgpu_surrogate_gradient(ftgpu_surrogate *s, long long n, const float *x, const float *t,
+                             float *grad, double *loss);
+/* FP32 parameter vector out (get) and/or in (set); layout W0 b0 W1 b1 W2 b2 W3 b3 */
+int ftgpu_surrogate_params(ftgpu_surrogate *s, float *get, const float *set);
+/* the first n generated samples: features x[n][16], targets t[n][8] */
+int ftgpu_surrogate_samples(ftgpu_surrogate *s, long long n, float *x, float *t);
+int ftgpu_surrogate_num_params(void);
+
 /* ---- allocation-free internal force (no counterpart in the reference) ----
  * For callers that cannot let a library allocate device memory (they own all
  * of it, e.g. through their own pool, or run under a fixed budget): the C3D8
