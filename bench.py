@@ -254,6 +254,62 @@ def make_workload(name, size=None):
     raise SystemExit("unknown workload " + name)
 
 
+def surrogate_compare(args, dev):
+    """Head-like mesh: plain mixed path vs the learned surrogate for the GOH +
+    Prony core, same steps, both against an FP64 run of the plain path (the
+    FP64 GPU path matches the CPU oracle to ~1e-13 in the parity tests)."""
+    import torch
+    import femtech_gb300 as ft
+    from femtech_gb300.surrogate import Surrogate
+    wl = make_workload("head", args.size)
+    mesh, mats, loads = wl["mesh"], wl["mats"], wl["loads"]
+    E = len(mesh["etype"])
+    props7 = list(mats["properties"].reshape(-1, 9)[1])
+    t0 = time.perf_counter()
+    s = Surrogate(props7, device=dev, seed=1)
+    s.generate(args.train_samples, seed=2)
+    loss = s.train(epochs=args.train_epochs, batch=8192, lr=2e-3)
+    torch.cuda.synchronize(dev)
+    t_train = time.perf_counter() - t0
+    res = {}
+    total = args.warmup + args.steps
+    for name in ("plain", "surrogate", "fp64"):
+        m = ft.Model(mesh, mats, precision=ft.FP64 if name == "fp64" else ft.MIXED, device=dev,
+                     loads=loads)
+        if name == "surrogate":
+            m.set_surrogate(s, trust_e2=args.trust_e2)
+        m.init_explicit(0.9, 0.0, 1e300)
+        m.run(args.warmup)
+        steps, ms = timed_run(m, args.steps)
+        res[name] = dict(steps=steps, ms=ms, u=m.state()["u"],
+                         value=E * steps / (ms / 1e3))
+        m.close()
+    ref = res["fp64"]["u"]
+
+    def rel(a):
+        return float(np.linalg.norm(a - ref) / max(np.linalg.norm(ref), 1e-300))
+
+    line = {
+        "metric": "element-updates/s", "value": res["surrogate"]["value"],
+        "unit": "element-updates/s", "n_gpus": 1, "steps": res["surrogate"]["steps"],
+        "warmup": args.warmup, "ms_per_step": res["surrogate"]["ms"] / max(args.steps, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16 surrogate MLP (fp32 accumulate) / f32 element kernels / f64 nodal state",
+        "data": "synthetic (seeded, generated in-run)",
+        "config": {"workload": wl["label"] + "_surrogate", "elements": E, "total_steps": total,
+                   "trust_e2": args.trust_e2},
+        "surrogate": {"train_samples": args.train_samples, "epochs": args.train_epochs,
+                      "final_batch_mse": loss, "train_s": t_train,
+                      "plain_value": res["plain"]["value"],
+                      "speedup_vs_plain": res["surrogate"]["value"] / res["plain"]["value"],
+                      "rel_disp_err_vs_fp64": rel(res["surrogate"]["u"]),
+                      "plain_mixed_rel_disp_err_vs_fp64": rel(res["plain"]["u"]),
+                      "fp64_value": res["fp64"]["value"]},
+    }
+    s.close()
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -264,6 +320,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--size", default=None,
                     help="block: nx,ny,nz; head: target elements; ensemble: instances")
+    ap.add_argument("--surrogate", action="store_true",
+                    help="head workload: plain vs learned surrogate vs FP64")
+    ap.add_argument("--train-samples", type=int, default=10_000_000)
+    ap.add_argument("--train-epochs", type=int, default=3)
+    ap.add_argument("--trust-e2", type=float, default=0.25)
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
@@ -273,6 +334,11 @@ def main():
 
     import torch
     import femtech_gb300 as ft
+
+    if args.surrogate:
+        if rank == 0:
+            surrogate_compare(args, local)
+        return
 
     if world > 1:
         import torch.distributed as dist

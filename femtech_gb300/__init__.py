@@ -217,6 +217,15 @@ class Model:
                                               st.ctypes.data, dn.ctypes.data))
         return dict(time=t, dt=dt, step=st, done=dn)
 
+    def set_surrogate(self, surrogate, trust_e2=0.25):
+        """Use a trained femtech_gb300.surrogate.Surrogate for material-7 elements
+        (None detaches); Gauss points with |E|_F^2 > trust_e2 use the plain law."""
+        L = lib()
+        L.ftgpu_set_surrogate.argtypes = [C.c_void_p, C.c_void_p, C.c_double]
+        self._surrogate = surrogate
+        _check(L.ftgpu_set_surrogate(self.h, None if surrogate is None else surrogate.h,
+                                     float(trust_e2)))
+
     def launches_per_step(self):
         return lib().ftgpu_launches_per_step(self.h)
 

@@ -217,6 +217,11 @@ struct ftgpu_model {
   std::vector<cudaEvent_t> prof_ev;
   Clock *h_clock = nullptr;  // pinned
   int *h_err = nullptr;
+  // learned surrogate for material-7 groups
+  ftgpu_surrogate *surr = nullptr;
+  SurrogateLaw surr_law{};
+  DBuf surr_x, surr_y;                // [gp][16] BF16, [gp][8] FP32
+  std::vector<long long> surr_base;   // per group: first Gauss point in the buffers
   ~ftgpu_model() {
     if (chunk_exec) cudaGraphExecDestroy(chunk_exec);
     if (prof_exec) cudaGraphExecDestroy(prof_exec);
@@ -282,6 +287,9 @@ ElemArgs<R> elem_args(ftgpu_model *m, const PatchGroup &g, int gi) {
   long long gpb = 0;
   for (int k = 0; k < gi; ++k) gpb += (long long)m->ps.groups[k].nelem * (m->ps.groups[k].etype == 0 ? 8 : 1);
   A.gpbase = gpb;
+  A.surr_x = nullptr;
+  A.surr_y = nullptr;
+  A.law = m->surr_law;
   return A;
 }
 
@@ -349,6 +357,21 @@ int launch_groups_t(ftgpu_model *m, int parity, int use_clock, double dt_direct,
     A.use_clock = use_clock;
     A.dt_direct = dt_direct;
     const size_t smem = elem_smem_bytes_host<R>(g.etype, PE);
+    if (m->surr && g.mat == 7 && dt_only == kPassForce && sizeof(R) == 4) {
+      // surrogate: features of every Gauss point, one fused MLP pass, then
+      // the force pass reading the network outputs
+      const long long base = m->surr_base[gi];
+      const long long ngp = (long long)g.nelem * (g.etype == 0 ? 8 : 1);
+      A.surr_x = m->surr_x.as<uint16_t>() + base * kMlpIn;
+      int r = launch_elem<R>(g.etype, g.mat, 0, g.npatch, PE, smem, m->stream, A,
+                             kPassSurrogateFeatures);
+      if (r) return r;
+      r = surrogate_infer(m->surr, A.surr_x, ngp, m->surr_y.as<float>() + base * kMlpOut,
+                          m->stream);
+      if (r) return r;
+      A.surr_x = nullptr;
+      A.surr_y = m->surr_y.as<float>() + base * kMlpOut;
+    }
     int r = launch_elem<R>(g.etype, g.mat, gp, g.npatch, PE, smem, m->stream, A, dt_only);
     if (r) return r;
   }
@@ -905,6 +928,28 @@ int ftgpu_set_patch_size(ftgpu_model *m, int pe) {
   if (!m || pe < 0 || pe > kMaxPatchElems) return fail(FTGPU_ERR_INPUT, "set_patch_size");
   m->patch_elems = pe;
   m->setup_done = false;
+  return FTGPU_OK;
+}
+
+int ftgpu_set_surrogate(ftgpu_model *m, ftgpu_surrogate *s, double trust_e2) {
+  if (!m || !m->setup_done) return fail(FTGPU_ERR_STATE, "set_surrogate before setup");
+  if (s && is_fp64(m)) return fail(FTGPU_ERR_STATE, "the surrogate runs in mixed precision only");
+  drop_graphs(m);
+  m->surr = s;
+  if (!s) return FTGPU_OK;
+  if (surrogate_device(s) != m->device) return fail(FTGPU_ERR_INPUT, "surrogate on another device");
+  m->surr_law = surrogate_law(s);
+  m->surr_law.trust_e2 = trust_e2;
+  m->surr_base.assign(m->ps.groups.size(), 0);
+  long long n = 0;
+  for (size_t gi = 0; gi < m->ps.groups.size(); ++gi) {
+    const PatchGroup &g = m->ps.groups[gi];
+    m->surr_base[gi] = n;
+    if (g.mat == 7) n += (long long)g.nelem * (g.etype == 0 ? 8 : 1);
+  }
+  if (n == 0) return FTGPU_OK;
+  CKI(m->surr_x.alloc(n * kMlpIn * sizeof(uint16_t)));
+  CKI(m->surr_y.alloc(n * kMlpOut * sizeof(float)));
   return FTGPU_OK;
 }
 

@@ -5,6 +5,7 @@
 #include <cstdint>
 
 #include "ft_materials.cuh"
+#include "ft_mlp.cuh"
 
 namespace ftgpu {
 
@@ -83,7 +84,14 @@ struct ElemArgs {
   int use_clock;              // 1: dt and done flags from the clock; 0: dt_direct
   double dt_direct;
   long long gpbase;
+  // learned surrogate of the material-7 isochoric stress (null when off):
+  // pass 2 writes BF16 features [gp][16], the force pass reads outputs [gp][8]
+  uint16_t *surr_x;
+  const float *surr_y;
+  SurrogateLaw law;
 };
+
+enum { kPassForce = 0, kPassDt = 1, kPassSurrogateFeatures = 2 };
 
 struct NodeArgs {
   const int *slot_off;        // [N+1]

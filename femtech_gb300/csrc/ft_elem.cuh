@@ -72,10 +72,70 @@ __device__ __forceinline__ void adj3(const R (&A)[3][3], R (&J)[3][3], R &det) {
 // Per-Gauss-point material update on the displacement gradient D = F - I.
 // hist points at this element's first history component (stride hs per
 // component, gstride per Gauss point).
+// Green strain (Voigt, tensor shear) from D
+template <class R>
+__device__ __forceinline__ void green_strain(const R (&D)[3][3], R (&E)[6]) {
+  const Sym6<R> e = two_E(D);
+  E[0] = R(0.5) * e.xx;
+  E[1] = R(0.5) * e.yy;
+  E[2] = R(0.5) * e.zz;
+  E[3] = R(0.5) * e.yz;
+  E[4] = R(0.5) * e.xz;
+  E[5] = R(0.5) * e.xy;
+}
+
+// Surrogate input features of one Gauss point as 16 BF16 values (32 bytes).
+template <class R>
+__device__ __forceinline__ void write_surrogate_features(const R (&D)[3][3], const R (&a0)[3],
+                                                         const SurrogateLaw &law, uint16_t *out) {
+  R E[6], Slin[6], scale;
+  green_strain(D, E);
+  float x[kMlpUsedIn];
+  surrogate_features(E, a0, law, x, Slin, scale);
+  uint32_t w[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const float lo = 2 * k < kMlpUsedIn ? x[2 * k] : 0.f;
+    const float hi = 2 * k + 1 < kMlpUsedIn ? x[2 * k + 1] : 0.f;
+    w[k] = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(lo)) |
+           ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(hi)) << 16);
+  }
+  reinterpret_cast<uint4 *>(out)[0] = make_uint4(w[0], w[1], w[2], w[3]);
+  reinterpret_cast<uint4 *>(out)[1] = make_uint4(w[4], w[5], w[6], w[7]);
+}
+
+// Material 7 isochoric stress from the surrogate's output sy (inside the trust
+// region |E|_F^2 <= trust_e2), else from the plain law; volumetric part exact.
+template <class R>
+__device__ __forceinline__ void goh_parts_surrogate(const MatP<R> &mp, const R (&D)[3][3], R Jm1,
+                                                    const R (&a0)[3], const float *sy,
+                                                    const SurrogateLaw &law, Sym6<R> &Si,
+                                                    Sym6<R> &Sv) {
+  R E[6], Slin[6], scale;
+  green_strain(D, E);
+  const R e2 = E[0] * E[0] + E[1] * E[1] + E[2] * E[2] +
+               R(2) * (E[3] * E[3] + E[4] * E[4] + E[5] * E[5]);
+  if (!(e2 <= R(law.trust_e2))) {
+    mat_hgo_parts<R, true>(mp, D, Jm1, a0, Si, Sv);
+    return;
+  }
+  float x[kMlpUsedIn];
+  surrogate_features(E, a0, law, x, Slin, scale);
+  Si = Sym6<R>{Slin[0] + scale * R(sy[0]), Slin[1] + scale * R(sy[1]),
+               Slin[2] + scale * R(sy[2]), Slin[3] + scale * R(sy[3]),
+               Slin[4] + scale * R(sy[4]), Slin[5] + scale * R(sy[5])};
+  const Sym6<R> ce = two_E(D);
+  const Sym6<R> ac = adj_I_plus(ce);
+  const R J = 1 + Jm1;
+  const R Jp = R(0.5) * mp.K * Jm1 * (2 + Jm1) / (J * J);
+  Sv = sym_scale(ac, Jp);
+}
+
 template <class R, int MAT>
 __device__ __forceinline__ Sym6<R> stress_at(const MatP<R> &mp, const R (&D)[3][3], R Jm1,
                                              const R (&a0)[3], R *hist, long long hs,
-                                             const R (&pc)[4]) {
+                                             const R (&pc)[4], const float *sy,
+                                             const SurrogateLaw &law) {
   Sym6<R> S;
   if (MAT == 0) {
     S = Sym6<R>{0, 0, 0, 0, 0, 0};
@@ -94,7 +154,10 @@ __device__ __forceinline__ Sym6<R> stress_at(const MatP<R> &mp, const R (&D)[3][
     S = mat_ogden(mp, D, Jm1);
   } else {  // 5 / 7: HGO family + Prony series (HGOIsotropicViscoelastic.cpp:98-159)
     Sym6<R> Si, Sv;
-    mat_hgo_parts<R, MAT == 7>(mp, D, Jm1, a0, Si, Sv);
+    if (MAT == 7 && sy != nullptr)
+      goh_parts_surrogate(mp, D, Jm1, a0, sy, law, Si, Sv);
+    else
+      mat_hgo_parts<R, MAT == 7>(mp, D, Jm1, a0, Si, Sv);
     R sd[6] = {Si.xx, Si.yy, Si.zz, Si.yz, Si.xz, Si.xy};
     R sv[6] = {Sv.xx, Sv.yy, Sv.zz, Sv.yz, Sv.xz, Sv.xy};
     constexpr int NT = MAT == 5 ? 2 : 1;
@@ -179,8 +242,9 @@ template <class R, int MAT, bool GP>
 __device__ __forceinline__ void hex_element(const R (&x)[8][3], const R (&u)[8][3],
                                             const MatP<R> &mp, const R (&pc)[4],
                                             const R (&a0)[3], R *hist, long long hs,
-                                            long long gs, bool dt_only, R (&f)[8][3], R &le,
+                                            long long gs, int pass, R (&f)[8][3], R &le,
                                             int &bad, const ElemArgs<R> &A, long long gpo) {
+  const bool dt_only = pass == kPassDt;
   // characteristic length on the current geometry first (volume / max face
   // area, CalculateCharacteristicLength_C3D8.cpp:6-29) so that the nodal
   // values are dead before the Gauss loop; the 2x2x2 Gauss sum of
@@ -248,7 +312,13 @@ __device__ __forceinline__ void hex_element(const R (&x)[8][3], const R (&u)[8][
     const R Jm1 = jm1_of(D);
     if (!(Jm1 > R(-1)) || !(detA != 0)) bad = 1;
     vol += (1 + Jm1) * detA;
-    Sym6<R> S = stress_at<R, MAT>(mp, D, Jm1, a0, hist + g * gs, hs, pc);
+    const long long sg = gpo - A.gpbase + g;  // Gauss point within the group
+    if (MAT == 7 && pass == kPassSurrogateFeatures) {
+      write_surrogate_features(D, a0, A.law, A.surr_x + sg * kMlpIn);
+      continue;
+    }
+    const float *sy = (MAT == 7 && A.surr_y) ? A.surr_y + sg * kMlpOut : nullptr;
+    Sym6<R> S = stress_at<R, MAT>(mp, D, Jm1, a0, hist + g * gs, hs, pc, sy, A.law);
     if (GP) {
       long long q = gpo + g;
 #pragma unroll
@@ -285,7 +355,7 @@ __device__ __forceinline__ void hex_element(const R (&x)[8][3], const R (&u)[8][
       m[6][i] += ez * g0 + xz * g1 + xe * g2;
     }
   }
-  if (!dt_only) {
+  if (pass == kPassForce) {
     // inverse transform: f_a = 1/8 sum_k sign_k(a) m_k
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
@@ -314,8 +384,9 @@ template <class R, int MAT, bool GP>
 __device__ __forceinline__ void tet_element(const R (&x)[4][3], const R (&u)[4][3],
                                             const MatP<R> &mp, const R (&pc)[4],
                                             const R (&a0)[3], R *hist, long long hs,
-                                            bool dt_only, R (&f)[4][3], R &le, int &bad,
+                                            int pass, R (&f)[4][3], R &le, int &bad,
                                             const ElemArgs<R> &A, long long gpo) {
+  const bool dt_only = pass != kPassForce;
   R Am[3][3], H[3][3];
 #pragma unroll
   for (int r = 0; r < 3; ++r)
@@ -335,8 +406,15 @@ __device__ __forceinline__ void tet_element(const R (&x)[4][3], const R (&u)[4][
       D[i][j] = idet * (H[i][0] * Ad[j][0] + H[i][1] * Ad[j][1] + H[i][2] * Ad[j][2]);
   const R Jm1 = jm1_of(D);
   if (!(Jm1 > R(-1)) || !(detA != 0)) bad = 1;
+  const long long sg = gpo - A.gpbase;  // Gauss point within the group
+  if (MAT == 7 && pass == kPassSurrogateFeatures) {
+    write_surrogate_features(D, a0, A.law, A.surr_x + sg * kMlpIn);
+    le = R(1);
+    return;
+  }
   if (!dt_only) {
-    Sym6<R> S = stress_at<R, MAT>(mp, D, Jm1, a0, hist, hs, pc);
+    const float *sy = (MAT == 7 && A.surr_y) ? A.surr_y + sg * kMlpOut : nullptr;
+    Sym6<R> S = stress_at<R, MAT>(mp, D, Jm1, a0, hist, hs, pc, sy, A.law);
     if (GP) {
 #pragma unroll
       for (int i = 0; i < 3; ++i)
@@ -405,7 +483,7 @@ template <class R, int ET, int MAT, bool GP>
 // At most 128 registers per thread (two 256-thread or four 128-thread blocks
 // per SM); only the rarely taken eigen-decomposition fallback of the Ogden law
 // needs more and spills there.
-__global__ void __launch_bounds__(kElemThreads, 2) k_elem(const ElemArgs<R> A, int dt_only) {
+__global__ void __launch_bounds__(kElemThreads, 2) k_elem(const ElemArgs<R> A, int pass) {
   constexpr int NC = ET == 0 ? 8 : 4;
   constexpr int NGP = ET == 0 ? 8 : 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -473,12 +551,12 @@ __global__ void __launch_bounds__(kElemThreads, 2) k_elem(const ElemArgs<R> A, i
     if (ET == 0)
       hex_element<R, MAT, GP>(reinterpret_cast<const R(&)[8][3]>(x),
                               reinterpret_cast<const R(&)[8][3]>(u), mp, pc, a0, hist, hs, gs,
-                              dt_only != 0, reinterpret_cast<R(&)[8][3]>(f), le, bad, A, gpo);
+                              pass, reinterpret_cast<R(&)[8][3]>(f), le, bad, A, gpo);
     else
       tet_element<R, MAT, GP>(reinterpret_cast<const R(&)[4][3]>(x),
                               reinterpret_cast<const R(&)[4][3]>(u), mp, pc, a0, hist, hs,
-                              dt_only != 0, reinterpret_cast<R(&)[4][3]>(f), le, bad, A, gpo);
-    if (!dt_only) {
+                              pass, reinterpret_cast<R(&)[4][3]>(f), le, bad, A, gpo);
+    if (pass == kPassForce) {
 #pragma unroll
       for (int a = 0; a < NC; ++a)
 #pragma unroll
@@ -487,6 +565,7 @@ __global__ void __launch_bounds__(kElemThreads, 2) k_elem(const ElemArgs<R> A, i
     if (!skip) dte = dt_of<R>(le, mp);
   }
   if (bad) atomicOr(A.err, (bad & 1 ? kErrInverted : 0) | (bad & 2 ? kErrIndex : 0));
+  if (pass == kPassSurrogateFeatures) return;  // features only (uniform per block)
   // block minimum of the element time steps -> one FP64 atomicMin per block
   // (positive doubles order like their bit patterns)
 #pragma unroll
@@ -499,7 +578,7 @@ __global__ void __launch_bounds__(kElemThreads, 2) k_elem(const ElemArgs<R> A, i
     for (int w = 1; w < (PE + 31) / 32; ++w) mn = fmin(mn, wmin[w]);
     atomicMin(A.dtmin + A.parity * A.ninst + inst, (unsigned long long)__double_as_longlong(mn));
   }
-  if (dt_only) return;
+  if (pass != kPassForce) return;
   // in-block assembly: local node i sums its corners in (element, corner) order
   const uint16_t *lp = A.lptr + s0 + p;
   const uint16_t *le = A.lent + A.patch_ent_off[p];

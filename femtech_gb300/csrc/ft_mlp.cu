@@ -500,6 +500,33 @@ int backward(ftgpu_surrogate *s, const bf16 *X, const float *T, long long B) {
 
 }  // namespace
 
+namespace ftgpu {
+
+int surrogate_infer(ftgpu_surrogate *s, const uint16_t *X, long long n, float *Y,
+                    cudaStream_t st) {
+  static bool attr_set[64] = {false};
+  if (n <= 0) return 0;
+  if (s->device >= 0 && s->device < 64 && !attr_set[s->device]) {
+    if (cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kInferSmem) != cudaSuccess)
+      return FTGPU_ERR_CUDA;
+    attr_set[s->device] = true;
+  }
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
+  const long long tiles = (n + 15) / 16;
+  long long grid = std::min<long long>((long long)sms * 2, (tiles + 7) / 8);
+  if (grid < 1) grid = 1;
+  k_mlp_infer<<<(unsigned)grid, 256, kInferSmem, st>>>(reinterpret_cast<const bf16 *>(X), n, s->Wb,
+                                                       s->P, Y);
+  return cudaGetLastError() == cudaSuccess ? 0 : FTGPU_ERR_CUDA;
+}
+
+SurrogateLaw surrogate_law(const ftgpu_surrogate *s) { return s->law; }
+int surrogate_device(const ftgpu_surrogate *s) { return s->device; }
+
+}  // namespace ftgpu
+
 extern "C" {
 
 int ftgpu_surrogate_create(ftgpu_surrogate **out, int device, const double *props,
@@ -632,6 +659,24 @@ int ftgpu_surrogate_forward(ftgpu_surrogate *s, long long n, const float *x, flo
   SCK(cudaStreamSynchronize(s->stream));
   SCK(cudaMemcpy(y, s->Y, n * kMlpOut * 4, cudaMemcpyDeviceToHost));
   cudaFree(dX);
+  return r;
+}
+
+// the same outputs through the fused persistent inference kernel (in-loop path)
+int ftgpu_surrogate_infer(ftgpu_surrogate *s, long long n, const float *x, float *y) {
+  if (!s || n <= 0 || !x || !y) return FTGPU_ERR_INPUT;
+  SCK(cudaSetDevice(s->device));
+  std::vector<bf16> xb(n * kMlpIn);
+  for (long long i = 0; i < n * kMlpIn; ++i) xb[i] = __float2bfloat16_rn(x[i]);
+  bf16 *dX = nullptr;
+  float *dY = nullptr;
+  if (dalloc(&dX, n * kMlpIn) || dalloc(&dY, n * kMlpOut)) return FTGPU_ERR_ALLOC;
+  SCK(cudaMemcpy(dX, xb.data(), n * kMlpIn * 2, cudaMemcpyHostToDevice));
+  int r = surrogate_infer(s, reinterpret_cast<const uint16_t *>(dX), n, dY, s->stream);
+  SCK(cudaStreamSynchronize(s->stream));
+  SCK(cudaMemcpy(y, dY, n * kMlpOut * 4, cudaMemcpyDeviceToHost));
+  cudaFree(dX);
+  cudaFree(dY);
   return r;
 }
 

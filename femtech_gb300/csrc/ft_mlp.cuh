@@ -17,6 +17,9 @@
 #pragma once
 
 #include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
 
 #include "ft_materials.cuh"
 
@@ -72,4 +75,14 @@ __host__ __device__ inline void surrogate_features(const R (&E)[6], const R (&a0
   x[8] = float(a0[2]);
 }
 
+}  // namespace ftgpu
+
+struct ftgpu_surrogate;
+namespace ftgpu {
+// host side, implemented in ft_mlp.cu: fused inference of n feature rows
+// (BF16 bits [n][16]) into outputs [n][8] on stream st; the trained law
+int surrogate_infer(ftgpu_surrogate *s, const uint16_t *X, long long n, float *Y,
+                    cudaStream_t st);
+SurrogateLaw surrogate_law(const ftgpu_surrogate *s);
+int surrogate_device(const ftgpu_surrogate *s);
 }  // namespace ftgpu

@@ -207,6 +207,8 @@ int ftgpu_surrogate_train(ftgpu_surrogate *s, int epochs, int batch, double lr,
                           double *final_loss);
 /* raw network outputs y[n][8] for features x[n][16] (host arrays) */
 int ftgpu_surrogate_forward(ftgpu_surrogate *s, long long n, const float *x, float *y);
+/* the same through the fused persistent inference kernel used in the loop */
+int ftgpu_surrogate_infer(ftgpu_surrogate *s, long long n, const float *x, float *y);
 /* MSE loss and its gradient w.r.t. the FP32 parameter vector for one batch */
 int ftgpu_surrogate_gradient(ftgpu_surrogate *s, long long n, const float *x, const float *t,
                              float *grad, double *loss);
@@ -215,6 +217,10 @@ int ftgpu_surrogate_params(ftgpu_surrogate *s, float *get, const float *set);
 /* the first n generated samples: features x[n][16], targets t[n][8] */
 int ftgpu_surrogate_samples(ftgpu_surrogate *s, long long n, float *x, float *t);
 int ftgpu_surrogate_num_params(void);
+/* Use the surrogate for every material-7 element of the model (mixed
+ * precision; after ftgpu_setup).  Gauss points with |E|_F^2 > trust_e2 fall
+ * back to the plain law.  s = NULL detaches it. */
+int ftgpu_set_surrogate(ftgpu_model *m, ftgpu_surrogate *s, double trust_e2);
 
 /* ---- allocation-free internal force (no counterpart in the reference) ----
  * For callers that cannot let a library allocate device memory (they own all

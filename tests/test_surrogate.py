@@ -118,6 +118,43 @@ def test_training_samples_follow_the_plain_law():
 
 
 @pytest.mark.gpu
+def test_fused_inference_kernel_matches_training_forward():
+    from femtech_gb300.surrogate import Surrogate
+    import ctypes as C
+    s = Surrogate(PROPS7, seed=6)
+    rng = np.random.default_rng(2)
+    s.params = rand_params(rng).astype(np.float32)
+    x, _ = rand_batch(rng, 3001)  # not a multiple of the 16-row tiles
+    x = x.astype(np.float32)
+    y_gen = s.forward(x)
+    y_fused = np.zeros_like(y_gen)
+    s.L.ftgpu_surrogate_infer.argtypes = [C.c_void_p, C.c_longlong, C.c_void_p, C.c_void_p]
+    assert s.L.ftgpu_surrogate_infer(s.h, len(x), x.ctypes.data, y_fused.ctypes.data) == 0
+    assert np.abs(y_fused - y_gen).max() <= 1e-2 * np.abs(y_gen).max()
+    s.close()
+
+
+@pytest.mark.gpu
+def test_surrogate_outside_trust_region_equals_plain_path():
+    import femtech_gb300 as ft
+    from femtech_gb300 import meshgen as mg
+    from femtech_gb300.surrogate import Surrogate
+    mesh, mats, loads = mg.head_case(target_elements=8_000, seed=2)
+    s = Surrogate(PROPS7, seed=1)  # untrained: every Gauss point must fall back
+    out = []
+    for use in (False, True):
+        m = ft.Model(mesh, mats, precision=ft.MIXED, loads=loads)
+        if use:
+            m.set_surrogate(s, trust_e2=-1.0)
+        m.init_explicit(0.9, 0.0, 1.0)
+        m.run(120)
+        out.append(m.state()["u"])
+        m.close()
+    assert np.array_equal(out[0], out[1])
+    s.close()
+
+
+@pytest.mark.gpu
 def test_trained_network_gains_over_the_linearised_law():
     from femtech_gb300.surrogate import Surrogate, linear_part
     s = Surrogate(PROPS7, seed=5)
