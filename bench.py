@@ -324,7 +324,7 @@ def main():
                     help="head workload: plain vs learned surrogate vs FP64")
     ap.add_argument("--train-samples", type=int, default=10_000_000)
     ap.add_argument("--train-epochs", type=int, default=3)
-    ap.add_argument("--trust-e2", type=float, default=0.25)
+    ap.add_argument("--trust-e2", type=float, default=0.04)
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":

@@ -217,7 +217,7 @@ class Model:
                                               st.ctypes.data, dn.ctypes.data))
         return dict(time=t, dt=dt, step=st, done=dn)
 
-    def set_surrogate(self, surrogate, trust_e2=0.25):
+    def set_surrogate(self, surrogate, trust_e2=0.04):
         """Use a trained femtech_gb300.surrogate.Surrogate for material-7 elements
         (None detaches); Gauss points with |E|_F^2 > trust_e2 use the plain law."""
         L = lib()

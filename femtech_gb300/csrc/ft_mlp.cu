@@ -212,6 +212,51 @@ __global__ void k_sum(const float *v, long long n, float *out) {
   if (threadIdx.x == 0) *out = red[0];
 }
 
+// sum of squares of the used target columns, FP64, one partial per block
+// (summed on the host in block order, so the result is reproducible)
+__global__ void k_target_sumsq(const float *T, long long n, double *out) {
+  __shared__ double red[256];
+  double s = 0.0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n * kMlpOut;
+       i += (long long)gridDim.x * blockDim.x)
+    if ((i % kMlpOut) < kMlpUsedOut) s += double(T[i]) * double(T[i]);
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[blockIdx.x] = red[0];
+}
+
+__global__ void k_scale(float *v, long long n, float a) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    v[i] *= a;
+}
+
+// features of host-given strains (for ftgpu_surrogate_predict): BF16 rows,
+// the linear part and the output scale, as the element kernel forms them
+__global__ void k_predict_features(long long n, const double *E, const double *a0,
+                                   SurrogateLaw law, bf16 *X, double *Slin, double *scale) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double e[6], a[3], sl[6], sc;
+  for (int k = 0; k < 6; ++k) e[k] = E[6 * i + k];
+  for (int k = 0; k < 3; ++k) a[k] = a0[3 * i + k];
+  float xf[kMlpUsedIn];
+  surrogate_features(e, a, law, xf, sl, sc);
+  for (int k = 0; k < kMlpIn; ++k) X[i * kMlpIn + k] = __float2bfloat16_rn(k < kMlpUsedIn ? xf[k] : 0.f);
+  for (int k = 0; k < 6; ++k) Slin[6 * i + k] = sl[k];
+  scale[i] = sc;
+}
+
+__global__ void k_predict_combine(long long n, const float *Y, double *Slin, const double *scale) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int k = 0; k < 6; ++k) Slin[6 * i + k] += scale[i] * double(Y[i * kMlpOut + k]);
+}
+
 // Adam on the FP32 master parameters, then the BF16 weight copies
 __global__ void k_adam(float *P, const float *G, float *Mo, float *V, int n, float lr, float b1,
                        float b2, float eps, float c1, float c2, bf16 *Wb) {
@@ -552,7 +597,7 @@ int ftgpu_surrogate_create(ftgpu_surrogate **out, int device, const double *prop
   s->law.kappa = props[7];
   s->law.s0 = props[1] + props[3];
   s->law.out_scale = 1.0;
-  s->law.trust_e2 = 0.25;
+  s->law.trust_e2 = 0.04;
   int r = dalloc(&s->P, kMlpParams) | dalloc(&s->G, kMlpParams) | dalloc(&s->Mo, kMlpParams) |
           dalloc(&s->V, kMlpParams) | dalloc(&s->Wb, kMlpParams);
   if (r) return FTGPU_ERR_ALLOC;
@@ -597,8 +642,27 @@ int ftgpu_surrogate_generate(ftgpu_surrogate *s, long long n, unsigned long long
   SCK(cudaSetDevice(s->device));
   int r = dalloc(&s->X, n * kMlpIn) | dalloc(&s->T, n * kMlpOut);
   if (r) return FTGPU_ERR_ALLOC;
+  // targets relative to s0 |E|^2 first, then normalised to unit RMS; the RMS
+  // becomes the law's out_scale
+  s->law.out_scale = 1.0;
   k_mlp_gen<<<(unsigned)((n + 127) / 128), 128, 0, s->stream>>>(n, seed, stretch_lo, stretch_hi,
                                                                  s->mp, s->law, s->X, s->T);
+  SCK(cudaGetLastError());
+  constexpr int kParts = 1024;
+  double *dss = nullptr;
+  if (dalloc(&dss, kParts)) return FTGPU_ERR_ALLOC;
+  k_target_sumsq<<<kParts, 256, 0, s->stream>>>(s->T, n, dss);
+  std::vector<double> part(kParts);
+  SCK(cudaMemcpyAsync(part.data(), dss, kParts * sizeof(double), cudaMemcpyDeviceToHost,
+                      s->stream));
+  SCK(cudaStreamSynchronize(s->stream));
+  cudaFree(dss);
+  double ss = 0.0;
+  for (double v : part) ss += v;
+  const double rms = sqrt(ss / (double(n) * kMlpUsedOut));
+  if (!(rms > 0.0) || !std::isfinite(rms)) return FTGPU_ERR_INPUT;
+  s->law.out_scale = rms;
+  k_scale<<<1024, 256, 0, s->stream>>>(s->T, n * kMlpOut, float(1.0 / rms));
   SCK(cudaGetLastError());
   SCK(cudaStreamSynchronize(s->stream));
   s->nsamples = n;
@@ -730,5 +794,38 @@ int ftgpu_surrogate_samples(ftgpu_surrogate *s, long long n, float *x, float *t)
 }
 
 int ftgpu_surrogate_num_params(void) { return kMlpParams; }
+
+// isochoric PK2 (Voigt) predicted for Green strains E[n][6] (tensor shears) and
+// fibres a0[n][3]: the element kernel's features, fused inference, S_lin +
+// scale * NN, all on the device
+int ftgpu_surrogate_predict(ftgpu_surrogate *s, long long n, const double *E, const double *a0,
+                            double *S) {
+  if (!s || n <= 0 || !E || !a0 || !S) return FTGPU_ERR_INPUT;
+  SCK(cudaSetDevice(s->device));
+  double *dE = nullptr, *dA = nullptr, *dS = nullptr, *dsc = nullptr;
+  bf16 *dX = nullptr;
+  float *dY = nullptr;
+  int r = dalloc(&dE, 6 * n) | dalloc(&dA, 3 * n) | dalloc(&dS, 6 * n) | dalloc(&dsc, n) |
+          dalloc(&dX, n * kMlpIn) | dalloc(&dY, n * kMlpOut);
+  if (!r) {
+    SCK(cudaMemcpy(dE, E, 6 * n * sizeof(double), cudaMemcpyHostToDevice));
+    SCK(cudaMemcpy(dA, a0, 3 * n * sizeof(double), cudaMemcpyHostToDevice));
+    const unsigned g = (unsigned)((n + 127) / 128);
+    k_predict_features<<<g, 128, 0, s->stream>>>(n, dE, dA, s->law, dX, dS, dsc);
+    r = surrogate_infer(s, reinterpret_cast<const uint16_t *>(dX), n, dY, s->stream);
+    k_predict_combine<<<g, 128, 0, s->stream>>>(n, dY, dS, dsc);
+    SCK(cudaStreamSynchronize(s->stream));
+    SCK(cudaMemcpy(S, dS, 6 * n * sizeof(double), cudaMemcpyDeviceToHost));
+  } else {
+    r = FTGPU_ERR_ALLOC;
+  }
+  cudaFree(dE);
+  cudaFree(dA);
+  cudaFree(dS);
+  cudaFree(dsc);
+  cudaFree(dX);
+  cudaFree(dY);
+  return r;
+}
 
 }  // extern "C"

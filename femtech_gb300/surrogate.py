@@ -2,9 +2,13 @@
 
 ``Surrogate`` wraps the ftgpu_surrogate_* entry points: generate training
 samples from the plain law on the GPU, train the BF16 MLP with the GPU's
-forward / backward / Adam kernels, predict.  ``features`` and ``reconstruct``
-are the host mirror of ``surrogate_features`` in csrc/ft_mlp.cuh: the network
-predicts S_iso = S_lin(E, a0) + s0 * out_scale * |E|^2 * NN(x).
+forward / backward / Adam kernels, predict.  The network predicts
+S_iso = S_lin(E, a0) + s0 * out_scale * |E|^2 * NN(x); ``linear_part``,
+``features`` and ``e2_of`` are the host mirror of ``surrogate_features`` in
+csrc/ft_mlp.cuh, and ``predict`` runs that reconstruction on the device.
+
+The default sampling box (principal stretches 0.77..1.19) covers the default
+trust region |E|_F^2 <= 0.04 (every |E_ii| <= 0.2), where the network is used.
 """
 import ctypes as C
 
@@ -16,6 +20,8 @@ N_IN, N_HID, N_OUT = 16, 128, 8
 USED_IN, USED_OUT = 9, 6
 STRAIN_SCALE = 0.5
 E2_FLOOR = 1e-14
+TRUST_E2 = 0.04
+STRETCH_LO, STRETCH_HI = 0.77, 1.19
 
 
 def _bind():
@@ -30,6 +36,7 @@ def _bind():
     L.ftgpu_surrogate_params.argtypes = [vp, vp, vp]
     L.ftgpu_surrogate_samples.argtypes = [vp, C.c_longlong, vp, vp]
     L.ftgpu_surrogate_num_params.restype = C.c_int
+    L.ftgpu_surrogate_predict.argtypes = [vp, C.c_longlong, vp, vp, vp]
     return L
 
 
@@ -90,7 +97,7 @@ class Surrogate:
         except Exception:
             pass
 
-    def generate(self, n, seed=1, lo=0.7, hi=1.4):
+    def generate(self, n, seed=1, lo=STRETCH_LO, hi=STRETCH_HI):
         _check(self.L.ftgpu_surrogate_generate(self.h, int(n), int(seed), float(lo), float(hi)))
 
     def train(self, epochs=2, batch=8192, lr=2e-3):
@@ -131,6 +138,10 @@ class Surrogate:
         return x, t
 
     def predict(self, E, a0):
-        """S_iso (Voigt) from Green strains E[n,6] and fibres a0[n,3]."""
-        y = self.forward(features(E, a0)).astype(np.float64)[:, :USED_OUT]
-        return linear_part(E, a0, self.mu, self.k1, self.kappa) + (self.s0 * e2_of(E))[:, None] * y
+        """S_iso (Voigt) from Green strains E[n,6] and fibres a0[n,3], on the device."""
+        E = np.ascontiguousarray(E, np.float64)
+        a0 = np.ascontiguousarray(a0, np.float64)
+        S = np.zeros((len(E), 6))
+        _check(self.L.ftgpu_surrogate_predict(self.h, len(E), E.ctypes.data, a0.ctypes.data,
+                                              S.ctypes.data))
+        return S

@@ -199,7 +199,9 @@ typedef struct ftgpu_surrogate ftgpu_surrogate;
 int ftgpu_surrogate_create(ftgpu_surrogate **out, int device, const double *properties,
                            unsigned long long seed);
 int ftgpu_surrogate_destroy(ftgpu_surrogate *s);
-/* nsamples states: random rotation, principal stretches in [lo, hi], random fibre */
+/* nsamples states: random rotation, principal stretches in [lo, hi], random
+ * fibre; targets normalised to unit RMS (the RMS becomes the output scale).
+ * The sampled box should cover the trust region: |E_ii| <= sqrt(trust_e2). */
 int ftgpu_surrogate_generate(ftgpu_surrogate *s, long long nsamples, unsigned long long seed,
                              double stretch_lo, double stretch_hi);
 /* Adam (cosine-decayed lr) over the generated samples; *final_loss = last batch MSE */
@@ -217,6 +219,11 @@ int ftgpu_surrogate_params(ftgpu_surrogate *s, float *get, const float *set);
 /* the first n generated samples: features x[n][16], targets t[n][8] */
 int ftgpu_surrogate_samples(ftgpu_surrogate *s, long long n, float *x, float *t);
 int ftgpu_surrogate_num_params(void);
+/* predicted isochoric PK2 S[n][6] (Voigt 11 22 33 23 13 12) for Green strains
+ * E[n][6] (same order, tensor shears) and unit fibres a0[n][3], through the
+ * element kernel's features and the fused inference kernel */
+int ftgpu_surrogate_predict(ftgpu_surrogate *s, long long n, const double *E, const double *a0,
+                            double *S);
 /* Use the surrogate for every material-7 element of the model (mixed
  * precision; after ftgpu_setup).  Gauss points with |E|_F^2 > trust_e2 fall
  * back to the plain law.  s = NULL detaches it. */

@@ -158,14 +158,17 @@ def test_surrogate_outside_trust_region_equals_plain_path():
 def test_trained_network_gains_over_the_linearised_law():
     from femtech_gb300.surrogate import Surrogate, linear_part
     s = Surrogate(PROPS7, seed=5)
-    s.generate(400_000, seed=11)
-    loss = s.train(epochs=6, batch=4096, lr=2e-3)
+    s.generate(1_000_000, seed=11)
+    loss = s.train(epochs=8, batch=4096, lr=2e-3)
     assert np.isfinite(loss)
+    # held-out states inside the sampled box (stretches 0.85..1.15, |E|_F^2 < 0.06);
+    # the method without the network is the law's linearisation S_lin
     rng = np.random.default_rng(12)
-    E, A, S = held_out_states(rng, 400)
+    E, A, S = held_out_states(rng, 400, 0.85, 1.15)
     pred = s.predict(E, A)
     lin = linear_part(E, A, s.mu, s.k1, s.kappa)
     err_nn = np.linalg.norm(pred - S) / np.linalg.norm(S)
     err_lin = np.linalg.norm(lin - S) / np.linalg.norm(S)
+    print("held-out relative stress error: network %.4f, linearisation %.4f" % (err_nn, err_lin))
     assert err_nn < 0.05 and err_nn < err_lin / 5, (err_nn, err_lin)
     s.close()
