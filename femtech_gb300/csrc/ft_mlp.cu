@@ -795,6 +795,12 @@ int ftgpu_surrogate_samples(ftgpu_surrogate *s, long long n, float *x, float *t)
 
 int ftgpu_surrogate_num_params(void) { return kMlpParams; }
 
+int ftgpu_surrogate_output_scale(ftgpu_surrogate *s, double *out_scale) {
+  if (!s || !out_scale) return FTGPU_ERR_INPUT;
+  *out_scale = s->law.out_scale;
+  return FTGPU_OK;
+}
+
 // isochoric PK2 (Voigt) predicted for Green strains E[n][6] (tensor shears) and
 // fibres a0[n][3]: the element kernel's features, fused inference, S_lin +
 // scale * NN, all on the device

@@ -5,7 +5,8 @@ samples from the plain law on the GPU, train the BF16 MLP with the GPU's
 forward / backward / Adam kernels, predict.  The network predicts
 S_iso = S_lin(E, a0) + s0 * out_scale * |E|^2 * NN(x); ``linear_part``,
 ``features`` and ``e2_of`` are the host mirror of ``surrogate_features`` in
-csrc/ft_mlp.cuh, and ``predict`` runs that reconstruction on the device.
+csrc/ft_mlp.cuh (S_lin uses the exact fibre strain Ebar for the fibre switch),
+and ``predict`` runs that reconstruction on the device.
 
 The default sampling box (principal stretches 0.77..1.19) covers the default
 trust region |E|_F^2 <= 0.04 (every |E_ii| <= 0.2), where the network is used.
@@ -17,8 +18,8 @@ import numpy as np
 from . import _check, lib
 
 N_IN, N_HID, N_OUT = 16, 128, 8
-USED_IN, USED_OUT = 9, 6
-STRAIN_SCALE = 0.5
+USED_IN, USED_OUT = 11, 6
+STRAIN_SCALE = 0.2
 E2_FLOOR = 1e-14
 TRUST_E2 = 0.04
 STRETCH_LO, STRETCH_HI = 0.77, 1.19
@@ -37,20 +38,35 @@ def _bind():
     L.ftgpu_surrogate_samples.argtypes = [vp, C.c_longlong, vp, vp]
     L.ftgpu_surrogate_num_params.restype = C.c_int
     L.ftgpu_surrogate_predict.argtypes = [vp, C.c_longlong, vp, vp, vp]
+    L.ftgpu_surrogate_output_scale.argtypes = [vp, C.POINTER(C.c_double)]
     return L
 
 
+def fibre_strain(E, a0, kappa):
+    """Exact GOH fibre strain kappa (I1bar - 3) + (1 - 3 kappa)(I4bar - 1)."""
+    X = 2.0 * np.asarray(E, np.float64)
+    a0 = np.asarray(a0, np.float64)
+    tr = X[:, 0] + X[:, 1] + X[:, 2]
+    i2 = ((X[:, 0] * X[:, 1] - X[:, 5] ** 2) + (X[:, 0] * X[:, 2] - X[:, 4] ** 2)
+          + (X[:, 1] * X[:, 2] - X[:, 3] ** 2))
+    i3 = (X[:, 0] * (X[:, 1] * X[:, 2] - X[:, 3] ** 2) - X[:, 5] * (X[:, 5] * X[:, 2] - X[:, 3] * X[:, 4])
+          + X[:, 4] * (X[:, 5] * X[:, 3] - X[:, 1] * X[:, 4]))
+    jm = np.expm1(-np.log1p(tr + i2 + i3) / 3.0)
+    aXa = (a0[:, 0] ** 2 * X[:, 0] + a0[:, 1] ** 2 * X[:, 1] + a0[:, 2] ** 2 * X[:, 2]
+           + 2 * (a0[:, 1] * a0[:, 2] * X[:, 3] + a0[:, 0] * a0[:, 2] * X[:, 4]
+                  + a0[:, 0] * a0[:, 1] * X[:, 5]))
+    return kappa * (jm * (3.0 + tr) + tr) + (1.0 - 3.0 * kappa) * (jm * (1.0 + aXa) + aXa)
+
+
 def linear_part(E, a0, mu, k1, kappa):
-    """S_lin (Voigt 11,22,33,23,13,12) for strains E[n,6] (tensor shear) and fibres a0[n,3]."""
+    """S_lin (Voigt 11,22,33,23,13,12) for strains E[n,6] (tensor shear) and fibres a0[n,3]:
+    2 mu dev E + 2 k1 (1 - 3 kappa) max(Ebar, 0) dev(a0 a0), Ebar the exact fibre strain."""
     E = np.asarray(E, np.float64)
     a0 = np.asarray(a0, np.float64)
     tr3 = (E[:, 0] + E[:, 1] + E[:, 2]) / 3.0
-    aEa = (a0[:, 0] ** 2 * E[:, 0] + a0[:, 1] ** 2 * E[:, 1] + a0[:, 2] ** 2 * E[:, 2]
-           + 2 * (a0[:, 1] * a0[:, 2] * E[:, 3] + a0[:, 0] * a0[:, 2] * E[:, 4]
-                  + a0[:, 0] * a0[:, 1] * E[:, 5]))
     c4 = 1.0 - 3.0 * kappa
-    Ea = 2.0 * c4 * (aEa - tr3)
-    f = np.where(Ea > 0, 2.0 * k1 * c4 * Ea, 0.0)
+    Eb = fibre_strain(E, a0, kappa)
+    f = np.where(Eb > 0, 2.0 * k1 * c4 * Eb, 0.0)
     S = np.empty_like(E)
     S[:, 0] = 2 * mu * (E[:, 0] - tr3) + f * (a0[:, 0] ** 2 - 1 / 3)
     S[:, 1] = 2 * mu * (E[:, 1] - tr3) + f * (a0[:, 1] ** 2 - 1 / 3)
@@ -61,17 +77,28 @@ def linear_part(E, a0, mu, k1, kappa):
     return S
 
 
-def features(E, a0):
-    x = np.zeros((len(E), N_IN), np.float32)
-    x[:, :6] = np.asarray(E) / STRAIN_SCALE
-    x[:, 6:9] = a0
-    return x
-
-
 def e2_of(E):
     E = np.asarray(E)
     e2 = E[:, 0] ** 2 + E[:, 1] ** 2 + E[:, 2] ** 2 + 2 * (E[:, 3] ** 2 + E[:, 4] ** 2 + E[:, 5] ** 2)
     return np.maximum(e2, E2_FLOOR)
+
+
+def features(E, a0, kappa):
+    """Network inputs: E / |E|_F, |E|_F / 0.2, a0, Ebar / |E|_F."""
+    E = np.asarray(E, np.float64)
+    en = np.sqrt(e2_of(E))
+    x = np.zeros((len(E), N_IN), np.float32)
+    x[:, :6] = E / en[:, None]
+    x[:, 6] = en / STRAIN_SCALE
+    x[:, 7:10] = a0
+    x[:, 10] = fibre_strain(E, a0, kappa) / en
+    return x
+
+
+def strain_of(x):
+    """Green strain back from (BF16-rounded) features."""
+    x = np.asarray(x, np.float64)
+    return x[:, :6] * (x[:, 6] * STRAIN_SCALE)[:, None]
 
 
 class Surrogate:
@@ -130,6 +157,13 @@ class Surrogate:
     def params(self, p):
         p = np.ascontiguousarray(p, np.float32)
         _check(self.L.ftgpu_surrogate_params(self.h, None, p.ctypes.data))
+
+    @property
+    def out_scale(self):
+        """RMS of the generated targets: the network output is in these units."""
+        v = C.c_double()
+        _check(self.L.ftgpu_surrogate_output_scale(self.h, C.byref(v)))
+        return v.value
 
     def samples(self, n):
         x = np.zeros((n, N_IN), np.float32)

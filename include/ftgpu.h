@@ -190,11 +190,12 @@ int ftgpu_check(ftgpu_model *m);
 /* ---- learned constitutive surrogate for material 7 (no counterpart in the
  * reference; it replaces the isochoric part of HGOIsotropicViscoelastic's
  * stress, HGOIsotropicViscoelastic.cpp:53-97, generalised to fibres) ----
- * An MLP 16(9 used)->128->128->128->8(6 used), SiLU, BF16 weights and
+ * An MLP 16(11 used)->128->128->128->8(6 used), SiLU, BF16 weights and
  * activations, FP32 accumulation, trained on the GPU on samples of the plain
- * law.  It predicts S_iso = S_lin + s0 |E|^2 NN(E, a0) (S_lin: the law's
- * small-strain linearisation); the volumetric stress and the Prony recurrence
- * stay exact.  properties: the 9 material-7 parameters. */
+ * law.  It predicts S_iso = S_lin + s0 out_scale |E|^2 NN(x) (S_lin: the
+ * law's first-order model with its exact fibre switch; x: strain direction and
+ * magnitude, fibre, fibre strain); the volumetric stress and the Prony
+ * recurrence stay exact.  properties: the 9 material-7 parameters. */
 typedef struct ftgpu_surrogate ftgpu_surrogate;
 int ftgpu_surrogate_create(ftgpu_surrogate **out, int device, const double *properties,
                            unsigned long long seed);
@@ -219,6 +220,9 @@ int ftgpu_surrogate_params(ftgpu_surrogate *s, float *get, const float *set);
 /* the first n generated samples: features x[n][16], targets t[n][8] */
 int ftgpu_surrogate_samples(ftgpu_surrogate *s, long long n, float *x, float *t);
 int ftgpu_surrogate_num_params(void);
+/* the RMS of the generated targets (1 before generation): network outputs are
+ * in units of s0 * out_scale * |E|_F^2 */
+int ftgpu_surrogate_output_scale(ftgpu_surrogate *s, double *out_scale);
 /* predicted isochoric PK2 S[n][6] (Voigt 11 22 33 23 13 12) for Green strains
  * E[n][6] (same order, tensor shears) and unit fibres a0[n][3], through the
  * element kernel's features and the fused inference kernel */

@@ -3,7 +3,7 @@
 CPU: the FP64 MLP checker (oracle/mlp_oracle.py) against finite differences.
 GPU: the BF16 tensor-core forward/backward against that checker, the training
 data against the plain law, and what the trained network gains over the
-method without it (the law's small-strain linearisation)."""
+method without it (the law's first-order model S_lin)."""
 import numpy as np
 import pytest
 
@@ -72,6 +72,42 @@ def held_out_states(rng, n, lo=0.7, hi=1.4):
     return np.array(Es), np.array(As), np.array(Ss)
 
 
+def test_fibre_strain_mirror_matches_invariants():
+    from femtech_gb300.surrogate import fibre_strain
+    rng = np.random.default_rng(3)
+    kappa = PROPS7[7]
+    for _ in range(50):
+        Q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        U = Q @ np.diag(rng.uniform(0.8, 1.2, 3)) @ Q.T
+        a0 = rng.normal(size=3)
+        a0 /= np.linalg.norm(a0)
+        C = U.T @ U
+        E = 0.5 * (C - np.eye(3))
+        Ev = np.array([[E[0, 0], E[1, 1], E[2, 2], E[1, 2], E[0, 2], E[0, 1]]])
+        j23 = np.linalg.det(C) ** (-1.0 / 3.0)
+        want = kappa * (j23 * np.trace(C) - 3) + (1 - 3 * kappa) * (j23 * a0 @ C @ a0 - 1)
+        assert abs(fibre_strain(Ev, a0[None], kappa)[0] - want) <= 1e-12
+
+
+def test_first_order_model_residual_is_second_order():
+    """(S_iso - S_lin) / |E|^2 stays bounded as the strain shrinks: the network
+    only has to carry an O(|E|^2) correction (plain law from the oracle)."""
+    from femtech_gb300.surrogate import linear_part, e2_of
+    rng = np.random.default_rng(4)
+    Q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+    d = np.array([0.7, -0.2, 0.4])
+    a0 = np.array([0.6, 0.0, 0.8])
+    ratios = []
+    for eps in (1e-1, 1e-2, 1e-3):
+        U = Q @ np.diag(1 + eps * d) @ Q.T
+        E = 0.5 * (U.T @ U - np.eye(3))
+        Ev = np.array([[E[0, 0], E[1, 1], E[2, 2], E[1, 2], E[0, 2], E[0, 1]]])
+        r = goh_iso_fp64(U, a0) - linear_part(Ev, a0[None], PROPS7[1], PROPS7[3], PROPS7[7])[0]
+        ratios.append(np.linalg.norm(r) / e2_of(Ev)[0])
+    assert max(ratios) < 10 * (PROPS7[1] + PROPS7[3]), ratios
+    assert ratios[2] < 2 * ratios[1] + 1.0, ratios
+
+
 @pytest.mark.gpu
 def test_tensor_core_gradient_matches_fp64_checker():
     from femtech_gb300.surrogate import Surrogate
@@ -100,9 +136,10 @@ def test_training_samples_follow_the_plain_law():
     x, t = s.samples(64)
     assert np.all(np.isfinite(t)) and np.all(t[:, 6:] == 0)
     # rebuild the strain from the (BF16) features and check the residual target
-    E = x[:, :6].astype(np.float64) * sg.STRAIN_SCALE
-    a0 = x[:, 6:9].astype(np.float64)
+    E = sg.strain_of(x)
+    a0 = x[:, 7:10].astype(np.float64)
     a0 /= np.linalg.norm(a0, axis=1, keepdims=True)
+    assert s.out_scale > 0
     errs = []
     for i in range(len(E)):
         Em = np.array([[E[i, 0], E[i, 5], E[i, 4]], [E[i, 5], E[i, 1], E[i, 3]],
@@ -111,7 +148,7 @@ def test_training_samples_follow_the_plain_law():
         U = V @ np.diag(np.sqrt(w)) @ V.T
         S = goh_iso_fp64(U, a0[i])
         r = (S - sg.linear_part(E[i:i + 1], a0[i:i + 1], s.mu, s.k1, s.kappa)[0]) / (
-            s.s0 * sg.e2_of(E[i:i + 1])[0])
+            s.s0 * s.out_scale * sg.e2_of(E[i:i + 1])[0])
         errs.append(np.abs(r - t[i, :6]).max() / max(np.abs(t[i, :6]).max(), 1e-3))
     assert np.median(errs) < 0.05  # features are BF16-rounded strains
     s.close()
