@@ -131,11 +131,13 @@ __device__ __forceinline__ void goh_parts_surrogate(const MatP<R> &mp, const R (
   Sv = sym_scale(ac, Jp);
 }
 
+// hin: the Gauss point's history already loaded into registers (same order
+// as hist[c * hs]), or nullptr to read it from hist
 template <class R, int MAT>
 __device__ __forceinline__ Sym6<R> stress_at(const MatP<R> &mp, const R (&D)[3][3], R Jm1,
                                              const R (&a0)[3], R *hist, long long hs,
                                              const R (&pc)[4], const float *sy,
-                                             const SurrogateLaw &law) {
+                                             const SurrogateLaw &law, const R *hin = nullptr) {
   Sym6<R> S;
   if (MAT == 0) {
     S = Sym6<R>{0, 0, 0, 0, 0, 0};
@@ -164,13 +166,13 @@ __device__ __forceinline__ Sym6<R> stress_at(const MatP<R> &mp, const R (&D)[3][
     R out[6];
 #pragma unroll
     for (int c = 0; c < 6; ++c) {
-      R s0 = hist[(NT * 6 + c) * hs];
+      R s0 = hin ? hin[NT * 6 + c] : hist[(NT * 6 + c) * hs];
       R dS = sd[c] - s0;
-      R h1 = pc[0] * hist[c * hs] + pc[1] * dS;
+      R h1 = pc[0] * (hin ? hin[c] : hist[c * hs]) + pc[1] * dS;
       hist[c * hs] = h1;
       R acc = sd[c] + sv[c] + h1;
       if (NT == 2) {
-        R h2 = pc[2] * hist[(6 + c) * hs] + pc[3] * dS;
+        R h2 = pc[2] * (hin ? hin[6 + c] : hist[(6 + c) * hs]) + pc[3] * dS;
         hist[(6 + c) * hs] = h2;
         acc += h2;
       }
@@ -385,7 +387,7 @@ __device__ __forceinline__ void tet_element(const R (&x)[4][3], const R (&u)[4][
                                             const MatP<R> &mp, const R (&pc)[4],
                                             const R (&a0)[3], R *hist, long long hs,
                                             int pass, R (&f)[4][3], R &le, int &bad,
-                                            const ElemArgs<R> &A, long long gpo) {
+                                            const ElemArgs<R> &A, long long gpo, const R *hin) {
   const bool dt_only = pass != kPassForce;
   R Am[3][3], H[3][3];
 #pragma unroll
@@ -414,7 +416,7 @@ __device__ __forceinline__ void tet_element(const R (&x)[4][3], const R (&u)[4][
   }
   if (!dt_only) {
     const float *sy = (MAT == 7 && A.surr_y) ? A.surr_y + sg * kMlpOut : nullptr;
-    Sym6<R> S = stress_at<R, MAT>(mp, D, Jm1, a0, hist, hs, pc, sy, A.law);
+    Sym6<R> S = stress_at<R, MAT>(mp, D, Jm1, a0, hist, hs, pc, sy, A.law, hin);
     if (GP) {
 #pragma unroll
       for (int i = 0; i < 3; ++i)
@@ -480,12 +482,17 @@ __device__ __forceinline__ double dt_of<double>(double le, const MatP<double> &m
 }
 
 template <class R, int ET, int MAT, bool GP>
-// At most 128 registers per thread (two 256-thread or four 128-thread blocks
-// per SM); only the rarely taken eigen-decomposition fallback of the Ogden law
-// needs more and spills there.
-__global__ void __launch_bounds__(kElemThreads, 2) k_elem(const ElemArgs<R> A, int pass) {
+// C3D8: at most 128 registers per thread (two 256-thread or four 128-thread
+// blocks per SM); only the rarely taken eigen-decomposition fallback of the
+// Ogden law needs more and spills there.  C3D4 (one Gauss point, latency
+// bound): at most 85, for three 256-thread or six 128-thread blocks per SM.
+__global__ void __launch_bounds__(kElemThreads, ET == 0 ? 2 : 3)
+    k_elem(const ElemArgs<R> A, int pass) {
   constexpr int NC = ET == 0 ? 8 : 4;
   constexpr int NGP = ET == 0 ? 8 : 1;
+  // one-point elements with a Prony history load it with the other
+  // per-element data, before the slot staging
+  constexpr int NH = (ET == 1 && (MAT == 5 || MAT == 7)) ? (MAT == 5 ? 18 : 12) : 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   R *shX = reinterpret_cast<R *>(smem_raw);
   R *shU = shX + 3 * kMaxLocalNodes;
@@ -494,11 +501,40 @@ __global__ void __launch_bounds__(kElemThreads, 2) k_elem(const ElemArgs<R> A, i
   const int t = threadIdx.x;
   const int p = A.patch_begin + blockIdx.x;
   const int inst = A.patch_inst[p];
-  const Clock *ck = A.clock + A.parity * A.ninst + inst;
-  if (A.use_clock && ck->done) return;
-  const R dt = A.use_clock ? R(ck->dt) : R(A.dt_direct);
   const int e0 = A.patch_elem_off[p], ne = A.patch_elem_off[p + 1] - e0;
   const int s0 = A.patch_node_off[p], ns = A.patch_node_off[p + 1] - s0;
+  // per-element loads first: none depends on the staged slots, so their
+  // latency overlaps the staging below
+  const bool act = t < ne;
+  const int e = e0 + (act ? t : 0);
+  const long long el = e - A.elem_begin;
+  const long long gs = A.nelem, hs = (long long)NGP * A.nelem;
+  uint4 cv = make_uint4(0u, 0u, 0u, 0u);
+  int pw = 0;
+  R a0[3] = {R(1), R(0), R(0)};
+  R hin[NH];
+#pragma unroll
+  for (int k = 0; k < NH; ++k) hin[k] = R(0);
+  if (act) {
+    if (NC == 8) {
+      cv = *reinterpret_cast<const uint4 *>(A.lconn + 8ll * el);
+    } else {
+      const uint2 v = *reinterpret_cast<const uint2 *>(A.lconn + 4ll * el);
+      cv.x = v.x;
+      cv.y = v.y;
+    }
+    pw = A.epid[e];
+    if (MAT == 7) {
+      a0[0] = A.fib[e];
+      a0[1] = A.fib[A.E + e];
+      a0[2] = A.fib[2 * A.E + e];
+    }
+    if (NH > 1 && pass == kPassForce) {
+#pragma unroll
+      for (int k = 0; k < NH; ++k) hin[k] = A.hist[el + k * hs];
+    }
+  }
+  const Clock *ck = A.clock + A.parity * A.ninst + inst;
   for (int i = t; i < ns; i += PE) {
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
@@ -506,19 +542,18 @@ __global__ void __launch_bounds__(kElemThreads, 2) k_elem(const ElemArgs<R> A, i
       shU[d * kMaxLocalNodes + i] = A.sU[d * A.S + s0 + i];
     }
   }
+  // an instance past its end time: the whole block leaves (uniform per patch)
+  if (A.use_clock && ck->done) return;
+  const R dt = A.use_clock ? R(ck->dt) : R(A.dt_direct);
   __syncthreads();
   double dte = r_inf<double>();
   int bad = 0;
-  if (t < ne) {
-    const int e = e0 + t;
+  if (act) {
     int lc[NC];
+    lc[0] = cv.x & 0xffff; lc[1] = cv.x >> 16; lc[2] = cv.y & 0xffff; lc[3] = cv.y >> 16;
     if (NC == 8) {
-      uint4 v = *reinterpret_cast<const uint4 *>(A.lconn + 8ll * (e - A.elem_begin));
-      lc[0] = v.x & 0xffff; lc[1] = v.x >> 16; lc[2] = v.y & 0xffff; lc[3] = v.y >> 16;
-      lc[4] = v.z & 0xffff; lc[5] = v.z >> 16; lc[6] = v.w & 0xffff; lc[7] = v.w >> 16;
-    } else {
-      uint2 v = *reinterpret_cast<const uint2 *>(A.lconn + 4ll * (e - A.elem_begin));
-      lc[0] = v.x & 0xffff; lc[1] = v.x >> 16; lc[2] = v.y & 0xffff; lc[3] = v.y >> 16;
+      lc[4 % NC] = cv.z & 0xffff; lc[5 % NC] = cv.z >> 16;
+      lc[6 % NC] = cv.w & 0xffff; lc[7 % NC] = cv.w >> 16;
     }
     R x[NC][3], u[NC][3];
 #pragma unroll
@@ -531,20 +566,11 @@ __global__ void __launch_bounds__(kElemThreads, 2) k_elem(const ElemArgs<R> A, i
         u[a][d] = shU[d * kMaxLocalNodes + l];
       }
     }
-    const int pw = A.epid[e];
     const bool skip = pw < 0;
     const MatP<R> mp = A.mats[pw & 0x7fffffff];
-    R a0[3] = {R(1), R(0), R(0)};
-    if (MAT == 7) {
-      a0[0] = A.fib[e];
-      a0[1] = A.fib[A.E + e];
-      a0[2] = A.fib[2 * A.E + e];
-    }
     R pc[4];
     prony_consts<R, MAT>(mp, dt, pc);
-    const long long el = e - A.elem_begin;
     R *hist = A.hist ? A.hist + el : nullptr;
-    const long long gs = A.nelem, hs = (long long)NGP * A.nelem;
     R f[NC][3];
     R le;
     const long long gpo = A.gpbase + el * NGP;
@@ -555,7 +581,8 @@ __global__ void __launch_bounds__(kElemThreads, 2) k_elem(const ElemArgs<R> A, i
     else
       tet_element<R, MAT, GP>(reinterpret_cast<const R(&)[4][3]>(x),
                               reinterpret_cast<const R(&)[4][3]>(u), mp, pc, a0, hist, hs,
-                              pass, reinterpret_cast<R(&)[4][3]>(f), le, bad, A, gpo);
+                              pass, reinterpret_cast<R(&)[4][3]>(f), le, bad, A, gpo,
+                              NH > 1 ? hin : nullptr);
     if (pass == kPassForce) {
 #pragma unroll
       for (int a = 0; a < NC; ++a)
