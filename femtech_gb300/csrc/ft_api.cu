@@ -206,6 +206,7 @@ struct ftgpu_model {
   DBuf sX, sU, sF, mats;
   std::vector<std::unique_ptr<DBuf>> hist;
   DBuf clock, dtmin, err, instp;
+  DBuf stepsc, rottrig;  // per-instance step scalars / rotation trigonometry
   DBuf slot_off, slots, node_inst, nbc, fnsbuf;
   DBuf dX, u, v, a, vh, mass, minv, fi;
   DBuf gpF, gpJ, gpS;
@@ -324,6 +325,8 @@ NodeArgs node_args(ftgpu_model *m, int mode, int parity) {
   A.nrot = 0;
   for (size_t i = 0; i < m->fns.size() && A.nrot < kMaxRotFns; ++i)
     if (m->fns[i].kind == kBckRot) A.rot_ids[A.nrot++] = (int)i;
+  A.stepsc = m->stepsc.as<StepScalars>();
+  A.rottrig = m->rottrig.as<double>();
   return A;
 }
 
@@ -332,6 +335,7 @@ int launch_node(ftgpu_model *m, int mode, int parity) {
   const int th = m->node_threads;
   const long long nb = (m->nNodes + th - 1) / th;
   const bool step = mode == kNodeFused || mode == kNodeFinish;
+  if (step) k_step_scalars<<<(unsigned)((m->ninst + 127) / 128), 128, 0, m->stream>>>(A);
   if (is_fp64(m)) {
     if (step)
       k_node_step<double><<<(unsigned)nb, th, 0, m->stream>>>(A);
@@ -613,6 +617,8 @@ int setup_t(ftgpu_model *m) {
   for (auto &c : ck) c = Clock{0.0, 0.0, 0, 0, 0};
   CKI(m->clock.upload(ck.data(), ck.size()));
   CKI(m->dtmin.alloc(2 * m->ninst * sizeof(unsigned long long)));
+  CKI(m->stepsc.alloc(m->ninst * sizeof(StepScalars)));
+  CKI(m->rottrig.alloc((size_t)m->ninst * kMaxRotFns * 3 * sizeof(double)));
   CKI(m->err.alloc(sizeof(int)));
   CK(cudaMemset(m->err.p, 0, sizeof(int)));
   CKI(fill_dtmin(m));
@@ -1142,7 +1148,11 @@ int ftgpu_launches_per_step(ftgpu_model *m) {
   if (!m || !m->setup_done) return 0;
   int g = 0;
   for (auto &x : m->ps.groups) g += x.npatch > 0;
-  return g + 1;
+  // element groups, k_step_scalars, k_node_step; a surrogate adds the
+  // feature pass and the inference kernel of each material-7 group
+  if (m->surr)
+    for (auto &x : m->ps.groups) g += 2 * (x.npatch > 0 && x.mat == 7);
+  return g + 2;
 }
 
 int ftgpu_check(ftgpu_model *m) {

@@ -93,6 +93,16 @@ struct ElemArgs {
 
 enum { kPassForce = 0, kPassDt = 1, kPassSurrogateFeatures = 2 };
 
+// Per-instance scalars of one end-of-step launch (k_step_scalars)
+struct StepScalars {
+  double t_np1, t_np2, ndt;
+  double c1;   // t_{n+1} - t_half         (full-step velocity)
+  double c2;   // t_half' - t_{n+1}        (next half-step velocity)
+  double c12;  // t_half' - t_half         (both at once)
+  int done;
+  bool advance;
+};
+
 struct NodeArgs {
   const int *slot_off;        // [N+1]
   const int *slots;           // node -> slots
@@ -117,6 +127,8 @@ struct NodeArgs {
   int fp64;                   // slot arrays are double
   int nrot;                   // rigid-rotation functions with a cache slot
   int rot_ids[kMaxRotFns];    // their indices in fns
+  StepScalars *stepsc;        // [ninst] written by k_step_scalars
+  double *rottrig;            // [ninst][kMaxRotFns][3] cos, sin, omega at t_{n+2}
 };
 
 enum { kNodeBegin = 0, kNodeFused = 1, kNodeFinish = 2, kNodeInit = 3, kNodeGather = 4,

@@ -83,15 +83,6 @@ __device__ __forceinline__ void bc_value(const BcFn &b, int d, double t, const d
 // Time bookkeeping of one step, as the driver does it on the host
 // (ex9.cpp:107-113,172): t_{n+1} = t_n + dt, t_half = (t_{n+1} + t_n) / 2, the
 // next dt = ExplicitTimeStepReduction * StableTimeStep(), and the stop tests.
-struct StepScalars {
-  double t_np1, t_np2, ndt;
-  double c1;   // t_{n+1} - t_half         (full-step velocity)
-  double c2;   // t_half' - t_{n+1}        (next half-step velocity)
-  double c12;  // t_half' - t_half         (both at once)
-  int done;
-  bool advance;
-};
-
 __device__ __forceinline__ StepScalars step_scalars(const Clock &ck, const InstParams &ip,
                                                     unsigned long long dtbits, int mode) {
   StepScalars s;
@@ -190,41 +181,58 @@ __global__ void __launch_bounds__(512) k_node(const NodeArgs A) {
 
 }
 
+// Step scalars of every instance for one end-of-step launch: the new dt from
+// the dt minimum, the time levels, the velocity coefficients, the done flags
+// and the trigonometry of the rigid-rotation functions at the new time.  One
+// thread per instance, launched between the element pass and k_node_step, so
+// that the FP64 divisions and sin/cos run once per instance and step rather
+// than once per node block (FP64 issue is slow on this GPU).
+__global__ void k_step_scalars(const NodeArgs A) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= A.ninst) return;
+  const Clock ck = A.clock[A.parity * A.ninst + i];
+  const StepScalars sc = step_scalars(ck, A.inst[i], A.dtmin[A.parity * A.ninst + i], A.mode);
+  A.stepsc[i] = sc;
+  if (sc.advance && !ck.done)
+    for (int k = 0; k < A.nrot; ++k) {
+      double *r = A.rottrig + 3 * ((long long)i * kMaxRotFns + k);
+      rot_trig(A.fns[A.rot_ids[k]], sc.t_np2, r[0], r[1], r[2]);
+    }
+}
+
 // End of step n (mode kNodeFused also starts step n+1; kNodeFinish stops
-// there).  The step scalars are computed once per block by thread 0 for the
-// instance of the block's first node; nodes of another instance (blocks that
-// straddle two instances of a batch) compute their own.
+// there), with the step scalars k_step_scalars left for the node's instance.
 // At most 64 registers: the kernel waits on memory, so resident warps matter.
-// The trigonometry of rigid-rotation functions (at the new time) is also
-// evaluated once per block, for up to kMaxRotFns functions.
 template <class R>
 __global__ void __launch_bounds__(512, 2) k_node_step(const NodeArgs A) {
-  __shared__ StepScalars shs;
-  __shared__ Clock shck;
-  __shared__ int shinst;
-  __shared__ double shrot[kMaxRotFns][3];
   const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (threadIdx.x == 0) {
-    const long long n0 = (long long)blockIdx.x * blockDim.x;
-    const int i0 = A.node_inst ? A.node_inst[n0] : 0;
-    shck = A.clock[A.parity * A.ninst + i0];
-    shs = step_scalars(shck, A.inst[i0], A.dtmin[A.parity * A.ninst + i0], A.mode);
-    shinst = i0;
-    if (shs.advance)
-      for (int k = 0; k < A.nrot; ++k)
-        rot_trig(A.fns[A.rot_ids[k]], shs.t_np2, shrot[k][0], shrot[k][1], shrot[k][2]);
-  }
-  __syncthreads();
   if (n >= A.N) return;
-  const int inst = A.node_inst ? A.node_inst[n] : 0;
-  const bool same = inst == shinst;
-  const InstParams &ip = A.inst[inst];
-  const bool leader = (n == ip.node_begin);
+  const long long N = A.N, S = A.S;
   const R *sF = reinterpret_cast<const R *>(A.sF);
   R *sU = reinterpret_cast<R *>(A.sU);
+  const int inst = A.node_inst ? A.node_inst[n] : 0;
   const int sb = A.slot_off[n], se = A.slot_off[n + 1];
-  const long long N = A.N, S = A.S;
-  const Clock ck = same ? shck : A.clock[A.parity * A.ninst + inst];
+  int nbc[3];
+  double u0[3], vh0[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    nbc[d] = A.nbc[d * N + n];
+    u0[d] = A.u[d * N + n];
+    vh0[d] = A.vh[d * N + n];
+  }
+  // 1/m (mixed mode; FP64 mode divides by m as the reference does)
+  const double minv = sizeof(R) == 8 ? 0.0 : A.minv[n];
+  // sum of the patch partials in slot order (in the element precision)
+  R fs0 = 0, fs1 = 0, fs2 = 0;
+  for (int k = sb; k < se; ++k) {
+    const int s = A.slots[k];
+    fs0 += sF[s];
+    fs1 += sF[S + s];
+    fs2 += sF[2 * S + s];
+  }
+  const InstParams &ip = A.inst[inst];
+  const bool leader = (n == ip.node_begin);
+  const Clock ck = A.clock[A.parity * A.ninst + inst];
   // kNodeFused / kNodeFinish: end of step n (+ start of step n+1 when fused)
   Clock *nxt = A.clock + (A.parity ^ 1) * A.ninst + inst;
   if (ck.done) {
@@ -235,20 +243,10 @@ __global__ void __launch_bounds__(512, 2) k_node_step(const NodeArgs A) {
     }
     return;
   }
-  const StepScalars sc =
-      same ? shs : step_scalars(ck, ip, A.dtmin[A.parity * A.ninst + inst], A.mode);
+  const StepScalars sc = A.stepsc[inst];
   const bool advance = sc.advance;
   constexpr bool kF64 = sizeof(R) == 8;
-  // sum of the patch partials in slot order (in the element precision)
-  R fs0 = 0, fs1 = 0, fs2 = 0;
-  for (int k = sb; k < se; ++k) {
-    const int s = A.slots[k];
-    fs0 += sF[s];
-    fs1 += sF[S + s];
-    fs2 += sF[2 * S + s];
-  }
   const double fsum[3] = {double(fs0), double(fs1), double(fs2)};
-  const double minv = kF64 ? 0.0 : A.minv[n];
   double un[3];
   // a rigid rotation drives all its DOFs at once: evaluate it once per node
   double ur[3] = {0.0, 0.0, 0.0}, vr[3] = {0.0, 0.0, 0.0};
@@ -256,16 +254,17 @@ __global__ void __launch_bounds__(512, 2) k_node_step(const NodeArgs A) {
   if (advance) {
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      const int fn = A.nbc[d * N + n];
+      const int fn = nbc[d];
       if (fn >= 0 && rot_fn < 0 && A.fns[fn].kind == kBckRot) rot_fn = fn;
     }
     if (rot_fn >= 0) {
       const BcFn &b = A.fns[rot_fn];
       double c, s, om;
-      if (same && b.pad >= 0 && b.pad < A.nrot) {
-        c = shrot[b.pad][0];
-        s = shrot[b.pad][1];
-        om = shrot[b.pad][2];
+      if (b.pad >= 0 && b.pad < A.nrot) {
+        const double *r = A.rottrig + 3 * ((long long)inst * kMaxRotFns + b.pad);
+        c = r[0];
+        s = r[1];
+        om = r[2];
       } else {
         rot_trig(b, sc.t_np2, c, s, om);
       }
@@ -274,11 +273,11 @@ __global__ void __launch_bounds__(512, 2) k_node_step(const NodeArgs A) {
   }
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    const int fn = A.nbc[d * N + n];
-    double u = A.u[d * N + n];
+    const int fn = nbc[d];
+    double u = u0[d];
     if (fn == kBcFree) {
       const double acc = kF64 ? -fsum[d] / A.mass[n] : -fsum[d] * minv;
-      const double vh = A.vh[d * N + n];
+      const double vh = vh0[d];
       if (advance) {
         double vh2;
         if (kF64) {  // the two half-step updates of ex9.cpp:147-152 and :116-123
