@@ -371,7 +371,7 @@ int launch_groups_t(ftgpu_model *m, int parity, int use_clock, double dt_direct,
                              kPassSurrogateFeatures);
       if (r) return r;
       r = surrogate_infer(m->surr, A.surr_x, ngp, m->surr_y.as<float>() + base * kMlpOut,
-                          m->stream);
+                          m->stream, m->err.as<int>());
       if (r) return r;
       A.surr_x = nullptr;
       A.surr_y = m->surr_y.as<float>() + base * kMlpOut;
@@ -422,6 +422,7 @@ int check_err(ftgpu_model *m) {
   int e = *m->h_err;
   if (e & kErrInverted) return fail(FTGPU_ERR_INVERTED, "non-positive or non-finite Jacobian");
   if (e & kErrIndex) return fail(FTGPU_ERR_INPUT, "local node index out of range");
+  if (e & kErrWait) return fail(FTGPU_ERR_CUDA, "tensor-core inference gave up waiting");
   return 0;
 }
 
@@ -769,6 +770,10 @@ int run_impl(ftgpu_model *m, int max_steps, int *steps_done, bool prof, double *
     prev = m->h_clock[0].step;
     if (*m->h_err & kErrInverted) {
       rc = fail(FTGPU_ERR_INVERTED, "non-positive or non-finite Jacobian");
+      break;
+    }
+    if (*m->h_err & kErrWait) {
+      rc = fail(FTGPU_ERR_CUDA, "tensor-core inference gave up waiting");
       break;
     }
     bool all = true, dterr = false;

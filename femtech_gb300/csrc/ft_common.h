@@ -48,7 +48,7 @@ constexpr int kMaxRotFns = 8;
 
 enum { kBcFree = -1, kBcHold = -2 };
 enum { kBckFixed = 0, kBckRamp = 1, kBckSine = 2, kBckRot = 3 };
-enum { kErrInverted = 1, kErrDt = 2, kErrIndex = 4 };
+enum { kErrInverted = 1, kErrDt = 2, kErrIndex = 4, kErrWait = 8 };
 
 template <class Real>
 struct ElemArgs {

@@ -15,6 +15,7 @@
 #include <string>
 #include <vector>
 
+#include "ft_common.h"
 #include "ft_mlp.cuh"
 #include "ftgpu.h"
 
@@ -400,6 +401,318 @@ __global__ void __launch_bounds__(256) k_mlp_infer(const bf16 *__restrict__ X, l
   }
 }
 
+// ---------------- fused inference on the 5th-generation tensor cores ----------------
+// One CTA of 128 threads processes tiles of 128 rows: thread t owns row t of
+// the tile, which is TMEM lane t of every accumulator.  Each layer is a chain
+// of tcgen05.mma (M = 128, K = 16 per instruction, BF16 x BF16 -> FP32 in
+// TMEM) issued by thread 0 and signalled through one mbarrier; the epilogue
+// reads the accumulator with tcgen05.ld, adds the bias, applies SiLU and
+// writes the BF16 activations back to shared memory as the next layer's A
+// operand.  Two CTAs share an SM (113 KB of shared memory and 256 TMEM
+// columns each), so one CTA's epilogue overlaps the other's MMAs.
+//
+// Shared-memory operand images are K-major without swizzle: 8-row x 16-byte
+// core matrices, element (r, k) of an image with K columns at byte
+//   (r / 8) * 16 K + (k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2,
+// i.e. leading-dimension (K-direction) byte offset 128 and stride-dimension
+// (8-row group) byte offset 16 K in the matrix descriptors.
+namespace tc {
+constexpr uint32_t kW0 = 0;                        // [128 x 16]     4 KB
+constexpr uint32_t kW1 = kW0 + 128 * 16 * 2;       // [128 x 128]   32 KB
+constexpr uint32_t kW2 = kW1 + 128 * 128 * 2;      // [128 x 128]   32 KB
+constexpr uint32_t kW3 = kW2 + 128 * 128 * 2;      // [16 x 128]     4 KB (rows 8..15 zero)
+constexpr uint32_t kXs = kW3 + 16 * 128 * 2;       // [128 x 16]     4 KB input tile
+constexpr uint32_t kHs = kXs + 128 * 16 * 2;       // [128 x 128]   32 KB activations
+constexpr uint32_t kBias = kHs + 128 * 128 * 2;    // FP32 b0 b1 b2 (128 each), b3 (16)
+constexpr uint32_t kBar = kBias + (3 * 128 + 16) * 4;  // mbarrier (8 B), TMEM base (4 B)
+constexpr uint32_t kSmem = kBar + 16 + 128;        // + alignment slack of the base
+constexpr uint32_t kTmemCols = 256;                // D0/D2 in columns 0..127, D1/D3 128..
+constexpr int kWaitLimit = 1 << 20;                // try_wait rounds before giving up
+}  // namespace tc
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// shared-memory matrix descriptor: start, leading / stride byte offsets,
+// descriptor version 1 (bits 46-47), no swizzle (bits 61-63 = 0)
+__device__ __forceinline__ uint64_t umma_sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) |
+         ((uint64_t)(sbo >> 4) << 32) | (1ull << 46);
+}
+
+// instruction descriptor of kind::f16: D FP32 (bits 4-5 = 1), A and B BF16
+// (bits 7-9 = 1, 10-12 = 1), both K-major, N >> 3 at bit 17, M >> 4 at bit 24
+__host__ __device__ constexpr uint32_t umma_idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc,
+                                          uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   bar)
+               : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// bounded wait for the completion of phase `parity` of an mbarrier
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (int it = 0; it < tc::kWaitLimit; ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+// 32 consecutive FP32 accumulator columns of this thread's TMEM lane (the
+// wait for the load is part of the same statement, so no use can precede it)
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n\t"
+      "tcgen05.wait::ld.sync.aligned;\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15}, [%16];\n\t"
+      "tcgen05.wait::ld.sync.aligned;\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// SiLU with one MUFU operation: z sigmoid(z) = h + h tanh(h), h = z / 2
+__device__ __forceinline__ float silu_tanh(float z) {
+  const float h = 0.5f * z;
+  float th;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(th) : "f"(h));
+  return fmaf(h, th, h);
+}
+
+// rows [0, rows) x K columns of a row-major BF16 matrix into the K-major
+// core-matrix image (rows up to rows_pad, the extra ones zero)
+__device__ __forceinline__ void stage_kmajor(unsigned char *img, const bf16 *src, int rows,
+                                             int rows_pad, int K) {
+  const int kc = K / 8;
+  for (int c = threadIdx.x; c < rows_pad * kc; c += blockDim.x) {
+    const int r = c / kc, q = c - r * kc;
+    uint4 v = make_uint4(0u, 0u, 0u, 0u);
+    if (r < rows) v = *reinterpret_cast<const uint4 *>(src + (long long)r * K + 8 * q);
+    *reinterpret_cast<uint4 *>(img + (r / 8) * (16 * K) + q * 128 + (r % 8) * 16) = v;
+  }
+}
+
+// bias + SiLU of 128 accumulator columns of this thread's lane into row t of
+// the activation image
+__device__ __forceinline__ void tc_hidden_epilogue(uint32_t taddr, const float *bias,
+                                                   unsigned char *hs, int t) {
+  unsigned char *dst = hs + (t / 8) * 2048 + (t % 8) * 16;
+#pragma unroll 1
+  for (int ch = 0; ch < 4; ++ch) {
+    float v[32];
+    tmem_ld32(taddr + 32 * ch, v);
+    uint32_t pk[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j)
+      pk[j] = pack_f2(silu_tanh(v[2 * j] + bias[32 * ch + 2 * j]),
+                      silu_tanh(v[2 * j + 1] + bias[32 * ch + 2 * j + 1]));
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+      *reinterpret_cast<uint4 *>(dst + (4 * ch + i) * 128) =
+          make_uint4(pk[4 * i], pk[4 * i + 1], pk[4 * i + 2], pk[4 * i + 3]);
+  }
+}
+
+__global__ void __launch_bounds__(128, 1) k_mlp_infer_tc(const bf16 *__restrict__ X, long long n,
+                                                         const bf16 *__restrict__ Wg,
+                                                         const float *__restrict__ P,
+                                                         float *__restrict__ Y, int *err) {
+  extern __shared__ __align__(128) unsigned char tc_raw[];
+  unsigned char *sm = tc_raw + ((128 - (smem_u32(tc_raw) & 127)) & 127);
+  const int t = threadIdx.x, warp = t >> 5;
+  float *bias = reinterpret_cast<float *>(sm + tc::kBias);
+  uint64_t *bar = reinterpret_cast<uint64_t *>(sm + tc::kBar);
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(sm + tc::kBar + 8);
+  const uint32_t bar_a = smem_u32(bar);
+
+  // weights and biases, once per CTA
+  stage_kmajor(sm + tc::kW0, Wg + kOffW0, kMlpHid, kMlpHid, kMlpIn);
+  stage_kmajor(sm + tc::kW1, Wg + kOffW1, kMlpHid, kMlpHid, kMlpHid);
+  stage_kmajor(sm + tc::kW2, Wg + kOffW2, kMlpHid, kMlpHid, kMlpHid);
+  stage_kmajor(sm + tc::kW3, Wg + kOffW3, kMlpOut, 16, kMlpHid);
+  for (int i = t; i < kMlpHid; i += blockDim.x) {
+    bias[i] = P[kOffB0 + i];
+    bias[kMlpHid + i] = P[kOffB1 + i];
+    bias[2 * kMlpHid + i] = P[kOffB2 + i];
+  }
+  if (t < 16) bias[3 * kMlpHid + t] = t < kMlpOut ? P[kOffB3 + t] : 0.f;
+  if (t == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_a) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(tc::kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_proxy_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = *tmem_slot;
+  const uint32_t tlane = tbase + ((uint32_t)(32 * warp) << 16);  // this warp's lanes
+
+  const uint32_t sW0 = smem_u32(sm + tc::kW0), sW1 = smem_u32(sm + tc::kW1);
+  const uint32_t sW2 = smem_u32(sm + tc::kW2), sW3 = smem_u32(sm + tc::kW3);
+  const uint32_t sX = smem_u32(sm + tc::kXs), sH = smem_u32(sm + tc::kHs);
+  constexpr uint32_t id128 = umma_idesc_bf16(128, 128), id16 = umma_idesc_bf16(128, 16);
+
+  uint32_t phase = 0;
+  int bad = 0;
+  const long long tiles = (n + 127) / 128;
+  for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const long long row = tile * 128 + t;
+    uint4 x0 = make_uint4(0u, 0u, 0u, 0u), x1 = x0;
+    if (row < n) {
+      const uint4 *src = reinterpret_cast<const uint4 *>(X + row * kMlpIn);
+      x0 = src[0];
+      x1 = src[1];
+    }
+    unsigned char *xd = sm + tc::kXs + (t / 8) * 256 + (t % 8) * 16;
+    *reinterpret_cast<uint4 *>(xd) = x0;
+    *reinterpret_cast<uint4 *>(xd + 128) = x1;
+    fence_proxy_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    // layer 0: D[0..128) = X W0^T (K = 16)
+    if (t == 0) {
+      tc_fence_after();
+      umma_bf16(tbase, umma_sdesc(sX, 128, 256), umma_sdesc(sW0, 128, 256), id128, 0u);
+      umma_commit(bar_a);
+    }
+    bad |= !mbar_wait(bar_a, phase);
+    phase ^= 1u;
+    tc_fence_after();
+    __syncwarp();
+    tc_hidden_epilogue(tlane, bias, sm + tc::kHs, t);
+    fence_proxy_async_smem();
+    tc_fence_before();
+    if (__syncthreads_or(bad)) break;
+    // layer 1: D[128..256) = H W1^T (K = 128 in 8 steps)
+    if (t == 0) {
+      tc_fence_after();
+#pragma unroll
+      for (int kk = 0; kk < 8; ++kk)
+        umma_bf16(tbase + 128, umma_sdesc(sH + 256 * kk, 128, 2048),
+                  umma_sdesc(sW1 + 256 * kk, 128, 2048), id128, kk > 0 ? 1u : 0u);
+      umma_commit(bar_a);
+    }
+    bad |= !mbar_wait(bar_a, phase);
+    phase ^= 1u;
+    tc_fence_after();
+    __syncwarp();
+    tc_hidden_epilogue(tlane + 128, bias + kMlpHid, sm + tc::kHs, t);
+    fence_proxy_async_smem();
+    tc_fence_before();
+    if (__syncthreads_or(bad)) break;
+    // layer 2: D[0..128) = H W2^T
+    if (t == 0) {
+      tc_fence_after();
+#pragma unroll
+      for (int kk = 0; kk < 8; ++kk)
+        umma_bf16(tbase, umma_sdesc(sH + 256 * kk, 128, 2048),
+                  umma_sdesc(sW2 + 256 * kk, 128, 2048), id128, kk > 0 ? 1u : 0u);
+      umma_commit(bar_a);
+    }
+    bad |= !mbar_wait(bar_a, phase);
+    phase ^= 1u;
+    tc_fence_after();
+    __syncwarp();
+    tc_hidden_epilogue(tlane, bias + 2 * kMlpHid, sm + tc::kHs, t);
+    fence_proxy_async_smem();
+    tc_fence_before();
+    if (__syncthreads_or(bad)) break;
+    // layer 3: D[128..144) = H W3^T (N = 16, outputs 8..15 are zero rows)
+    if (t == 0) {
+      tc_fence_after();
+#pragma unroll
+      for (int kk = 0; kk < 8; ++kk)
+        umma_bf16(tbase + 128, umma_sdesc(sH + 256 * kk, 128, 2048),
+                  umma_sdesc(sW3 + 256 * kk, 128, 2048), id16, kk > 0 ? 1u : 0u);
+      umma_commit(bar_a);
+    }
+    bad |= !mbar_wait(bar_a, phase);
+    phase ^= 1u;
+    tc_fence_after();
+    __syncwarp();
+    float o[16];
+    tmem_ld16(tlane + 128, o);
+    if (row < n) {
+      const float *b3 = bias + 3 * kMlpHid;
+      float4 *yd = reinterpret_cast<float4 *>(Y + row * kMlpOut);
+      yd[0] = make_float4(o[0] + b3[0], o[1] + b3[1], o[2] + b3[2], o[3] + b3[3]);
+      yd[1] = make_float4(o[4] + b3[4], o[5] + b3[5], o[6] + b3[6], o[7] + b3[7]);
+    }
+    tc_fence_before();
+    if (__syncthreads_or(bad)) break;
+  }
+  if (bad && t == 0) {
+    atomicOr(err, kErrWait);
+    mbar_wait(bar_a, phase ^ 1u);  // the MMAs of the wait that gave up (bounded)
+  }
+  // every MMA this CTA issued has completed (or the wait gave up): free TMEM
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase),
+                 "r"(tc::kTmemCols)
+                 : "memory");
+}
+
 }  // namespace ftgpu
 
 using namespace ftgpu;
@@ -421,12 +734,13 @@ struct ftgpu_surrogate {
   bf16 *H1 = nullptr, *H2 = nullptr, *H3 = nullptr, *dY = nullptr, *dZ1 = nullptr, *dZ2 = nullptr,
        *dZ3 = nullptr;
   long long adam_t = 0;
+  int *derr = nullptr;  // device error word of standalone inference calls
   std::string err;
   ~ftgpu_surrogate() {
     for (void *p : {(void *)P, (void *)G, (void *)Mo, (void *)V, (void *)Wb, (void *)X, (void *)T,
                     (void *)Z1, (void *)Z2, (void *)Z3, (void *)Y, (void *)rowloss, (void *)loss,
                     (void *)H1, (void *)H2, (void *)H3, (void *)dY, (void *)dZ1, (void *)dZ2,
-                    (void *)dZ3})
+                    (void *)dZ3, (void *)derr})
       if (p) cudaFree(p);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -547,8 +861,30 @@ int backward(ftgpu_surrogate *s, const bf16 *X, const float *T, long long B) {
 
 namespace ftgpu {
 
+// fused inference on the tensor cores (tcgen05, the in-loop path); device
+// errors (a wait that gave up) are or-ed into *err
 int surrogate_infer(ftgpu_surrogate *s, const uint16_t *X, long long n, float *Y,
-                    cudaStream_t st) {
+                    cudaStream_t st, int *err) {
+  static bool attr_set[64] = {false};
+  if (n <= 0) return 0;
+  if (s->device >= 0 && s->device < 64 && !attr_set[s->device]) {
+    if (cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)tc::kSmem) != cudaSuccess)
+      return FTGPU_ERR_CUDA;
+    attr_set[s->device] = true;
+  }
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
+  const long long tiles = (n + 127) / 128;
+  const long long grid = std::max<long long>(1, std::min<long long>((long long)sms * 2, tiles));
+  k_mlp_infer_tc<<<(unsigned)grid, 128, tc::kSmem, st>>>(reinterpret_cast<const bf16 *>(X), n,
+                                                          s->Wb, s->P, Y, err);
+  return cudaGetLastError() == cudaSuccess ? 0 : FTGPU_ERR_CUDA;
+}
+
+// the same on the warp-level mma.sync path (kept as a cross-check)
+int surrogate_infer_mma(ftgpu_surrogate *s, const uint16_t *X, long long n, float *Y,
+                        cudaStream_t st) {
   static bool attr_set[64] = {false};
   if (n <= 0) return 0;
   if (s->device >= 0 && s->device < 64 && !attr_set[s->device]) {
@@ -599,7 +935,7 @@ int ftgpu_surrogate_create(ftgpu_surrogate **out, int device, const double *prop
   s->law.out_scale = 1.0;
   s->law.trust_e2 = 0.04;
   int r = dalloc(&s->P, kMlpParams) | dalloc(&s->G, kMlpParams) | dalloc(&s->Mo, kMlpParams) |
-          dalloc(&s->V, kMlpParams) | dalloc(&s->Wb, kMlpParams);
+          dalloc(&s->V, kMlpParams) | dalloc(&s->Wb, kMlpParams) | dalloc(&s->derr, 1);
   if (r) return FTGPU_ERR_ALLOC;
   // Kaiming-uniform-style init (fan-in scaled), seeded, on the host
   std::vector<float> p(kMlpParams, 0.f);
@@ -726,8 +1062,10 @@ int ftgpu_surrogate_forward(ftgpu_surrogate *s, long long n, const float *x, flo
   return r;
 }
 
-// the same outputs through the fused persistent inference kernel (in-loop path)
-int ftgpu_surrogate_infer(ftgpu_surrogate *s, long long n, const float *x, float *y) {
+// the same outputs through the fused inference kernel of the explicit loop
+// (tensor_cores = 1: tcgen05 with TMEM accumulators; 0: warp-level mma.sync)
+static int surrogate_infer_host(ftgpu_surrogate *s, long long n, const float *x, float *y,
+                                int tensor_cores) {
   if (!s || n <= 0 || !x || !y) return FTGPU_ERR_INPUT;
   SCK(cudaSetDevice(s->device));
   std::vector<bf16> xb(n * kMlpIn);
@@ -736,12 +1074,26 @@ int ftgpu_surrogate_infer(ftgpu_surrogate *s, long long n, const float *x, float
   float *dY = nullptr;
   if (dalloc(&dX, n * kMlpIn) || dalloc(&dY, n * kMlpOut)) return FTGPU_ERR_ALLOC;
   SCK(cudaMemcpy(dX, xb.data(), n * kMlpIn * 2, cudaMemcpyHostToDevice));
-  int r = surrogate_infer(s, reinterpret_cast<const uint16_t *>(dX), n, dY, s->stream);
+  SCK(cudaMemset(s->derr, 0, sizeof(int)));
+  int r = tensor_cores
+              ? surrogate_infer(s, reinterpret_cast<const uint16_t *>(dX), n, dY, s->stream, s->derr)
+              : surrogate_infer_mma(s, reinterpret_cast<const uint16_t *>(dX), n, dY, s->stream);
   SCK(cudaStreamSynchronize(s->stream));
+  int e = 0;
+  SCK(cudaMemcpy(&e, s->derr, sizeof(int), cudaMemcpyDeviceToHost));
+  if (!r && e) r = FTGPU_ERR_CUDA;
   SCK(cudaMemcpy(y, dY, n * kMlpOut * 4, cudaMemcpyDeviceToHost));
   cudaFree(dX);
   cudaFree(dY);
   return r;
+}
+
+int ftgpu_surrogate_infer(ftgpu_surrogate *s, long long n, const float *x, float *y) {
+  return surrogate_infer_host(s, n, x, y, 1);
+}
+
+int ftgpu_surrogate_infer_mma(ftgpu_surrogate *s, long long n, const float *x, float *y) {
+  return surrogate_infer_host(s, n, x, y, 0);
 }
 
 // loss and parameter gradient of one batch given on the host (gradient checks)
@@ -818,7 +1170,8 @@ int ftgpu_surrogate_predict(ftgpu_surrogate *s, long long n, const double *E, co
     SCK(cudaMemcpy(dA, a0, 3 * n * sizeof(double), cudaMemcpyHostToDevice));
     const unsigned g = (unsigned)((n + 127) / 128);
     k_predict_features<<<g, 128, 0, s->stream>>>(n, dE, dA, s->law, dX, dS, dsc);
-    r = surrogate_infer(s, reinterpret_cast<const uint16_t *>(dX), n, dY, s->stream);
+    SCK(cudaMemset(s->derr, 0, sizeof(int)));
+    r = surrogate_infer(s, reinterpret_cast<const uint16_t *>(dX), n, dY, s->stream, s->derr);
     k_predict_combine<<<g, 128, 0, s->stream>>>(n, dY, dS, dsc);
     SCK(cudaStreamSynchronize(s->stream));
     SCK(cudaMemcpy(S, dS, 6 * n * sizeof(double), cudaMemcpyDeviceToHost));

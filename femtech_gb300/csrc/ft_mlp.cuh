@@ -100,10 +100,11 @@ __device__ inline void surrogate_features(const R (&E)[6], const R (&a0)[3],
 
 struct ftgpu_surrogate;
 namespace ftgpu {
-// host side, implemented in ft_mlp.cu: fused inference of n feature rows
-// (BF16 bits [n][16]) into outputs [n][8] on stream st; the trained law
+// host side, implemented in ft_mlp.cu: fused tensor-core inference of n
+// feature rows (BF16 bits [n][16]) into outputs [n][8] on stream st (a device
+// wait that gives up or-s kErrWait into *err); the trained law
 int surrogate_infer(ftgpu_surrogate *s, const uint16_t *X, long long n, float *Y,
-                    cudaStream_t st);
+                    cudaStream_t st, int *err);
 SurrogateLaw surrogate_law(const ftgpu_surrogate *s);
 int surrogate_device(const ftgpu_surrogate *s);
 }  // namespace ftgpu

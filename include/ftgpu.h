@@ -210,8 +210,11 @@ int ftgpu_surrogate_train(ftgpu_surrogate *s, int epochs, int batch, double lr,
                           double *final_loss);
 /* raw network outputs y[n][8] for features x[n][16] (host arrays) */
 int ftgpu_surrogate_forward(ftgpu_surrogate *s, long long n, const float *x, float *y);
-/* the same through the fused persistent inference kernel used in the loop */
+/* the same through the fused inference kernel used in the loop (tcgen05 MMAs,
+ * FP32 accumulators in tensor memory) */
 int ftgpu_surrogate_infer(ftgpu_surrogate *s, long long n, const float *x, float *y);
+/* the same through a warp-level mma.sync kernel (a cross-check of the above) */
+int ftgpu_surrogate_infer_mma(ftgpu_surrogate *s, long long n, const float *x, float *y);
 /* MSE loss and its gradient w.r.t. the FP32 parameter vector for one batch */
 int ftgpu_surrogate_gradient(ftgpu_surrogate *s, long long n, const float *x, const float *t,
                              float *grad, double *loss);

@@ -155,19 +155,31 @@ def test_training_samples_follow_the_plain_law():
 
 
 @pytest.mark.gpu
-def test_fused_inference_kernel_matches_training_forward():
+@pytest.mark.parametrize("n", [5, 3001, 70000])
+def test_tensor_core_inference_matches_mma_and_training_forward(n):
+    """tcgen05 inference (TMEM accumulators) against the warp-level mma.sync
+    kernel and the training forward: fewer rows than one 128-row tile, a
+    ragged last tile, and many tiles per CTA."""
     from femtech_gb300.surrogate import Surrogate
     import ctypes as C
     s = Surrogate(PROPS7, seed=6)
     rng = np.random.default_rng(2)
     s.params = rand_params(rng).astype(np.float32)
-    x, _ = rand_batch(rng, 3001)  # not a multiple of the 16-row tiles
+    x, _ = rand_batch(rng, n)
     x = x.astype(np.float32)
     y_gen = s.forward(x)
-    y_fused = np.zeros_like(y_gen)
-    s.L.ftgpu_surrogate_infer.argtypes = [C.c_void_p, C.c_longlong, C.c_void_p, C.c_void_p]
-    assert s.L.ftgpu_surrogate_infer(s.h, len(x), x.ctypes.data, y_fused.ctypes.data) == 0
-    assert np.abs(y_fused - y_gen).max() <= 1e-2 * np.abs(y_gen).max()
+    out = {}
+    for name in ("ftgpu_surrogate_infer", "ftgpu_surrogate_infer_mma"):
+        f = getattr(s.L, name)
+        f.argtypes = [C.c_void_p, C.c_longlong, C.c_void_p, C.c_void_p]
+        y = np.zeros_like(y_gen)
+        assert f(s.h, len(x), x.ctypes.data, y.ctypes.data) == 0, name
+        out[name] = y
+    scale = np.abs(y_gen).max()
+    assert np.all(out["ftgpu_surrogate_infer"][:, 6:] == 0)
+    assert np.abs(out["ftgpu_surrogate_infer"] - y_gen).max() <= 1e-2 * scale
+    assert np.abs(out["ftgpu_surrogate_infer_mma"] - y_gen).max() <= 1e-2 * scale
+    assert np.abs(out["ftgpu_surrogate_infer"] - out["ftgpu_surrogate_infer_mma"]).max() <= 1e-2 * scale
     s.close()
 
 
