@@ -176,7 +176,9 @@ def test_tensor_core_inference_matches_mma_and_training_forward(n):
         assert f(s.h, len(x), x.ctypes.data, y.ctypes.data) == 0, name
         out[name] = y
     scale = np.abs(y_gen).max()
-    assert np.all(out["ftgpu_surrogate_infer"][:, 6:] == 0)
+    e_tc = np.abs(out["ftgpu_surrogate_infer"] - y_gen).max() / scale
+    e_mma = np.abs(out["ftgpu_surrogate_infer_mma"] - y_gen).max() / scale
+    print("n=%d: tcgen05 %.2e, mma.sync %.2e (max error / max |y|)" % (n, e_tc, e_mma))
     assert np.abs(out["ftgpu_surrogate_infer"] - y_gen).max() <= 1e-2 * scale
     assert np.abs(out["ftgpu_surrogate_infer_mma"] - y_gen).max() <= 1e-2 * scale
     assert np.abs(out["ftgpu_surrogate_infer"] - out["ftgpu_surrogate_infer_mma"]).max() <= 1e-2 * scale
