@@ -402,14 +402,18 @@ __global__ void __launch_bounds__(256) k_mlp_infer(const bf16 *__restrict__ X, l
 }
 
 // ---------------- fused inference on the 5th-generation tensor cores ----------------
-// One CTA of 128 threads processes tiles of 128 rows: thread t owns row t of
-// the tile, which is TMEM lane t of every accumulator.  Each layer is a chain
-// of tcgen05.mma (M = 128, K = 16 per instruction, BF16 x BF16 -> FP32 in
-// TMEM) issued by thread 0 and signalled through one mbarrier; the epilogue
-// reads the accumulator with tcgen05.ld, adds the bias, applies SiLU and
-// writes the BF16 activations back to shared memory as the next layer's A
-// operand.  Two CTAs share an SM (113 KB of shared memory and 256 TMEM
-// columns each), so one CTA's epilogue overlaps the other's MMAs.
+// One CTA of 256 threads processes tiles of 128 rows.  Row r of a tile is
+// TMEM lane r of every accumulator; warps w and w + 4 share lane quarter w
+// (tcgen05.ld/st reach lanes 32 (w mod 4) .. +31) and split the columns.
+// Each layer is a chain of tcgen05.mma (M = 128, K = 16 per instruction,
+// BF16 x BF16 -> FP32 in TMEM) issued by thread 0 and signalled through one
+// mbarrier, accumulating onto the layer's bias, which the epilogue of the
+// previous reader of those columns stored there with tcgen05.st.  W0..W2 and
+// b0..b2 are staged pre-multiplied by 1/2 (exact), so an accumulator holds
+// h = z / 2 and SiLU(z) = z sigmoid(z) = h + h tanh(h) costs one MUFU tanh
+// and one FMA.  The epilogue writes BF16 activations back to shared memory as
+// the next layer's A operand.  Two CTAs share an SM (113 KB of shared memory
+// and 256 TMEM columns each), so one CTA's epilogue overlaps the other's MMAs.
 //
 // Shared-memory operand images are K-major without swizzle: 8-row x 16-byte
 // core matrices, element (r, k) of an image with K columns at byte
@@ -417,16 +421,17 @@ __global__ void __launch_bounds__(256) k_mlp_infer(const bf16 *__restrict__ X, l
 // i.e. leading-dimension (K-direction) byte offset 128 and stride-dimension
 // (8-row group) byte offset 16 K in the matrix descriptors.
 namespace tc {
+constexpr int kThreads = 256;
 constexpr uint32_t kW0 = 0;                        // [128 x 16]     4 KB
 constexpr uint32_t kW1 = kW0 + 128 * 16 * 2;       // [128 x 128]   32 KB
 constexpr uint32_t kW2 = kW1 + 128 * 128 * 2;      // [128 x 128]   32 KB
 constexpr uint32_t kW3 = kW2 + 128 * 128 * 2;      // [16 x 128]     4 KB (rows 8..15 zero)
 constexpr uint32_t kXs = kW3 + 16 * 128 * 2;       // [128 x 16]     4 KB input tile
 constexpr uint32_t kHs = kXs + 128 * 16 * 2;       // [128 x 128]   32 KB activations
-constexpr uint32_t kBias = kHs + 128 * 128 * 2;    // FP32 b0 b1 b2 (128 each), b3 (16)
+constexpr uint32_t kBias = kHs + 128 * 128 * 2;    // FP32 b0/2 b1/2 b2/2 (128 each), b3 (16)
 constexpr uint32_t kBar = kBias + (3 * 128 + 16) * 4;  // mbarrier (8 B), TMEM base (4 B)
 constexpr uint32_t kSmem = kBar + 16 + 128;        // + alignment slack of the base
-constexpr uint32_t kTmemCols = 256;                // D0/D2 in columns 0..127, D1/D3 128..
+constexpr uint32_t kTmemCols = 256;                // layers 0/2 in columns 0..127, 1/3 in 128..
 constexpr int kWaitLimit = 1 << 20;                // try_wait rounds before giving up
 }  // namespace tc
 
@@ -448,6 +453,7 @@ __host__ __device__ constexpr uint32_t umma_idesc_bf16(int M, int N) {
          ((uint32_t)(M >> 4) << 24);
 }
 
+// D (+)= A B^T for one K = 16 step
 __device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc,
                                           uint32_t accumulate) {
   asm volatile(
@@ -522,69 +528,106 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
 }
 
-// SiLU with one MUFU operation: z sigmoid(z) = h + h tanh(h), h = z / 2
-__device__ __forceinline__ float silu_tanh(float z) {
-  const float h = 0.5f * z;
+// the same value row (bias) into n = 32 or 16 consecutive columns of this
+// thread's lane; completion is awaited with tmem_st_wait before the MMA
+__device__ __forceinline__ void tmem_st_row32(uint32_t taddr, const float *row) {
+  const float4 *q = reinterpret_cast<const float4 *>(row);
+  float4 a[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) a[i] = q[i];
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
+      "%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};\n" ::"r"(
+          taddr),
+      "f"(a[0].x), "f"(a[0].y), "f"(a[0].z), "f"(a[0].w), "f"(a[1].x), "f"(a[1].y), "f"(a[1].z),
+      "f"(a[1].w), "f"(a[2].x), "f"(a[2].y), "f"(a[2].z), "f"(a[2].w), "f"(a[3].x), "f"(a[3].y),
+      "f"(a[3].z), "f"(a[3].w), "f"(a[4].x), "f"(a[4].y), "f"(a[4].z), "f"(a[4].w), "f"(a[5].x),
+      "f"(a[5].y), "f"(a[5].z), "f"(a[5].w), "f"(a[6].x), "f"(a[6].y), "f"(a[6].z), "f"(a[6].w),
+      "f"(a[7].x), "f"(a[7].y), "f"(a[7].z), "f"(a[7].w)
+      : "memory");
+}
+__device__ __forceinline__ void tmem_st_row16(uint32_t taddr, const float *row) {
+  const float4 *q = reinterpret_cast<const float4 *>(row);
+  float4 a[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) a[i] = q[i];
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
+      "%13,%14,%15,%16};\n" ::"r"(taddr),
+      "f"(a[0].x), "f"(a[0].y), "f"(a[0].z), "f"(a[0].w), "f"(a[1].x), "f"(a[1].y), "f"(a[1].z),
+      "f"(a[1].w), "f"(a[2].x), "f"(a[2].y), "f"(a[2].z), "f"(a[2].w), "f"(a[3].x), "f"(a[3].y),
+      "f"(a[3].z), "f"(a[3].w)
+      : "memory");
+}
+__device__ __forceinline__ void tmem_st_wait() {
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
+// SiLU(z) for h = z / 2: z sigmoid(z) = h + h tanh(h), one MUFU operation
+__device__ __forceinline__ float silu_half(float h) {
   float th;
   asm("tanh.approx.f32 %0, %1;" : "=f"(th) : "f"(h));
   return fmaf(h, th, h);
 }
 
-// rows [0, rows) x K columns of a row-major BF16 matrix into the K-major
-// core-matrix image (rows up to rows_pad, the extra ones zero)
+// rows [0, rows) x K columns of a row-major BF16 matrix (times `scale`, a
+// power of two) into the K-major core-matrix image, rows up to rows_pad zero;
+// consecutive threads write consecutive 16-byte chunks of the image
 __device__ __forceinline__ void stage_kmajor(unsigned char *img, const bf16 *src, int rows,
-                                             int rows_pad, int K) {
-  const int kc = K / 8;
-  for (int c = threadIdx.x; c < rows_pad * kc; c += blockDim.x) {
-    const int r = c / kc, q = c - r * kc;
+                                             int rows_pad, int K, float scale) {
+  for (int d = threadIdx.x; d < rows_pad * (K / 8); d += blockDim.x) {
+    const int g = d / K, rem = d - g * K;  // 8-row group, chunk within the group
+    const int q = rem >> 3, r = 8 * g + (rem & 7);
     uint4 v = make_uint4(0u, 0u, 0u, 0u);
-    if (r < rows) v = *reinterpret_cast<const uint4 *>(src + (long long)r * K + 8 * q);
-    *reinterpret_cast<uint4 *>(img + (r / 8) * (16 * K) + q * 128 + (r % 8) * 16) = v;
+    if (r < rows) {
+      v = *reinterpret_cast<const uint4 *>(src + (long long)r * K + 8 * q);
+      if (scale != 1.f) {
+        bf16 *e = reinterpret_cast<bf16 *>(&v);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) e[j] = __float2bfloat16_rn(__bfloat162float(e[j]) * scale);
+      }
+    }
+    *reinterpret_cast<uint4 *>(img + 16 * d) = v;
   }
 }
 
-// bias + SiLU of 128 accumulator columns of this thread's lane into row t of
-// the activation image
-__device__ __forceinline__ void tc_hidden_epilogue(uint32_t taddr, const float *bias,
-                                                   unsigned char *hs, int t) {
-  unsigned char *dst = hs + (t / 8) * 2048 + (t % 8) * 16;
-#pragma unroll 1
-  for (int ch = 0; ch < 4; ++ch) {
-    float v[32];
-    tmem_ld32(taddr + 32 * ch, v);
-    uint32_t pk[16];
+// SiLU of one 32-column accumulator chunk of this thread's lane into row r of
+// the activation image (columns c0 .. c0 + 31)
+__device__ __forceinline__ void tc_silu_chunk(uint32_t taddr, unsigned char *hs, int r, int c0) {
+  float v[32];
+  tmem_ld32(taddr, v);
+  uint32_t pk[16];
 #pragma unroll
-    for (int j = 0; j < 16; ++j)
-      pk[j] = pack_f2(silu_tanh(v[2 * j] + bias[32 * ch + 2 * j]),
-                      silu_tanh(v[2 * j + 1] + bias[32 * ch + 2 * j + 1]));
+  for (int j = 0; j < 16; ++j) pk[j] = pack_f2(silu_half(v[2 * j]), silu_half(v[2 * j + 1]));
+  unsigned char *dst = hs + (r / 8) * 2048 + (r % 8) * 16 + (c0 / 8) * 128;
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
-      *reinterpret_cast<uint4 *>(dst + (4 * ch + i) * 128) =
-          make_uint4(pk[4 * i], pk[4 * i + 1], pk[4 * i + 2], pk[4 * i + 3]);
-  }
+  for (int i = 0; i < 4; ++i)
+    *reinterpret_cast<uint4 *>(dst + i * 128) =
+        make_uint4(pk[4 * i], pk[4 * i + 1], pk[4 * i + 2], pk[4 * i + 3]);
 }
 
-__global__ void __launch_bounds__(128, 1) k_mlp_infer_tc(const bf16 *__restrict__ X, long long n,
-                                                         const bf16 *__restrict__ Wg,
-                                                         const float *__restrict__ P,
-                                                         float *__restrict__ Y, int *err) {
+__global__ void __launch_bounds__(tc::kThreads, 2)
+    k_mlp_infer_tc(const bf16 *__restrict__ X, long long n, const bf16 *__restrict__ Wg,
+                   const float *__restrict__ P, float *__restrict__ Y, int *err) {
   extern __shared__ __align__(128) unsigned char tc_raw[];
   unsigned char *sm = tc_raw + ((128 - (smem_u32(tc_raw) & 127)) & 127);
   const int t = threadIdx.x, warp = t >> 5;
+  const int r = t & 127;     // row of the tile = TMEM lane
+  const int half = t >> 7;   // column half (64 of each 128) handled by this thread
   float *bias = reinterpret_cast<float *>(sm + tc::kBias);
   uint64_t *bar = reinterpret_cast<uint64_t *>(sm + tc::kBar);
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(sm + tc::kBar + 8);
   const uint32_t bar_a = smem_u32(bar);
 
-  // weights and biases, once per CTA
-  stage_kmajor(sm + tc::kW0, Wg + kOffW0, kMlpHid, kMlpHid, kMlpIn);
-  stage_kmajor(sm + tc::kW1, Wg + kOffW1, kMlpHid, kMlpHid, kMlpHid);
-  stage_kmajor(sm + tc::kW2, Wg + kOffW2, kMlpHid, kMlpHid, kMlpHid);
-  stage_kmajor(sm + tc::kW3, Wg + kOffW3, kMlpOut, 16, kMlpHid);
+  // weights and biases, once per CTA (layers 0..2 times 1/2, see above)
+  stage_kmajor(sm + tc::kW0, Wg + kOffW0, kMlpHid, kMlpHid, kMlpIn, 0.5f);
+  stage_kmajor(sm + tc::kW1, Wg + kOffW1, kMlpHid, kMlpHid, kMlpHid, 0.5f);
+  stage_kmajor(sm + tc::kW2, Wg + kOffW2, kMlpHid, kMlpHid, kMlpHid, 0.5f);
+  stage_kmajor(sm + tc::kW3, Wg + kOffW3, kMlpOut, 16, kMlpHid, 1.f);
   for (int i = t; i < kMlpHid; i += blockDim.x) {
-    bias[i] = P[kOffB0 + i];
-    bias[kMlpHid + i] = P[kOffB1 + i];
-    bias[2 * kMlpHid + i] = P[kOffB2 + i];
+    bias[i] = 0.5f * P[kOffB0 + i];
+    bias[kMlpHid + i] = 0.5f * P[kOffB1 + i];
+    bias[2 * kMlpHid + i] = 0.5f * P[kOffB2 + i];
   }
   if (t < 16) bias[3 * kMlpHid + t] = t < kMlpOut ? P[kOffB3 + t] : 0.f;
   if (t == 0) {
@@ -603,98 +646,124 @@ __global__ void __launch_bounds__(128, 1) k_mlp_infer_tc(const bf16 *__restrict_
   __syncthreads();
   tc_fence_after();
   const uint32_t tbase = *tmem_slot;
-  const uint32_t tlane = tbase + ((uint32_t)(32 * warp) << 16);  // this warp's lanes
+  const uint32_t tlane = tbase + ((uint32_t)(32 * (warp & 3)) << 16);  // this warp's lanes
+  const int cA = 64 * half, cB = cA + 32;  // this thread's two 32-column chunks
+  const float *b0 = bias, *b1 = bias + kMlpHid, *b2 = bias + 2 * kMlpHid, *b3 = bias + 3 * kMlpHid;
 
   const uint32_t sW0 = smem_u32(sm + tc::kW0), sW1 = smem_u32(sm + tc::kW1);
   const uint32_t sW2 = smem_u32(sm + tc::kW2), sW3 = smem_u32(sm + tc::kW3);
   const uint32_t sX = smem_u32(sm + tc::kXs), sH = smem_u32(sm + tc::kHs);
   constexpr uint32_t id128 = umma_idesc_bf16(128, 128), id16 = umma_idesc_bf16(128, 16);
 
+  // layer 0's bias into columns 0..127 for the first tile
+  tmem_st_row32(tlane + cA, b0 + cA);
+  tmem_st_row32(tlane + cB, b0 + cB);
+  tmem_st_wait();
+
   uint32_t phase = 0;
   int bad = 0;
   const long long tiles = (n + 127) / 128;
+  // this thread's 16-byte half of its row of the next tile, loaded ahead
+  uint4 xn = make_uint4(0u, 0u, 0u, 0u);
+  {
+    const long long row = (long long)blockIdx.x * 128 + r;
+    if ((long long)blockIdx.x < tiles && row < n)
+      xn = reinterpret_cast<const uint4 *>(X + row * kMlpIn)[half];
+  }
   for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-    const long long row = tile * 128 + t;
-    uint4 x0 = make_uint4(0u, 0u, 0u, 0u), x1 = x0;
-    if (row < n) {
-      const uint4 *src = reinterpret_cast<const uint4 *>(X + row * kMlpIn);
-      x0 = src[0];
-      x1 = src[1];
-    }
-    unsigned char *xd = sm + tc::kXs + (t / 8) * 256 + (t % 8) * 16;
-    *reinterpret_cast<uint4 *>(xd) = x0;
-    *reinterpret_cast<uint4 *>(xd + 128) = x1;
+    const long long row = tile * 128 + r;
+    *reinterpret_cast<uint4 *>(sm + tc::kXs + (r / 8) * 256 + half * 128 + (r % 8) * 16) = xn;
     fence_proxy_async_smem();
     tc_fence_before();
     __syncthreads();
-    // layer 0: D[0..128) = X W0^T (K = 16)
+    // layer 0: D[0..128) = b0/2 + X W0^T/2 (K = 16)
     if (t == 0) {
       tc_fence_after();
-      umma_bf16(tbase, umma_sdesc(sX, 128, 256), umma_sdesc(sW0, 128, 256), id128, 0u);
+      umma_bf16(tbase, umma_sdesc(sX, 128, 256), umma_sdesc(sW0, 128, 256), id128, 1u);
       umma_commit(bar_a);
+    }
+    {  // prefetch the next tile's row while this one runs
+      const long long nrow = (tile + gridDim.x) * 128 + r;
+      xn = make_uint4(0u, 0u, 0u, 0u);
+      if (tile + gridDim.x < tiles && nrow < n)
+        xn = reinterpret_cast<const uint4 *>(X + nrow * kMlpIn)[half];
     }
     bad |= !mbar_wait(bar_a, phase);
     phase ^= 1u;
     tc_fence_after();
     __syncwarp();
-    tc_hidden_epilogue(tlane, bias, sm + tc::kHs, t);
+    tc_silu_chunk(tlane + cA, sm + tc::kHs, r, cA);
+    tc_silu_chunk(tlane + cB, sm + tc::kHs, r, cB);
+    tmem_st_row32(tlane + cA, b2 + cA);        // layer 2 accumulates here next
+    tmem_st_row32(tlane + cB, b2 + cB);
+    tmem_st_row32(tlane + 128 + cA, b1 + cA);  // layer 1 accumulates here
+    tmem_st_row32(tlane + 128 + cB, b1 + cB);
+    tmem_st_wait();
     fence_proxy_async_smem();
     tc_fence_before();
     if (__syncthreads_or(bad)) break;
-    // layer 1: D[128..256) = H W1^T (K = 128 in 8 steps)
+    // layer 1: D[128..256) = b1/2 + H W1^T/2 (K = 128 in 8 steps)
     if (t == 0) {
       tc_fence_after();
 #pragma unroll
       for (int kk = 0; kk < 8; ++kk)
         umma_bf16(tbase + 128, umma_sdesc(sH + 256 * kk, 128, 2048),
-                  umma_sdesc(sW1 + 256 * kk, 128, 2048), id128, kk > 0 ? 1u : 0u);
+                  umma_sdesc(sW1 + 256 * kk, 128, 2048), id128, 1u);
       umma_commit(bar_a);
     }
     bad |= !mbar_wait(bar_a, phase);
     phase ^= 1u;
     tc_fence_after();
     __syncwarp();
-    tc_hidden_epilogue(tlane + 128, bias + kMlpHid, sm + tc::kHs, t);
+    tc_silu_chunk(tlane + 128 + cA, sm + tc::kHs, r, cA);
+    if (half == 0) tmem_st_row16(tlane + 128, b3);  // layer 3 accumulates in 128..143
+    tc_silu_chunk(tlane + 128 + cB, sm + tc::kHs, r, cB);
+    tmem_st_wait();
     fence_proxy_async_smem();
     tc_fence_before();
     if (__syncthreads_or(bad)) break;
-    // layer 2: D[0..128) = H W2^T
+    // layer 2: D[0..128) = b2/2 + H W2^T/2
     if (t == 0) {
       tc_fence_after();
 #pragma unroll
       for (int kk = 0; kk < 8; ++kk)
         umma_bf16(tbase, umma_sdesc(sH + 256 * kk, 128, 2048),
-                  umma_sdesc(sW2 + 256 * kk, 128, 2048), id128, kk > 0 ? 1u : 0u);
+                  umma_sdesc(sW2 + 256 * kk, 128, 2048), id128, 1u);
       umma_commit(bar_a);
     }
     bad |= !mbar_wait(bar_a, phase);
     phase ^= 1u;
     tc_fence_after();
     __syncwarp();
-    tc_hidden_epilogue(tlane, bias + 2 * kMlpHid, sm + tc::kHs, t);
+    tc_silu_chunk(tlane + cA, sm + tc::kHs, r, cA);
+    tc_silu_chunk(tlane + cB, sm + tc::kHs, r, cB);
+    tmem_st_row32(tlane + cA, b0 + cA);  // the next tile's layer 0
+    tmem_st_row32(tlane + cB, b0 + cB);
+    tmem_st_wait();
     fence_proxy_async_smem();
     tc_fence_before();
     if (__syncthreads_or(bad)) break;
-    // layer 3: D[128..144) = H W3^T (N = 16, outputs 8..15 are zero rows)
+    // layer 3: D[128..144) = b3 + H W3^T (N = 16, outputs 8..15 are zero rows)
     if (t == 0) {
       tc_fence_after();
 #pragma unroll
       for (int kk = 0; kk < 8; ++kk)
         umma_bf16(tbase + 128, umma_sdesc(sH + 256 * kk, 128, 2048),
-                  umma_sdesc(sW3 + 256 * kk, 128, 2048), id16, kk > 0 ? 1u : 0u);
+                  umma_sdesc(sW3 + 256 * kk, 128, 2048), id16, 1u);
       umma_commit(bar_a);
     }
     bad |= !mbar_wait(bar_a, phase);
     phase ^= 1u;
     tc_fence_after();
     __syncwarp();
-    float o[16];
-    tmem_ld16(tlane + 128, o);
-    if (row < n) {
-      const float *b3 = bias + 3 * kMlpHid;
-      float4 *yd = reinterpret_cast<float4 *>(Y + row * kMlpOut);
-      yd[0] = make_float4(o[0] + b3[0], o[1] + b3[1], o[2] + b3[2], o[3] + b3[3]);
-      yd[1] = make_float4(o[4] + b3[4], o[5] + b3[5], o[6] + b3[6], o[7] + b3[7]);
+    if (half == 0) {
+      float o[16];
+      tmem_ld16(tlane + 128, o);
+      if (row < n) {
+        float4 *yd = reinterpret_cast<float4 *>(Y + row * kMlpOut);
+        yd[0] = make_float4(o[0], o[1], o[2], o[3]);
+        yd[1] = make_float4(o[4], o[5], o[6], o[7]);
+      }
     }
     tc_fence_before();
     if (__syncthreads_or(bad)) break;
@@ -877,7 +946,7 @@ int surrogate_infer(ftgpu_surrogate *s, const uint16_t *X, long long n, float *Y
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
   const long long tiles = (n + 127) / 128;
   const long long grid = std::max<long long>(1, std::min<long long>((long long)sms * 2, tiles));
-  k_mlp_infer_tc<<<(unsigned)grid, 128, tc::kSmem, st>>>(reinterpret_cast<const bf16 *>(X), n,
+  k_mlp_infer_tc<<<(unsigned)grid, tc::kThreads, tc::kSmem, st>>>(reinterpret_cast<const bf16 *>(X), n,
                                                           s->Wb, s->P, Y, err);
   return cudaGetLastError() == cudaSuccess ? 0 : FTGPU_ERR_CUDA;
 }
