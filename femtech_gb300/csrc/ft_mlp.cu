@@ -402,18 +402,22 @@ __global__ void __launch_bounds__(256) k_mlp_infer(const bf16 *__restrict__ X, l
 }
 
 // ---------------- fused inference on the 5th-generation tensor cores ----------------
-// One CTA of 256 threads processes tiles of 128 rows.  Row r of a tile is
-// TMEM lane r of every accumulator; warps w and w + 4 share lane quarter w
-// (tcgen05.ld/st reach lanes 32 (w mod 4) .. +31) and split the columns.
-// Each layer is a chain of tcgen05.mma (M = 128, K = 16 per instruction,
-// BF16 x BF16 -> FP32 in TMEM) issued by thread 0 and signalled through one
-// mbarrier, accumulating onto the layer's bias, which the epilogue of the
-// previous reader of those columns stored there with tcgen05.st.  W0..W2 and
-// b0..b2 are staged pre-multiplied by 1/2 (exact), so an accumulator holds
-// h = z / 2 and SiLU(z) = z sigmoid(z) = h + h tanh(h) costs one MUFU tanh
-// and one FMA.  The epilogue writes BF16 activations back to shared memory as
-// the next layer's A operand.  Two CTAs share an SM (113 KB of shared memory
-// and 256 TMEM columns each), so one CTA's epilogue overlaps the other's MMAs.
+// A persistent, warp-specialised kernel: one CTA per SM stages the weights
+// once and keeps four 128-row tiles in flight, one per *slot*.  Slot s owns an
+// input image, an activation image and TMEM columns [128 s, 128 s + 128); row r
+// of its tile is TMEM lane r.  Warps 4s .. 4s+3 are the slot's epilogue (warp
+// 4s + q reaches lanes 32 q .. 32 q + 31); warp 16 issues every MMA from one
+// thread.  Per layer the slot's epilogue stores the layer's bias into the
+// accumulator columns (tcgen05.st), makes its operands visible and arrives on
+// full[s]; the MMA thread waits on full[s], issues the layer (tcgen05.mma,
+// M = 128, K = 16 per instruction, BF16 x BF16 -> FP32 accumulating onto the
+// bias) and commits to done[s]; the epilogue waits on done[s], reads the
+// accumulator (tcgen05.ld), applies SiLU and writes the BF16 activations as
+// the next layer's A operand.  While one slot runs its epilogue the tensor
+// core serves the others.  W0..W2 and b0..b2 are staged times 1/2 (exact), so
+// an accumulator holds h = z / 2 and SiLU(z) = z sigmoid(z) = h + h tanh(h)
+// costs one MUFU tanh and one FMA.  Every wait is bounded; a wait that gives
+// up raises a shared abort flag that ends all roles, and the error word.
 //
 // Shared-memory operand images are K-major without swizzle: 8-row x 16-byte
 // core matrices, element (r, k) of an image with K columns at byte
@@ -421,18 +425,20 @@ __global__ void __launch_bounds__(256) k_mlp_infer(const bf16 *__restrict__ X, l
 // i.e. leading-dimension (K-direction) byte offset 128 and stride-dimension
 // (8-row group) byte offset 16 K in the matrix descriptors.
 namespace tc {
-constexpr int kThreads = 256;
+constexpr int kSlots = 4;
+constexpr int kMmaWarp = 4 * kSlots;               // warp 16
+constexpr int kThreads = 32 * (kMmaWarp + 1);      // 544
 constexpr uint32_t kW0 = 0;                        // [128 x 16]     4 KB
 constexpr uint32_t kW1 = kW0 + 128 * 16 * 2;       // [128 x 128]   32 KB
 constexpr uint32_t kW2 = kW1 + 128 * 128 * 2;      // [128 x 128]   32 KB
 constexpr uint32_t kW3 = kW2 + 128 * 128 * 2;      // [16 x 128]     4 KB (rows 8..15 zero)
-constexpr uint32_t kXs = kW3 + 16 * 128 * 2;       // [128 x 16]     4 KB input tile
-constexpr uint32_t kHs = kXs + 128 * 16 * 2;       // [128 x 128]   32 KB activations
-constexpr uint32_t kBias = kHs + 128 * 128 * 2;    // FP32 b0/2 b1/2 b2/2 (128 each), b3 (16)
-constexpr uint32_t kBar = kBias + (3 * 128 + 16) * 4;  // mbarrier (8 B), TMEM base (4 B)
-constexpr uint32_t kSmem = kBar + 16 + 128;        // + alignment slack of the base
-constexpr uint32_t kTmemCols = 256;                // layers 0/2 in columns 0..127, 1/3 in 128..
-constexpr int kWaitLimit = 1 << 20;                // try_wait rounds before giving up
+constexpr uint32_t kXs = kW3 + 16 * 128 * 2;       // per slot [128 x 16]    4 KB
+constexpr uint32_t kHs = kXs + kSlots * 4096;      // per slot [128 x 128]  32 KB
+constexpr uint32_t kBias = kHs + kSlots * 32768;   // FP32 b0/2 b1/2 b2/2 (128 each), b3 (16)
+constexpr uint32_t kBar = kBias + (3 * 128 + 16) * 4;  // full[4], done[4], TMEM base, abort
+constexpr uint32_t kSmem = kBar + 72 + 128;        // + alignment slack of the base
+constexpr uint32_t kTmemCols = 128 * kSlots;       // 512: all of this SM's TMEM
+constexpr int kWaitLimit = 1 << 21;                // try_wait rounds before giving up
 }  // namespace tc
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -479,8 +485,9 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
-// bounded wait for the completion of phase `parity` of an mbarrier
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+// bounded wait for the completion of phase `parity` of an mbarrier; gives up
+// (false) after kWaitLimit rounds or when another role raised *abort
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort) {
   for (int it = 0; it < tc::kWaitLimit; ++it) {
     uint32_t ok;
     asm volatile(
@@ -490,8 +497,14 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
         : "r"(bar), "r"(parity)
         : "memory");
     if (ok) return true;
+    if (*abort) return false;
   }
+  *abort = 1;
   return false;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
 // 32 consecutive FP32 accumulator columns of this thread's TMEM lane (the
@@ -606,18 +619,33 @@ __device__ __forceinline__ void tc_silu_chunk(uint32_t taddr, unsigned char *hs,
         make_uint4(pk[4 * i], pk[4 * i + 1], pk[4 * i + 2], pk[4 * i + 3]);
 }
 
-__global__ void __launch_bounds__(tc::kThreads, 2)
+// issue one layer of a slot: D (+)= A B^T over K = 16 steps
+__device__ __forceinline__ void tc_issue_layer(int layer, uint32_t tmem_d, uint32_t sX,
+                                               uint32_t sH, uint32_t sW0, uint32_t sW1,
+                                               uint32_t sW2, uint32_t sW3) {
+  constexpr uint32_t id128 = umma_idesc_bf16(128, 128), id16 = umma_idesc_bf16(128, 16);
+  if (layer == 0) {
+    umma_bf16(tmem_d, umma_sdesc(sX, 128, 256), umma_sdesc(sW0, 128, 256), id128, 1u);
+    return;
+  }
+  const uint32_t sW = layer == 1 ? sW1 : (layer == 2 ? sW2 : sW3);
+  const uint32_t id = layer == 3 ? id16 : id128;
+#pragma unroll
+  for (int kk = 0; kk < 8; ++kk)
+    umma_bf16(tmem_d, umma_sdesc(sH + 256 * kk, 128, 2048), umma_sdesc(sW + 256 * kk, 128, 2048),
+              id, 1u);
+}
+
+__global__ void __maxnreg__(120)
     k_mlp_infer_tc(const bf16 *__restrict__ X, long long n, const bf16 *__restrict__ Wg,
                    const float *__restrict__ P, float *__restrict__ Y, int *err) {
   extern __shared__ __align__(128) unsigned char tc_raw[];
   unsigned char *sm = tc_raw + ((128 - (smem_u32(tc_raw) & 127)) & 127);
-  const int t = threadIdx.x, warp = t >> 5;
-  const int r = t & 127;     // row of the tile = TMEM lane
-  const int half = t >> 7;   // column half (64 of each 128) handled by this thread
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   float *bias = reinterpret_cast<float *>(sm + tc::kBias);
-  uint64_t *bar = reinterpret_cast<uint64_t *>(sm + tc::kBar);
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(sm + tc::kBar + 8);
-  const uint32_t bar_a = smem_u32(bar);
+  const uint32_t full0 = smem_u32(sm + tc::kBar), done0 = full0 + 8 * tc::kSlots;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(sm + tc::kBar + 64);
+  volatile int *abort = reinterpret_cast<volatile int *>(sm + tc::kBar + 68);
 
   // weights and biases, once per CTA (layers 0..2 times 1/2, see above)
   stage_kmajor(sm + tc::kW0, Wg + kOffW0, kMlpHid, kMlpHid, kMlpIn, 0.5f);
@@ -631,7 +659,11 @@ __global__ void __launch_bounds__(tc::kThreads, 2)
   }
   if (t < 16) bias[3 * kMlpHid + t] = t < kMlpOut ? P[kOffB3 + t] : 0.f;
   if (t == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_a) : "memory");
+    for (int sl = 0; sl < tc::kSlots; ++sl) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 128;" ::"r"(full0 + 8 * sl) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(done0 + 8 * sl) : "memory");
+    }
+    *abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -646,133 +678,111 @@ __global__ void __launch_bounds__(tc::kThreads, 2)
   __syncthreads();
   tc_fence_after();
   const uint32_t tbase = *tmem_slot;
-  const uint32_t tlane = tbase + ((uint32_t)(32 * (warp & 3)) << 16);  // this warp's lanes
-  const int cA = 64 * half, cB = cA + 32;  // this thread's two 32-column chunks
-  const float *b0 = bias, *b1 = bias + kMlpHid, *b2 = bias + 2 * kMlpHid, *b3 = bias + 3 * kMlpHid;
-
   const uint32_t sW0 = smem_u32(sm + tc::kW0), sW1 = smem_u32(sm + tc::kW1);
   const uint32_t sW2 = smem_u32(sm + tc::kW2), sW3 = smem_u32(sm + tc::kW3);
-  const uint32_t sX = smem_u32(sm + tc::kXs), sH = smem_u32(sm + tc::kHs);
-  constexpr uint32_t id128 = umma_idesc_bf16(128, 128), id16 = umma_idesc_bf16(128, 16);
+  const long long tiles = (n + 127) / 128, stride = (long long)tc::kSlots * gridDim.x;
 
-  // layer 0's bias into columns 0..127 for the first tile
-  tmem_st_row32(tlane + cA, b0 + cA);
-  tmem_st_row32(tlane + cB, b0 + cB);
-  tmem_st_wait();
-
-  uint32_t phase = 0;
-  int bad = 0;
-  const long long tiles = (n + 127) / 128;
-  // this thread's 16-byte half of its row of the next tile, loaded ahead
-  uint4 xn = make_uint4(0u, 0u, 0u, 0u);
-  {
-    const long long row = (long long)blockIdx.x * 128 + r;
-    if ((long long)blockIdx.x < tiles && row < n)
-      xn = reinterpret_cast<const uint4 *>(X + row * kMlpIn)[half];
-  }
-  for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-    const long long row = tile * 128 + r;
-    *reinterpret_cast<uint4 *>(sm + tc::kXs + (r / 8) * 256 + half * 128 + (r % 8) * 16) = xn;
-    fence_proxy_async_smem();
-    tc_fence_before();
-    __syncthreads();
-    // layer 0: D[0..128) = b0/2 + X W0^T/2 (K = 16)
-    if (t == 0) {
-      tc_fence_after();
-      umma_bf16(tbase, umma_sdesc(sX, 128, 256), umma_sdesc(sW0, 128, 256), id128, 1u);
-      umma_commit(bar_a);
+  if (warp < tc::kMmaWarp) {
+    // ---- epilogue of slot s: tiles first, first + stride, ...
+    const int s = warp >> 2, q = warp & 3, r = 32 * q + lane;
+    const uint32_t tl = tbase + ((uint32_t)(32 * q) << 16) + 128u * s;
+    const uint32_t full = full0 + 8 * s, done = done0 + 8 * s;
+    unsigned char *xs = sm + tc::kXs + 4096 * s, *hs = sm + tc::kHs + 32768 * s;
+    const long long first = (long long)tc::kSlots * blockIdx.x + s;
+    uint32_t j = 0;  // steps (layers) completed: the parity of the next wait
+    uint4 xa = make_uint4(0u, 0u, 0u, 0u), xb = xa;
+    if (first < tiles && first * 128 + r < n) {
+      const uint4 *src = reinterpret_cast<const uint4 *>(X + (first * 128 + r) * kMlpIn);
+      xa = src[0];
+      xb = src[1];
     }
-    {  // prefetch the next tile's row while this one runs
-      const long long nrow = (tile + gridDim.x) * 128 + r;
-      xn = make_uint4(0u, 0u, 0u, 0u);
-      if (tile + gridDim.x < tiles && nrow < n)
-        xn = reinterpret_cast<const uint4 *>(X + nrow * kMlpIn)[half];
-    }
-    bad |= !mbar_wait(bar_a, phase);
-    phase ^= 1u;
-    tc_fence_after();
-    __syncwarp();
-    tc_silu_chunk(tlane + cA, sm + tc::kHs, r, cA);
-    tc_silu_chunk(tlane + cB, sm + tc::kHs, r, cB);
-    tmem_st_row32(tlane + cA, b2 + cA);        // layer 2 accumulates here next
-    tmem_st_row32(tlane + cB, b2 + cB);
-    tmem_st_row32(tlane + 128 + cA, b1 + cA);  // layer 1 accumulates here
-    tmem_st_row32(tlane + 128 + cB, b1 + cB);
-    tmem_st_wait();
-    fence_proxy_async_smem();
-    tc_fence_before();
-    if (__syncthreads_or(bad)) break;
-    // layer 1: D[128..256) = b1/2 + H W1^T/2 (K = 128 in 8 steps)
-    if (t == 0) {
-      tc_fence_after();
+    bool ok = true;
+    for (long long tile = first; tile < tiles && ok; tile += stride) {
+      const long long row = tile * 128 + r;
+      // layer 0 operands: the input rows and b0 in the accumulator
+      unsigned char *xd = xs + (r / 8) * 256 + (r % 8) * 16;
+      *reinterpret_cast<uint4 *>(xd) = xa;
+      *reinterpret_cast<uint4 *>(xd + 128) = xb;
 #pragma unroll
-      for (int kk = 0; kk < 8; ++kk)
-        umma_bf16(tbase + 128, umma_sdesc(sH + 256 * kk, 128, 2048),
-                  umma_sdesc(sW1 + 256 * kk, 128, 2048), id128, 1u);
-      umma_commit(bar_a);
-    }
-    bad |= !mbar_wait(bar_a, phase);
-    phase ^= 1u;
-    tc_fence_after();
-    __syncwarp();
-    tc_silu_chunk(tlane + 128 + cA, sm + tc::kHs, r, cA);
-    if (half == 0) tmem_st_row16(tlane + 128, b3);  // layer 3 accumulates in 128..143
-    tc_silu_chunk(tlane + 128 + cB, sm + tc::kHs, r, cB);
-    tmem_st_wait();
-    fence_proxy_async_smem();
-    tc_fence_before();
-    if (__syncthreads_or(bad)) break;
-    // layer 2: D[0..128) = b2/2 + H W2^T/2
-    if (t == 0) {
-      tc_fence_after();
-#pragma unroll
-      for (int kk = 0; kk < 8; ++kk)
-        umma_bf16(tbase, umma_sdesc(sH + 256 * kk, 128, 2048),
-                  umma_sdesc(sW2 + 256 * kk, 128, 2048), id128, 1u);
-      umma_commit(bar_a);
-    }
-    bad |= !mbar_wait(bar_a, phase);
-    phase ^= 1u;
-    tc_fence_after();
-    __syncwarp();
-    tc_silu_chunk(tlane + cA, sm + tc::kHs, r, cA);
-    tc_silu_chunk(tlane + cB, sm + tc::kHs, r, cB);
-    tmem_st_row32(tlane + cA, b0 + cA);  // the next tile's layer 0
-    tmem_st_row32(tlane + cB, b0 + cB);
-    tmem_st_wait();
-    fence_proxy_async_smem();
-    tc_fence_before();
-    if (__syncthreads_or(bad)) break;
-    // layer 3: D[128..144) = b3 + H W3^T (N = 16, outputs 8..15 are zero rows)
-    if (t == 0) {
-      tc_fence_after();
-#pragma unroll
-      for (int kk = 0; kk < 8; ++kk)
-        umma_bf16(tbase + 128, umma_sdesc(sH + 256 * kk, 128, 2048),
-                  umma_sdesc(sW3 + 256 * kk, 128, 2048), id16, 1u);
-      umma_commit(bar_a);
-    }
-    bad |= !mbar_wait(bar_a, phase);
-    phase ^= 1u;
-    tc_fence_after();
-    __syncwarp();
-    if (half == 0) {
-      float o[16];
-      tmem_ld16(tlane + 128, o);
-      if (row < n) {
-        float4 *yd = reinterpret_cast<float4 *>(Y + row * kMlpOut);
-        yd[0] = make_float4(o[0], o[1], o[2], o[3]);
-        yd[1] = make_float4(o[4], o[5], o[6], o[7]);
+      for (int c = 0; c < 4; ++c) tmem_st_row32(tl + 32 * c, bias + 32 * c);
+      {  // the next tile's rows, loaded while this one runs
+        const long long nrow = (tile + stride) * 128 + r;
+        xa = make_uint4(0u, 0u, 0u, 0u);
+        xb = xa;
+        if (tile + stride < tiles && nrow < n) {
+          const uint4 *src = reinterpret_cast<const uint4 *>(X + nrow * kMlpIn);
+          xa = src[0];
+          xb = src[1];
+        }
+      }
+      tmem_st_wait();
+      fence_proxy_async_smem();
+      tc_fence_before();
+      mbar_arrive(full);
+      for (int l = 0; l < 4; ++l) {
+        ok = mbar_wait(done, j & 1u, abort);
+        ++j;
+        tc_fence_after();
+        ok = __all_sync(0xffffffffu, ok);  // warp-uniform before the .sync.aligned TMEM ops
+        if (!ok) break;
+        if (l < 3) {
+#pragma unroll 1
+          for (int c = 0; c < 4; ++c) {
+            tc_silu_chunk(tl + 32 * c, hs, r, 32 * c);
+            if (l < 2)
+              tmem_st_row32(tl + 32 * c, bias + 128 * (l + 1) + 32 * c);
+            else if (c == 0)
+              tmem_st_row16(tl, bias + 3 * kMlpHid);
+          }
+          tmem_st_wait();
+          fence_proxy_async_smem();
+          tc_fence_before();
+          mbar_arrive(full);
+        } else {
+          float o[16];
+          tmem_ld16(tl, o);
+          if (row < n) {
+            float4 *yd = reinterpret_cast<float4 *>(Y + row * kMlpOut);
+            yd[0] = make_float4(o[0], o[1], o[2], o[3]);
+            yd[1] = make_float4(o[4], o[5], o[6], o[7]);
+          }
+        }
       }
     }
-    tc_fence_before();
-    if (__syncthreads_or(bad)) break;
+    if (!ok && lane == 0) atomicOr(err, kErrWait);
+  } else if (lane == 0) {
+    // ---- the MMA issuer: slots round-robin, one layer per visit
+    long long nt[tc::kSlots];
+    uint32_t js[tc::kSlots];
+    for (int sl = 0; sl < tc::kSlots; ++sl) {
+      const long long f = (long long)tc::kSlots * blockIdx.x + sl;
+      nt[sl] = f < tiles ? (tiles - 1 - f) / stride + 1 : 0;
+      js[sl] = 0;
+    }
+    bool ok = true, any = true;
+    while (ok && any) {
+      any = false;
+      for (int sl = 0; sl < tc::kSlots && ok; ++sl) {
+        if ((long long)js[sl] >= 4 * nt[sl]) continue;
+        any = true;
+        ok = mbar_wait(full0 + 8 * sl, js[sl] & 1u, abort);
+        if (!ok) break;
+        tc_fence_after();
+        tc_issue_layer((int)(js[sl] & 3u), tbase + 128u * sl,
+                       smem_u32(sm + tc::kXs + 4096 * sl), smem_u32(sm + tc::kHs + 32768 * sl),
+                       sW0, sW1, sW2, sW3);
+        umma_commit(done0 + 8 * sl);
+        ++js[sl];
+      }
+    }
+    if (!ok) {
+      atomicOr(err, kErrWait);
+      // the MMAs already issued (bounded): the last commit of every slot
+      for (int sl = 0; sl < tc::kSlots; ++sl)
+        if (js[sl] > 0) mbar_wait(done0 + 8 * sl, (js[sl] - 1) & 1u, abort);
+    }
   }
-  if (bad && t == 0) {
-    atomicOr(err, kErrWait);
-    mbar_wait(bar_a, phase ^ 1u);  // the MMAs of the wait that gave up (bounded)
-  }
-  // every MMA this CTA issued has completed (or the wait gave up): free TMEM
+  // every MMA has completed (or a wait gave up): free TMEM
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -945,7 +955,8 @@ int surrogate_infer(ftgpu_surrogate *s, const uint16_t *X, long long n, float *Y
   int sms = 152;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
   const long long tiles = (n + 127) / 128;
-  const long long grid = std::max<long long>(1, std::min<long long>((long long)sms * 2, tiles));
+  const long long grid =
+      std::max<long long>(1, std::min<long long>((long long)sms, (tiles + tc::kSlots - 1) / tc::kSlots));
   k_mlp_infer_tc<<<(unsigned)grid, tc::kThreads, tc::kSmem, st>>>(reinterpret_cast<const bf16 *>(X), n,
                                                           s->Wb, s->P, Y, err);
   return cudaGetLastError() == cudaSuccess ? 0 : FTGPU_ERR_CUDA;
