@@ -25,6 +25,9 @@ static int fail(int code, const std::string &msg) {
   return code;
 }
 
+// shared with the surrogate translation unit
+int record_error(int code, const char *msg) { return fail(code, msg); }
+
 #define CK(call)                                                                          \
   do {                                                                                    \
     cudaError_t e_ = (call);                                                              \

@@ -21,6 +21,8 @@
 
 namespace ftgpu {
 
+int record_error(int code, const char *msg);  // ft_api.cu: sets ftgpu_last_error()
+
 typedef __nv_bfloat16 bf16;
 
 // ---------------- counter-based random numbers ----------------
@@ -403,10 +405,12 @@ __global__ void __launch_bounds__(256) k_mlp_infer(const bf16 *__restrict__ X, l
 
 // ---------------- fused inference on the 5th-generation tensor cores ----------------
 // A persistent, warp-specialised kernel: one CTA per SM stages the weights
-// once and keeps four 128-row tiles in flight, one per *slot*.  Slot s owns an
+// once and keeps three 128-row tiles in flight, one per *slot* (13 warps: the
+// register file is split over the SM's four schedulers, and 4 warps of 128
+// registers fill one scheduler's share).  Slot s owns an
 // input image, an activation image and TMEM columns [128 s, 128 s + 128); row r
 // of its tile is TMEM lane r.  Warps 4s .. 4s+3 are the slot's epilogue (warp
-// 4s + q reaches lanes 32 q .. 32 q + 31); warp 16 issues every MMA from one
+// 4s + q reaches lanes 32 q .. 32 q + 31); warp 12 issues every MMA from one
 // thread.  Per layer the slot's epilogue stores the layer's bias into the
 // accumulator columns (tcgen05.st), makes its operands visible and arrives on
 // full[s]; the MMA thread waits on full[s], issues the layer (tcgen05.mma,
@@ -425,9 +429,9 @@ __global__ void __launch_bounds__(256) k_mlp_infer(const bf16 *__restrict__ X, l
 // i.e. leading-dimension (K-direction) byte offset 128 and stride-dimension
 // (8-row group) byte offset 16 K in the matrix descriptors.
 namespace tc {
-constexpr int kSlots = 4;
-constexpr int kMmaWarp = 4 * kSlots;               // warp 16
-constexpr int kThreads = 32 * (kMmaWarp + 1);      // 544
+constexpr int kSlots = 3;
+constexpr int kMmaWarp = 4 * kSlots;               // warp 12
+constexpr int kThreads = 32 * (kMmaWarp + 1);      // 416: at most 4 warps per SMSP
 constexpr uint32_t kW0 = 0;                        // [128 x 16]     4 KB
 constexpr uint32_t kW1 = kW0 + 128 * 16 * 2;       // [128 x 128]   32 KB
 constexpr uint32_t kW2 = kW1 + 128 * 128 * 2;      // [128 x 128]   32 KB
@@ -435,9 +439,9 @@ constexpr uint32_t kW3 = kW2 + 128 * 128 * 2;      // [16 x 128]     4 KB (rows 
 constexpr uint32_t kXs = kW3 + 16 * 128 * 2;       // per slot [128 x 16]    4 KB
 constexpr uint32_t kHs = kXs + kSlots * 4096;      // per slot [128 x 128]  32 KB
 constexpr uint32_t kBias = kHs + kSlots * 32768;   // FP32 b0/2 b1/2 b2/2 (128 each), b3 (16)
-constexpr uint32_t kBar = kBias + (3 * 128 + 16) * 4;  // full[4], done[4], TMEM base, abort
+constexpr uint32_t kBar = kBias + (3 * 128 + 16) * 4;  // full[], done[], TMEM base, abort
 constexpr uint32_t kSmem = kBar + 72 + 128;        // + alignment slack of the base
-constexpr uint32_t kTmemCols = 128 * kSlots;       // 512: all of this SM's TMEM
+constexpr uint32_t kTmemCols = 512;               // 128 per slot, rounded to a power of 2
 constexpr int kWaitLimit = 1 << 21;                // try_wait rounds before giving up
 }  // namespace tc
 
@@ -636,7 +640,7 @@ __device__ __forceinline__ void tc_issue_layer(int layer, uint32_t tmem_d, uint3
               id, 1u);
 }
 
-__global__ void __maxnreg__(120)
+__global__ void __maxnreg__(128)
     k_mlp_infer_tc(const bf16 *__restrict__ X, long long n, const bf16 *__restrict__ Wg,
                    const float *__restrict__ P, float *__restrict__ Y, int *err) {
   extern __shared__ __align__(128) unsigned char tc_raw[];
@@ -827,14 +831,16 @@ struct ftgpu_surrogate {
 
 namespace {
 
-int sfail(int code) { return code; }
-
-#define SCK(x)                                        \
-  do {                                                \
-    if ((x) != cudaSuccess) {                         \
-      cudaGetLastError();                             \
-      return sfail(FTGPU_ERR_CUDA);                   \
-    }                                                 \
+// CUDA failures of the surrogate calls: the call and the CUDA error text
+// become ftgpu_last_error()
+#define SCK(x)                                                                      \
+  do {                                                                              \
+    const cudaError_t e_ = (x);                                                     \
+    if (e_ != cudaSuccess) {                                                        \
+      cudaGetLastError();                                                           \
+      return record_error(FTGPU_ERR_CUDA,                                           \
+                          (std::string(#x) + ": " + cudaGetErrorString(e_)).c_str()); \
+    }                                                                               \
   } while (0)
 
 template <class T>
@@ -947,9 +953,13 @@ int surrogate_infer(ftgpu_surrogate *s, const uint16_t *X, long long n, float *Y
   static bool attr_set[64] = {false};
   if (n <= 0) return 0;
   if (s->device >= 0 && s->device < 64 && !attr_set[s->device]) {
-    if (cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)tc::kSmem) != cudaSuccess)
-      return FTGPU_ERR_CUDA;
+    const cudaError_t e = cudaFuncSetAttribute(
+        k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::kSmem);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return record_error(FTGPU_ERR_CUDA, (std::string("tensor-core inference shared memory: ") +
+                                           cudaGetErrorString(e)).c_str());
+    }
     attr_set[s->device] = true;
   }
   int sms = 152;
@@ -959,7 +969,11 @@ int surrogate_infer(ftgpu_surrogate *s, const uint16_t *X, long long n, float *Y
       std::max<long long>(1, std::min<long long>((long long)sms, (tiles + tc::kSlots - 1) / tc::kSlots));
   k_mlp_infer_tc<<<(unsigned)grid, tc::kThreads, tc::kSmem, st>>>(reinterpret_cast<const bf16 *>(X), n,
                                                           s->Wb, s->P, Y, err);
-  return cudaGetLastError() == cudaSuccess ? 0 : FTGPU_ERR_CUDA;
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess)
+    return record_error(FTGPU_ERR_CUDA, (std::string("tensor-core inference launch: ") +
+                                         cudaGetErrorString(e)).c_str());
+  return 0;
 }
 
 // the same on the warp-level mma.sync path (kept as a cross-check)
@@ -1161,7 +1175,7 @@ static int surrogate_infer_host(ftgpu_surrogate *s, long long n, const float *x,
   SCK(cudaStreamSynchronize(s->stream));
   int e = 0;
   SCK(cudaMemcpy(&e, s->derr, sizeof(int), cudaMemcpyDeviceToHost));
-  if (!r && e) r = FTGPU_ERR_CUDA;
+  if (!r && e) r = record_error(FTGPU_ERR_CUDA, "tensor-core inference gave up waiting");
   SCK(cudaMemcpy(y, dY, n * kMlpOut * 4, cudaMemcpyDeviceToHost));
   cudaFree(dX);
   cudaFree(dY);
