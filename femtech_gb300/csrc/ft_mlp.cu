@@ -97,7 +97,23 @@ __device__ inline uint32_t pack2(bf16 lo, bf16 hi) {
   return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
 }
 
-__device__ inline float silu(float z) { return z / (1.f + __expf(-z)); }
+// The activation of every forward path (training, both inference kernels):
+// SiLU on BF16 pairs, h = z / 2 rounded to BF16, then h + h tanh(h) with a
+// BF16-pair tanh and fused multiply-add -- one MUFU operation per two values.
+// The activations are stored in BF16 anyway; training with the same rounding
+// makes the trained network exact for the fast inference arithmetic.
+__device__ __forceinline__ uint32_t silu_h_bf16x2(float h0, float h1) {
+  uint32_t hp, th, out;
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(hp) : "f"(h1), "f"(h0));  // h0 low, h1 high
+  asm("tanh.approx.bf16x2 %0, %1;" : "=r"(th) : "r"(hp));
+  asm("fma.rn.bf16x2 %0, %1, %2, %1;" : "=r"(out) : "r"(hp), "r"(th));
+  return out;
+}
+__device__ __forceinline__ uint32_t silu_bf16x2(float z0, float z1) {
+  return silu_h_bf16x2(0.5f * z0, 0.5f * z1);
+}
+
+// derivative of the exact SiLU at the FP32 pre-activation (backward pass)
 __device__ inline float dsilu(float z) {
   const float s = 1.f / (1.f + __expf(-z));
   return s * (1.f + z * (1.f - s));
@@ -151,6 +167,21 @@ __global__ void __launch_bounds__(128) k_gemm(const GemmArgs g) {
           : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
     }
   }
+  if (EPI == kEpiBiasSilu) {  // column pairs (c, c + 1) -> one BF16 pair (N is even)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int hp = 0; hp < 2; ++hp) {
+        const long long i = m0 + gq + 8 * hp;
+        const int c = n0 + 8 * j + 2 * tq;
+        if (i >= g.M || c >= g.N) continue;
+        const float v0 = acc[j][2 * hp] + g.bias[c], v1 = acc[j][2 * hp + 1] + g.bias[c + 1];
+        g.Z[i * g.N + c] = v0;
+        g.Z[i * g.N + c + 1] = v1;
+        *reinterpret_cast<uint32_t *>(g.H + i * g.N + c) = silu_bf16x2(v0, v1);
+      }
+    return;
+  }
 #pragma unroll
   for (int j = 0; j < 4; ++j)
 #pragma unroll
@@ -163,10 +194,6 @@ __global__ void __launch_bounds__(128) k_gemm(const GemmArgs g) {
         g.C[i * g.scm + (long long)c * g.scn] = v;
       } else if (EPI == kEpiBias) {
         g.C[i * g.scm + (long long)c * g.scn] = v + g.bias[c];
-      } else if (EPI == kEpiBiasSilu) {
-        v += g.bias[c];
-        g.Z[i * g.N + c] = v;
-        g.H[i * g.N + c] = __float2bfloat16_rn(silu(v));
       } else {  // kEpiSiluGrad
         g.dZ[i * g.N + c] = __float2bfloat16_rn(v * dsilu(g.Zp[i * g.N + c]));
       }
@@ -300,10 +327,6 @@ __device__ inline void mma16816(float (&c)[4], const uint32_t (&a)[4], uint32_t 
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-__device__ inline uint32_t pack_f2(float lo, float hi) {
-  return pack2(__float2bfloat16_rn(lo), __float2bfloat16_rn(hi));
-}
-
 // one hidden layer 128 -> 128: a (8 k-chunks) -> bias + SiLU -> next (8 k-chunks)
 __device__ inline void hidden_layer(const uint32_t (&a)[8][4], uint32_t (&nx)[8][4],
                                     const bf16 *W, const float *b, int gq, int tq) {
@@ -321,10 +344,10 @@ __device__ inline void hidden_layer(const uint32_t (&a)[8][4], uint32_t (&nx)[8]
     }
     const float bA0 = b[16 * kc + 2 * tq], bA1 = b[16 * kc + 2 * tq + 1];
     const float bB0 = b[16 * kc + 8 + 2 * tq], bB1 = b[16 * kc + 8 + 2 * tq + 1];
-    nx[kc][0] = pack_f2(silu(c0[0] + bA0), silu(c0[1] + bA1));
-    nx[kc][1] = pack_f2(silu(c0[2] + bA0), silu(c0[3] + bA1));
-    nx[kc][2] = pack_f2(silu(c1[0] + bB0), silu(c1[1] + bB1));
-    nx[kc][3] = pack_f2(silu(c1[2] + bB0), silu(c1[3] + bB1));
+    nx[kc][0] = silu_bf16x2(c0[0] + bA0, c0[1] + bA1);
+    nx[kc][1] = silu_bf16x2(c0[2] + bA0, c0[3] + bA1);
+    nx[kc][2] = silu_bf16x2(c1[0] + bB0, c1[1] + bB1);
+    nx[kc][3] = silu_bf16x2(c1[2] + bB0, c1[3] + bB1);
   }
 }
 
@@ -377,10 +400,10 @@ __global__ void __launch_bounds__(256) k_mlp_infer(const bf16 *__restrict__ X, l
                *reinterpret_cast<const uint32_t *>(w1 + 8));
       const float bA0 = bs[16 * kc + 2 * tq], bA1 = bs[16 * kc + 2 * tq + 1];
       const float bB0 = bs[16 * kc + 8 + 2 * tq], bB1 = bs[16 * kc + 8 + 2 * tq + 1];
-      h[kc][0] = pack_f2(silu(c0[0] + bA0), silu(c0[1] + bA1));
-      h[kc][1] = pack_f2(silu(c0[2] + bA0), silu(c0[3] + bA1));
-      h[kc][2] = pack_f2(silu(c1[0] + bB0), silu(c1[1] + bB1));
-      h[kc][3] = pack_f2(silu(c1[2] + bB0), silu(c1[3] + bB1));
+      h[kc][0] = silu_bf16x2(c0[0] + bA0, c0[1] + bA1);
+      h[kc][1] = silu_bf16x2(c0[2] + bA0, c0[3] + bA1);
+      h[kc][2] = silu_bf16x2(c1[0] + bB0, c1[1] + bB1);
+      h[kc][3] = silu_bf16x2(c1[2] + bB0, c1[3] + bB1);
     }
     hidden_layer(h, g, W1, bs + kMlpHid, gq, tq);
     hidden_layer(g, h, W2, bs + 2 * kMlpHid, gq, tq);
@@ -420,7 +443,8 @@ __global__ void __launch_bounds__(256) k_mlp_infer(const bf16 *__restrict__ X, l
 // the next layer's A operand.  While one slot runs its epilogue the tensor
 // core serves the others.  W0..W2 and b0..b2 are staged times 1/2 (exact), so
 // an accumulator holds h = z / 2 and SiLU(z) = z sigmoid(z) = h + h tanh(h)
-// costs one MUFU tanh and one FMA.  Every wait is bounded; a wait that gives
+// is evaluated on BF16 pairs: one MUFU tanh and one FMA per two values.
+// Every wait is bounded; a wait that gives
 // up raises a shared abort flag that ends all roles, and the error word.
 //
 // Shared-memory operand images are K-major without swizzle: 8-row x 16-byte
@@ -580,13 +604,6 @@ __device__ __forceinline__ void tmem_st_wait() {
   asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
 
-// SiLU(z) for h = z / 2: z sigmoid(z) = h + h tanh(h), one MUFU operation
-__device__ __forceinline__ float silu_half(float h) {
-  float th;
-  asm("tanh.approx.f32 %0, %1;" : "=f"(th) : "f"(h));
-  return fmaf(h, th, h);
-}
-
 // rows [0, rows) x K columns of a row-major BF16 matrix (times `scale`, a
 // power of two) into the K-major core-matrix image, rows up to rows_pad zero;
 // consecutive threads write consecutive 16-byte chunks of the image
@@ -615,7 +632,7 @@ __device__ __forceinline__ void tc_silu_chunk(uint32_t taddr, unsigned char *hs,
   tmem_ld32(taddr, v);
   uint32_t pk[16];
 #pragma unroll
-  for (int j = 0; j < 16; ++j) pk[j] = pack_f2(silu_half(v[2 * j]), silu_half(v[2 * j + 1]));
+  for (int j = 0; j < 16; ++j) pk[j] = silu_h_bf16x2(v[2 * j], v[2 * j + 1]);
   unsigned char *dst = hs + (r / 8) * 2048 + (r % 8) * 16 + (c0 / 8) * 128;
 #pragma unroll
   for (int i = 0; i < 4; ++i)

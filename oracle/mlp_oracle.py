@@ -5,7 +5,12 @@ Same network as femtech_gb300/csrc/ft_mlp.cu: 16 -> 128 -> 128 -> 128 -> 8,
 SiLU, parameter vector layout W0[128][16] b0 W1[128][128] b1 W2[128][128] b2
 W3[8][128] b3; loss = mean over (rows, 6 used outputs) of the squared error.
 ``quantize=True`` rounds inputs, weights and hidden activations to BF16 the
-way the GPU stores them, so the comparison isolates accumulation error.
+way the GPU stores them, so the comparison isolates accumulation error.  The
+GPU evaluates the activation on BF16 pairs, SiLU(z) = h + h tanh(h) with
+h = z / 2 rounded to BF16, tanh rounded to BF16 and the fused multiply-add
+rounded once; ``quantize=True`` follows those roundings (with an exact tanh,
+so hardware tanh approximation remains a small difference).  The backward
+pass uses the exact SiLU derivative of the FP32 pre-activation, as the GPU.
 """
 import numpy as np
 
@@ -45,16 +50,23 @@ def dsilu(z):
     return s * (1.0 + z * (1.0 - s))
 
 
+def silu_bf16(z):
+    """The GPU's activation: h = bf16(z / 2), bf16(h + h * bf16(tanh(h)))."""
+    h = bf16(0.5 * np.asarray(z, np.float64))
+    return bf16(h + h * bf16(np.tanh(h)))
+
+
 def forward(p, x, quantize=True):
     q = bf16 if quantize else (lambda a: np.asarray(a, np.float64))
+    act = silu_bf16 if quantize else silu
     w = unpack(p)
     x = q(x)
     z1 = x @ q(w["W0"]).T + w["b0"]
-    h1 = q(silu(z1))
+    h1 = act(z1)
     z2 = h1 @ q(w["W1"]).T + w["b1"]
-    h2 = q(silu(z2))
+    h2 = act(z2)
     z3 = h2 @ q(w["W2"]).T + w["b2"]
-    h3 = q(silu(z3))
+    h3 = act(z3)
     y = h3 @ q(w["W3"]).T + w["b3"]
     return y, (x, z1, h1, z2, h2, z3, h3)
 
