@@ -366,29 +366,46 @@ __device__ __forceinline__ Sym6<R> mat_ogden(const MatP<R> &m, const R (&D)[3][3
     //         = c [A - Ci - tr(B)/3 (I + Ci)],
     // A = (I+M)^{alpha/2-1} - I, B = (I+M)^{alpha/2} - I, Ci = (I+M)^{-1} - I,
     // each a binomial series in powers of M (exact to FP32 rounding while
-    // |M|_F < 0.04, no eigenvectors, no cancellation of O(1) terms).
-    Sym6<R> P = e;
-    Sym6<R> A = sym_scale(e, m.ser_a[0]);
-    Sym6<R> Ci = sym_scale(e, R(-1));
-    R trB = m.ser_b[0] * (e.xx + e.yy + e.zz);
+    // |M|_F < 0.04, no eigenvectors, no cancellation of O(1) terms).  By
+    // Cayley-Hamilton every power is M^p = a I + b M + c M^2 with
+    //   M^{p+1}: (a, b, c) <- (c I3, a - c I2, b + c I1),
+    // so the three series reduce to scalar coefficients of I, M and M^2.
+    const Sym6<R> M2 = sym_mul(e, e);
+    const R I1 = e.xx + e.yy + e.zz;
+    const R trM2 = M2.xx + M2.yy + M2.zz;
+    const R I2 = R(0.5) * (I1 * I1 - trM2);
+    const R I3 = e.xx * (e.yy * e.zz - e.yz * e.yz) - e.xy * (e.xy * e.zz - e.yz * e.xz) +
+                 e.xz * (e.xy * e.yz - e.yy * e.xz);
+    // power 1: (0, 1, 0)
+    R pa = 0, pb = 1, pc = 0;
+    R Aa = 0, Ab = m.ser_a[0], Ag = 0;  // A  = Aa I + Ab M + Ag M^2
+    R Ca = 0, Cb = -1, Cg = 0;          // Ci = Ca I + Cb M + Cg M^2
+    R trB = m.ser_b[0] * I1;
 #pragma unroll
     for (int k = 1; k < kOgdenSeries; ++k) {
-      P = sym_mul(P, e);
+      const R na = pc * I3, nb = pa - pc * I2, nc = pb + pc * I1;
+      pa = na;
+      pb = nb;
+      pc = nc;
       const R sa = m.ser_a[k], sc = (k & 1) ? R(1) : R(-1);
-      A = Sym6<R>{A.xx + sa * P.xx, A.yy + sa * P.yy, A.zz + sa * P.zz, A.yz + sa * P.yz,
-                  A.xz + sa * P.xz, A.xy + sa * P.xy};
-      Ci = Sym6<R>{Ci.xx + sc * P.xx, Ci.yy + sc * P.yy, Ci.zz + sc * P.zz, Ci.yz + sc * P.yz,
-                   Ci.xz + sc * P.xz, Ci.xy + sc * P.xy};
-      trB += m.ser_b[k] * (P.xx + P.yy + P.zz);
+      Aa += sa * pa;
+      Ab += sa * pb;
+      Ag += sa * pc;
+      Ca += sc * pa;
+      Cb += sc * pb;
+      Cg += sc * pc;
+      trB += m.ser_b[k] * (R(3) * pa + pb * I1 + pc * trM2);
     }
     const R c = 2 * mu / alpha * d_exp(-alpha * R(1.0 / 3.0) * lnJ);
     const R t = trB * R(1.0 / 3.0);
-    S.xx = c * (A.xx - Ci.xx - t * (1 + Ci.xx));
-    S.yy = c * (A.yy - Ci.yy - t * (1 + Ci.yy));
-    S.zz = c * (A.zz - Ci.zz - t * (1 + Ci.zz));
-    S.yz = c * (A.yz - Ci.yz - t * Ci.yz);
-    S.xz = c * (A.xz - Ci.xz - t * Ci.xz);
-    S.xy = c * (A.xy - Ci.xy - t * Ci.xy);
+    const R ka = c * (Aa - Ca - t * (1 + Ca)), kb = c * (Ab - Cb - t * Cb),
+            kg = c * (Ag - Cg - t * Cg);
+    S.xx = ka + kb * e.xx + kg * M2.xx;
+    S.yy = ka + kb * e.yy + kg * M2.yy;
+    S.zz = ka + kb * e.zz + kg * M2.zz;
+    S.yz = kb * e.yz + kg * M2.yz;
+    S.xz = kb * e.xz + kg * M2.xz;
+    S.xy = kb * e.xy + kg * M2.xy;
   } else {
     R w[3], V[3][3];
     jacobi_sym3<R, sizeof(R) == 4 ? 4 : 6>(e, w, V);
