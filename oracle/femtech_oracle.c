@@ -777,6 +777,15 @@ int or_explicit_run(or_model *m, const int *dof_fn, const or_bc_fn *fns, int nfn
   int *boundary = (int *)calloc(nDOF, sizeof(int));
   double *fi = (double *)calloc(nDOF, sizeof(double));
   double *vh = (double *)calloc(nDOF, sizeof(double));
+  /* energy balance (CheckEnergy.cpp:3-85): previous displacements,
+   * accelerations and internal forces; no external forces on this path */
+  double *u_prev = NULL, *a_prev = NULL, *fi_prev = NULL;
+  double Wint = 0.0, Wext = 0.0;
+  if (m->energy) {
+    u_prev = (double *)calloc(nDOF, sizeof(double));
+    a_prev = (double *)calloc(nDOF, sizeof(double));
+    fi_prev = (double *)calloc(nDOF, sizeof(double));
+  }
   for (int i = 0; i < nDOF; ++i) boundary[i] = dof_fn[i] != OR_BC_FREE;
   double Time = t0;
   *n_out = 0;
@@ -795,6 +804,11 @@ int or_explicit_run(or_model *m, const int *dof_fn, const or_bc_fn *fns, int nfn
     double dt_nphalf = dt, t_nphalf = 0.5 * (t_np1 + t_n);
     for (int i = 0; i < nDOF; ++i)
       vh[i] = boundary[i] ? v[i] : v[i] + (t_nphalf - t_n) * a[i];
+    if (m->energy) { /* ex9.cpp:124-129 */
+      memcpy(u_prev, u, nDOF * sizeof(double));
+      memcpy(a_prev, a, nDOF * sizeof(double));
+      memcpy(fi_prev, fi, nDOF * sizeof(double));
+    }
     for (int i = 0; i < nDOF; ++i)
       if (!boundary[i]) u[i] = u[i] + dt_nphalf * vh[i];
     or_apply_bc(m, dof_fn, fns, Time, u, v, a);
@@ -803,6 +817,26 @@ int or_explicit_run(or_model *m, const int *dof_fn, const or_bc_fn *fns, int nfn
       if (!boundary[i]) a[i] = -fi[i] / m->mass[i];
     for (int i = 0; i < nDOF; ++i)
       if (!boundary[i]) v[i] = vh[i] + (t_np1 - t_nphalf) * a[i];
+    if (m->energy && step < m->energy_cap) {
+      /* CheckEnergy.cpp:18-55 on one rank: kinetic energy, internal work
+       * increment (equ 6.2.14) and the work of the reactions of constrained
+       * DOFs (fe = 0) */
+      double wke = 0.0, dwi = 0.0, dwe = 0.0;
+      for (int i = 0; i < nDOF; ++i) {
+        double dd = u[i] - u_prev[i];
+        wke += m->mass[i] * v[i] * v[i];
+        if (boundary[i]) {
+          double reaction = fi_prev[i] + fi[i] + m->mass[i] * (a[i] + a_prev[i]);
+          dwe += dd * reaction;
+        }
+        dwi += dd * (fi_prev[i] + fi[i]);
+      }
+      Wint += 0.5 * dwi;
+      Wext += 0.5 * dwe;
+      m->energy[3 * step + 0] = Wint;
+      m->energy[3 * step + 1] = Wext;
+      m->energy[3 * step + 2] = 0.5 * wke;
+    }
     ++step;
     if (out_every > 0 && step % out_every == 0 && *n_out < max_out) {
       memcpy(u_out + (size_t)(*n_out) * nDOF, u, nDOF * sizeof(double));
@@ -820,5 +854,8 @@ done:
   free(boundary);
   free(fi);
   free(vh);
+  free(u_prev);
+  free(a_prev);
+  free(fi_prev);
   return rc;
 }

@@ -63,6 +63,11 @@ typedef struct or_model {
   double *fe;   /* scratch: 24 doubles per element                   */
   double *ce;   /* dilatational wave speed per part                  */
   int nthreads;
+  /* optional output of or_explicit_run: per step the cumulative internal
+   * work, external work and the kinetic energy of CheckEnergy
+   * (src/fem/SolidMechanics/CheckEnergy.cpp:3-85); NULL = not computed */
+  double *energy;
+  int energy_cap; /* steps the energy buffer holds (3 doubles each)    */
 } or_model;
 
 int or_setup(or_model *m);

@@ -44,6 +44,7 @@ class _Model(C.Structure):
         ("F", C.c_void_p), ("detF", C.c_void_p), ("pk2", C.c_void_p),
         ("hist", C.c_void_p), ("mass", C.c_void_p), ("fe", C.c_void_p), ("ce", C.c_void_p),
         ("nthreads", C.c_int),
+        ("energy", C.c_void_p), ("energy_cap", C.c_int),
     ]
 
 
@@ -168,8 +169,13 @@ class Oracle:
                                               np.ascontiguousarray(boundary, np.int32).ravel())
 
     def explicit_run(self, dof_fn, fns, tmax, reduction, max_steps, out_every, t0=0.0,
-                     failure_dt=0.0, u=None, v=None, a=None, max_out=None):
+                     failure_dt=0.0, u=None, v=None, a=None, max_out=None, energy=False):
+        """The ex9 loop; energy=True adds per step (Wint, Wext, WKE) of
+        CheckEnergy (cumulative works, kinetic energy) as result['energy']."""
         n = 3 * self.nNodes
+        ebuf = np.zeros(3 * max(max_steps, 1)) if energy else None
+        self.m.energy = None if ebuf is None else ebuf.ctypes.data
+        self.m.energy_cap = max_steps if energy else 0
         u = np.zeros(n) if u is None else np.array(u, np.float64).ravel()
         v = np.zeros(n) if v is None else np.array(v, np.float64).ravel()
         a = np.zeros(n) if a is None else np.array(a, np.float64).ravel()
@@ -184,9 +190,14 @@ class Oracle:
             C.byref(self.m), np.ascontiguousarray(dof_fn, np.int32).ravel(), C.cast(tab, C.c_void_p),
             len(fns), t0, tmax, reduction, failure_dt, max_steps, out_every, u, v, a, uo, to,
             max_out, C.byref(nout), C.byref(steps), C.byref(tt), C.byref(dd))
+        self.m.energy = None
+        self.m.energy_cap = 0
         k = nout.value
-        return dict(rc=rc, u=u, v=v, a=a, u_out=uo[: k * n].reshape(k, n), t_out=to[:k],
-                    steps=steps.value, time=tt.value, dt=dd.value)
+        res = dict(rc=rc, u=u, v=v, a=a, u_out=uo[: k * n].reshape(k, n), t_out=to[:k],
+                   steps=steps.value, time=tt.value, dt=dd.value)
+        if energy:
+            res["energy"] = ebuf.reshape(-1, 3)[: steps.value].copy()
+        return res
 
 
 def material_stress(mat, props, F, J=None, a0=None, dt=0.0, hist=None):
@@ -231,6 +242,7 @@ class RefBuild:
             L.ref_get_force.argtypes = [_dp, C.c_double, _dp, _dp]
             L.ref_stable_time_step.argtypes = [_dp, _ip]
             L.ref_stable_time_step.restype = C.c_double
+            L.ref_set_energy_out.argtypes = [C.c_void_p, C.c_int]
             L.ref_explicit_run.argtypes = [_ip, C.c_void_p, C.c_int, C.c_double, C.c_double,
                                            C.c_double, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp,
                                            C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
@@ -281,9 +293,14 @@ class RefBuild:
                                                np.ascontiguousarray(boundary, np.int32).ravel())
 
     def explicit_run(self, dof_fn, fns, tmax, reduction, max_steps, out_every, t0=0.0,
-                     max_out=None):
+                     max_out=None, energy=False):
+        """energy=True: per step (Wint, Wext, WKE) as the reference's CheckEnergy
+        logs them (works accumulate over the process: one energy run per process)."""
         n = 3 * self.nNodes
         u, v, a = np.zeros(n), np.zeros(n), np.zeros(n)
+        ebuf = np.zeros(3 * max(max_steps, 1)) if energy else None
+        self.lib().ref_set_energy_out(None if ebuf is None else ebuf.ctypes.data,
+                                      max_steps if energy else 0)
         if max_out is None:
             max_out = max(1, max_steps // max(out_every, 1) + 1)
         uo, to = np.zeros(max_out * n), np.zeros(max_out)
@@ -294,6 +311,10 @@ class RefBuild:
                                          C.cast(tab, C.c_void_p), len(fns), t0, tmax, reduction,
                                          max_steps, out_every, u, v, a, uo, to, max_out,
                                          C.byref(nout), C.byref(steps), C.byref(tt), C.byref(dd))
+        self.lib().ref_set_energy_out(None, 0)
         k = nout.value
-        return dict(rc=rc, u=u, v=v, a=a, u_out=uo[: k * n].reshape(k, n), t_out=to[:k],
-                    steps=steps.value, time=tt.value, dt=dd.value)
+        res = dict(rc=rc, u=u, v=v, a=a, u_out=uo[: k * n].reshape(k, n), t_out=to[:k],
+                   steps=steps.value, time=tt.value, dt=dd.value)
+        if energy:
+            res["energy"] = ebuf.reshape(-1, 3)[: steps.value].copy()
+        return res

@@ -100,7 +100,21 @@ extern "C" void dgetrf_(int *, int *, double *, int *, int *, int *info) { *info
 extern "C" void dgetrs_(char *, int *, int *, double *, int *, int *, double *, int *, int *info) { *info = -1; }
 
 /* ---------------- logging: errors and warnings to stderr ---------------- */
+/* CheckEnergy (src/fem/SolidMechanics/CheckEnergy.cpp:60-63) keeps its
+ * running works in function statics and only logs them; while an energy
+ * buffer is set, the logged values (the first double argument) are taken
+ * from the log calls, and its violation warnings are not printed. */
+static double *g_energy = nullptr;
+static int g_energy_cap = 0;
+static double g_wint = 0.0, g_wext = 0.0, g_wke = 0.0;
 static void vlog(enum logLevel level, const char *fmt, va_list ap) {
+  if (g_energy) {
+    if (strncmp(fmt, "Internal Work", 13) == 0) { g_wint = va_arg(ap, double); return; }
+    if (strncmp(fmt, "External Work", 13) == 0) { g_wext = va_arg(ap, double); return; }
+    if (strncmp(fmt, "Kinetic Energy", 14) == 0) { g_wke = va_arg(ap, double); return; }
+    if (strncmp(fmt, "Total Energy", 12) == 0 || strncmp(fmt, "Energy Violation", 16) == 0)
+      return;
+  }
   if (level > WARNING) return;
   vfprintf(stderr, fmt, ap);
   fputc('\n', stderr);
@@ -284,6 +298,16 @@ double ref_stable_time_step(const double *u, const int *bnd) {
 
 /* The explicit loop of examples/ex9/ex9.cpp:79-175 with driver-side
  * boundary conditions given as per-DOF function indices (see or_apply_bc). */
+/* Energy output of the next ref_explicit_run: per step the cumulative internal
+ * and external work and the kinetic energy that the reference's own
+ * CheckEnergy() logs (ex9.cpp:154-156 calls it after every step).  Its works
+ * accumulate in statics over the life of the process, so one energy run per
+ * process gives works from zero. */
+void ref_set_energy_out(double *buf, int cap) {
+  g_energy = buf;
+  g_energy_cap = cap;
+}
+
 int ref_explicit_run(const int *dof_fn, const or_bc_fn *fns, int nfn, double t0, double tMax,
                      double reduction, int max_steps, int out_every, double *uInOut,
                      double *vInOut, double *aInOut, double *u_out, double *t_out, int max_out,
@@ -319,6 +343,12 @@ int ref_explicit_run(const int *dof_fn, const or_bc_fn *fns, int nfn, double t0,
         else
           velocities_half[i] = velocities[i] + (t_nphalf - t_n) * accelerations[i];
       }
+      if (g_energy) {  // ex9.cpp:124-129
+        memcpy(displacements_prev, displacements, nDOF * sizeof(double));
+        memcpy(accelerations_prev, accelerations, nDOF * sizeof(double));
+        memcpy(fi_prev, fi, nDOF * sizeof(double));
+        memcpy(fe_prev, fe, nDOF * sizeof(double));
+      }
       for (int i = 0; i < nDOF; i++)
         if (!boundary[i]) displacements[i] = displacements[i] + dt_nphalf * velocities_half[i];
       or_apply_bc(&bcm, dof_fn, fns, Time, displacements, velocities, accelerations);
@@ -326,6 +356,12 @@ int ref_explicit_run(const int *dof_fn, const or_bc_fn *fns, int nfn, double t0,
       CalculateAccelerations();
       for (int i = 0; i < nDOF; i++)
         if (!boundary[i]) velocities[i] = velocities_half[i] + (t_np1 - t_nphalf) * accelerations[i];
+      if (g_energy && step < g_energy_cap) {
+        CheckEnergy(Time, 1);  // writeFlag != 0: log only (ex9.cpp:154-156)
+        g_energy[3 * step + 0] = g_wint;
+        g_energy[3 * step + 1] = g_wext;
+        g_energy[3 * step + 2] = g_wke;
+      }
       ++step;
       if (out_every > 0 && step % out_every == 0 && *n_out < max_out) {
         memcpy(u_out + (size_t)(*n_out) * nDOF, displacements, sizeof(double) * nDOF);

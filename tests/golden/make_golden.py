@@ -17,7 +17,10 @@ Fixtures:
   ref_cube.npz    the CPU-runnable configuration: 10x10x10 C3D8 cube 0.01 m,
                   Neo-Hookean rho 1000, mu 3.4 kPa, K 2 MPa, z=0 fixed, top
                   face ramped to 10 % strain over 10 ms, 0.9 dt factor, all
-                  displacements every 100 steps.
+                  displacements every 100 steps, and per step the internal
+                  work, external work and kinetic energy of the reference's
+                  CheckEnergy (the only energy run of the process, so its
+                  works start from zero).
 """
 import os
 import sys
@@ -129,9 +132,9 @@ def cube_case():
     mesh, mats, loads = mg.cube_tension_case(n=10)
     r = orc.RefBuild(mesh, mats)
     res = r.explicit_run(loads.dof_fn, loads.fns, tmax=0.01, reduction=0.9, max_steps=100000,
-                         out_every=100)
+                         out_every=100, energy=True)
     return dict(u_out=res["u_out"], t_out=res["t_out"], steps=res["steps"], time=res["time"],
-                u=res["u"], v=res["v"], a=res["a"])
+                u=res["u"], v=res["v"], a=res["a"], energy=res["energy"])
 
 
 def main():

@@ -47,7 +47,10 @@ def test_cube_tension_matches_reference(oracle_lib, golden):
     mesh, mats, loads = mg.cube_tension_case(n=10)
     o = oracle_lib.Oracle(mesh, mats, threads=4)
     res = o.explicit_run(loads.dof_fn, loads.fns, tmax=0.01, reduction=0.9, max_steps=100000,
-                         out_every=100)
+                         out_every=100, energy=True)
     assert res["steps"] == int(g["steps"])
     np.testing.assert_allclose(res["t_out"], g["t_out"], rtol=1e-14)
     assert rel(res["u_out"], g["u_out"]) < 1e-12
+    # CheckEnergy every step: internal work, external work, kinetic energy
+    assert res["energy"].shape == g["energy"].shape
+    assert rel(res["energy"], g["energy"]) < 1e-12
