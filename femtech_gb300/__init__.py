@@ -78,6 +78,7 @@ def lib():
     L.ftgpu_get_instance_clock.argtypes = [vp, vp, vp, vp, vp]
     L.ftgpu_launches_per_step.argtypes = [vp]
     L.ftgpu_check.argtypes = [vp]
+    L.ftgpu_set_energy.argtypes = [vp, C.c_int]
     _lib = L
     return L
 
@@ -225,6 +226,22 @@ class Model:
         self._surrogate = surrogate
         _check(L.ftgpu_set_surrogate(self.h, None if surrogate is None else surrogate.h,
                                      float(trust_e2)))
+
+    def set_energy(self, enable=True):
+        """Track CheckEnergy's balance in the device loop (call before init_explicit)."""
+        _check(lib().ftgpu_set_energy(self.h, int(bool(enable))))
+
+    def energy(self):
+        """Cumulative internal / external work, kinetic energy, worst balance ratio, violations."""
+        L = lib()
+        L.ftgpu_get_energy.argtypes = [C.c_void_p] + [C.POINTER(C.c_double)] * 4 + [
+            C.POINTER(C.c_longlong)]
+        wi, we, ke, mx = C.c_double(), C.c_double(), C.c_double(), C.c_double()
+        nv = C.c_longlong()
+        _check(L.ftgpu_get_energy(self.h, C.byref(wi), C.byref(we), C.byref(ke), C.byref(mx),
+                                  C.byref(nv)))
+        return dict(internal_work=wi.value, external_work=we.value, kinetic=ke.value,
+                    max_violation=mx.value, violations=nv.value)
 
     def launches_per_step(self):
         return lib().ftgpu_launches_per_step(self.h)

@@ -210,6 +210,9 @@ struct ftgpu_model {
   std::vector<std::unique_ptr<DBuf>> hist;
   DBuf clock, dtmin, err, instp;
   DBuf stepsc, rottrig;  // per-instance step scalars / rotation trigonometry
+  // energy balance of the explicit loop (CheckEnergy), single instance only
+  bool energy_on = false;
+  DBuf du, fprev, epart, estate;
   DBuf slot_off, slots, node_inst, nbc, fnsbuf;
   DBuf dX, u, v, a, vh, mass, minv, fi;
   DBuf gpF, gpJ, gpS;
@@ -330,6 +333,12 @@ NodeArgs node_args(ftgpu_model *m, int mode, int parity) {
     if (m->fns[i].kind == kBckRot) A.rot_ids[A.nrot++] = (int)i;
   A.stepsc = m->stepsc.as<StepScalars>();
   A.rottrig = m->rottrig.as<double>();
+  if (m->energy_on) {
+    A.du = m->du.as<double>();
+    A.fprev = m->fprev.as<double>();
+    A.epart = m->epart.as<double>();
+    A.energy = m->estate.as<EnergyState>();
+  }
   return A;
 }
 
@@ -339,17 +348,23 @@ int launch_node(ftgpu_model *m, int mode, int parity) {
   const long long nb = (m->nNodes + th - 1) / th;
   const bool step = mode == kNodeFused || mode == kNodeFinish;
   if (step) k_step_scalars<<<(unsigned)((m->ninst + 127) / 128), 128, 0, m->stream>>>(A);
+  const bool en = step && m->energy_on;
   if (is_fp64(m)) {
-    if (step)
-      k_node_step<double><<<(unsigned)nb, th, 0, m->stream>>>(A);
+    if (en)
+      k_node_step<double, true><<<(unsigned)nb, th, 0, m->stream>>>(A);
+    else if (step)
+      k_node_step<double, false><<<(unsigned)nb, th, 0, m->stream>>>(A);
     else
       k_node<double><<<(unsigned)nb, th, 0, m->stream>>>(A);
   } else {
-    if (step)
-      k_node_step<float><<<(unsigned)nb, th, 0, m->stream>>>(A);
+    if (en)
+      k_node_step<float, true><<<(unsigned)nb, th, 0, m->stream>>>(A);
+    else if (step)
+      k_node_step<float, false><<<(unsigned)nb, th, 0, m->stream>>>(A);
     else
       k_node<float><<<(unsigned)nb, th, 0, m->stream>>>(A);
   }
+  if (en) k_energy_reduce<<<1, 1024, 0, m->stream>>>(A, (int)nb);
   return (int)cudaGetLastError();
 }
 
@@ -1092,6 +1107,10 @@ int ftgpu_init_explicit(ftgpu_model *m, double reduction, double failure_dt, dou
       m->ninst, m->t0);
   CK(cudaGetLastError());
   CKI(launch_groups(m, 0, 1, 0.0, 0, 0));
+  if (m->energy_on) {  // CheckEnergy's works start from zero with the loop
+    CK(cudaMemsetAsync(m->du.p, 0, 3 * (size_t)m->nNodes * sizeof(double), m->stream));
+    CK(cudaMemsetAsync(m->estate.p, 0, sizeof(EnergyState), m->stream));
+  }
   CKI(launch_node(m, kNodeInit, 0));
   CKI(check_err(m));
   CK(cudaMemcpyAsync(m->h_clock, m->clock.p, sizeof(Clock) * m->ninst, cudaMemcpyDeviceToHost,
@@ -1160,7 +1179,45 @@ int ftgpu_launches_per_step(ftgpu_model *m) {
   // feature pass and the inference kernel of each material-7 group
   if (m->surr)
     for (auto &x : m->ps.groups) g += 2 * (x.npatch > 0 && x.mat == 7);
-  return g + 2;
+  return g + 2 + (m->energy_on ? 1 : 0);  // + k_energy_reduce
+}
+
+int ftgpu_set_energy(ftgpu_model *m, int enable) {
+  if (!m || !m->setup_done) return fail(FTGPU_ERR_STATE, "set_energy before setup");
+  if (enable && m->ninst != 1)
+    return fail(FTGPU_ERR_INPUT, "energy balance is kept for single-instance models");
+  CK(cudaSetDevice(m->device));
+  CK(cudaStreamSynchronize(m->stream));
+  if (enable && !m->energy_on) {
+    const size_t n3 = 3 * (size_t)m->nNodes;
+    const size_t maxblocks = ((size_t)m->nNodes + 63) / 64;  // smallest node block: 64
+    CKI(m->du.alloc(n3 * sizeof(double)));
+    CKI(m->fprev.alloc(n3 * sizeof(double)));
+    CKI(m->epart.alloc(3 * maxblocks * sizeof(double)));
+    CKI(m->estate.alloc(sizeof(EnergyState)));
+    CK(cudaMemset(m->du.p, 0, n3 * sizeof(double)));
+    CK(cudaMemset(m->fprev.p, 0, n3 * sizeof(double)));
+    CK(cudaMemset(m->estate.p, 0, sizeof(EnergyState)));
+  }
+  m->energy_on = enable != 0;
+  drop_graphs(m);
+  m->init_done = false;  // the loop must start again from init_explicit
+  return FTGPU_OK;
+}
+
+int ftgpu_get_energy(ftgpu_model *m, double *internal_work, double *external_work,
+                     double *kinetic_energy, double *max_violation, long long *violations) {
+  if (!m || !m->energy_on) return fail(FTGPU_ERR_STATE, "energy balance is off");
+  CK(cudaSetDevice(m->device));
+  EnergyState e;
+  CK(cudaMemcpyAsync(&e, m->estate.p, sizeof(e), cudaMemcpyDeviceToHost, m->stream));
+  CK(cudaStreamSynchronize(m->stream));
+  if (internal_work) *internal_work = e.Wint;
+  if (external_work) *external_work = e.Wext;
+  if (kinetic_energy) *kinetic_energy = e.WKE;
+  if (max_violation) *max_violation = e.max_ratio;
+  if (violations) *violations = e.violations;
+  return FTGPU_OK;
 }
 
 int ftgpu_check(ftgpu_model *m) {

@@ -93,6 +93,16 @@ struct ElemArgs {
 
 enum { kPassForce = 0, kPassDt = 1, kPassSurrogateFeatures = 2 };
 
+// Energy balance of the explicit loop (CheckEnergy.cpp:3-85): cumulative
+// internal and external work, kinetic energy of the last step, the balance
+// |WKE + Wint - Wext| and its worst ratio to max(|Wint|, |Wext|, |WKE|), and
+// the steps whose balance exceeded 1 % of that maximum (the reference's
+// "Energy Violation" warning).
+struct EnergyState {
+  double Wint, Wext, WKE, total, max_ratio;
+  long long steps, violations;
+};
+
 // Per-instance scalars of one end-of-step launch (k_step_scalars)
 struct StepScalars {
   double t_np1, t_np2, ndt;
@@ -129,6 +139,11 @@ struct NodeArgs {
   int rot_ids[kMaxRotFns];    // their indices in fns
   StepScalars *stepsc;        // [ninst] written by k_step_scalars
   double *rottrig;            // [ninst][kMaxRotFns][3] cos, sin, omega at t_{n+2}
+  // energy balance (single instance; null when off)
+  double *du;                 // [3][N] u_{n+1} - u_n of the step being finished
+  double *fprev;              // [3][N] internal force of the previous step
+  double *epart;              // [node blocks][3] partial sums: kinetic, internal, external
+  EnergyState *energy;
 };
 
 enum { kNodeBegin = 0, kNodeFused = 1, kNodeFinish = 2, kNodeInit = 3, kNodeGather = 4,

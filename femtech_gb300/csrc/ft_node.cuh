@@ -144,7 +144,8 @@ __global__ void __launch_bounds__(512) k_node(const NodeArgs A) {
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       const int fn = A.nbc[d * N + n];
-      double u = A.u[d * N + n];
+      const double uold = A.u[d * N + n];
+      double u = uold;
       if (fn == kBcFree) {
         const double vh = A.v[d * N + n] + (t_half - t_n) * A.a[d * N + n];
         u = u + dt * vh;
@@ -157,6 +158,7 @@ __global__ void __launch_bounds__(512) k_node(const NodeArgs A) {
         A.v[d * N + n] = vb;
         A.a[d * N + n] = 0.0;
       }
+      if (A.du) A.du[d * N + n] = u - uold;  // energy balance: this step's increment
       un[d] = u;
     }
     for (int k = sb; k < se; ++k) {
@@ -170,6 +172,11 @@ __global__ void __launch_bounds__(512) k_node(const NodeArgs A) {
     // accelerations after the pre-loop GetForce (ex9.cpp:90-93)
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
+      if (A.fprev) {  // energy balance: f of the pre-loop state, summed as k_node_step does
+        R fr = 0;
+        for (int k = sb; k < se; ++k) fr += sF[d * S + A.slots[k]];
+        A.fprev[d * N + n] = double(fr);
+      }
       if (A.nbc[d * N + n] != kBcFree) continue;
       double f = 0.0;
       for (int k = sb; k < se; ++k) f += double(sF[d * S + A.slots[k]]);
@@ -203,10 +210,13 @@ __global__ void k_step_scalars(const NodeArgs A) {
 // End of step n (mode kNodeFused also starts step n+1; kNodeFinish stops
 // there), with the step scalars k_step_scalars left for the node's instance.
 // At most 64 registers: the kernel waits on memory, so resident warps matter.
-template <class R>
-__global__ void __launch_bounds__(512, 2) k_node_step(const NodeArgs A) {
-  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= A.N) return;
+// One node of k_node_step.  EN: also this node's share of the energy balance
+// (CheckEnergy.cpp:18-55 with fe = 0): kinetic energy m v_{n+1}^2, internal
+// work du (f_prev + f) and, for constrained DOFs, the work of the reaction
+// du (f_prev + f + m (a + a_prev)) with a = a_prev = 0 on constrained DOFs.
+template <class R, bool EN>
+__device__ __forceinline__ void node_step(const NodeArgs &A, long long n, double &eke,
+                                          double &ewi, double &ewe) {
   const long long N = A.N, S = A.S;
   const R *sF = reinterpret_cast<const R *>(A.sF);
   R *sU = reinterpret_cast<R *>(A.sU);
@@ -222,6 +232,15 @@ __global__ void __launch_bounds__(512, 2) k_node_step(const NodeArgs A) {
   }
   // 1/m (mixed mode; FP64 mode divides by m as the reference does)
   const double minv = sizeof(R) == 8 ? 0.0 : A.minv[n];
+  double du0[3] = {0.0, 0.0, 0.0}, fp0[3] = {0.0, 0.0, 0.0}, vb0[3] = {0.0, 0.0, 0.0};
+  if (EN) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      du0[d] = A.du[d * N + n];
+      fp0[d] = A.fprev[d * N + n];
+      vb0[d] = A.v[d * N + n];  // velocity of a constrained DOF at t_{n+1}
+    }
+  }
   // sum of the patch partials in slot order (in the element precision)
   R fs0 = 0, fs1 = 0, fs2 = 0;
   for (int k = sb; k < se; ++k) {
@@ -271,10 +290,24 @@ __global__ void __launch_bounds__(512, 2) k_node_step(const NodeArgs A) {
       rot_apply(b, c, s, om, A.X, N, n, ur, vr);
     }
   }
+  const double mass = EN ? A.mass[n] : 0.0;
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const int fn = nbc[d];
     double u = u0[d];
+    if (EN) {
+      const double fi = fsum[d], w = du0[d] * (fp0[d] + fi);
+      if (fn == kBcFree) {
+        const double acc = kF64 ? -fi / A.mass[n] : -fi * minv;
+        const double v1 = vh0[d] + sc.c1 * acc;
+        eke += mass * v1 * v1;
+      } else {
+        eke += mass * vb0[d] * vb0[d];
+        ewe += w;
+      }
+      ewi += w;
+      A.fprev[d * N + n] = fi;
+    }
     if (fn == kBcFree) {
       const double acc = kF64 ? -fsum[d] / A.mass[n] : -fsum[d] * minv;
       const double vh = vh0[d];
@@ -307,6 +340,10 @@ __global__ void __launch_bounds__(512, 2) k_node_step(const NodeArgs A) {
     }
     un[d] = u;
   }
+  if (EN && advance) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) A.du[d * N + n] = un[d] - u0[d];
+  }
   if (advance) {
     const R r0 = R(un[0]), r1 = R(un[1]), r2 = R(un[2]);
     for (int k = sb; k < se; ++k) {
@@ -326,6 +363,71 @@ __global__ void __launch_bounds__(512, 2) k_node_step(const NodeArgs A) {
     *nxt = c;
     A.dtmin[(A.parity ^ 1) * A.ninst + inst] = kDtHugeBits;
   }
+}
+
+template <class R, bool EN>
+__global__ void __launch_bounds__(512, 2) k_node_step(const NodeArgs A) {
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double eke = 0.0, ewi = 0.0, ewe = 0.0;
+  if (!EN) {
+    if (n < A.N) node_step<R, false>(A, n, eke, ewi, ewe);
+    return;
+  }
+  if (n < A.N) node_step<R, true>(A, n, eke, ewi, ewe);
+  // block partials in a fixed order (warp butterfly, then warps in order)
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    eke += __shfl_xor_sync(0xffffffffu, eke, o);
+    ewi += __shfl_xor_sync(0xffffffffu, ewi, o);
+    ewe += __shfl_xor_sync(0xffffffffu, ewe, o);
+  }
+  __shared__ double part[16][3];
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    part[w][0] = eke;
+    part[w][1] = ewi;
+    part[w][2] = ewe;
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double s = 0.0;
+    for (int k = 0; k < (int)(blockDim.x + 31) / 32; ++k) s += part[k][threadIdx.x];
+    A.epart[3 * (long long)blockIdx.x + threadIdx.x] = s;
+  }
+}
+
+// The energy balance of the step just finished from the block partials of
+// k_node_step (one block, fixed summation order): the reference's CheckEnergy
+// after the velocity update (ex9.cpp:154-156).  Skipped for a step that did
+// not run (the instance was already done).
+__global__ void __launch_bounds__(1024) k_energy_reduce(const NodeArgs A, int nblocks) {
+  __shared__ double red[3][1024];
+  double s[3] = {0.0, 0.0, 0.0};
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) s[k] += A.epart[3 * (long long)b + k];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) red[k][threadIdx.x] = s[k];
+  __syncthreads();
+  for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x != 0) return;
+  if (A.clock[A.parity * A.ninst].done) return;
+  EnergyState e = *A.energy;
+  const double wke = 0.5 * red[0][0];
+  e.Wint += 0.5 * red[1][0];
+  e.Wext += 0.5 * red[2][0];
+  e.WKE = wke;
+  e.total = fabs(wke + e.Wint - e.Wext);
+  const double mx = fmax(fabs(e.Wint), fmax(fabs(e.Wext), fabs(wke)));
+  if (e.total > 0.01 * mx) ++e.violations;
+  if (mx > 0.0) e.max_ratio = fmax(e.max_ratio, e.total / mx);
+  ++e.steps;
+  *A.energy = e;
 }
 
 // Pre-loop clock: dt = reduction * StableTimeStep() at t0 (ex9.cpp:87).

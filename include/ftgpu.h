@@ -187,6 +187,22 @@ int ftgpu_launches_per_step(ftgpu_model *m);
 /* Synchronise and return the device error word (0 = none). */
 int ftgpu_check(ftgpu_model *m);
 
+/* ---- energy balance of the explicit loop ----
+ * CheckEnergy() (src/fem/SolidMechanics/CheckEnergy.cpp:3-85), which every
+ * example driver calls after each step (examples/ex9/ex9.cpp:154-156): per
+ * step the kinetic energy 1/2 sum m v^2, the internal work increment
+ * 1/2 sum du (f_prev + f) and the work of the reactions of constrained DOFs
+ * (no external forces on this path), accumulated from the start of the loop.
+ * Fused into the nodal step (one extra launch per step for the fixed-order
+ * reduction).  ftgpu_set_energy after ftgpu_setup, before
+ * ftgpu_init_explicit (it resets the loop); single-instance models only. */
+int ftgpu_set_energy(ftgpu_model *m, int enable);
+/* cumulative internal and external work, the last step's kinetic energy, the
+ * largest |WKE + Wint - Wext| / max(|Wint|, |Wext|, |WKE|) seen and the number
+ * of steps where it exceeded 1 % (the reference's "Energy Violation" warning) */
+int ftgpu_get_energy(ftgpu_model *m, double *internal_work, double *external_work,
+                     double *kinetic_energy, double *max_violation, long long *violations);
+
 /* ---- learned constitutive surrogate for material 7 (no counterpart in the
  * reference; it replaces the isochoric part of HGOIsotropicViscoelastic's
  * stress, HGOIsotropicViscoelastic.cpp:53-97, generalised to fibres) ----
