@@ -321,6 +321,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--size", default=None,
                     help="block: nx,ny,nz; head: target elements; ensemble: instances")
+    ap.add_argument("--energy", action="store_true",
+                    help="track the energy balance (CheckEnergy) in the loop (single instance)")
     ap.add_argument("--surrogate", action="store_true",
                     help="head workload: plain vs learned surrogate vs FP64")
     ap.add_argument("--train-samples", type=int, default=10_000_000)
@@ -354,6 +356,8 @@ def main():
     model = ft.Model(mesh, mats, precision=ft.MIXED, device=dev, loads=loads,
                      instances=wl["instances"])
     log("setup %.1f s (%d elements, %d nodes)" % (time.perf_counter() - t0, E, N))
+    if args.energy:
+        model.set_energy(True)
     model.init_explicit(reduction=0.9, failure_dt=0.0, tmax=1e300)
     model.run(args.warmup)
     torch.cuda.synchronize(dev)
@@ -409,7 +413,8 @@ def main():
         "ms_per_step": ms / max(steps, 1), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 element kernels / f64 nodal state",
         "data": "synthetic (seeded, generated in-run)",
-        "config": {"workload": wl["label"], "elements": E, "nodes": N,
+        "config": {"workload": wl["label"] + ("_energy_balance" if args.energy else ""),
+                   "elements": E, "nodes": N,
                    "material": wl["material"], "precision": "mixed",
                    "l2": "inputs larger than L2 (%.2f GB resident)" % ((E * 48 + N * 140) / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
@@ -425,6 +430,8 @@ def main():
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline and args.workload == "block":
         line["cpu_baseline"] = cpu_reference_rate(os.cpu_count() or 1)
+    if args.energy:
+        line["energy"] = model.energy()
     if rank == 0:
         print(json.dumps(line), flush=True)
     model.close()

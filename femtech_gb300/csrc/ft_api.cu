@@ -334,8 +334,8 @@ NodeArgs node_args(ftgpu_model *m, int mode, int parity) {
   A.stepsc = m->stepsc.as<StepScalars>();
   A.rottrig = m->rottrig.as<double>();
   if (m->energy_on) {
-    A.du = m->du.as<double>();
-    A.fprev = m->fprev.as<double>();
+    A.du = m->du.p;
+    A.fprev = m->fprev.p;
     A.epart = m->epart.as<double>();
     A.energy = m->estate.as<EnergyState>();
   }
@@ -1108,7 +1108,7 @@ int ftgpu_init_explicit(ftgpu_model *m, double reduction, double failure_dt, dou
   CK(cudaGetLastError());
   CKI(launch_groups(m, 0, 1, 0.0, 0, 0));
   if (m->energy_on) {  // CheckEnergy's works start from zero with the loop
-    CK(cudaMemsetAsync(m->du.p, 0, 3 * (size_t)m->nNodes * sizeof(double), m->stream));
+    CK(cudaMemsetAsync(m->du.p, 0, m->du.bytes, m->stream));
     CK(cudaMemsetAsync(m->estate.p, 0, sizeof(EnergyState), m->stream));
   }
   CKI(launch_node(m, kNodeInit, 0));
@@ -1189,14 +1189,15 @@ int ftgpu_set_energy(ftgpu_model *m, int enable) {
   CK(cudaSetDevice(m->device));
   CK(cudaStreamSynchronize(m->stream));
   if (enable && !m->energy_on) {
-    const size_t n3 = 3 * (size_t)m->nNodes;
+    // du and f_prev in the element precision (FP32 in mixed mode)
+    const size_t n3b = 3 * (size_t)m->nNodes * (is_fp64(m) ? sizeof(double) : sizeof(float));
     const size_t maxblocks = ((size_t)m->nNodes + 63) / 64;  // smallest node block: 64
-    CKI(m->du.alloc(n3 * sizeof(double)));
-    CKI(m->fprev.alloc(n3 * sizeof(double)));
+    CKI(m->du.alloc(n3b));
+    CKI(m->fprev.alloc(n3b));
     CKI(m->epart.alloc(3 * maxblocks * sizeof(double)));
     CKI(m->estate.alloc(sizeof(EnergyState)));
-    CK(cudaMemset(m->du.p, 0, n3 * sizeof(double)));
-    CK(cudaMemset(m->fprev.p, 0, n3 * sizeof(double)));
+    CK(cudaMemset(m->du.p, 0, n3b));
+    CK(cudaMemset(m->fprev.p, 0, n3b));
     CK(cudaMemset(m->estate.p, 0, sizeof(EnergyState)));
   }
   m->energy_on = enable != 0;

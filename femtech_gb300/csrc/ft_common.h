@@ -140,8 +140,8 @@ struct NodeArgs {
   StepScalars *stepsc;        // [ninst] written by k_step_scalars
   double *rottrig;            // [ninst][kMaxRotFns][3] cos, sin, omega at t_{n+2}
   // energy balance (single instance; null when off)
-  double *du;                 // [3][N] u_{n+1} - u_n of the step being finished
-  double *fprev;              // [3][N] internal force of the previous step
+  void *du;                   // [3][N] u_{n+1} - u_n of the step being finished (Real)
+  void *fprev;                // [3][N] internal force of the previous step (Real)
   double *epart;              // [node blocks][3] partial sums: kinetic, internal, external
   EnergyState *energy;
 };

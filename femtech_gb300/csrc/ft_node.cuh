@@ -158,7 +158,7 @@ __global__ void __launch_bounds__(512) k_node(const NodeArgs A) {
         A.v[d * N + n] = vb;
         A.a[d * N + n] = 0.0;
       }
-      if (A.du) A.du[d * N + n] = u - uold;  // energy balance: this step's increment
+      if (A.du) reinterpret_cast<R *>(A.du)[d * N + n] = R(u - uold);  // energy: this step's du
       un[d] = u;
     }
     for (int k = sb; k < se; ++k) {
@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(512) k_node(const NodeArgs A) {
       if (A.fprev) {  // energy balance: f of the pre-loop state, summed as k_node_step does
         R fr = 0;
         for (int k = sb; k < se; ++k) fr += sF[d * S + A.slots[k]];
-        A.fprev[d * N + n] = double(fr);
+        reinterpret_cast<R *>(A.fprev)[d * N + n] = fr;
       }
       if (A.nbc[d * N + n] != kBcFree) continue;
       double f = 0.0;
@@ -214,9 +214,12 @@ __global__ void k_step_scalars(const NodeArgs A) {
 // (CheckEnergy.cpp:18-55 with fe = 0): kinetic energy m v_{n+1}^2, internal
 // work du (f_prev + f) and, for constrained DOFs, the work of the reaction
 // du (f_prev + f + m (a + a_prev)) with a = a_prev = 0 on constrained DOFs.
+// The terms are formed in the element precision R (FP32 in mixed mode, where
+// du and f are FP32 already: FP64 issue is slow on this GPU), FP64 in FP64
+// mode.
 template <class R, bool EN>
-__device__ __forceinline__ void node_step(const NodeArgs &A, long long n, double &eke,
-                                          double &ewi, double &ewe) {
+__device__ __forceinline__ void node_step(const NodeArgs &A, long long n, R &eke, R &ewi,
+                                          R &ewe) {
   const long long N = A.N, S = A.S;
   const R *sF = reinterpret_cast<const R *>(A.sF);
   R *sU = reinterpret_cast<R *>(A.sU);
@@ -232,15 +235,21 @@ __device__ __forceinline__ void node_step(const NodeArgs &A, long long n, double
   }
   // 1/m (mixed mode; FP64 mode divides by m as the reference does)
   const double minv = sizeof(R) == 8 ? 0.0 : A.minv[n];
-  double du0[3] = {0.0, 0.0, 0.0}, fp0[3] = {0.0, 0.0, 0.0}, vb0[3] = {0.0, 0.0, 0.0};
+  // energy inputs of all three DOFs, issued with the other loads and before
+  // any store of this node (the stores could alias them and serialise loads)
+  R *du = reinterpret_cast<R *>(A.du), *fp = reinterpret_cast<R *>(A.fprev);
+  R du_[3] = {0, 0, 0}, fp_[3] = {0, 0, 0};
+  double vb_[3] = {0.0, 0.0, 0.0};
+  const double mass = EN ? A.mass[n] : 0.0;
   if (EN) {
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      du0[d] = A.du[d * N + n];
-      fp0[d] = A.fprev[d * N + n];
-      vb0[d] = A.v[d * N + n];  // velocity of a constrained DOF at t_{n+1}
+      du_[d] = du[d * N + n];
+      fp_[d] = fp[d * N + n];
+      if (nbc[d] != kBcFree) vb_[d] = A.v[d * N + n];  // constrained DOF: v(t_{n+1})
     }
   }
+
   // sum of the patch partials in slot order (in the element precision)
   R fs0 = 0, fs1 = 0, fs2 = 0;
   for (int k = sb; k < se; ++k) {
@@ -290,23 +299,28 @@ __device__ __forceinline__ void node_step(const NodeArgs &A, long long n, double
       rot_apply(b, c, s, om, A.X, N, n, ur, vr);
     }
   }
-  const double mass = EN ? A.mass[n] : 0.0;
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const int fn = nbc[d];
     double u = u0[d];
     if (EN) {
-      const double fi = fsum[d], w = du0[d] * (fp0[d] + fi);
+      const R fi = R(fsum[d]);  // exact: a sum in the element precision
+      const R w = du_[d] * (fp_[d] + fi);
       if (fn == kBcFree) {
-        const double acc = kF64 ? -fi / A.mass[n] : -fi * minv;
-        const double v1 = vh0[d] + sc.c1 * acc;
-        eke += mass * v1 * v1;
+        R v1;
+        if (kF64) {
+          v1 = R(vh0[d] + sc.c1 * (-fsum[d] / A.mass[n]));
+        } else {
+          v1 = R(vh0[d]) + R(sc.c1) * (-fi * R(minv));
+        }
+        eke += R(mass) * v1 * v1;
       } else {
-        eke += mass * vb0[d] * vb0[d];
+        const R vb = R(vb_[d]);
+        eke += R(mass) * vb * vb;
         ewe += w;
       }
       ewi += w;
-      A.fprev[d * N + n] = fi;
+      fp[d * N + n] = fi;
     }
     if (fn == kBcFree) {
       const double acc = kF64 ? -fsum[d] / A.mass[n] : -fsum[d] * minv;
@@ -342,7 +356,7 @@ __device__ __forceinline__ void node_step(const NodeArgs &A, long long n, double
   }
   if (EN && advance) {
 #pragma unroll
-    for (int d = 0; d < 3; ++d) A.du[d * N + n] = un[d] - u0[d];
+    for (int d = 0; d < 3; ++d) du[d * N + n] = R(un[d] - u0[d]);
   }
   if (advance) {
     const R r0 = R(un[0]), r1 = R(un[1]), r2 = R(un[2]);
@@ -366,15 +380,16 @@ __device__ __forceinline__ void node_step(const NodeArgs &A, long long n, double
 }
 
 template <class R, bool EN>
-__global__ void __launch_bounds__(512, 2) k_node_step(const NodeArgs A) {
+__global__ void __launch_bounds__(512, EN ? 1 : 2) k_node_step(const NodeArgs A) {
   const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  double eke = 0.0, ewi = 0.0, ewe = 0.0;
+  R eke = 0, ewi = 0, ewe = 0;
   if (!EN) {
     if (n < A.N) node_step<R, false>(A, n, eke, ewi, ewe);
     return;
   }
   if (n < A.N) node_step<R, true>(A, n, eke, ewi, ewe);
-  // block partials in a fixed order (warp butterfly, then warps in order)
+  // block partials in a fixed order: warp butterfly in R, then the warps in
+  // order in FP64
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     eke += __shfl_xor_sync(0xffffffffu, eke, o);
@@ -384,9 +399,9 @@ __global__ void __launch_bounds__(512, 2) k_node_step(const NodeArgs A) {
   __shared__ double part[16][3];
   const int w = threadIdx.x >> 5;
   if ((threadIdx.x & 31) == 0) {
-    part[w][0] = eke;
-    part[w][1] = ewi;
-    part[w][2] = ewe;
+    part[w][0] = double(eke);
+    part[w][1] = double(ewi);
+    part[w][2] = double(ewe);
   }
   __syncthreads();
   if (threadIdx.x < 3) {
