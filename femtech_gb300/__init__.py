@@ -202,8 +202,17 @@ class Model:
         _check(lib().ftgpu_run(self.h, int(max_steps), C.byref(s)))
         return s.value
 
-    def state(self):
+    def state(self, out=None):
+        """u, v, a (AoS [node*3+d]), time, dt, step.  out: optional dict of
+        preallocated float64 arrays 'u', 'v', 'a' (pinned host memory gives
+        full-bandwidth copies); a missing key is not read back."""
         n = 3 * self.nNodes
+        if out is not None:
+            u, v, a = out.get("u"), out.get("v"), out.get("a")
+            t, dt, st = C.c_double(), C.c_double(), C.c_longlong()
+            _check(lib().ftgpu_get_state(self.h, _ptr(u), _ptr(v), _ptr(a), C.byref(t),
+                                         C.byref(dt), C.byref(st)))
+            return dict(u=u, v=v, a=a, time=t.value, dt=dt.value, step=st.value)
         u, v, a = np.zeros(n), np.zeros(n), np.zeros(n)
         t, dt, st = C.c_double(), C.c_double(), C.c_longlong()
         _check(lib().ftgpu_get_state(self.h, u.ctypes.data, v.ctypes.data, a.ctypes.data,

@@ -210,6 +210,7 @@ struct ftgpu_model {
   std::vector<std::unique_ptr<DBuf>> hist;
   DBuf clock, dtmin, err, instp;
   DBuf stepsc, rottrig;  // per-instance step scalars / rotation trigonometry
+  DBuf stage;            // AoS staging of host <-> device state copies
   // energy balance of the explicit loop (CheckEnergy), single instance only
   bool energy_on = false;
   DBuf du, fprev, epart, estate;
@@ -412,13 +413,42 @@ int fill_dtmin(ftgpu_model *m) {
   return (int)cudaGetLastError();
 }
 
-// AoS [3N] host -> SoA [3][N] device
+// Host arrays are AoS [node*3 + d] (the reference's layout), device state is
+// SoA [3][N]: the transpose runs on the device through a staging buffer, and
+// the host copy is one contiguous cudaMemcpyAsync straight from / into the
+// caller's array (full link bandwidth when the caller's memory is pinned).
+__global__ void k_aos_to_soa(const double *aos, double *soa, long long N) {
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) soa[k * N + n] = aos[3 * n + k];
+}
+__global__ void k_soa_to_aos(const double *soa, double *aos, long long N) {
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) aos[3 * n + k] = soa[k * N + n];
+}
+
+int ensure_stage(ftgpu_model *m) {
+  const size_t b = 3 * (size_t)m->nNodes * sizeof(double);
+  if (m->stage.bytes >= b) return 0;
+  return m->stage.alloc(b);
+}
+
+// AoS [3N] host -> SoA [3][N] device (h == NULL: zero)
 int upload_aos(ftgpu_model *m, const double *h, DBuf &d) {
   const long long N = m->nNodes;
-  std::vector<double> t(3 * N);
-  for (long long n = 0; n < N; ++n)
-    for (int k = 0; k < 3; ++k) t[k * N + n] = h ? h[3 * n + k] : 0.0;
-  CK(cudaMemcpyAsync(d.p, t.data(), 3 * N * sizeof(double), cudaMemcpyHostToDevice, m->stream));
+  if (!h) {
+    CK(cudaMemsetAsync(d.p, 0, 3 * N * sizeof(double), m->stream));
+    CK(cudaStreamSynchronize(m->stream));
+    return 0;
+  }
+  CKI(ensure_stage(m));
+  CK(cudaMemcpyAsync(m->stage.p, h, 3 * N * sizeof(double), cudaMemcpyHostToDevice, m->stream));
+  k_aos_to_soa<<<(unsigned)((N + 255) / 256), 256, 0, m->stream>>>(m->stage.as<double>(),
+                                                                    d.as<double>(), N);
+  CK(cudaGetLastError());
   CK(cudaStreamSynchronize(m->stream));
   return 0;
 }
@@ -426,11 +456,12 @@ int upload_aos(ftgpu_model *m, const double *h, DBuf &d) {
 int download_aos(ftgpu_model *m, const DBuf &d, double *h) {
   if (!h) return 0;
   const long long N = m->nNodes;
-  std::vector<double> t(3 * N);
-  CK(cudaMemcpyAsync(t.data(), d.p, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, m->stream));
+  CKI(ensure_stage(m));
+  k_soa_to_aos<<<(unsigned)((N + 255) / 256), 256, 0, m->stream>>>(d.as<double>(),
+                                                                    m->stage.as<double>(), N);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(h, m->stage.p, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, m->stream));
   CK(cudaStreamSynchronize(m->stream));
-  for (long long n = 0; n < N; ++n)
-    for (int k = 0; k < 3; ++k) h[3 * n + k] = t[k * N + n];
   return 0;
 }
 
