@@ -767,6 +767,60 @@ void or_apply_bc(const or_model *m, const int *dof_fn, const or_bc_fn *fns, doub
  * full-step velocity and the next stable dt.  Energy checks and VTU output
  * are left out.  u, v, a hold the initial state on entry and the final state
  * on return.  Every out_every steps u and Time are appended to u_out/t_out. */
+/* CalculateStrain.cpp:8-75 (CalculateMaximumPrincipalStrain): the Gauss-point
+ * average of the Green-Lagrange strain from the F of the last or_get_force,
+ * E = sum_gp (0.5 / nGP) F^T F - 0.5 I (the dgemm of the reference: for column
+ * j, row i, s = sum_l F[l,i] F[l,j], E[i,j] = 0.5/nGP s + E[i,j]), then the
+ * principal strains from the trigonometric solution of the characteristic
+ * equation; ps_max clamped at >= 0, ps_min at <= 0, shear = (max - min) / 2.
+ * Any output may be NULL. */
+void or_element_strain(const or_model *m, double *Eavg9, double *ps_max, double *ps_min,
+                       double *shear_max) {
+  const double kPi = 4.0 * atan(1.0);
+  for (int elm = 0; elm < m->nelements; ++elm) {
+    double E[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const int ngp = m->nGP[elm];
+    const double pre = 0.5 / (double)ngp;
+    for (int gp = 0; gp < ngp; ++gp) {
+      const double *F = m->F + m->fptr[elm] + 9 * gp;
+      for (int j = 0; j < 3; ++j)
+        for (int i = 0; i < 3; ++i) {
+          double s = 0.0;
+          for (int l = 0; l < 3; ++l) s += F[l + 3 * i] * F[l + 3 * j];
+          E[i + 3 * j] = pre * s + E[i + 3 * j];
+        }
+    }
+    E[0] -= 0.5;
+    E[4] -= 0.5;
+    E[8] -= 0.5;
+    if (Eavg9) memcpy(Eavg9 + 9 * (size_t)elm, E, sizeof(E));
+    const double a = E[0], b = E[1], c = E[2], d = E[4], e = E[5], f = E[8];
+    const double p1 = b * b + c * c + e * e;
+    double e1, e2, e3;
+    if (p1 == 0) {
+      e1 = a;
+      e2 = d;
+      e3 = f;
+    } else {
+      double I1 = a + d + f;
+      const double I2 = a * (d + f) + d * f - b * b - c * c - e * e;
+      const double I3 = a * d * f + 2.0 * b * c * e - b * b * f - c * c * d - e * e * a;
+      const double Q = (3.0 * I2 - I1 * I1) / 9.0;
+      const double R = (2.0 * I1 * I1 * I1 - 9.0 * I1 * I2 + 27.0 * I3) / 54.0;
+      const double theta = acos(R / sqrt(-Q * Q * Q));
+      const double sq = 2.0 * sqrt(-Q);
+      I1 = I1 / 3.0;
+      e1 = sq * cos(theta / 3.0) + I1;
+      e2 = sq * cos((theta + 2.0 * kPi) / 3.0) + I1;
+      e3 = sq * cos((theta + 4.0 * kPi) / 3.0) + I1;
+    }
+    const double mx = fmax(e3, fmax(e2, e1)), mn = fmin(e3, fmin(e2, e1));
+    if (shear_max) shear_max[elm] = 0.5 * (mx - mn);
+    if (ps_max) ps_max[elm] = mx > 0.0 ? mx : 0.0;
+    if (ps_min) ps_min[elm] = mn < 0.0 ? mn : 0.0;
+  }
+}
+
 int or_explicit_run(or_model *m, const int *dof_fn, const or_bc_fn *fns, int nfn,
                     double t0, double tMax, double reduction, double failure_dt,
                     int max_steps, int out_every, double *u, double *v, double *a,

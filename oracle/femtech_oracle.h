@@ -81,6 +81,8 @@ int or_explicit_run(or_model *m, const int *dof_fn, const or_bc_fn *fns, int nfn
                     int max_steps, int out_every, double *u, double *v, double *a,
                     double *u_out, double *t_out, int max_out, int *n_out,
                     int *steps_done, double *time_out, double *dt_out);
+void or_element_strain(const or_model *m, double *Eavg9, double *ps_max, double *ps_min,
+                       double *shear_max);
 void or_apply_bc(const or_model *m, const int *dof_fn, const or_bc_fn *fns,
                  double t, double *u, double *v, double *a);
 void or_set_threads(or_model *m, int n);

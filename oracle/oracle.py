@@ -95,6 +95,7 @@ class Oracle:
                                           _dp, _dp, _dp, C.c_int, C.POINTER(C.c_int),
                                           C.POINTER(C.c_int), C.POINTER(C.c_double),
                                           C.POINTER(C.c_double)]
+            L.or_element_strain.argtypes = [M, _dp, _dp, _dp, _dp]
             L.or_set_threads.argtypes = [M, C.c_int]
             L.or_max_threads.restype = C.c_int
             cls._lib = L
@@ -168,6 +169,14 @@ class Oracle:
                                               np.ascontiguousarray(u, np.float64).ravel(),
                                               np.ascontiguousarray(boundary, np.int32).ravel())
 
+    def element_strain(self):
+        """CalculateMaximumPrincipalStrain of every element on the F of the last
+        get_force: Eavg [nE, 9] (reference layout), max / min principal strain,
+        max shear."""
+        E9, mx, mn, sh = _strain_outputs(self.nE)
+        self.lib().or_element_strain(C.byref(self.m), E9, mx, mn, sh)
+        return E9.reshape(-1, 9), mx, mn, sh
+
     def explicit_run(self, dof_fn, fns, tmax, reduction, max_steps, out_every, t0=0.0,
                      failure_dt=0.0, u=None, v=None, a=None, max_out=None, energy=False):
         """The ex9 loop; energy=True adds per step (Wint, Wext, WKE) of
@@ -198,6 +207,10 @@ class Oracle:
         if energy:
             res["energy"] = ebuf.reshape(-1, 3)[: steps.value].copy()
         return res
+
+
+def _strain_outputs(nE):
+    return np.zeros(9 * nE), np.zeros(nE), np.zeros(nE), np.zeros(nE)
 
 
 def material_stress(mat, props, F, J=None, a0=None, dt=0.0, hist=None):
@@ -243,6 +256,7 @@ class RefBuild:
             L.ref_stable_time_step.argtypes = [_dp, _ip]
             L.ref_stable_time_step.restype = C.c_double
             L.ref_set_energy_out.argtypes = [C.c_void_p, C.c_int]
+            L.ref_element_strain.argtypes = [_dp, _dp, _dp, _dp]
             L.ref_explicit_run.argtypes = [_ip, C.c_void_p, C.c_int, C.c_double, C.c_double,
                                            C.c_double, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp,
                                            C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
@@ -287,6 +301,15 @@ class RefBuild:
         if rc:
             raise RuntimeError("ref_get_force failed %d" % rc)
         return fi
+
+    def element_strain(self):
+        """The reference's CalculateMaximumPrincipalStrain on every element (F of
+        the last get_force)."""
+        E9, mx, mn, sh = _strain_outputs(self.nE)
+        rc = self.lib().ref_element_strain(E9, mx, mn, sh)
+        if rc:
+            raise RuntimeError("ref_element_strain failed %d" % rc)
+        return E9.reshape(-1, 9), mx, mn, sh
 
     def stable_time_step(self, u, boundary):
         return self.lib().ref_stable_time_step(np.ascontiguousarray(u, np.float64).ravel(),

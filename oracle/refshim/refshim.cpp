@@ -298,6 +298,25 @@ double ref_stable_time_step(const double *u, const int *bnd) {
 
 /* The explicit loop of examples/ex9/ex9.cpp:79-175 with driver-side
  * boundary conditions given as per-DOF function indices (see or_apply_bc). */
+/* CalculateMaximumPrincipalStrain (CalculateStrain.cpp:8-75) of every element
+ * on the F of the last ref_get_force: Eavg (9 per element, the reference's
+ * Eavg layout), the clamped max / min principal strains and the max shear. */
+int ref_element_strain(double *Eavg9, double *ps_max, double *ps_min, double *shear_max) {
+  try {
+    for (int elm = 0; elm < nelements; ++elm) {
+      double mx, mn, sh;
+      CalculateMaximumPrincipalStrain(elm, &mx, &mn, &sh);
+      if (Eavg9) memcpy(Eavg9 + 9 * (size_t)elm, Eavg + 9 * (size_t)elm, 9 * sizeof(double));
+      if (ps_max) ps_max[elm] = mx;
+      if (ps_min) ps_min[elm] = mn;
+      if (shear_max) shear_max[elm] = sh;
+    }
+    return 0;
+  } catch (RefTerminate &t) {
+    return -t.code;
+  }
+}
+
 /* Energy output of the next ref_explicit_run: per step the cumulative internal
  * and external work and the kinetic energy that the reference's own
  * CheckEnergy() logs (ex9.cpp:154-156 calls it after every step).  Its works

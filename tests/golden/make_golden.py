@@ -9,7 +9,9 @@ the reference tree.
 Fixtures:
   ref_force.npz   GetForce / mass / StableTimeStep / Gauss-point pk2 of the
                   reference on jittered C3D8 and C3D4 meshes, materials 1-5,
-                  including three consecutive viscoelastic calls (material 5).
+                  including three consecutive viscoelastic calls (material 5);
+                  for material 1 also CalculateMaximumPrincipalStrain of every
+                  element (Eavg[9], max / min principal strain, max shear).
   ref_ex9.npz     examples/ex9 (one C3D8, Neo-Hookean, ramped tension, 0.8
                   dt factor, t = 0..1 s) run by the reference loop, plus the
                   last row of examples/ex9/abaqus/abaqus.rpt (the CI target of
@@ -67,13 +69,18 @@ def force_cases():
         for mid, props in MATS.items():
             mats = mg.materials([(mid, props)])
             r = orc.RefBuild(mesh, mats)
-            fis, pk2s = [], []
+            fis, pk2s, strains = [], [], []
             for k in range(3):
                 fis.append(r.get_force(u[k], 1.0e-6))
                 pk2s.append(r.gp_arrays()[2])
                 assert np.all(np.isfinite(fis[-1])), (name, mid, k)
+                if mid == 1:  # CalculateMaximumPrincipalStrain on this state's F
+                    E9, mx, mn, sh = r.element_strain()
+                    strains.append(np.concatenate([E9, mx[:, None], mn[:, None], sh[:, None]], 1))
             out["%s_m%d_fi" % (name, mid)] = np.array(fis)
             out["%s_m%d_pk2" % (name, mid)] = np.array(pk2s)
+            if strains:
+                out["%s_strain" % name] = np.array(strains)
             out["%s_m%d_mass" % (name, mid)] = r.mass
             b = np.zeros(3 * n, np.int32)
             out["%s_m%d_dt" % (name, mid)] = np.array([r.stable_time_step(u[k], b) for k in range(3)])

@@ -26,6 +26,19 @@ def test_force_mass_dt_pk2_match_reference(oracle_lib, golden, name, mid):
                                                             rel=1e-14)
 
 
+@pytest.mark.parametrize("name", ["hex", "tet"])
+def test_element_strain_matches_reference(oracle_lib, golden, name):
+    """CalculateMaximumPrincipalStrain (CalculateStrain.cpp:8-75) on three states."""
+    f = golden["ref_force"]
+    mesh = golden_mesh(golden, name)
+    o = oracle_lib.Oracle(mesh, mg.materials([(1, MATS[1])]))
+    for k in range(3):
+        o.get_force(f[name + "_u"][k], 1.0e-6)
+        E9, mx, mn, sh = o.element_strain()
+        got = np.concatenate([E9, mx[:, None], mn[:, None], sh[:, None]], 1)
+        np.testing.assert_array_equal(got, f[name + "_strain"][k])
+
+
 def test_ex9_loop_matches_reference_and_abaqus(oracle_lib, golden):
     g = golden["ref_ex9"]
     mesh, mats, loads = ex9_mesh_loads()
