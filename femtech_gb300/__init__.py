@@ -236,6 +236,15 @@ class Model:
         _check(L.ftgpu_set_surrogate(self.h, None if surrogate is None else surrogate.h,
                                      float(trust_e2)))
 
+    def element_strain(self):
+        """CalculateMaximumPrincipalStrain of every element on the current state:
+        Eavg [nE, 9] (column-major 3x3), max / min principal strain, max shear."""
+        L = lib()
+        L.ftgpu_element_strain.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
+        E9, mx, mn, sh = np.zeros(9 * self.nE), np.zeros(self.nE), np.zeros(self.nE), np.zeros(self.nE)
+        _check(L.ftgpu_element_strain(self.h, E9, mx, mn, sh))
+        return E9.reshape(-1, 9), mx, mn, sh
+
     def set_energy(self, enable=True):
         """Track CheckEnergy's balance in the device loop (call before init_explicit)."""
         _check(lib().ftgpu_set_energy(self.h, int(bool(enable))))

@@ -465,6 +465,60 @@ int download_aos(ftgpu_model *m, const DBuf &d, double *h) {
   return 0;
 }
 
+// Reference layout and principal strains of the averaged Green strain of
+// each element (CalculateStrain.cpp:38-74, FP64): out per element = Eavg
+// column-major 3x3, max principal strain clamped >= 0, min clamped <= 0,
+// max shear (max - min) / 2 of the unclamped extremes.
+__global__ void k_principal_strain(const double *E6, long long nE, double *out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nE) return;
+  const double xx = E6[6 * i], yy = E6[6 * i + 1], zz = E6[6 * i + 2];
+  const double yz = E6[6 * i + 3], xz = E6[6 * i + 4], xy = E6[6 * i + 5];
+  double *o = out + 12 * i;
+  o[0] = xx; o[1] = xy; o[2] = xz;
+  o[3] = xy; o[4] = yy; o[5] = yz;
+  o[6] = xz; o[7] = yz; o[8] = zz;
+  const double a = xx, b = xy, c = xz, d = yy, e = yz, f = zz;
+  const double p1 = b * b + c * c + e * e;
+  double e1, e2, e3;
+  if (p1 == 0) {
+    e1 = a;
+    e2 = d;
+    e3 = f;
+  } else {  // trigonometric roots of x^3 - I1 x^2 + I2 x - I3 (as the reference)
+    double I1 = a + d + f;
+    const double I2 = a * (d + f) + d * f - b * b - c * c - e * e;
+    const double I3 = a * d * f + 2.0 * b * c * e - b * b * f - c * c * d - e * e * a;
+    const double Q = (3.0 * I2 - I1 * I1) / 9.0;
+    const double R = (2.0 * I1 * I1 * I1 - 9.0 * I1 * I2 + 27.0 * I3) / 54.0;
+    const double theta = acos(R / sqrt(-Q * Q * Q));
+    const double sq = 2.0 * sqrt(-Q);
+    const double kPi = 3.141592653589793;
+    I1 = I1 / 3.0;
+    e1 = sq * cos(theta / 3.0) + I1;
+    e2 = sq * cos((theta + 2.0 * kPi) / 3.0) + I1;
+    e3 = sq * cos((theta + 4.0 * kPi) / 3.0) + I1;
+  }
+  const double mx = fmax(e3, fmax(e2, e1)), mn = fmin(e3, fmin(e2, e1));
+  o[9] = mx > 0.0 ? mx : 0.0;
+  o[10] = mn < 0.0 ? mn : 0.0;
+  o[11] = 0.5 * (mx - mn);
+}
+
+template <class R>
+int strain_groups_t(ftgpu_model *m, double *E6) {
+  const int PE = max_patch(m);
+  for (size_t gi = 0; gi < m->ps.groups.size(); ++gi) {
+    const PatchGroup &g = m->ps.groups[gi];
+    const ElemArgs<R> A = elem_args<R>(m, g, (int)gi);
+    const size_t smem = elem_smem_bytes_host<R>(g.etype, PE);
+    const int r = launch_strain<R>(g.etype, g.npatch, PE, smem, m->stream, A, E6);
+    if (r) return fail(FTGPU_ERR_CUDA, std::string("element strain pass: ") +
+                                           cudaGetErrorString((cudaError_t)r));
+  }
+  return 0;
+}
+
 int check_err(ftgpu_model *m) {
   CK(cudaMemcpyAsync(m->h_err, m->err.p, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
   CK(cudaStreamSynchronize(m->stream));
@@ -1211,6 +1265,36 @@ int ftgpu_launches_per_step(ftgpu_model *m) {
   if (m->surr)
     for (auto &x : m->ps.groups) g += 2 * (x.npatch > 0 && x.mat == 7);
   return g + 2 + (m->energy_on ? 1 : 0);  // + k_energy_reduce
+}
+
+int ftgpu_element_strain(ftgpu_model *m, double *Eavg, double *ps_max, double *ps_min,
+                         double *shear_max) {
+  if (!m || !m->setup_done) return fail(FTGPU_ERR_STATE, "element_strain before setup");
+  CK(cudaSetDevice(m->device));
+  const long long nE = m->nE;
+  DBuf e6, out;
+  CKI(e6.alloc(6 * (size_t)nE * sizeof(double)));
+  CKI(out.alloc(12 * (size_t)nE * sizeof(double)));
+  CKI(launch_node(m, kNodeScatterU, 0));
+  CKI(is_fp64(m) ? strain_groups_t<double>(m, e6.as<double>())
+                 : strain_groups_t<float>(m, e6.as<double>()));
+  k_principal_strain<<<(unsigned)((nE + 255) / 256), 256, 0, m->stream>>>(e6.as<double>(), nE,
+                                                                          out.as<double>());
+  CK(cudaGetLastError());
+  std::vector<double> h(12 * (size_t)nE);
+  CK(cudaMemcpyAsync(h.data(), out.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                     m->stream));
+  CK(cudaStreamSynchronize(m->stream));
+  // group order -> reference element order
+  for (long long q = 0; q < nE; ++q) {
+    const int e = m->ps.elem_order[q];
+    const double *r = &h[12 * q];
+    if (Eavg) memcpy(Eavg + 9 * (size_t)e, r, 9 * sizeof(double));
+    if (ps_max) ps_max[e] = r[9];
+    if (ps_min) ps_min[e] = r[10];
+    if (shear_max) shear_max[e] = r[11];
+  }
+  return FTGPU_OK;
 }
 
 int ftgpu_set_energy(ftgpu_model *m, int enable) {

@@ -625,6 +625,114 @@ __global__ void __launch_bounds__(kElemThreads, ET == 0 ? 2 : 3)
   }
 }
 
+// Gauss-point average of the Green-Lagrange strain of every element of a group
+// (CalculateStrain.cpp:8-33) on the current displacement slots, from the
+// displacement gradient D = F - I of each Gauss point:
+//   E = (1 / nGP) sum_gp (D + D^T + D^T D) / 2,
+// the same quantity as the reference's sum (0.5 / nGP) F^T F - 0.5 I without
+// the cancellation of F^T F - I.  Output per element (group order, FP64):
+// Voigt xx, yy, zz, yz, xz, xy.
+template <class R, int ET>
+__global__ void __launch_bounds__(kElemThreads) k_elem_strain(const ElemArgs<R> A, double *Eout) {
+  constexpr int NC = ET == 0 ? 8 : 4;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  R *shX = reinterpret_cast<R *>(smem_raw);
+  R *shU = shX + 3 * kMaxLocalNodes;
+  const int PE = blockDim.x;
+  const int t = threadIdx.x;
+  const int p = A.patch_begin + blockIdx.x;
+  const int e0 = A.patch_elem_off[p], ne = A.patch_elem_off[p + 1] - e0;
+  const int s0 = A.patch_node_off[p], ns = A.patch_node_off[p + 1] - s0;
+  for (int i = t; i < ns; i += PE) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      shX[d * kMaxLocalNodes + i] = A.sX[d * A.S + s0 + i];
+      shU[d * kMaxLocalNodes + i] = A.sU[d * A.S + s0 + i];
+    }
+  }
+  __syncthreads();
+  if (t >= ne) return;
+  const int e = e0 + t;
+  const long long el = e - A.elem_begin;
+  int lc[NC];
+  if (NC == 8) {
+    const uint4 v = *reinterpret_cast<const uint4 *>(A.lconn + 8ll * el);
+    lc[0] = v.x & 0xffff; lc[1] = v.x >> 16; lc[2] = v.y & 0xffff; lc[3] = v.y >> 16;
+    lc[4 % NC] = v.z & 0xffff; lc[5 % NC] = v.z >> 16; lc[6 % NC] = v.w & 0xffff; lc[7 % NC] = v.w >> 16;
+  } else {
+    const uint2 v = *reinterpret_cast<const uint2 *>(A.lconn + 4ll * el);
+    lc[0] = v.x & 0xffff; lc[1] = v.x >> 16; lc[2] = v.y & 0xffff; lc[3] = v.y >> 16;
+  }
+  R x[NC][3], u[NC][3];
+#pragma unroll
+  for (int a = 0; a < NC; ++a) {
+    const int l = lc[a] < ns ? lc[a] : 0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      x[a][d] = shX[d * kMaxLocalNodes + l];
+      u[a][d] = shU[d * kMaxLocalNodes + l];
+    }
+  }
+  R Es[6] = {0, 0, 0, 0, 0, 0};
+  if (ET == 0) {
+    R hx[7][3], hu[7][3];
+    hex_hadamard(reinterpret_cast<const R(&)[8][3]>(x), hx);
+    hex_hadamard(reinterpret_cast<const R(&)[8][3]>(u), hu);
+    const R G = R(0.577350269189626);
+#pragma unroll 1
+    for (int g = 0; g < 8; ++g) {  // Gauss points as in hex_element
+      const R xi = ((g + 1) & 2) ? G : -G, et = (g & 2) ? G : -G, ze = g < 4 ? G : -G;
+      const R ez = et * ze, xz = xi * ze, xe = xi * et;
+      R Am[3][3], H[3][3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        Am[0][d] = hx[0][d] + et * hx[3][d] + ze * hx[4][d] + ez * hx[6][d];
+        Am[1][d] = hx[1][d] + xi * hx[3][d] + ze * hx[5][d] + xz * hx[6][d];
+        Am[2][d] = hx[2][d] + xi * hx[4][d] + et * hx[5][d] + xe * hx[6][d];
+        H[d][0] = hu[0][d] + et * hu[3][d] + ze * hu[4][d] + ez * hu[6][d];
+        H[d][1] = hu[1][d] + xi * hu[3][d] + ze * hu[5][d] + xz * hu[6][d];
+        H[d][2] = hu[2][d] + xi * hu[4][d] + et * hu[5][d] + xe * hu[6][d];
+      }
+      R Ad[3][3], detA;
+      adj3(Am, Ad, detA);
+      const R idet = 1 / detA;
+      R D[3][3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+          D[i][j] = idet * (H[i][0] * Ad[j][0] + H[i][1] * Ad[j][1] + H[i][2] * Ad[j][2]);
+      R E[6];
+      green_strain(D, E);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) Es[k] += E[k];
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) Es[k] *= R(0.125);
+  } else {
+    R Am[3][3], H[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        Am[r][d] = x[r][d] - x[3][d];
+        H[d][r] = u[r][d] - u[3][d];
+      }
+    R Ad[3][3], detA;
+    adj3(Am, Ad, detA);
+    const R idet = 1 / detA;
+    R D[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        D[i][j] = idet * (H[i][0] * Ad[j][0] + H[i][1] * Ad[j][1] + H[i][2] * Ad[j][2]);
+    green_strain(D, Es);
+  }
+#pragma unroll
+  for (int k = 0; k < 6; ++k) Eout[6 * (long long)e + k] = double(Es[k]);
+}
+
 template <class R>
 size_t elem_smem_bytes(int ET, int PE) {
   const int NC = ET == 0 ? 8 : 4;

@@ -29,6 +29,16 @@ static int by_mat(int mat, int gp, int nb, int th, size_t sm, cudaStream_t s,
   }
 }
 
+int launch_strain_f32(int etype, int nblocks, int threads, size_t smem, cudaStream_t s,
+                      const ElemArgs<float> &A, double *Eout) {
+  if (nblocks <= 0) return 0;
+  if (etype == 0)
+    k_elem_strain<float, 0><<<nblocks, threads, smem, s>>>(A, Eout);
+  else
+    k_elem_strain<float, 1><<<nblocks, threads, smem, s>>>(A, Eout);
+  return (int)cudaGetLastError();
+}
+
 int launch_elem_f32(int etype, int mat, int gp, int nblocks, int threads, size_t smem,
                     cudaStream_t s, const ElemArgs<float> &A, int dt_only) {
   if (nblocks <= 0) return 0;

@@ -29,6 +29,16 @@ static int by_mat(int mat, int gp, int nb, int th, size_t sm, cudaStream_t s,
   }
 }
 
+int launch_strain_f64(int etype, int nblocks, int threads, size_t smem, cudaStream_t s,
+                      const ElemArgs<double> &A, double *Eout) {
+  if (nblocks <= 0) return 0;
+  if (etype == 0)
+    k_elem_strain<double, 0><<<nblocks, threads, smem, s>>>(A, Eout);
+  else
+    k_elem_strain<double, 1><<<nblocks, threads, smem, s>>>(A, Eout);
+  return (int)cudaGetLastError();
+}
+
 int launch_elem_f64(int etype, int mat, int gp, int nblocks, int threads, size_t smem,
                     cudaStream_t s, const ElemArgs<double> &A, int dt_only) {
   if (nblocks <= 0) return 0;

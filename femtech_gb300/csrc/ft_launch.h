@@ -15,6 +15,26 @@ int launch_elem_f32(int etype, int mat, int gp, int nblocks, int threads, size_t
 int launch_elem_f64(int etype, int mat, int gp, int nblocks, int threads, size_t smem,
                     cudaStream_t s, const ElemArgs<double> &A, int dt_only);
 
+// Element strain pass (k_elem_strain) of one group: Voigt Green strain per
+// element into Eout (group order).  Returns a cudaError_t value.
+int launch_strain_f32(int etype, int nblocks, int threads, size_t smem, cudaStream_t s,
+                      const ElemArgs<float> &A, double *Eout);
+int launch_strain_f64(int etype, int nblocks, int threads, size_t smem, cudaStream_t s,
+                      const ElemArgs<double> &A, double *Eout);
+template <class R>
+inline int launch_strain(int etype, int nblocks, int threads, size_t smem, cudaStream_t s,
+                         const ElemArgs<R> &A, double *Eout);
+template <>
+inline int launch_strain<float>(int etype, int nblocks, int threads, size_t smem, cudaStream_t s,
+                                const ElemArgs<float> &A, double *Eout) {
+  return launch_strain_f32(etype, nblocks, threads, smem, s, A, Eout);
+}
+template <>
+inline int launch_strain<double>(int etype, int nblocks, int threads, size_t smem,
+                                 cudaStream_t s, const ElemArgs<double> &A, double *Eout) {
+  return launch_strain_f64(etype, nblocks, threads, smem, s, A, Eout);
+}
+
 // Dynamic shared memory of one element block: node X and u for
 // kMaxLocalNodes slots plus NC*3 corner forces per element.
 template <class R>

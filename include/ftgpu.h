@@ -187,6 +187,18 @@ int ftgpu_launches_per_step(ftgpu_model *m);
 /* Synchronise and return the device error word (0 = none). */
 int ftgpu_check(ftgpu_model *m);
 
+/* ---- element strain (output steps) ----
+ * CalculateStrain() + CalculateMaximumPrincipalStrain()
+ * (src/elements/ElementCalculations/CalculateStrain.cpp:8-97) on the model's
+ * current displacements: per element the Gauss-point average of the
+ * Green-Lagrange strain Eavg[9*e .. 9*e+8] (column-major 3x3, the layout of
+ * the reference's Eavg global that WriteVTU writes), the largest principal
+ * strain clamped at >= 0, the smallest clamped at <= 0 and the largest shear
+ * strain (max - min) / 2, in the reference's element order.  Any output may
+ * be NULL. */
+int ftgpu_element_strain(ftgpu_model *m, double *Eavg, double *ps_max, double *ps_min,
+                         double *shear_max);
+
 /* ---- energy balance of the explicit loop ----
  * CheckEnergy() (src/fem/SolidMechanics/CheckEnergy.cpp:3-85), which every
  * example driver calls after each step (examples/ex9/ex9.cpp:154-156): per
