@@ -35,6 +35,20 @@ class FtgpuError(RuntimeError):
         self.status = status
 
 
+class Injury(C.Structure):
+    """ftgpu_injury: the running record of the injury criteria."""
+    _fields_ = [(k, C.c_double) for k in ("max_strain", "max_strain_time", "min_strain",
+                                           "min_strain_time", "max_shear", "max_shear_time",
+                                           "max_psxsr", "max_psxsr_time")] + \
+               [(k, C.c_int) for k in ("max_strain_elem", "min_strain_elem", "max_shear_elem",
+                                        "max_psxsr_elem")] + \
+               [(k, C.c_double) for k in ("mps95", "mps95_time", "mpsxsr95", "mpsxsr95_time")] + \
+               [("mps95_count", C.c_int), ("mpsxsr95_count", C.c_int), ("steps", C.c_longlong)]
+
+
+INJ_MPS15, INJ_MPS30, INJ_PSR120, INJ_PSXSR28, INJ_MPS95, INJ_PSXSR95 = 1, 2, 4, 8, 16, 32
+
+
 class BcFn(C.Structure):
     _fields_ = [("kind", C.c_int), ("pad", C.c_int), ("p", C.c_double * 8)]
 
@@ -244,6 +258,28 @@ class Model:
         E9, mx, mn, sh = np.zeros(9 * self.nE), np.zeros(self.nE), np.zeros(self.nE), np.zeros(self.nE)
         _check(L.ftgpu_element_strain(self.h, E9, mx, mn, sh))
         return E9.reshape(-1, 9), mx, mn, sh
+
+    def set_injury(self, element_ids):
+        """Per-step injury criteria (ex5's CalculateInjuryCriterions) over these
+        elements (call before init_explicit; an empty list turns them off)."""
+        L = lib()
+        L.ftgpu_set_injury.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        ids = np.ascontiguousarray(element_ids, np.int32)
+        self._inj_n = len(ids)
+        _check(L.ftgpu_set_injury(self.h, len(ids), ids.ctypes.data if len(ids) else None))
+
+    def injury(self):
+        """The record (dict), per listed element the flag bits and the last MPS."""
+        L = lib()
+        L.ftgpu_get_injury.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        rec = Injury()
+        n = self._inj_n
+        flags, ps = np.zeros(n, np.int32), np.zeros(n)
+        _check(L.ftgpu_get_injury(self.h, C.byref(rec), flags.ctypes.data, ps.ctypes.data))
+        out = {k: getattr(rec, k) for k, _ in Injury._fields_}
+        out["flags"] = flags
+        out["ps"] = ps
+        return out
 
     def set_energy(self, enable=True):
         """Track CheckEnergy's balance in the device loop (call before init_explicit)."""

@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "ft_common.h"
+#include "ft_injury.cuh"
 #include "ft_launch.h"
 #include "ft_node.cuh"
 #include "ft_patches.h"
@@ -211,6 +212,11 @@ struct ftgpu_model {
   DBuf clock, dtmin, err, instp;
   DBuf stepsc, rottrig;  // per-instance step scalars / rotation trigonometry
   DBuf stage;            // AoS staging of host <-> device state copies
+  // injury criteria of the brain drivers (single instance only)
+  bool injury_on = false;
+  int inj_n = 0;
+  DBuf inj_elem_g, inj_elem_ref, inj_E6, inj_ps_old, inj_psxsr, inj_flags, inj_part, inj_state,
+      inj_hist;
   // energy balance of the explicit loop (CheckEnergy), single instance only
   bool energy_on = false;
   DBuf du, fprev, epart, estate;
@@ -789,6 +795,54 @@ int ensure_gp(ftgpu_model *m) {
 // One chunk: BEGIN, K x (element groups, node), the last node pass FINISH.
 // With prof, event-record nodes bracket every element pass and node pass
 // (events 2k / 2k+1 / 2k+2 around step k).
+constexpr int kInjHistWords = 2 * 8 * kRadixBins + 2;  // histograms + two counters
+
+template <class R>
+InjuryArgs<R> injury_args(ftgpu_model *m, int parity) {
+  InjuryArgs<R> A;
+  A.elem_g = m->inj_elem_g.as<int>();
+  A.elem_ref = m->inj_elem_ref.as<int>();
+  A.E6 = m->inj_E6.as<double>();
+  A.ps_old = m->inj_ps_old.as<R>();
+  A.psxsr = m->inj_psxsr.as<R>();
+  A.flags = m->inj_flags.as<uint8_t>();
+  A.part = m->inj_part.as<InjuryPart>();
+  A.state = m->inj_state.as<InjuryState>();
+  A.clock = m->clock.as<Clock>();
+  A.hist = m->inj_hist.as<unsigned>();
+  A.count = A.hist + 2 * 8 * kRadixBins;
+  A.n = m->inj_n;
+  A.parity = parity;
+  return A;
+}
+
+// One step of the injury criteria, between the element pass and the nodal
+// update (the slots still hold this step's displacements): element strain,
+// per-element update, the step's extremes, two radix selections.
+template <class R>
+int launch_injury_t(ftgpu_model *m, int parity) {
+  const InjuryArgs<R> A = injury_args<R>(m, parity);
+  int r = strain_groups_t<R>(m, m->inj_E6.as<double>());
+  if (r) return r;
+  const int nb = (m->inj_n + kInjThreads - 1) / kInjThreads;
+  k_injury_update<R><<<nb, kInjThreads, 0, m->stream>>>(A);
+  k_injury_reduce<R><<<1, 32, 0, m->stream>>>(A, nb);
+  CK(cudaMemsetAsync(m->inj_hist.p, 0, kInjHistWords * sizeof(unsigned), m->stream));
+  const int hb = std::min(nb, 1024);
+  for (int sel = 0; sel < 2; ++sel) {
+    for (int pass = 0; pass < (int)sizeof(R); ++pass)
+      k_radix_hist<R><<<hb, kInjThreads, 0, m->stream>>>(A, sel, pass);
+    k_radix_list<R><<<hb, kInjThreads, 0, m->stream>>>(A, sel);
+  }
+  k_radix_final<R><<<1, 32, 0, m->stream>>>(A);
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int launch_injury(ftgpu_model *m, int parity) {
+  return is_fp64(m) ? launch_injury_t<double>(m, parity) : launch_injury_t<float>(m, parity);
+}
+
 int capture_chunk(ftgpu_model *m, int K, bool prof) {
   cudaGraphExec_t &exec = prof ? m->prof_exec : m->chunk_exec;
   int &steps = prof ? m->prof_steps : m->chunk_steps;
@@ -808,6 +862,7 @@ int capture_chunk(ftgpu_model *m, int K, bool prof) {
     if (!r) r = launch_groups(m, k & 1, 1, 0.0, 0, 0);
     if (prof && !r)
       r = (int)cudaEventRecordWithFlags(m->prof_ev[2 * k + 1], m->stream, cudaEventRecordExternal);
+    if (!r && m->injury_on) r = launch_injury(m, k & 1);
     if (!r) r = launch_node(m, k == K - 1 ? kNodeFinish : kNodeFused, k & 1);
   }
   if (prof && !r) r = (int)cudaEventRecordWithFlags(m->prof_ev[2 * K], m->stream, cudaEventRecordExternal);
@@ -1192,6 +1247,13 @@ int ftgpu_init_explicit(ftgpu_model *m, double reduction, double failure_dt, dou
       m->ninst, m->t0);
   CK(cudaGetLastError());
   CKI(launch_groups(m, 0, 1, 0.0, 0, 0));
+  if (m->injury_on) {  // the injury state starts from zero with the loop
+    const size_t rb = is_fp64(m) ? sizeof(double) : sizeof(float);
+    CK(cudaMemsetAsync(m->inj_ps_old.p, 0, m->inj_n * rb, m->stream));
+    CK(cudaMemsetAsync(m->inj_psxsr.p, 0, m->inj_n * rb, m->stream));
+    CK(cudaMemsetAsync(m->inj_flags.p, 0, m->inj_n, m->stream));
+    CK(cudaMemsetAsync(m->inj_state.p, 0, sizeof(InjuryState), m->stream));
+  }
   if (m->energy_on) {  // CheckEnergy's works start from zero with the loop
     CK(cudaMemsetAsync(m->du.p, 0, m->du.bytes, m->stream));
     CK(cudaMemsetAsync(m->estate.p, 0, sizeof(EnergyState), m->stream));
@@ -1264,7 +1326,13 @@ int ftgpu_launches_per_step(ftgpu_model *m) {
   // feature pass and the inference kernel of each material-7 group
   if (m->surr)
     for (auto &x : m->ps.groups) g += 2 * (x.npatch > 0 && x.mat == 7);
-  return g + 2 + (m->energy_on ? 1 : 0);  // + k_energy_reduce
+  int inj = 0;
+  if (m->injury_on) {  // strain groups, update, reduce, memset, 2 x (passes + list), final
+    int sg = 0;
+    for (auto &x : m->ps.groups) sg += x.npatch > 0;
+    inj = sg + 3 + 2 * ((is_fp64(m) ? 8 : 4) + 1) + 1;
+  }
+  return g + 2 + (m->energy_on ? 1 : 0) + inj;  // + k_energy_reduce
 }
 
 int ftgpu_element_strain(ftgpu_model *m, double *Eavg, double *ps_max, double *ps_min,
@@ -1293,6 +1361,73 @@ int ftgpu_element_strain(ftgpu_model *m, double *Eavg, double *ps_max, double *p
     if (ps_max) ps_max[e] = r[9];
     if (ps_min) ps_min[e] = r[10];
     if (shear_max) shear_max[e] = r[11];
+  }
+  return FTGPU_OK;
+}
+
+static_assert(sizeof(ftgpu_injury) == sizeof(InjuryState), "injury record layout");
+
+int ftgpu_set_injury(ftgpu_model *m, int n, const int *element_ids) {
+  if (!m || !m->setup_done) return fail(FTGPU_ERR_STATE, "set_injury before setup");
+  CK(cudaSetDevice(m->device));
+  CK(cudaStreamSynchronize(m->stream));
+  drop_graphs(m);
+  m->init_done = false;  // the loop must start again from init_explicit
+  if (n <= 0) {
+    m->injury_on = false;
+    m->inj_n = 0;
+    return FTGPU_OK;
+  }
+  if (!element_ids) return fail(FTGPU_ERR_INPUT, "set_injury: no element list");
+  if (m->ninst != 1)
+    return fail(FTGPU_ERR_INPUT, "injury criteria are kept for single-instance models");
+  const int E = m->nE;
+  std::vector<int> g_of(E), eg(n);
+  for (int ge = 0; ge < E; ++ge) g_of[m->ps.elem_order[ge]] = ge;
+  for (int j = 0; j < n; ++j) {
+    if (element_ids[j] < 0 || element_ids[j] >= E)
+      return fail(FTGPU_ERR_INPUT, "set_injury: element id out of range");
+    eg[j] = g_of[element_ids[j]];
+  }
+  const size_t rb = is_fp64(m) ? sizeof(double) : sizeof(float);
+  const int nb = (n + kInjThreads - 1) / kInjThreads;
+  CKI(m->inj_elem_g.upload(eg.data(), n));
+  CKI(m->inj_elem_ref.upload(element_ids, n));
+  CKI(m->inj_E6.alloc(6 * (size_t)E * sizeof(double)));
+  CKI(m->inj_ps_old.alloc(n * rb));
+  CKI(m->inj_psxsr.alloc(n * rb));
+  CKI(m->inj_flags.alloc(n));
+  CKI(m->inj_part.alloc(nb * sizeof(InjuryPart)));
+  CKI(m->inj_state.alloc(sizeof(InjuryState)));
+  CKI(m->inj_hist.alloc(kInjHistWords * sizeof(unsigned)));
+  CK(cudaMemset(m->inj_ps_old.p, 0, n * rb));
+  CK(cudaMemset(m->inj_psxsr.p, 0, n * rb));
+  CK(cudaMemset(m->inj_flags.p, 0, n));
+  CK(cudaMemset(m->inj_state.p, 0, sizeof(InjuryState)));
+  m->inj_n = n;
+  m->injury_on = true;
+  return FTGPU_OK;
+}
+
+int ftgpu_get_injury(ftgpu_model *m, ftgpu_injury *out, int *flags, double *ps) {
+  if (!m || !m->injury_on) return fail(FTGPU_ERR_STATE, "injury criteria are off");
+  CK(cudaSetDevice(m->device));
+  CK(cudaStreamSynchronize(m->stream));
+  if (out) CK(cudaMemcpy(out, m->inj_state.p, sizeof(ftgpu_injury), cudaMemcpyDeviceToHost));
+  const int n = m->inj_n;
+  if (flags) {
+    std::vector<uint8_t> f(n);
+    CK(cudaMemcpy(f.data(), m->inj_flags.p, n, cudaMemcpyDeviceToHost));
+    for (int j = 0; j < n; ++j) flags[j] = f[j];
+  }
+  if (ps) {
+    if (is_fp64(m)) {
+      CK(cudaMemcpy(ps, m->inj_ps_old.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+    } else {
+      std::vector<float> v(n);
+      CK(cudaMemcpy(v.data(), m->inj_ps_old.p, n * sizeof(float), cudaMemcpyDeviceToHost));
+      for (int j = 0; j < n; ++j) ps[j] = v[j];
+    }
   }
   return FTGPU_OK;
 }

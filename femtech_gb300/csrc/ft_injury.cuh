@@ -1,0 +1,314 @@
+// ft_injury.cuh -- per-step injury criteria of the brain drivers on the GPU
+// (examples/ex5/ex5.cpp:1311-1430, CalculateInjuryCriterions): principal
+// strains of the listed elements, running extremes, sticky threshold flags and
+// the largest 95th percentiles of MPS and of MPS x strain rate, by an exact
+// radix selection.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <type_traits>
+
+#include "ft_common.h"
+
+namespace ftgpu {
+
+// running state (FP64 values; element ids are the reference's)
+struct InjuryState {
+  double max_strain, max_strain_time, min_strain, min_strain_time;
+  double max_shear, max_shear_time, max_psxsr, max_psxsr_time;
+  int max_strain_elem, min_strain_elem, max_shear_elem, max_psxsr_elem;
+  double mps95, mps95_time, mpsxsr95, mpsxsr95_time;
+  int mps95_count, mpsxsr95_count;
+  long long steps;
+};
+
+// flags per injury element (bits)
+enum { kInjMps15 = 1, kInjMps30 = 2, kInjPsr120 = 4, kInjPsxsr28 = 8, kInjInMps95 = 16,
+       kInjInMpsxsr95 = 32 };
+
+// per-block partial extremes of one step: value and the smallest list index
+struct InjuryPart {
+  double v[4];  // max strain, min strain, max shear, max psxsr
+  int j[4];
+};
+
+constexpr int kInjThreads = 256;
+constexpr int kRadixBins = 256;
+
+template <class R>
+struct InjuryArgs {
+  const int *elem_g;     // [n] group-order index of each listed element
+  const int *elem_ref;   // [n] reference element id
+  const double *E6;      // [E] Voigt averaged Green strain (group order)
+  R *ps_old, *psxsr;     // [n]
+  uint8_t *flags;        // [n]
+  InjuryPart *part;      // [blocks]
+  InjuryState *state;
+  const Clock *clock;    // clock[0] of the step (single instance)
+  unsigned *hist;        // [2 selections][passes][256]
+  unsigned *count;       // [2] elements at or above a new maximum
+  int n, parity;
+};
+
+// principal strains of the symmetric strain in the trigonometric form of
+// CalculateStrain.cpp:38-74
+template <class T>
+__device__ __forceinline__ void principal_strains(T xx, T yy, T zz, T yz, T xz, T xy, T &mx,
+                                                  T &mn, T &sh) {
+  const T a = xx, b = xy, c = xz, d = yy, e = yz, f = zz;
+  const T p1 = b * b + c * c + e * e;
+  T e1, e2, e3;
+  if (p1 == T(0)) {
+    e1 = a;
+    e2 = d;
+    e3 = f;
+  } else {
+    T I1 = a + d + f;
+    const T I2 = a * (d + f) + d * f - b * b - c * c - e * e;
+    const T I3 = a * d * f + T(2) * b * c * e - b * b * f - c * c * d - e * e * a;
+    const T Q = (T(3) * I2 - I1 * I1) / T(9);
+    const T Rr = (T(2) * I1 * I1 * I1 - T(9) * I1 * I2 + T(27) * I3) / T(54);
+    const T theta = acos(Rr / sqrt(-Q * Q * Q));
+    const T sq = T(2) * sqrt(-Q);
+    const T kPi = T(3.141592653589793);
+    I1 = I1 / T(3);
+    e1 = sq * cos(theta / T(3)) + I1;
+    e2 = sq * cos((theta + T(2) * kPi) / T(3)) + I1;
+    e3 = sq * cos((theta + T(4) * kPi) / T(3)) + I1;
+  }
+  const T hi = fmax(e3, fmax(e2, e1)), lo = fmin(e3, fmin(e2, e1));
+  sh = T(0.5) * (hi - lo);
+  mx = hi > T(0) ? hi : T(0);
+  mn = lo < T(0) ? lo : T(0);
+}
+
+// order-preserving unsigned keys of floating-point values
+__device__ __forceinline__ uint32_t fkey(float x) {
+  const uint32_t b = __float_as_uint(x);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float fkey_inv(uint32_t k) {
+  return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+__device__ __forceinline__ uint64_t fkey(double x) {
+  const uint64_t b = (uint64_t)__double_as_longlong(x);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double fkey_inv(uint64_t k) {
+  return __longlong_as_double((long long)((k >> 63) ? (k & 0x7fffffffffffffffull) : ~k));
+}
+
+// One step of CalculateInjuryCriterions for every listed element, with the
+// block partial extremes.
+template <class R>
+__global__ void __launch_bounds__(kInjThreads) k_injury_update(const InjuryArgs<R> A) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const Clock ck = A.clock[A.parity];
+  const bool run = !ck.done;
+  double v[4] = {-1e300, 1e300, -1e300, -1e300};
+  int jj[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
+  if (run && j < A.n) {
+    const double *e = A.E6 + 6 * (long long)A.elem_g[j];
+    R mx, mn, sh;
+    principal_strains<R>(R(e[0]), R(e[1]), R(e[2]), R(e[3]), R(e[4]), R(e[5]), mx, mn, sh);
+    uint8_t f = A.flags[j];
+    if (mx > R(0.15)) f |= kInjMps15;
+    if (mx > R(0.30)) f |= kInjMps30;
+    const R psr = (mx - A.ps_old[j]) / R(ck.dt);
+    const R psxsr = mx * psr;
+    if (psr > R(120)) f |= kInjPsr120;
+    if (psxsr > R(28)) f |= kInjPsxsr28;
+    A.flags[j] = f;
+    A.ps_old[j] = mx;
+    A.psxsr[j] = psxsr;
+    v[0] = double(mx);
+    v[1] = double(mn);
+    v[2] = double(sh);
+    v[3] = double(psxsr);
+    jj[0] = jj[1] = jj[2] = jj[3] = j;
+  }
+  // block extremes: best value, then smallest list index
+  __shared__ double sv[4][kInjThreads];
+  __shared__ int sj[4][kInjThreads];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    sv[k][threadIdx.x] = v[k];
+    sj[k][threadIdx.x] = jj[k];
+  }
+  __syncthreads();
+  for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const double a = sv[k][threadIdx.x], b = sv[k][threadIdx.x + h];
+        const int ja = sj[k][threadIdx.x], jb = sj[k][threadIdx.x + h];
+        const bool better = (k == 1) ? (b < a || (b == a && jb < ja)) : (b > a || (b == a && jb < ja));
+        if (better) {
+          sv[k][threadIdx.x] = b;
+          sj[k][threadIdx.x] = jb;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    InjuryPart p;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      p.v[k] = sv[k][0];
+      p.j[k] = sj[k][0];
+    }
+    A.part[blockIdx.x] = p;
+  }
+}
+
+// The step's extremes from the block partials (blocks in order) into the
+// running state: a strictly better value takes the element and the time
+// (the reference's ordered loop with strict comparisons).
+template <class R>
+__global__ void k_injury_reduce(const InjuryArgs<R> A, int nblocks) {
+  if (threadIdx.x != 0) return;
+  const Clock ck = A.clock[A.parity];
+  if (ck.done) return;
+  const double t = ck.time + ck.dt;
+  double v[4] = {-1e300, 1e300, -1e300, -1e300};
+  int jj[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
+  for (int b = 0; b < nblocks; ++b) {
+    const InjuryPart p = A.part[b];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const bool better = (k == 1) ? (p.v[k] < v[k] || (p.v[k] == v[k] && p.j[k] < jj[k]))
+                                   : (p.v[k] > v[k] || (p.v[k] == v[k] && p.j[k] < jj[k]));
+      if (better) {
+        v[k] = p.v[k];
+        jj[k] = p.j[k];
+      }
+    }
+  }
+  InjuryState s = *A.state;
+  if (jj[0] < A.n && s.max_strain < v[0]) {
+    s.max_strain = v[0];
+    s.max_strain_elem = A.elem_ref[jj[0]];
+    s.max_strain_time = t;
+  }
+  if (jj[1] < A.n && s.min_strain > v[1]) {
+    s.min_strain = v[1];
+    s.min_strain_elem = A.elem_ref[jj[1]];
+    s.min_strain_time = t;
+  }
+  if (jj[2] < A.n && s.max_shear < v[2]) {
+    s.max_shear = v[2];
+    s.max_shear_elem = A.elem_ref[jj[2]];
+    s.max_shear_time = t;
+  }
+  if (jj[3] < A.n && s.max_psxsr < v[3]) {
+    s.max_psxsr = v[3];
+    s.max_psxsr_elem = A.elem_ref[jj[3]];
+    s.max_psxsr_time = t;
+  }
+  ++s.steps;
+  *A.state = s;
+}
+
+// Radix selection of the value of rank k = (int)(0.95 n) - 1 (rank 0 if
+// negative) of sel = 0: ps_old, 1: psxsr, 8 bits per pass from the most
+// significant byte.  Every pass first recovers the digits fixed so far by
+// scanning the histograms of the previous passes (the same in every block).
+template <class K>
+__device__ __forceinline__ void radix_prefix(const unsigned *hist, int pass, int n, K &prefix,
+                                             unsigned &krem) {
+  int k = (int)(n * 0.95) - 1;
+  if (k < 0) k = 0;
+  krem = (unsigned)k;
+  prefix = 0;
+  constexpr int KB = sizeof(K) * 8;
+  for (int q = 0; q < pass; ++q) {
+    const unsigned *h = hist + q * kRadixBins;
+    unsigned below = 0;
+    int d = 0;
+    for (; d < kRadixBins; ++d) {
+      if (below + h[d] > krem) break;
+      below += h[d];
+    }
+    krem -= below;
+    prefix |= (K)d << (KB - 8 * (q + 1));
+  }
+}
+
+template <class R>
+__global__ void __launch_bounds__(kInjThreads) k_radix_hist(const InjuryArgs<R> A, int sel,
+                                                            int pass) {
+  typedef typename std::conditional<sizeof(R) == 8, uint64_t, uint32_t>::type K;
+  constexpr int KB = sizeof(K) * 8;
+  if (A.clock[A.parity].done) return;
+  unsigned *hist = A.hist + (sel * (KB / 8)) * kRadixBins;
+  __shared__ unsigned sh[kRadixBins];
+  for (int i = threadIdx.x; i < kRadixBins; i += blockDim.x) sh[i] = 0;
+  K prefix;
+  unsigned krem;
+  radix_prefix<K>(hist, pass, A.n, prefix, krem);
+  __syncthreads();
+  const R *val = sel == 0 ? A.ps_old : A.psxsr;
+  const K mask = pass == 0 ? K(0) : (K)(~K(0)) << (KB - 8 * pass);
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < A.n; j += gridDim.x * blockDim.x) {
+    const K key = fkey(val[j]);
+    if ((key & mask) == prefix) atomicAdd(&sh[(key >> (KB - 8 * (pass + 1))) & 0xffu], 1u);
+  }
+  __syncthreads();
+  unsigned *out = hist + pass * kRadixBins;
+  for (int i = threadIdx.x; i < kRadixBins; i += blockDim.x)
+    if (sh[i]) atomicAdd(&out[i], sh[i]);
+}
+
+// The selected value; where it beats the running maximum, the listed elements
+// at or above it are marked (flag bit) and counted.
+template <class R>
+__global__ void __launch_bounds__(kInjThreads) k_radix_list(const InjuryArgs<R> A, int sel) {
+  typedef typename std::conditional<sizeof(R) == 8, uint64_t, uint32_t>::type K;
+  constexpr int KB = sizeof(K) * 8;
+  if (A.clock[A.parity].done) return;
+  K prefix;
+  unsigned krem;
+  radix_prefix<K>(A.hist + (sel * (KB / 8)) * kRadixBins, KB / 8, A.n, prefix, krem);
+  const R v = fkey_inv(prefix);
+  const double prev = sel == 0 ? A.state->mps95 : A.state->mpsxsr95;
+  if (!(double(v) > prev)) return;
+  const R *val = sel == 0 ? A.ps_old : A.psxsr;
+  const uint8_t bit = sel == 0 ? kInjInMps95 : kInjInMpsxsr95;
+  unsigned cnt = 0;
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < A.n; j += gridDim.x * blockDim.x) {
+    const bool in = val[j] >= v;
+    A.flags[j] = in ? (A.flags[j] | bit) : (A.flags[j] & (uint8_t)~bit);
+    cnt += in;
+  }
+  if (cnt) atomicAdd(&A.count[sel], cnt);
+}
+
+// Running maxima of the two percentiles (after k_radix_list of both).
+template <class R>
+__global__ void k_radix_final(const InjuryArgs<R> A) {
+  typedef typename std::conditional<sizeof(R) == 8, uint64_t, uint32_t>::type K;
+  constexpr int KB = sizeof(K) * 8;
+  if (threadIdx.x != 0) return;
+  const Clock ck = A.clock[A.parity];
+  if (ck.done) return;
+  const double t = ck.time + ck.dt;
+  InjuryState s = *A.state;
+  for (int sel = 0; sel < 2; ++sel) {
+    K prefix;
+    unsigned krem;
+    radix_prefix<K>(A.hist + (sel * (KB / 8)) * kRadixBins, KB / 8, A.n, prefix, krem);
+    const double v = double(fkey_inv(prefix));
+    double &mx = sel == 0 ? s.mps95 : s.mpsxsr95;
+    if (v > mx) {
+      mx = v;
+      (sel == 0 ? s.mps95_time : s.mpsxsr95_time) = t;
+      (sel == 0 ? s.mps95_count : s.mpsxsr95_count) = (int)A.count[sel];
+    }
+  }
+  *A.state = s;
+}
+
+}  // namespace ftgpu

@@ -199,6 +199,35 @@ int ftgpu_check(ftgpu_model *m);
 int ftgpu_element_strain(ftgpu_model *m, double *Eavg, double *ps_max, double *ps_min,
                          double *shear_max);
 
+/* ---- per-step injury criteria (brain drivers) ----
+ * CalculateInjuryCriterions (examples/ex5/ex5.cpp:1311-1430), called after
+ * every step of the brain drivers, for the elements element_ids[0..n)
+ * (elementIDInjury of ex5.cpp:1248-1280): principal strains of each listed
+ * element (CalculateMaximumPrincipalStrain), running extremes with element and
+ * time, sticky flags, and the largest 95th percentiles of the maximum
+ * principal strain (MPS95) and of MPS x its rate, with the elements at or above
+ * them when each maximum was set.  PS_Old starts at 0.  Kept on the device
+ * inside the loop; set after ftgpu_setup, before ftgpu_init_explicit (it
+ * resets the loop); n = 0 turns it off.  Single-instance models only. */
+typedef struct ftgpu_injury {
+  double max_strain, max_strain_time, min_strain, min_strain_time;
+  double max_shear, max_shear_time, max_psxsr, max_psxsr_time;
+  int max_strain_elem, min_strain_elem, max_shear_elem, max_psxsr_elem;
+  double mps95, mps95_time, mpsxsr95, mpsxsr95_time;
+  int mps95_count, mpsxsr95_count;
+  long long steps;
+} ftgpu_injury;
+#define FTGPU_INJ_MPS15 1    /* MPS > 0.15 at some step (CSDM-15)   */
+#define FTGPU_INJ_MPS30 2    /* MPS > 0.30 (CSDM-30)                 */
+#define FTGPU_INJ_PSR120 4   /* MPS rate > 120 /s                    */
+#define FTGPU_INJ_PSXSR28 8  /* MPS x rate > 28 /s                   */
+#define FTGPU_INJ_MPS95 16   /* in the MPS95 element list            */
+#define FTGPU_INJ_PSXSR95 32 /* in the MPS x rate 95 element list    */
+int ftgpu_set_injury(ftgpu_model *m, int n, const int *element_ids);
+/* the record, per listed element the flag bits above and the last MPS;
+ * any output may be NULL */
+int ftgpu_get_injury(ftgpu_model *m, ftgpu_injury *out, int *flags, double *mps);
+
 /* ---- energy balance of the explicit loop ----
  * CheckEnergy() (src/fem/SolidMechanics/CheckEnergy.cpp:3-85), which every
  * example driver calls after each step (examples/ex9/ex9.cpp:154-156): per

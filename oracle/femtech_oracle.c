@@ -821,6 +821,88 @@ void or_element_strain(const or_model *m, double *Eavg9, double *ps_max, double 
   }
 }
 
+static int cmp_double(const void *a, const void *b) {
+  const double x = *(const double *)a, y = *(const double *)b;
+  return x < y ? -1 : (x > y ? 1 : 0);
+}
+
+double or_percentile95(const double *data, int n) {
+  if (n <= 0) return 0.0;
+  double *c = (double *)malloc(n * sizeof(double));
+  memcpy(c, data, n * sizeof(double));
+  qsort(c, n, sizeof(double), cmp_double);
+  int k = (int)(n * 0.95) - 1;
+  if (k < 0) k = 0;
+  const double v = c[k];
+  free(c);
+  return v;
+}
+
+/* ex5.cpp:1311-1430 on one rank; PS_Old starts at 0 (the driver leaves it
+ * uninitialised before the first call) */
+void or_injury_step(const or_model *m, or_injury *s, double time, double dt) {
+  const int nE = m->nelements;
+  double *mx = (double *)malloc(nE * sizeof(double));
+  double *mn = (double *)malloc(nE * sizeof(double));
+  double *sh = (double *)malloc(nE * sizeof(double));
+  or_element_strain(m, NULL, mx, mn, sh);
+  for (int j = 0; j < s->n; ++j) {
+    const int i = s->ids[j];
+    const double cmax = mx[i], cmin = mn[i], cshear = sh[i];
+    if (s->max_strain < cmax) {
+      s->max_strain = cmax;
+      s->max_strain_elem = i;
+      s->max_strain_time = time;
+    }
+    if (s->min_strain > cmin) {
+      s->min_strain = cmin;
+      s->min_strain_elem = i;
+      s->min_strain_time = time;
+    }
+    if (s->max_shear < cshear) {
+      s->max_shear = cshear;
+      s->max_shear_elem = i;
+      s->max_shear_time = time;
+    }
+    if (!s->mps15[j] && cmax > 0.15) s->mps15[j] = 1;
+    if (!s->mps30[j] && cmax > 0.30) s->mps30[j] = 1;
+    const double psr = (cmax - s->ps_old[j]) / dt;
+    const double psxsr = cmax * psr;
+    if (s->max_psxsr < psxsr) {
+      s->max_psxsr = psxsr;
+      s->max_psxsr_elem = i;
+      s->max_psxsr_time = time;
+    }
+    if (!s->psr120[j] && psr > 120.0) s->psr120[j] = 1;
+    if (!s->psxsr28[j] && psxsr > 28.0) s->psxsr28[j] = 1;
+    s->ps_old[j] = cmax;
+    s->psxsr[j] = psxsr;
+  }
+  const double mps95 = or_percentile95(s->ps_old, s->n);
+  if (mps95 > s->mps95) {
+    s->mps95 = mps95;
+    s->mps95_time = time;
+    s->mps95_count = 0;
+    for (int j = 0; j < s->n; ++j) {
+      s->in_mps95[j] = s->ps_old[j] >= mps95;
+      s->mps95_count += s->in_mps95[j];
+    }
+  }
+  const double x95 = or_percentile95(s->psxsr, s->n);
+  if (x95 > s->mpsxsr95) {
+    s->mpsxsr95 = x95;
+    s->mpsxsr95_time = time;
+    s->mpsxsr95_count = 0;
+    for (int j = 0; j < s->n; ++j) {
+      s->in_mpsxsr95[j] = s->psxsr[j] >= x95;
+      s->mpsxsr95_count += s->in_mpsxsr95[j];
+    }
+  }
+  free(mx);
+  free(mn);
+  free(sh);
+}
+
 int or_explicit_run(or_model *m, const int *dof_fn, const or_bc_fn *fns, int nfn,
                     double t0, double tMax, double reduction, double failure_dt,
                     int max_steps, int out_every, double *u, double *v, double *a,
@@ -891,6 +973,7 @@ int or_explicit_run(or_model *m, const int *dof_fn, const or_bc_fn *fns, int nfn
       m->energy[3 * step + 1] = Wext;
       m->energy[3 * step + 2] = 0.5 * wke;
     }
+    if (m->injury) or_injury_step(m, m->injury, Time, dt_nphalf);  /* ex5.cpp:238-240 */
     ++step;
     if (out_every > 0 && step % out_every == 0 && *n_out < max_out) {
       memcpy(u_out + (size_t)(*n_out) * nDOF, u, nDOF * sizeof(double));

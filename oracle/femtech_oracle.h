@@ -43,6 +43,24 @@ typedef struct or_bc_fn {
   double p[8];
 } or_bc_fn;
 
+/* Per-step injury criteria of the brain drivers (examples/ex5/ex5.cpp:
+ * 1311-1430, CalculateInjuryCriterions) for the elements ids[0..n): running
+ * extremes of the principal strains (value, element, time), sticky flags
+ * MPS > 0.15 / 0.30, principal strain rate > 120 /s, MPS x rate > 28 /s, and
+ * the largest 95th percentiles of MPS and of MPS x rate with the elements at
+ * or above them.  The caller owns every array (n entries each). */
+typedef struct or_injury {
+  int n;
+  const int *ids;
+  double *ps_old, *psxsr;
+  int *mps15, *mps30, *psr120, *psxsr28, *in_mps95, *in_mpsxsr95;
+  double max_strain, max_strain_time, min_strain, min_strain_time;
+  double max_shear, max_shear_time, max_psxsr, max_psxsr_time;
+  int max_strain_elem, min_strain_elem, max_shear_elem, max_psxsr_elem;
+  double mps95, mps95_time, mpsxsr95, mpsxsr95_time;
+  int mps95_count, mpsxsr95_count;
+} or_injury;
+
 typedef struct or_model {
   /* inputs, reference layout; owned by the caller */
   int nNodes, nelements, nPID;
@@ -68,6 +86,9 @@ typedef struct or_model {
    * (src/fem/SolidMechanics/CheckEnergy.cpp:3-85); NULL = not computed */
   double *energy;
   int energy_cap; /* steps the energy buffer holds (3 doubles each)    */
+  /* optional: injury criteria updated after every step of
+   * or_explicit_run (NULL = not computed) */
+  or_injury *injury;
 } or_model;
 
 int or_setup(or_model *m);
@@ -83,6 +104,11 @@ int or_explicit_run(or_model *m, const int *dof_fn, const or_bc_fn *fns, int nfn
                     int *steps_done, double *time_out, double *dt_out);
 void or_element_strain(const or_model *m, double *Eavg9, double *ps_max, double *ps_min,
                        double *shear_max);
+/* 95th percentile as compute95thPercentileValueBruteForce (math.cpp:160-196):
+ * the element of rank (int)(0.95 n) - 1 of the values (rank clamped at 0) */
+double or_percentile95(const double *data, int n);
+/* one call of CalculateInjuryCriterions on the F of the last or_get_force */
+void or_injury_step(const or_model *m, or_injury *s, double time, double dt);
 void or_apply_bc(const or_model *m, const int *dof_fn, const or_bc_fn *fns,
                  double t, double *u, double *v, double *a);
 void or_set_threads(or_model *m, int n);

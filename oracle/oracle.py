@@ -31,6 +31,50 @@ class BcFn(C.Structure):
     _fields_ = [("kind", C.c_int), ("pad", C.c_int), ("p", C.c_double * 8)]
 
 
+class _Injury(C.Structure):
+    _fields_ = [
+        ("n", C.c_int), ("ids", C.c_void_p), ("ps_old", C.c_void_p), ("psxsr", C.c_void_p),
+        ("mps15", C.c_void_p), ("mps30", C.c_void_p), ("psr120", C.c_void_p),
+        ("psxsr28", C.c_void_p), ("in_mps95", C.c_void_p), ("in_mpsxsr95", C.c_void_p),
+        ("max_strain", C.c_double), ("max_strain_time", C.c_double),
+        ("min_strain", C.c_double), ("min_strain_time", C.c_double),
+        ("max_shear", C.c_double), ("max_shear_time", C.c_double),
+        ("max_psxsr", C.c_double), ("max_psxsr_time", C.c_double),
+        ("max_strain_elem", C.c_int), ("min_strain_elem", C.c_int),
+        ("max_shear_elem", C.c_int), ("max_psxsr_elem", C.c_int),
+        ("mps95", C.c_double), ("mps95_time", C.c_double),
+        ("mpsxsr95", C.c_double), ("mpsxsr95_time", C.c_double),
+        ("mps95_count", C.c_int), ("mpsxsr95_count", C.c_int),
+    ]
+
+
+INJURY_SCALARS = ("max_strain", "max_strain_time", "max_strain_elem", "min_strain",
+                  "min_strain_time", "min_strain_elem", "max_shear", "max_shear_time",
+                  "max_shear_elem", "max_psxsr", "max_psxsr_time", "max_psxsr_elem", "mps95",
+                  "mps95_time", "mpsxsr95", "mpsxsr95_time", "mps95_count", "mpsxsr95_count")
+INJURY_ARRAYS = ("ps_old", "psxsr", "mps15", "mps30", "psr120", "psxsr28", "in_mps95",
+                 "in_mpsxsr95")
+
+
+def _injury_struct(ids):
+    ids = np.ascontiguousarray(ids, np.int32)
+    n = len(ids)
+    arrs = {k: np.zeros(n) for k in ("ps_old", "psxsr")}
+    arrs.update({k: np.zeros(n, np.int32) for k in INJURY_ARRAYS[2:]})
+    st = _Injury()
+    st.n = n
+    st.ids = ids.ctypes.data
+    for k, a in arrs.items():
+        setattr(st, k, a.ctypes.data)
+    return st, ids, arrs
+
+
+def _injury_result(st, arrs):
+    out = {k: getattr(st, k) for k in INJURY_SCALARS}
+    out.update({k: a.copy() for k, a in arrs.items()})
+    return out
+
+
 class _Model(C.Structure):
     _fields_ = [
         ("nNodes", C.c_int), ("nelements", C.c_int), ("nPID", C.c_int),
@@ -45,6 +89,7 @@ class _Model(C.Structure):
         ("hist", C.c_void_p), ("mass", C.c_void_p), ("fe", C.c_void_p), ("ce", C.c_void_p),
         ("nthreads", C.c_int),
         ("energy", C.c_void_p), ("energy_cap", C.c_int),
+        ("injury", C.c_void_p),
     ]
 
 
@@ -96,6 +141,8 @@ class Oracle:
                                           C.POINTER(C.c_int), C.POINTER(C.c_double),
                                           C.POINTER(C.c_double)]
             L.or_element_strain.argtypes = [M, _dp, _dp, _dp, _dp]
+            L.or_percentile95.argtypes = [_dp, C.c_int]
+            L.or_percentile95.restype = C.c_double
             L.or_set_threads.argtypes = [M, C.c_int]
             L.or_max_threads.restype = C.c_int
             cls._lib = L
@@ -178,10 +225,17 @@ class Oracle:
         return E9.reshape(-1, 9), mx, mn, sh
 
     def explicit_run(self, dof_fn, fns, tmax, reduction, max_steps, out_every, t0=0.0,
-                     failure_dt=0.0, u=None, v=None, a=None, max_out=None, energy=False):
+                     failure_dt=0.0, u=None, v=None, a=None, max_out=None, energy=False,
+                     injury_ids=None):
         """The ex9 loop; energy=True adds per step (Wint, Wext, WKE) of
-        CheckEnergy (cumulative works, kinetic energy) as result['energy']."""
+        CheckEnergy (cumulative works, kinetic energy) as result['energy'];
+        injury_ids adds the injury criteria of ex5 over those elements as
+        result['injury']."""
         n = 3 * self.nNodes
+        inj = None
+        if injury_ids is not None:
+            inj = _injury_struct(injury_ids)
+            self.m.injury = C.addressof(inj[0])
         ebuf = np.zeros(3 * max(max_steps, 1)) if energy else None
         self.m.energy = None if ebuf is None else ebuf.ctypes.data
         self.m.energy_cap = max_steps if energy else 0
@@ -201,16 +255,25 @@ class Oracle:
             max_out, C.byref(nout), C.byref(steps), C.byref(tt), C.byref(dd))
         self.m.energy = None
         self.m.energy_cap = 0
+        self.m.injury = None
         k = nout.value
         res = dict(rc=rc, u=u, v=v, a=a, u_out=uo[: k * n].reshape(k, n), t_out=to[:k],
                    steps=steps.value, time=tt.value, dt=dd.value)
         if energy:
             res["energy"] = ebuf.reshape(-1, 3)[: steps.value].copy()
+        if inj is not None:
+            res["injury"] = _injury_result(inj[0], inj[2])
         return res
 
 
 def _strain_outputs(nE):
     return np.zeros(9 * nE), np.zeros(nE), np.zeros(nE), np.zeros(nE)
+
+
+def percentile95(data):
+    """The oracle's 95th percentile (restating math.cpp:160-196)."""
+    d = np.ascontiguousarray(data, np.float64)
+    return Oracle.lib().or_percentile95(d, len(d))
 
 
 def material_stress(mat, props, F, J=None, a0=None, dt=0.0, hist=None):
@@ -257,6 +320,8 @@ class RefBuild:
             L.ref_stable_time_step.restype = C.c_double
             L.ref_set_energy_out.argtypes = [C.c_void_p, C.c_int]
             L.ref_element_strain.argtypes = [_dp, _dp, _dp, _dp]
+            L.ref_percentile95.argtypes = [_dp, C.c_int, C.POINTER(C.c_double),
+                                           C.POINTER(C.c_double)]
             L.ref_explicit_run.argtypes = [_ip, C.c_void_p, C.c_int, C.c_double, C.c_double,
                                            C.c_double, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp,
                                            C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
@@ -301,6 +366,17 @@ class RefBuild:
         if rc:
             raise RuntimeError("ref_get_force failed %d" % rc)
         return fi
+
+    @classmethod
+    def percentile95(cls, data):
+        """The reference's compute95thPercentileValueBruteForce and
+        compute95thPercentileValue (one rank) of the values."""
+        d = np.ascontiguousarray(data, np.float64).copy()
+        a, b = C.c_double(), C.c_double()
+        rc = cls.lib().ref_percentile95(d, len(d), C.byref(a), C.byref(b))
+        if rc:
+            raise RuntimeError("ref_percentile95 failed %d" % rc)
+        return a.value, b.value
 
     def element_strain(self):
         """The reference's CalculateMaximumPrincipalStrain on every element (F of

@@ -317,6 +317,18 @@ int ref_element_strain(double *Eavg9, double *ps_max, double *ps_min, double *sh
   }
 }
 
+/* The reference's 95th percentiles (math.cpp:160-196 and 198-325) of n values
+ * (one rank). */
+int ref_percentile95(double *data, int n, double *brute, double *parallel) {
+  try {
+    *brute = compute95thPercentileValueBruteForce(data, n);
+    *parallel = compute95thPercentileValue(data, n);
+    return 0;
+  } catch (RefTerminate &t) {
+    return -t.code;
+  }
+}
+
 /* Energy output of the next ref_explicit_run: per step the cumulative internal
  * and external work and the kinetic energy that the reference's own
  * CheckEnergy() logs (ex9.cpp:154-156 calls it after every step).  Its works

@@ -11,7 +11,9 @@ Fixtures:
                   reference on jittered C3D8 and C3D4 meshes, materials 1-5,
                   including three consecutive viscoelastic calls (material 5);
                   for material 1 also CalculateMaximumPrincipalStrain of every
-                  element (Eavg[9], max / min principal strain, max shear).
+                  element (Eavg[9], max / min principal strain, max shear);
+                  the 95th percentile (math.cpp, both implementations) of five
+                  seeded arrays (pct_data_i, pct_ref_i).
   ref_ex9.npz     examples/ex9 (one C3D8, Neo-Hookean, ramped tension, 0.8
                   dt factor, t = 0..1 s) run by the reference loop, plus the
                   last row of examples/ex9/abaqus/abaqus.rpt (the CI target of
@@ -87,6 +89,21 @@ def force_cases():
     return out
 
 
+def percentile_cases():
+    """The reference's 95th percentiles (math.cpp) of seeded arrays: normal,
+    rounded (ties), non-negative, tiny."""
+    rng = np.random.default_rng(95)
+    out = {}
+    arrays = [rng.normal(size=1000), np.round(rng.uniform(0.0, 3.0, 777), 1),
+              np.abs(rng.normal(size=12345)), rng.normal(size=21), rng.normal(size=20)]
+    for i, d in enumerate(arrays):
+        a, b = orc.RefBuild.percentile95(d)
+        assert a == b
+        out["pct_data_%d" % i] = d
+        out["pct_ref_%d" % i] = np.array(a)
+    return out
+
+
 def abaqus_last_row(path):
     rows = []
     with open(path) as f:
@@ -148,7 +165,8 @@ def main():
     orc.build()
     if not orc.RefBuild.available():
         raise SystemExit("reference build missing")
-    np.savez_compressed(os.path.join(HERE, "ref_force.npz"), **force_cases())
+    np.savez_compressed(os.path.join(HERE, "ref_force.npz"), **force_cases(),
+                        **percentile_cases())
     np.savez_compressed(os.path.join(HERE, "ref_ex9.npz"), **ex9_case())
     np.savez_compressed(os.path.join(HERE, "ref_cube.npz"), **cube_case())
     for f in ("ref_force.npz", "ref_ex9.npz", "ref_cube.npz"):

@@ -39,6 +39,16 @@ def test_element_strain_matches_reference(oracle_lib, golden, name):
         np.testing.assert_array_equal(got, f[name + "_strain"][k])
 
 
+def test_percentile95_matches_reference(oracle_lib, golden):
+    """compute95thPercentileValue(BruteForce) of math.cpp, incl. ties and n = 20, 21."""
+    f = golden["ref_force"]
+    i = 0
+    while "pct_data_%d" % i in f.files:
+        assert oracle_lib.percentile95(f["pct_data_%d" % i]) == float(f["pct_ref_%d" % i])
+        i += 1
+    assert i == 5
+
+
 def test_ex9_loop_matches_reference_and_abaqus(oracle_lib, golden):
     g = golden["ref_ex9"]
     mesh, mats, loads = ex9_mesh_loads()
