@@ -321,6 +321,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--size", default=None,
                     help="block: nx,ny,nz; head: target elements; ensemble: instances")
+    ap.add_argument("--injury", action="store_true",
+                    help="per-step injury criteria over the elements of part 1 and above "
+                         "(the brain drivers exclude the skull parts)")
     ap.add_argument("--energy", action="store_true",
                     help="track the energy balance (CheckEnergy) in the loop (single instance)")
     ap.add_argument("--surrogate", action="store_true",
@@ -358,6 +361,8 @@ def main():
     log("setup %.1f s (%d elements, %d nodes)" % (time.perf_counter() - t0, E, N))
     if args.energy:
         model.set_energy(True)
+    if args.injury:
+        model.set_injury(np.nonzero(np.asarray(mesh["pid"]) >= 1)[0])
     model.init_explicit(reduction=0.9, failure_dt=0.0, tmax=1e300)
     model.run(args.warmup)
     torch.cuda.synchronize(dev)
@@ -413,7 +418,8 @@ def main():
         "ms_per_step": ms / max(steps, 1), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 element kernels / f64 nodal state",
         "data": "synthetic (seeded, generated in-run)",
-        "config": {"workload": wl["label"] + ("_energy_balance" if args.energy else ""),
+        "config": {"workload": wl["label"] + ("_energy_balance" if args.energy else "")
+                   + ("_injury_criteria" if args.injury else ""),
                    "elements": E, "nodes": N,
                    "material": wl["material"], "precision": "mixed",
                    "l2": "inputs larger than L2 (%.2f GB resident)" % ((E * 48 + N * 140) / 1e9),
@@ -432,6 +438,10 @@ def main():
         line["cpu_baseline"] = cpu_reference_rate(os.cpu_count() or 1)
     if args.energy:
         line["energy"] = model.energy()
+    if args.injury:
+        inj = model.injury()
+        line["injury"] = {k: inj[k] for k in ("max_strain", "max_strain_elem", "mps95",
+                                              "mps95_count", "steps")}
     if rank == 0:
         print(json.dumps(line), flush=True)
     model.close()

@@ -215,7 +215,8 @@ struct ftgpu_model {
   // injury criteria of the brain drivers (single instance only)
   bool injury_on = false;
   int inj_n = 0;
-  DBuf inj_elem_g, inj_elem_ref, inj_E6, inj_ps_old, inj_psxsr, inj_flags, inj_part, inj_state,
+  std::vector<int> inj_upos;  // compact index -> position in the caller's list
+  DBuf inj_cidx, inj_upos_d, inj_eref, inj_ps_old, inj_psxsr, inj_flags, inj_part, inj_state,
       inj_hist;
   // energy balance of the explicit loop (CheckEnergy), single instance only
   bool energy_on = false;
@@ -800,9 +801,9 @@ constexpr int kInjHistWords = 2 * 8 * kRadixBins + 2;  // histograms + two count
 template <class R>
 InjuryArgs<R> injury_args(ftgpu_model *m, int parity) {
   InjuryArgs<R> A;
-  A.elem_g = m->inj_elem_g.as<int>();
-  A.elem_ref = m->inj_elem_ref.as<int>();
-  A.E6 = m->inj_E6.as<double>();
+  A.cidx = m->inj_cidx.as<int>();
+  A.upos = m->inj_upos_d.as<int>();
+  A.eref = m->inj_eref.as<int>();
   A.ps_old = m->inj_ps_old.as<R>();
   A.psxsr = m->inj_psxsr.as<R>();
   A.flags = m->inj_flags.as<uint8_t>();
@@ -813,28 +814,35 @@ InjuryArgs<R> injury_args(ftgpu_model *m, int parity) {
   A.count = A.hist + 2 * 8 * kRadixBins;
   A.n = m->inj_n;
   A.parity = parity;
+  int np = 0;
+  for (auto &g : m->ps.groups) np += g.npatch;
+  A.npart = np;
   return A;
 }
 
 // One step of the injury criteria, between the element pass and the nodal
-// update (the slots still hold this step's displacements): element strain,
-// per-element update, the step's extremes, two radix selections.
+// update (the slots still hold this step's displacements): per group the
+// fused strain / principal-strain / update pass, the step's extremes (which
+// also clears the histograms), the radix passes of both selections, the
+// element lists and the running maxima.
 template <class R>
 int launch_injury_t(ftgpu_model *m, int parity) {
-  const InjuryArgs<R> A = injury_args<R>(m, parity);
-  int r = strain_groups_t<R>(m, m->inj_E6.as<double>());
-  if (r) return r;
-  const int nb = (m->inj_n + kInjThreads - 1) / kInjThreads;
-  k_injury_update<R><<<nb, kInjThreads, 0, m->stream>>>(A);
-  k_injury_reduce<R><<<1, 32, 0, m->stream>>>(A, nb);
-  CK(cudaMemsetAsync(m->inj_hist.p, 0, kInjHistWords * sizeof(unsigned), m->stream));
-  const int hb = std::min(nb, 1024);
-  for (int sel = 0; sel < 2; ++sel) {
-    for (int pass = 0; pass < (int)sizeof(R); ++pass)
-      k_radix_hist<R><<<hb, kInjThreads, 0, m->stream>>>(A, sel, pass);
-    k_radix_list<R><<<hb, kInjThreads, 0, m->stream>>>(A, sel);
+  const InjuryArgs<R> J = injury_args<R>(m, parity);
+  const int PE = max_patch(m);
+  for (size_t gi = 0; gi < m->ps.groups.size(); ++gi) {
+    const PatchGroup &g = m->ps.groups[gi];
+    const ElemArgs<R> A = elem_args<R>(m, g, (int)gi);
+    const size_t smem = elem_smem_bytes_host<R>(g.etype, PE);
+    const int r = launch_injury_pass(g.etype, g.npatch, PE, smem, m->stream, A, J);
+    if (r) return fail(FTGPU_ERR_CUDA, std::string("injury pass: ") +
+                                           cudaGetErrorString((cudaError_t)r));
   }
-  k_radix_final<R><<<1, 32, 0, m->stream>>>(A);
+  k_injury_reduce<R><<<1, 1024, 0, m->stream>>>(J);
+  const int hb = std::min((m->inj_n + kInjThreads - 1) / kInjThreads, 512);
+  for (int pass = 0; pass < (int)sizeof(R); ++pass)
+    k_radix_hist<R><<<dim3(hb, 2), kInjThreads, 0, m->stream>>>(J, pass);
+  k_radix_list<R><<<dim3(hb, 2), kInjThreads, 0, m->stream>>>(J);
+  k_radix_final<R><<<1, 32, 0, m->stream>>>(J);
   CK(cudaGetLastError());
   return 0;
 }
@@ -1327,10 +1335,10 @@ int ftgpu_launches_per_step(ftgpu_model *m) {
   if (m->surr)
     for (auto &x : m->ps.groups) g += 2 * (x.npatch > 0 && x.mat == 7);
   int inj = 0;
-  if (m->injury_on) {  // strain groups, update, reduce, memset, 2 x (passes + list), final
+  if (m->injury_on) {  // injury pass per group, reduce, radix passes, list, final
     int sg = 0;
     for (auto &x : m->ps.groups) sg += x.npatch > 0;
-    inj = sg + 3 + 2 * ((is_fp64(m) ? 8 : 4) + 1) + 1;
+    inj = sg + 1 + (is_fp64(m) ? 8 : 4) + 2;
   }
   return g + 2 + (m->energy_on ? 1 : 0) + inj;  // + k_energy_reduce
 }
@@ -1382,22 +1390,33 @@ int ftgpu_set_injury(ftgpu_model *m, int n, const int *element_ids) {
   if (m->ninst != 1)
     return fail(FTGPU_ERR_INPUT, "injury criteria are kept for single-instance models");
   const int E = m->nE;
-  std::vector<int> g_of(E), eg(n);
-  for (int ge = 0; ge < E; ++ge) g_of[m->ps.elem_order[ge]] = ge;
+  std::vector<int> pos(E, -1);  // reference id -> position in the list
   for (int j = 0; j < n; ++j) {
     if (element_ids[j] < 0 || element_ids[j] >= E)
       return fail(FTGPU_ERR_INPUT, "set_injury: element id out of range");
-    eg[j] = g_of[element_ids[j]];
+    if (pos[element_ids[j]] >= 0) return fail(FTGPU_ERR_INPUT, "set_injury: repeated element");
+    pos[element_ids[j]] = j;
+  }
+  // listed elements in group order ("compact" index)
+  std::vector<int> cidx(E, -1), eref;
+  m->inj_upos.clear();
+  for (int ge = 0; ge < E; ++ge) {
+    const int e = m->ps.elem_order[ge];
+    if (pos[e] < 0) continue;
+    cidx[ge] = (int)eref.size();
+    eref.push_back(e);
+    m->inj_upos.push_back(pos[e]);
   }
   const size_t rb = is_fp64(m) ? sizeof(double) : sizeof(float);
-  const int nb = (n + kInjThreads - 1) / kInjThreads;
-  CKI(m->inj_elem_g.upload(eg.data(), n));
-  CKI(m->inj_elem_ref.upload(element_ids, n));
-  CKI(m->inj_E6.alloc(6 * (size_t)E * sizeof(double)));
+  int np = 0;
+  for (auto &g : m->ps.groups) np += g.npatch;
+  CKI(m->inj_cidx.upload(cidx.data(), E));
+  CKI(m->inj_upos_d.upload(m->inj_upos.data(), n));
+  CKI(m->inj_eref.upload(eref.data(), n));
   CKI(m->inj_ps_old.alloc(n * rb));
   CKI(m->inj_psxsr.alloc(n * rb));
   CKI(m->inj_flags.alloc(n));
-  CKI(m->inj_part.alloc(nb * sizeof(InjuryPart)));
+  CKI(m->inj_part.alloc(np * sizeof(InjuryPart)));
   CKI(m->inj_state.alloc(sizeof(InjuryState)));
   CKI(m->inj_hist.alloc(kInjHistWords * sizeof(unsigned)));
   CK(cudaMemset(m->inj_ps_old.p, 0, n * rb));
@@ -1414,20 +1433,22 @@ int ftgpu_get_injury(ftgpu_model *m, ftgpu_injury *out, int *flags, double *ps) 
   CK(cudaSetDevice(m->device));
   CK(cudaStreamSynchronize(m->stream));
   if (out) CK(cudaMemcpy(out, m->inj_state.p, sizeof(ftgpu_injury), cudaMemcpyDeviceToHost));
-  const int n = m->inj_n;
+  const int n = m->inj_n;  // device arrays are in group order: back to the caller's
   if (flags) {
     std::vector<uint8_t> f(n);
     CK(cudaMemcpy(f.data(), m->inj_flags.p, n, cudaMemcpyDeviceToHost));
-    for (int j = 0; j < n; ++j) flags[j] = f[j];
+    for (int c = 0; c < n; ++c) flags[m->inj_upos[c]] = f[c];
   }
   if (ps) {
+    std::vector<double> v(n);
     if (is_fp64(m)) {
-      CK(cudaMemcpy(ps, m->inj_ps_old.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(v.data(), m->inj_ps_old.p, n * sizeof(double), cudaMemcpyDeviceToHost));
     } else {
-      std::vector<float> v(n);
-      CK(cudaMemcpy(v.data(), m->inj_ps_old.p, n * sizeof(float), cudaMemcpyDeviceToHost));
-      for (int j = 0; j < n; ++j) ps[j] = v[j];
+      std::vector<float> w(n);
+      CK(cudaMemcpy(w.data(), m->inj_ps_old.p, n * sizeof(float), cudaMemcpyDeviceToHost));
+      for (int c = 0; c < n; ++c) v[c] = w[c];
     }
+    for (int c = 0; c < n; ++c) ps[m->inj_upos[c]] = v[c];
   }
   return FTGPU_OK;
 }

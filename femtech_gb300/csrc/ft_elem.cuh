@@ -26,6 +26,7 @@
 #pragma once
 
 #include "ft_common.h"
+#include "ft_injury.cuh"
 
 namespace ftgpu {
 
@@ -625,55 +626,13 @@ __global__ void __launch_bounds__(kElemThreads, ET == 0 ? 2 : 3)
   }
 }
 
-// Gauss-point average of the Green-Lagrange strain of every element of a group
-// (CalculateStrain.cpp:8-33) on the current displacement slots, from the
-// displacement gradient D = F - I of each Gauss point:
-//   E = (1 / nGP) sum_gp (D + D^T + D^T D) / 2,
-// the same quantity as the reference's sum (0.5 / nGP) F^T F - 0.5 I without
-// the cancellation of F^T F - I.  Output per element (group order, FP64):
-// Voigt xx, yy, zz, yz, xz, xy.
+// Gauss-point average of the Green strain of one element (see k_elem_strain)
 template <class R, int ET>
-__global__ void __launch_bounds__(kElemThreads) k_elem_strain(const ElemArgs<R> A, double *Eout) {
-  constexpr int NC = ET == 0 ? 8 : 4;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  R *shX = reinterpret_cast<R *>(smem_raw);
-  R *shU = shX + 3 * kMaxLocalNodes;
-  const int PE = blockDim.x;
-  const int t = threadIdx.x;
-  const int p = A.patch_begin + blockIdx.x;
-  const int e0 = A.patch_elem_off[p], ne = A.patch_elem_off[p + 1] - e0;
-  const int s0 = A.patch_node_off[p], ns = A.patch_node_off[p + 1] - s0;
-  for (int i = t; i < ns; i += PE) {
+__device__ __forceinline__ void element_green_strain(const R (&x)[ET == 0 ? 8 : 4][3],
+                                                     const R (&u)[ET == 0 ? 8 : 4][3],
+                                                     R (&Es)[6]) {
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      shX[d * kMaxLocalNodes + i] = A.sX[d * A.S + s0 + i];
-      shU[d * kMaxLocalNodes + i] = A.sU[d * A.S + s0 + i];
-    }
-  }
-  __syncthreads();
-  if (t >= ne) return;
-  const int e = e0 + t;
-  const long long el = e - A.elem_begin;
-  int lc[NC];
-  if (NC == 8) {
-    const uint4 v = *reinterpret_cast<const uint4 *>(A.lconn + 8ll * el);
-    lc[0] = v.x & 0xffff; lc[1] = v.x >> 16; lc[2] = v.y & 0xffff; lc[3] = v.y >> 16;
-    lc[4 % NC] = v.z & 0xffff; lc[5 % NC] = v.z >> 16; lc[6 % NC] = v.w & 0xffff; lc[7 % NC] = v.w >> 16;
-  } else {
-    const uint2 v = *reinterpret_cast<const uint2 *>(A.lconn + 4ll * el);
-    lc[0] = v.x & 0xffff; lc[1] = v.x >> 16; lc[2] = v.y & 0xffff; lc[3] = v.y >> 16;
-  }
-  R x[NC][3], u[NC][3];
-#pragma unroll
-  for (int a = 0; a < NC; ++a) {
-    const int l = lc[a] < ns ? lc[a] : 0;
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      x[a][d] = shX[d * kMaxLocalNodes + l];
-      u[a][d] = shU[d * kMaxLocalNodes + l];
-    }
-  }
-  R Es[6] = {0, 0, 0, 0, 0, 0};
+  for (int k = 0; k < 6; ++k) Es[k] = R(0);
   if (ET == 0) {
     R hx[7][3], hu[7][3];
     hex_hadamard(reinterpret_cast<const R(&)[8][3]>(x), hx);
@@ -729,8 +688,168 @@ __global__ void __launch_bounds__(kElemThreads) k_elem_strain(const ElemArgs<R> 
         D[i][j] = idet * (H[i][0] * Ad[j][0] + H[i][1] * Ad[j][1] + H[i][2] * Ad[j][2]);
     green_strain(D, Es);
   }
+}
+
+// Gauss-point average of the Green-Lagrange strain of every element of a group
+// (CalculateStrain.cpp:8-33) on the current displacement slots, from the
+// displacement gradient D = F - I of each Gauss point:
+//   E = (1 / nGP) sum_gp (D + D^T + D^T D) / 2,
+// the same quantity as the reference's sum (0.5 / nGP) F^T F - 0.5 I without
+// the cancellation of F^T F - I.  Output per element (group order, FP64):
+// Voigt xx, yy, zz, yz, xz, xy.
+template <class R, int ET>
+__global__ void __launch_bounds__(kElemThreads) k_elem_strain(const ElemArgs<R> A, double *Eout) {
+  constexpr int NC = ET == 0 ? 8 : 4;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  R *shX = reinterpret_cast<R *>(smem_raw);
+  R *shU = shX + 3 * kMaxLocalNodes;
+  const int PE = blockDim.x;
+  const int t = threadIdx.x;
+  const int p = A.patch_begin + blockIdx.x;
+  const int e0 = A.patch_elem_off[p], ne = A.patch_elem_off[p + 1] - e0;
+  const int s0 = A.patch_node_off[p], ns = A.patch_node_off[p + 1] - s0;
+  for (int i = t; i < ns; i += PE) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      shX[d * kMaxLocalNodes + i] = A.sX[d * A.S + s0 + i];
+      shU[d * kMaxLocalNodes + i] = A.sU[d * A.S + s0 + i];
+    }
+  }
+  __syncthreads();
+  if (t >= ne) return;
+  const int e = e0 + t;
+  const long long el = e - A.elem_begin;
+  int lc[NC];
+  if (NC == 8) {
+    const uint4 v = *reinterpret_cast<const uint4 *>(A.lconn + 8ll * el);
+    lc[0] = v.x & 0xffff; lc[1] = v.x >> 16; lc[2] = v.y & 0xffff; lc[3] = v.y >> 16;
+    lc[4 % NC] = v.z & 0xffff; lc[5 % NC] = v.z >> 16; lc[6 % NC] = v.w & 0xffff; lc[7 % NC] = v.w >> 16;
+  } else {
+    const uint2 v = *reinterpret_cast<const uint2 *>(A.lconn + 4ll * el);
+    lc[0] = v.x & 0xffff; lc[1] = v.x >> 16; lc[2] = v.y & 0xffff; lc[3] = v.y >> 16;
+  }
+  R x[NC][3], u[NC][3];
+#pragma unroll
+  for (int a = 0; a < NC; ++a) {
+    const int l = lc[a] < ns ? lc[a] : 0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      x[a][d] = shX[d * kMaxLocalNodes + l];
+      u[a][d] = shU[d * kMaxLocalNodes + l];
+    }
+  }
+  R Es[6];
+  element_green_strain<R, ET>(x, u, Es);
 #pragma unroll
   for (int k = 0; k < 6; ++k) Eout[6 * (long long)e + k] = double(Es[k]);
+}
+
+// One step of the injury criteria for the listed elements of a group
+// (ex5.cpp:1311-1365): the element's averaged Green strain (as k_elem_strain),
+// its principal strains (CalculateStrain.cpp:38-74, in R), the sticky flags,
+// the principal strain rate against the previous step, and this block's
+// extremes (best value, then smallest list position) into part[p].
+template <class R, int ET>
+__global__ void __launch_bounds__(kElemThreads) k_elem_injury(const ElemArgs<R> A,
+                                                              const InjuryArgs<R> J) {
+  constexpr int NC = ET == 0 ? 8 : 4;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  R *shX = reinterpret_cast<R *>(smem_raw);
+  R *shU = shX + 3 * kMaxLocalNodes;
+  const int PE = blockDim.x;
+  const int t = threadIdx.x;
+  const int p = A.patch_begin + blockIdx.x;
+  const int e0 = A.patch_elem_off[p], ne = A.patch_elem_off[p + 1] - e0;
+  const int s0 = A.patch_node_off[p], ns = A.patch_node_off[p + 1] - s0;
+  const Clock ck = J.clock[J.parity];
+  for (int i = t; i < ns; i += PE) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      shX[d * kMaxLocalNodes + i] = A.sX[d * A.S + s0 + i];
+      shU[d * kMaxLocalNodes + i] = A.sU[d * A.S + s0 + i];
+    }
+  }
+  __syncthreads();
+  double v[4] = {-1e300, 1e300, -1e300, -1e300};
+  int jj[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff}, cc[4] = {-1, -1, -1, -1};
+  const int e = e0 + t;
+  const int c = (t < ne && !ck.done) ? J.cidx[e] : -1;
+  if (c >= 0) {
+    const long long el = e - A.elem_begin;
+    int lc[NC];
+    if (NC == 8) {
+      const uint4 w = *reinterpret_cast<const uint4 *>(A.lconn + 8ll * el);
+      lc[0] = w.x & 0xffff; lc[1] = w.x >> 16; lc[2] = w.y & 0xffff; lc[3] = w.y >> 16;
+      lc[4 % NC] = w.z & 0xffff; lc[5 % NC] = w.z >> 16; lc[6 % NC] = w.w & 0xffff; lc[7 % NC] = w.w >> 16;
+    } else {
+      const uint2 w = *reinterpret_cast<const uint2 *>(A.lconn + 4ll * el);
+      lc[0] = w.x & 0xffff; lc[1] = w.x >> 16; lc[2] = w.y & 0xffff; lc[3] = w.y >> 16;
+    }
+    R x[NC][3], u[NC][3];
+#pragma unroll
+    for (int a = 0; a < NC; ++a) {
+      const int l = lc[a] < ns ? lc[a] : 0;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        x[a][d] = shX[d * kMaxLocalNodes + l];
+        u[a][d] = shU[d * kMaxLocalNodes + l];
+      }
+    }
+    R Es[6];
+    element_green_strain<R, ET>(x, u, Es);
+    R mx, mn, sh;
+    principal_strains<R>(Es[0], Es[1], Es[2], Es[3], Es[4], Es[5], mx, mn, sh);
+    uint8_t f = J.flags[c];
+    if (mx > R(0.15)) f |= kInjMps15;
+    if (mx > R(0.30)) f |= kInjMps30;
+    const R psr = (mx - J.ps_old[c]) / R(ck.dt);
+    const R psxsr = mx * psr;
+    if (psr > R(120)) f |= kInjPsr120;
+    if (psxsr > R(28)) f |= kInjPsxsr28;
+    J.flags[c] = f;
+    J.ps_old[c] = mx;
+    J.psxsr[c] = psxsr;
+    v[0] = double(mx);
+    v[1] = double(mn);
+    v[2] = double(sh);
+    v[3] = double(psxsr);
+    const int up = J.upos[c];
+    jj[0] = jj[1] = jj[2] = jj[3] = up;
+    cc[0] = cc[1] = cc[2] = cc[3] = c;
+  }
+  // block extremes (shared memory reuses the staging area)
+  __syncthreads();
+  double *sv = reinterpret_cast<double *>(smem_raw);  // [4][PE]
+  int *sj = reinterpret_cast<int *>(sv + 4 * PE);     // [4][PE]
+  int *sc = sj + 4 * PE;                              // [4][PE]
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    sv[k * PE + t] = v[k];
+    sj[k * PE + t] = jj[k];
+    sc[k * PE + t] = cc[k];
+  }
+  __syncthreads();
+  for (int h = PE > 1 ? 1 << (31 - __clz(PE - 1)) : 0; h > 0; h >>= 1) {
+    if (t < h && t + h < PE)
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (inj_better(k, sv[k * PE + t + h], sj[k * PE + t + h], sv[k * PE + t], sj[k * PE + t])) {
+          sv[k * PE + t] = sv[k * PE + t + h];
+          sj[k * PE + t] = sj[k * PE + t + h];
+          sc[k * PE + t] = sc[k * PE + t + h];
+        }
+    __syncthreads();
+  }
+  if (t == 0) {
+    InjuryPart q;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      q.v[k] = sv[k * PE];
+      q.j[k] = sj[k * PE];
+      q.c[k] = sc[k * PE];
+    }
+    J.part[p] = q;
+  }
 }
 
 template <class R>

@@ -29,6 +29,16 @@ static int by_mat(int mat, int gp, int nb, int th, size_t sm, cudaStream_t s,
   }
 }
 
+int launch_injury_f32(int etype, int nblocks, int threads, size_t smem, cudaStream_t s,
+                      const ElemArgs<float> &A, const InjuryArgs<float> &J) {
+  if (nblocks <= 0) return 0;
+  if (etype == 0)
+    k_elem_injury<float, 0><<<nblocks, threads, smem, s>>>(A, J);
+  else
+    k_elem_injury<float, 1><<<nblocks, threads, smem, s>>>(A, J);
+  return (int)cudaGetLastError();
+}
+
 int launch_strain_f32(int etype, int nblocks, int threads, size_t smem, cudaStream_t s,
                       const ElemArgs<float> &A, double *Eout) {
   if (nblocks <= 0) return 0;

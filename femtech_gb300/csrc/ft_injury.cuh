@@ -28,28 +28,34 @@ struct InjuryState {
 enum { kInjMps15 = 1, kInjMps30 = 2, kInjPsr120 = 4, kInjPsxsr28 = 8, kInjInMps95 = 16,
        kInjInMpsxsr95 = 32 };
 
-// per-block partial extremes of one step: value and the smallest list index
+// per-block partial extremes of one step: value, the caller's list position
+// (tie-break) and the compact index of the element
 struct InjuryPart {
   double v[4];  // max strain, min strain, max shear, max psxsr
-  int j[4];
+  int j[4];     // list position
+  int c[4];     // compact index
 };
 
 constexpr int kInjThreads = 256;
 constexpr int kRadixBins = 256;
 
+// The listed elements are kept in group order ("compact" index c): element e
+// (group order) is listed when cidx[e] >= 0; upos[c] is its position in the
+// caller's list (ties go to the smaller position, as in the reference's loop)
+// and eref[c] its reference id.
 template <class R>
 struct InjuryArgs {
-  const int *elem_g;     // [n] group-order index of each listed element
-  const int *elem_ref;   // [n] reference element id
-  const double *E6;      // [E] Voigt averaged Green strain (group order)
-  R *ps_old, *psxsr;     // [n]
-  uint8_t *flags;        // [n]
-  InjuryPart *part;      // [blocks]
+  const int *cidx;       // [E] compact index or -1
+  const int *upos;       // [n]
+  const int *eref;       // [n]
+  R *ps_old, *psxsr;     // [n] compact order
+  uint8_t *flags;        // [n] compact order
+  InjuryPart *part;      // [patches] block extremes of the step
   InjuryState *state;
   const Clock *clock;    // clock[0] of the step (single instance)
-  unsigned *hist;        // [2 selections][passes][256]
+  unsigned *hist;        // [2 selections][passes][256], then [2] counters
   unsigned *count;       // [2] elements at or above a new maximum
-  int n, parity;
+  int n, parity, npart;
 };
 
 // principal strains of the symmetric strain in the trigonometric form of
@@ -100,113 +106,71 @@ __device__ __forceinline__ double fkey_inv(uint64_t k) {
   return __longlong_as_double((long long)((k >> 63) ? (k & 0x7fffffffffffffffull) : ~k));
 }
 
-// One step of CalculateInjuryCriterions for every listed element, with the
-// block partial extremes.
+// better (value, list index) of two candidates for extreme k (k = 1 is a
+// minimum): the better value, then the smaller list index
+__device__ __forceinline__ bool inj_better(int k, double bv, int bj, double av, int aj) {
+  return (k == 1) ? (bv < av || (bv == av && bj < aj)) : (bv > av || (bv == av && bj < aj));
+}
+
+// The step's extremes from the block partials into the running state (one
+// block, fixed tree): a strictly better value takes the element and the time
+// (the reference's ordered loop with strict comparisons).  Also clears the
+// radix histograms of the step.
 template <class R>
-__global__ void __launch_bounds__(kInjThreads) k_injury_update(const InjuryArgs<R> A) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const Clock ck = A.clock[A.parity];
-  const bool run = !ck.done;
+__global__ void __launch_bounds__(1024) k_injury_reduce(const InjuryArgs<R> A) {
+  __shared__ double sv[4][1024];
+  __shared__ int sj[4][1024], sc[4][1024];
+  for (int i = threadIdx.x; i < 2 * 8 * kRadixBins + 2; i += blockDim.x) A.hist[i] = 0;
   double v[4] = {-1e300, 1e300, -1e300, -1e300};
-  int jj[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
-  if (run && j < A.n) {
-    const double *e = A.E6 + 6 * (long long)A.elem_g[j];
-    R mx, mn, sh;
-    principal_strains<R>(R(e[0]), R(e[1]), R(e[2]), R(e[3]), R(e[4]), R(e[5]), mx, mn, sh);
-    uint8_t f = A.flags[j];
-    if (mx > R(0.15)) f |= kInjMps15;
-    if (mx > R(0.30)) f |= kInjMps30;
-    const R psr = (mx - A.ps_old[j]) / R(ck.dt);
-    const R psxsr = mx * psr;
-    if (psr > R(120)) f |= kInjPsr120;
-    if (psxsr > R(28)) f |= kInjPsxsr28;
-    A.flags[j] = f;
-    A.ps_old[j] = mx;
-    A.psxsr[j] = psxsr;
-    v[0] = double(mx);
-    v[1] = double(mn);
-    v[2] = double(sh);
-    v[3] = double(psxsr);
-    jj[0] = jj[1] = jj[2] = jj[3] = j;
+  int jj[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff}, cc[4] = {-1, -1, -1, -1};
+  for (int b = threadIdx.x; b < A.npart; b += blockDim.x) {
+    const InjuryPart p = A.part[b];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (inj_better(k, p.v[k], p.j[k], v[k], jj[k])) {
+        v[k] = p.v[k];
+        jj[k] = p.j[k];
+        cc[k] = p.c[k];
+      }
   }
-  // block extremes: best value, then smallest list index
-  __shared__ double sv[4][kInjThreads];
-  __shared__ int sj[4][kInjThreads];
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     sv[k][threadIdx.x] = v[k];
     sj[k][threadIdx.x] = jj[k];
+    sc[k][threadIdx.x] = cc[k];
   }
   __syncthreads();
   for (int h = blockDim.x / 2; h > 0; h >>= 1) {
-    if ((int)threadIdx.x < h) {
+    if ((int)threadIdx.x < h)
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const double a = sv[k][threadIdx.x], b = sv[k][threadIdx.x + h];
-        const int ja = sj[k][threadIdx.x], jb = sj[k][threadIdx.x + h];
-        const bool better = (k == 1) ? (b < a || (b == a && jb < ja)) : (b > a || (b == a && jb < ja));
-        if (better) {
-          sv[k][threadIdx.x] = b;
-          sj[k][threadIdx.x] = jb;
+      for (int k = 0; k < 4; ++k)
+        if (inj_better(k, sv[k][threadIdx.x + h], sj[k][threadIdx.x + h], sv[k][threadIdx.x],
+                       sj[k][threadIdx.x])) {
+          sv[k][threadIdx.x] = sv[k][threadIdx.x + h];
+          sj[k][threadIdx.x] = sj[k][threadIdx.x + h];
+          sc[k][threadIdx.x] = sc[k][threadIdx.x + h];
         }
-      }
-    }
     __syncthreads();
   }
-  if (threadIdx.x == 0) {
-    InjuryPart p;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      p.v[k] = sv[k][0];
-      p.j[k] = sj[k][0];
-    }
-    A.part[blockIdx.x] = p;
-  }
-}
-
-// The step's extremes from the block partials (blocks in order) into the
-// running state: a strictly better value takes the element and the time
-// (the reference's ordered loop with strict comparisons).
-template <class R>
-__global__ void k_injury_reduce(const InjuryArgs<R> A, int nblocks) {
   if (threadIdx.x != 0) return;
   const Clock ck = A.clock[A.parity];
   if (ck.done) return;
   const double t = ck.time + ck.dt;
-  double v[4] = {-1e300, 1e300, -1e300, -1e300};
-  int jj[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
-  for (int b = 0; b < nblocks; ++b) {
-    const InjuryPart p = A.part[b];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const bool better = (k == 1) ? (p.v[k] < v[k] || (p.v[k] == v[k] && p.j[k] < jj[k]))
-                                   : (p.v[k] > v[k] || (p.v[k] == v[k] && p.j[k] < jj[k]));
-      if (better) {
-        v[k] = p.v[k];
-        jj[k] = p.j[k];
-      }
-    }
-  }
   InjuryState s = *A.state;
-  if (jj[0] < A.n && s.max_strain < v[0]) {
-    s.max_strain = v[0];
-    s.max_strain_elem = A.elem_ref[jj[0]];
-    s.max_strain_time = t;
-  }
-  if (jj[1] < A.n && s.min_strain > v[1]) {
-    s.min_strain = v[1];
-    s.min_strain_elem = A.elem_ref[jj[1]];
-    s.min_strain_time = t;
-  }
-  if (jj[2] < A.n && s.max_shear < v[2]) {
-    s.max_shear = v[2];
-    s.max_shear_elem = A.elem_ref[jj[2]];
-    s.max_shear_time = t;
-  }
-  if (jj[3] < A.n && s.max_psxsr < v[3]) {
-    s.max_psxsr = v[3];
-    s.max_psxsr_elem = A.elem_ref[jj[3]];
-    s.max_psxsr_time = t;
+  double *val[4] = {&s.max_strain, &s.min_strain, &s.max_shear, &s.max_psxsr};
+  double *tim[4] = {&s.max_strain_time, &s.min_strain_time, &s.max_shear_time,
+                    &s.max_psxsr_time};
+  int *el[4] = {&s.max_strain_elem, &s.min_strain_elem, &s.max_shear_elem, &s.max_psxsr_elem};
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int c = sc[k][0];
+    if (c < 0) continue;
+    const bool upd = (k == 1) ? (*val[k] > sv[k][0]) : (*val[k] < sv[k][0]);
+    if (upd) {
+      *val[k] = sv[k][0];
+      *el[k] = A.eref[c];
+      *tim[k] = t;
+    }
   }
   ++s.steps;
   *A.state = s;
@@ -237,42 +201,67 @@ __device__ __forceinline__ void radix_prefix(const unsigned *hist, int pass, int
   }
 }
 
+// Histogram of the next digit of the keys that share the digits fixed so far.
+// The values cluster (strains of one tissue), so most keys fall into a few
+// bins: lanes of a warp with the same bin are merged (__match_any_sync) and one
+// of them adds the count to its warp's own sub-histogram.
 template <class R>
-__global__ void __launch_bounds__(kInjThreads) k_radix_hist(const InjuryArgs<R> A, int sel,
-                                                            int pass) {
+__global__ void __launch_bounds__(kInjThreads) k_radix_hist(const InjuryArgs<R> A, int pass) {
+  const int sel = blockIdx.y;  // 0: MPS, 1: MPS x rate
   typedef typename std::conditional<sizeof(R) == 8, uint64_t, uint32_t>::type K;
   constexpr int KB = sizeof(K) * 8;
+  constexpr int kWarps = kInjThreads / 32;
   if (A.clock[A.parity].done) return;
   unsigned *hist = A.hist + (sel * (KB / 8)) * kRadixBins;
-  __shared__ unsigned sh[kRadixBins];
-  for (int i = threadIdx.x; i < kRadixBins; i += blockDim.x) sh[i] = 0;
-  K prefix;
-  unsigned krem;
-  radix_prefix<K>(hist, pass, A.n, prefix, krem);
+  __shared__ unsigned sh[kWarps][kRadixBins];
+  __shared__ K s_prefix;
+  for (int i = threadIdx.x; i < kWarps * kRadixBins; i += blockDim.x) (&sh[0][0])[i] = 0;
+  if (threadIdx.x == 0) {  // digits fixed so far: once per block
+    unsigned krem;
+    radix_prefix<K>(hist, pass, A.n, s_prefix, krem);
+  }
   __syncthreads();
+  const K prefix = s_prefix;
   const R *val = sel == 0 ? A.ps_old : A.psxsr;
   const K mask = pass == 0 ? K(0) : (K)(~K(0)) << (KB - 8 * pass);
-  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < A.n; j += gridDim.x * blockDim.x) {
-    const K key = fkey(val[j]);
-    if ((key & mask) == prefix) atomicAdd(&sh[(key >> (KB - 8 * (pass + 1))) & 0xffu], 1u);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // the same trip count for every lane of a warp (for __match_any_sync)
+  for (long long base = (long long)blockIdx.x * blockDim.x; base < A.n;
+       base += (long long)gridDim.x * blockDim.x) {
+    const long long j = base + threadIdx.x;
+    unsigned bin = 0xffffffffu;
+    if (j < A.n) {
+      const K key = fkey(val[j]);
+      if ((key & mask) == prefix) bin = (unsigned)(key >> (KB - 8 * (pass + 1))) & 0xffu;
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, bin);
+    if (bin != 0xffffffffu && lane == __ffs(peers) - 1) atomicAdd(&sh[warp][bin], __popc(peers));
   }
   __syncthreads();
   unsigned *out = hist + pass * kRadixBins;
-  for (int i = threadIdx.x; i < kRadixBins; i += blockDim.x)
-    if (sh[i]) atomicAdd(&out[i], sh[i]);
+  for (int i = threadIdx.x; i < kRadixBins; i += blockDim.x) {
+    unsigned c = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) c += sh[w][i];
+    if (c) atomicAdd(&out[i], c);
+  }
 }
 
 // The selected value; where it beats the running maximum, the listed elements
 // at or above it are marked (flag bit) and counted.
 template <class R>
-__global__ void __launch_bounds__(kInjThreads) k_radix_list(const InjuryArgs<R> A, int sel) {
+__global__ void __launch_bounds__(kInjThreads) k_radix_list(const InjuryArgs<R> A) {
+  const int sel = blockIdx.y;  // 0: MPS, 1: MPS x rate
   typedef typename std::conditional<sizeof(R) == 8, uint64_t, uint32_t>::type K;
   constexpr int KB = sizeof(K) * 8;
   if (A.clock[A.parity].done) return;
-  K prefix;
-  unsigned krem;
-  radix_prefix<K>(A.hist + (sel * (KB / 8)) * kRadixBins, KB / 8, A.n, prefix, krem);
-  const R v = fkey_inv(prefix);
+  __shared__ K s_prefix;
+  if (threadIdx.x == 0) {  // the selected key: once per block
+    unsigned krem;
+    radix_prefix<K>(A.hist + (sel * (KB / 8)) * kRadixBins, KB / 8, A.n, s_prefix, krem);
+  }
+  __syncthreads();
+  const R v = fkey_inv(s_prefix);
   const double prev = sel == 0 ? A.state->mps95 : A.state->mpsxsr95;
   if (!(double(v) > prev)) return;
   const R *val = sel == 0 ? A.ps_old : A.psxsr;

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include "ft_common.h"
+#include "ft_injury.cuh"
 
 namespace ftgpu {
 
@@ -33,6 +34,20 @@ template <>
 inline int launch_strain<double>(int etype, int nblocks, int threads, size_t smem,
                                  cudaStream_t s, const ElemArgs<double> &A, double *Eout) {
   return launch_strain_f64(etype, nblocks, threads, smem, s, A, Eout);
+}
+
+// Injury-criteria pass (k_elem_injury) of one group.  Returns a cudaError_t.
+int launch_injury_f32(int etype, int nblocks, int threads, size_t smem, cudaStream_t s,
+                      const ElemArgs<float> &A, const InjuryArgs<float> &J);
+int launch_injury_f64(int etype, int nblocks, int threads, size_t smem, cudaStream_t s,
+                      const ElemArgs<double> &A, const InjuryArgs<double> &J);
+inline int launch_injury_pass(int etype, int nblocks, int threads, size_t smem, cudaStream_t s,
+                              const ElemArgs<float> &A, const InjuryArgs<float> &J) {
+  return launch_injury_f32(etype, nblocks, threads, smem, s, A, J);
+}
+inline int launch_injury_pass(int etype, int nblocks, int threads, size_t smem, cudaStream_t s,
+                              const ElemArgs<double> &A, const InjuryArgs<double> &J) {
+  return launch_injury_f64(etype, nblocks, threads, smem, s, A, J);
 }
 
 // Dynamic shared memory of one element block: node X and u for
