@@ -216,8 +216,9 @@ struct ftgpu_model {
   bool injury_on = false;
   int inj_n = 0;
   std::vector<int> inj_upos;  // compact index -> position in the caller's list
-  DBuf inj_cidx, inj_upos_d, inj_eref, inj_ps_old, inj_psxsr, inj_flags, inj_part, inj_state,
-      inj_hist;
+  std::vector<int> inj_group_n;  // listed elements per group (groups with none are skipped)
+  DBuf inj_cidx, inj_upos_d, inj_eref, inj_ps_old, inj_psxsr, inj_flags, inj_part, inj_part2,
+      inj_done, inj_state, inj_hist;
   // energy balance of the explicit loop (CheckEnergy), single instance only
   bool energy_on = false;
   DBuf du, fprev, epart, estate;
@@ -808,6 +809,8 @@ InjuryArgs<R> injury_args(ftgpu_model *m, int parity) {
   A.psxsr = m->inj_psxsr.as<R>();
   A.flags = m->inj_flags.as<uint8_t>();
   A.part = m->inj_part.as<InjuryPart>();
+  A.part2 = m->inj_part2.as<InjuryPart>();
+  A.done_blocks = m->inj_done.as<unsigned>();
   A.state = m->inj_state.as<InjuryState>();
   A.clock = m->clock.as<Clock>();
   A.hist = m->inj_hist.as<unsigned>();
@@ -831,18 +834,19 @@ int launch_injury_t(ftgpu_model *m, int parity) {
   const int PE = max_patch(m);
   for (size_t gi = 0; gi < m->ps.groups.size(); ++gi) {
     const PatchGroup &g = m->ps.groups[gi];
+    if (m->inj_group_n[gi] == 0) continue;  // its partials keep the sentinel values
     const ElemArgs<R> A = elem_args<R>(m, g, (int)gi);
     const size_t smem = elem_smem_bytes_host<R>(g.etype, PE);
     const int r = launch_injury_pass(g.etype, g.npatch, PE, smem, m->stream, A, J);
     if (r) return fail(FTGPU_ERR_CUDA, std::string("injury pass: ") +
                                            cudaGetErrorString((cudaError_t)r));
   }
-  k_injury_reduce<R><<<1, 1024, 0, m->stream>>>(J);
+  k_injury_reduce<R><<<(J.npart + kInjReduceSpan - 1) / kInjReduceSpan, 256, 0, m->stream>>>(J);
   const int hb = std::min((m->inj_n + kInjThreads - 1) / kInjThreads, 512);
   for (int pass = 0; pass < (int)sizeof(R); ++pass)
     k_radix_hist<R><<<dim3(hb, 2), kInjThreads, 0, m->stream>>>(J, pass);
   k_radix_list<R><<<dim3(hb, 2), kInjThreads, 0, m->stream>>>(J);
-  k_radix_final<R><<<1, 32, 0, m->stream>>>(J);
+  k_radix_final<R><<<1, kRadixBins, 0, m->stream>>>(J);
   CK(cudaGetLastError());
   return 0;
 }
@@ -1338,6 +1342,9 @@ int ftgpu_launches_per_step(ftgpu_model *m) {
   if (m->injury_on) {  // injury pass per group, reduce, radix passes, list, final
     int sg = 0;
     for (auto &x : m->ps.groups) sg += x.npatch > 0;
+    sg = 0;
+    for (size_t gi = 0; gi < m->ps.groups.size(); ++gi)
+      sg += m->ps.groups[gi].npatch > 0 && m->inj_group_n[gi] > 0;
     inj = sg + 1 + (is_fp64(m) ? 8 : 4) + 2;
   }
   return g + 2 + (m->energy_on ? 1 : 0) + inj;  // + k_energy_reduce
@@ -1417,6 +1424,24 @@ int ftgpu_set_injury(ftgpu_model *m, int n, const int *element_ids) {
   CKI(m->inj_psxsr.alloc(n * rb));
   CKI(m->inj_flags.alloc(n));
   CKI(m->inj_part.alloc(np * sizeof(InjuryPart)));
+  CKI(m->inj_part2.alloc(((np + kInjReduceSpan - 1) / kInjReduceSpan) * sizeof(InjuryPart)));
+  CKI(m->inj_done.alloc(sizeof(unsigned)));
+  CK(cudaMemset(m->inj_done.p, 0, sizeof(unsigned)));
+  {  // sentinel partials (no element) for the patches of groups never launched
+    std::vector<InjuryPart> sp(np);
+    for (auto &q : sp)
+      for (int k = 0; k < 4; ++k) {
+        q.v[k] = k == 1 ? 1e300 : -1e300;
+        q.j[k] = 0x7fffffff;
+        q.c[k] = -1;
+      }
+    CK(cudaMemcpy(m->inj_part.p, sp.data(), np * sizeof(InjuryPart), cudaMemcpyHostToDevice));
+  }
+  m->inj_group_n.assign(m->ps.groups.size(), 0);
+  for (size_t gi = 0; gi < m->ps.groups.size(); ++gi) {
+    const PatchGroup &g = m->ps.groups[gi];
+    for (int k = 0; k < g.nelem; ++k) m->inj_group_n[gi] += cidx[g.elem_begin + k] >= 0;
+  }
   CKI(m->inj_state.alloc(sizeof(InjuryState)));
   CKI(m->inj_hist.alloc(kInjHistWords * sizeof(unsigned)));
   CK(cudaMemset(m->inj_ps_old.p, 0, n * rb));

@@ -51,6 +51,8 @@ struct InjuryArgs {
   R *ps_old, *psxsr;     // [n] compact order
   uint8_t *flags;        // [n] compact order
   InjuryPart *part;      // [patches] block extremes of the step
+  InjuryPart *part2;     // [reduction blocks] second level
+  unsigned *done_blocks; // finished reduction blocks (reset by the last one)
   InjuryState *state;
   const Clock *clock;    // clock[0] of the step (single instance)
   unsigned *hist;        // [2 selections][passes][256], then [2] counters
@@ -112,19 +114,15 @@ __device__ __forceinline__ bool inj_better(int k, double bv, int bj, double av, 
   return (k == 1) ? (bv < av || (bv == av && bj < aj)) : (bv > av || (bv == av && bj < aj));
 }
 
-// The step's extremes from the block partials into the running state (one
-// block, fixed tree): a strictly better value takes the element and the time
-// (the reference's ordered loop with strict comparisons).  Also clears the
-// radix histograms of the step.
-template <class R>
-__global__ void __launch_bounds__(1024) k_injury_reduce(const InjuryArgs<R> A) {
-  __shared__ double sv[4][1024];
-  __shared__ int sj[4][1024], sc[4][1024];
-  for (int i = threadIdx.x; i < 2 * 8 * kRadixBins + 2; i += blockDim.x) A.hist[i] = 0;
+// Best of each extreme over a range of partials, then over the threads of a
+// block (fixed tree); the result in slot 0 of the shared arrays.
+__device__ __forceinline__ void inj_block_best(const InjuryPart *part, int lo, int hi,
+                                               double (*sv)[256], int (*sj)[256],
+                                               int (*sc)[256]) {
   double v[4] = {-1e300, 1e300, -1e300, -1e300};
   int jj[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff}, cc[4] = {-1, -1, -1, -1};
-  for (int b = threadIdx.x; b < A.npart; b += blockDim.x) {
-    const InjuryPart p = A.part[b];
+  for (int b = lo + threadIdx.x; b < hi; b += blockDim.x) {
+    const InjuryPart p = part[b];
 #pragma unroll
     for (int k = 0; k < 4; ++k)
       if (inj_better(k, p.v[k], p.j[k], v[k], jj[k])) {
@@ -152,7 +150,42 @@ __global__ void __launch_bounds__(1024) k_injury_reduce(const InjuryArgs<R> A) {
         }
     __syncthreads();
   }
+}
+
+constexpr int kInjReduceSpan = 256;  // partials per reduction block
+
+// The step's extremes from the per-patch partials into the running state: each
+// block reduces kInjReduceSpan partials into part2[block]; the last block to
+// finish (counter in count[2]) reduces those in block order and updates the
+// state: a strictly better value takes the element and the time (the
+// reference's ordered loop with strict comparisons).  The last block also
+// clears the radix histograms and counters of the step.
+template <class R>
+__global__ void __launch_bounds__(256) k_injury_reduce(const InjuryArgs<R> A) {
+  __shared__ double sv[4][256];
+  __shared__ int sj[4][256], sc[4][256];
+  __shared__ bool last;
+  const int lo = blockIdx.x * kInjReduceSpan, hi = min(lo + kInjReduceSpan, A.npart);
+  inj_block_best(A.part, lo, hi, sv, sj, sc);
+  if (threadIdx.x == 0) {
+    InjuryPart q;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      q.v[k] = sv[k][0];
+      q.j[k] = sj[k][0];
+      q.c[k] = sc[k][0];
+    }
+    A.part2[blockIdx.x] = q;
+    __threadfence();
+    last = atomicAdd(A.done_blocks, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  inj_block_best(A.part2, 0, gridDim.x, sv, sj, sc);
+  for (int i = threadIdx.x; i < 2 * 8 * kRadixBins + 2; i += blockDim.x) A.hist[i] = 0;
   if (threadIdx.x != 0) return;
+  *A.done_blocks = 0;
   const Clock ck = A.clock[A.parity];
   if (ck.done) return;
   const double t = ck.time + ck.dt;
@@ -201,6 +234,21 @@ __device__ __forceinline__ void radix_prefix(const unsigned *hist, int pass, int
   }
 }
 
+// The digits fixed by the first `pass` histograms of a selection, computed by
+// one block: the histograms are staged in shared memory by all its threads,
+// then scanned by thread 0 (the result is in *prefix after the barrier).
+template <class K>
+__device__ __forceinline__ void block_radix_prefix(const unsigned *hist, int pass, int n,
+                                                   unsigned *stage, K *prefix) {
+  for (int i = threadIdx.x; i < pass * kRadixBins; i += blockDim.x) stage[i] = hist[i];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned krem;
+    radix_prefix<K>(stage, pass, n, *prefix, krem);
+  }
+  __syncthreads();
+}
+
 // Histogram of the next digit of the keys that share the digits fixed so far.
 // The values cluster (strains of one tissue), so most keys fall into a few
 // bins: lanes of a warp with the same bin are merged (__match_any_sync) and one
@@ -214,13 +262,10 @@ __global__ void __launch_bounds__(kInjThreads) k_radix_hist(const InjuryArgs<R> 
   if (A.clock[A.parity].done) return;
   unsigned *hist = A.hist + (sel * (KB / 8)) * kRadixBins;
   __shared__ unsigned sh[kWarps][kRadixBins];
+  __shared__ unsigned stage[(KB / 8) * kRadixBins];
   __shared__ K s_prefix;
   for (int i = threadIdx.x; i < kWarps * kRadixBins; i += blockDim.x) (&sh[0][0])[i] = 0;
-  if (threadIdx.x == 0) {  // digits fixed so far: once per block
-    unsigned krem;
-    radix_prefix<K>(hist, pass, A.n, s_prefix, krem);
-  }
-  __syncthreads();
+  block_radix_prefix<K>(hist, pass, A.n, stage, &s_prefix);  // digits fixed so far
   const K prefix = s_prefix;
   const R *val = sel == 0 ? A.ps_old : A.psxsr;
   const K mask = pass == 0 ? K(0) : (K)(~K(0)) << (KB - 8 * pass);
@@ -255,12 +300,9 @@ __global__ void __launch_bounds__(kInjThreads) k_radix_list(const InjuryArgs<R> 
   typedef typename std::conditional<sizeof(R) == 8, uint64_t, uint32_t>::type K;
   constexpr int KB = sizeof(K) * 8;
   if (A.clock[A.parity].done) return;
+  __shared__ unsigned stage[(KB / 8) * kRadixBins];
   __shared__ K s_prefix;
-  if (threadIdx.x == 0) {  // the selected key: once per block
-    unsigned krem;
-    radix_prefix<K>(A.hist + (sel * (KB / 8)) * kRadixBins, KB / 8, A.n, s_prefix, krem);
-  }
-  __syncthreads();
+  block_radix_prefix<K>(A.hist + (sel * (KB / 8)) * kRadixBins, KB / 8, A.n, stage, &s_prefix);
   const R v = fkey_inv(s_prefix);
   const double prev = sel == 0 ? A.state->mps95 : A.state->mpsxsr95;
   if (!(double(v) > prev)) return;
@@ -277,19 +319,21 @@ __global__ void __launch_bounds__(kInjThreads) k_radix_list(const InjuryArgs<R> 
 
 // Running maxima of the two percentiles (after k_radix_list of both).
 template <class R>
-__global__ void k_radix_final(const InjuryArgs<R> A) {
+__global__ void __launch_bounds__(kRadixBins) k_radix_final(const InjuryArgs<R> A) {
   typedef typename std::conditional<sizeof(R) == 8, uint64_t, uint32_t>::type K;
   constexpr int KB = sizeof(K) * 8;
-  if (threadIdx.x != 0) return;
   const Clock ck = A.clock[A.parity];
   if (ck.done) return;
+  __shared__ unsigned stage[(KB / 8) * kRadixBins];
+  __shared__ K s_prefix[2];
+  for (int sel = 0; sel < 2; ++sel)
+    block_radix_prefix<K>(A.hist + (sel * (KB / 8)) * kRadixBins, KB / 8, A.n, stage,
+                          &s_prefix[sel]);
+  if (threadIdx.x != 0) return;
   const double t = ck.time + ck.dt;
   InjuryState s = *A.state;
   for (int sel = 0; sel < 2; ++sel) {
-    K prefix;
-    unsigned krem;
-    radix_prefix<K>(A.hist + (sel * (KB / 8)) * kRadixBins, KB / 8, A.n, prefix, krem);
-    const double v = double(fkey_inv(prefix));
+    const double v = double(fkey_inv(s_prefix[sel]));
     double &mx = sel == 0 ? s.mps95 : s.mpsxsr95;
     if (v > mx) {
       mx = v;
