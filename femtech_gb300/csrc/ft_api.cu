@@ -845,7 +845,7 @@ int launch_injury_t(ftgpu_model *m, int parity) {
   const int hb = std::min((m->inj_n + kInjThreads - 1) / kInjThreads, 512);
   for (int pass = 0; pass < (int)sizeof(R); ++pass)
     k_radix_hist<R><<<dim3(hb, 2), kInjThreads, 0, m->stream>>>(J, pass);
-  k_radix_list<R><<<dim3(hb, 2), kInjThreads, 0, m->stream>>>(J);
+  k_radix_list<R><<<hb, kInjThreads, 0, m->stream>>>(J);
   k_radix_final<R><<<1, kRadixBins, 0, m->stream>>>(J);
   CK(cudaGetLastError());
   return 0;

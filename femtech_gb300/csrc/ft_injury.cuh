@@ -292,29 +292,39 @@ __global__ void __launch_bounds__(kInjThreads) k_radix_hist(const InjuryArgs<R> 
   }
 }
 
-// The selected value; where it beats the running maximum, the listed elements
-// at or above it are marked (flag bit) and counted.
+// The selected values; where one beats its running maximum, the listed
+// elements at or above it are marked (flag bit) and counted.  Both selections
+// in one pass per element, so each flag byte is written by one thread.
 template <class R>
 __global__ void __launch_bounds__(kInjThreads) k_radix_list(const InjuryArgs<R> A) {
-  const int sel = blockIdx.y;  // 0: MPS, 1: MPS x rate
   typedef typename std::conditional<sizeof(R) == 8, uint64_t, uint32_t>::type K;
   constexpr int KB = sizeof(K) * 8;
   if (A.clock[A.parity].done) return;
   __shared__ unsigned stage[(KB / 8) * kRadixBins];
-  __shared__ K s_prefix;
-  block_radix_prefix<K>(A.hist + (sel * (KB / 8)) * kRadixBins, KB / 8, A.n, stage, &s_prefix);
-  const R v = fkey_inv(s_prefix);
-  const double prev = sel == 0 ? A.state->mps95 : A.state->mpsxsr95;
-  if (!(double(v) > prev)) return;
-  const R *val = sel == 0 ? A.ps_old : A.psxsr;
-  const uint8_t bit = sel == 0 ? kInjInMps95 : kInjInMpsxsr95;
-  unsigned cnt = 0;
+  __shared__ K s_prefix[2];
+  for (int sel = 0; sel < 2; ++sel)
+    block_radix_prefix<K>(A.hist + (sel * (KB / 8)) * kRadixBins, KB / 8, A.n, stage,
+                          &s_prefix[sel]);
+  const R v0 = fkey_inv(s_prefix[0]), v1 = fkey_inv(s_prefix[1]);
+  const bool up0 = double(v0) > A.state->mps95, up1 = double(v1) > A.state->mpsxsr95;
+  if (!up0 && !up1) return;
+  unsigned c0 = 0, c1 = 0;
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < A.n; j += gridDim.x * blockDim.x) {
-    const bool in = val[j] >= v;
-    A.flags[j] = in ? (A.flags[j] | bit) : (A.flags[j] & (uint8_t)~bit);
-    cnt += in;
+    uint8_t f = A.flags[j];
+    if (up0) {
+      const bool in = A.ps_old[j] >= v0;
+      f = in ? (f | kInjInMps95) : (f & (uint8_t)~kInjInMps95);
+      c0 += in;
+    }
+    if (up1) {
+      const bool in = A.psxsr[j] >= v1;
+      f = in ? (f | kInjInMpsxsr95) : (f & (uint8_t)~kInjInMpsxsr95);
+      c1 += in;
+    }
+    A.flags[j] = f;
   }
-  if (cnt) atomicAdd(&A.count[sel], cnt);
+  if (c0) atomicAdd(&A.count[0], c0);
+  if (c1) atomicAdd(&A.count[1], c1);
 }
 
 // Running maxima of the two percentiles (after k_radix_list of both).
