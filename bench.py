@@ -242,6 +242,20 @@ def make_workload(name, size=None):
                     elem_bytes=eb, flop=None, kernel="k_elem<float,C3D4,NH|GOH+Prony>",
                     material="shell NH E=6GPa nu=0.3; core GOH mu=1kPa k1=5kPa k2=10 kappa=0.1 "
                              "lambda=2.19e8 + Prony g1=0.6 tau1=6ms")
+    if name == "head-impact":
+        # the brain drivers' set-up: rigid skull (material 0) moved by sampled
+        # angular and linear accelerations, integrated on the device each step
+        target = int(size) if size else 2_000_000
+        mesh, mats, loads, rec = mg.head_impact_case(target_elements=target)
+        E, N = len(mesh["etype"]), len(mesh["coordinates"])
+        inner = int((mesh["pid"] == 1).sum())
+        eb = E * (16 + 4) + inner * (12 + 96) + N * ELEM_BYTES_PER_NODE
+        return dict(mesh=mesh, mats=mats, loads=loads, instances=None, rigid=rec,
+                    label="head_tet4_ellipsoid_%dk_rigid_skull_GOH_prony_sampled_accelerations"
+                          % (E // 1000),
+                    elem_bytes=eb, flop=None, kernel="k_elem<float,C3D4,GOH+Prony>",
+                    material="shell rigid (material 0); core GOH mu=1kPa k1=5kPa k2=10 "
+                             "kappa=0.1 lambda=2.19e8 + Prony g1=0.6 tau1=6ms; 6 records at 10 kHz")
     if name == "ensemble":
         n = int(size) if size else 256
         mesh, mats, loads, off = mg.ensemble_case(n_instances=n)
@@ -317,7 +331,8 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="block", choices=["block", "head", "ensemble"])
+    ap.add_argument("--workload", default="block",
+                    choices=["block", "head", "head-impact", "ensemble"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--size", default=None,
                     help="block: nx,ny,nz; head: target elements; ensemble: instances")
@@ -359,6 +374,8 @@ def main():
     model = ft.Model(mesh, mats, precision=ft.MIXED, device=dev, loads=loads,
                      instances=wl["instances"])
     log("setup %.1f s (%d elements, %d nodes)" % (time.perf_counter() - t0, E, N))
+    if wl.get("rigid") is not None:
+        model.set_rigid_body(wl["rigid"])
     if args.energy:
         model.set_energy(True)
     if args.injury:
@@ -473,6 +490,8 @@ def end_to_end(ft, wl, dev, steps, E, N):
     torch.cuda.synchronize(dev)
     t = time.perf_counter()
     model.set_state(u0, v0, a0, 0.0)
+    if wl.get("rigid") is not None:
+        model.set_rigid_body(wl["rigid"])
     model.init_explicit(reduction=0.9, failure_dt=0.0, tmax=1e300)
     done = 0
     while done < steps:

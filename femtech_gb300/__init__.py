@@ -297,6 +297,36 @@ class Model:
         return dict(internal_work=wi.value, external_work=we.value, kinetic=ke.value,
                     max_violation=mx.value, violations=nv.value)
 
+    def set_rigid_body(self, channels, centre=None, inst=0):
+        """Acceleration records of instance ``inst``'s rigid body: six (times,
+        values) pairs, angular x, y, z (rad/s^2) then linear x, y, z (m/s^2);
+        ``channels=None`` removes them (call before init_explicit)."""
+        L = lib()
+        L.ftgpu_set_rigid_body.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                           C.c_void_p, C.c_void_p]
+        if channels is None:
+            _check(L.ftgpu_set_rigid_body(self.h, int(inst), None, None, None, None))
+            return
+        tabs = [(np.ascontiguousarray(t, np.float64), np.ascontiguousarray(v, np.float64))
+                for t, v in channels]
+        if len(tabs) != 6 or any(len(t) != len(v) for t, v in tabs):
+            raise ValueError("six (times, values) channels of equal lengths")
+        n = (C.c_int * 6)(*[len(t) for t, _ in tabs])
+        tp = (C.c_void_p * 6)(*[t.ctypes.data for t, _ in tabs])
+        vp = (C.c_void_p * 6)(*[v.ctypes.data for _, v in tabs])
+        c = None if centre is None else np.ascontiguousarray(centre, np.float64)
+        _check(L.ftgpu_set_rigid_body(self.h, int(inst), n, tp, vp,
+                                      None if c is None else c.ctypes.data))
+
+    def rigid_body(self, inst=0):
+        """Integrator state (y, yd) of instance ``inst``'s rigid body:
+        y = [omega, r, v_cm, x_cm], yd = dy/dt at the current time."""
+        L = lib()
+        L.ftgpu_get_rigid_body.argtypes = [C.c_void_p, C.c_int, _dp, _dp]
+        y, yd = np.zeros(12), np.zeros(12)
+        _check(L.ftgpu_get_rigid_body(self.h, int(inst), y, yd))
+        return y, yd
+
     def launches_per_step(self):
         return lib().ftgpu_launches_per_step(self.h)
 

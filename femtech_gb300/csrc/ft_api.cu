@@ -199,6 +199,10 @@ struct ftgpu_model {
   int node_threads = 256;
   bool setup_done = false, init_done = false;
   PatchSet ps;
+  // per group: material 0 (rigid, zero stress) with every node of every
+  // element fully constrained -- zero force and no stable-dt contribution,
+  // so the loop's force and dt passes skip it (its force slots stay zero)
+  std::vector<char> group_idle;
   std::vector<int> gp_off;  // reference Gauss-point offset of each element
   long long ngp_total = 0;
   long long S = 0;
@@ -222,6 +226,20 @@ struct ftgpu_model {
   // energy balance of the explicit loop (CheckEnergy), single instance only
   bool energy_on = false;
   DBuf du, fprev, epart, estate;
+  // rigid bodies driven by sampled accelerations, per instance
+  struct RigidHost {
+    bool on = false;
+    std::vector<double> tab[6];  // times then values of each channel
+    double c[3] = {0.0, 0.0, 0.0};
+  };
+  std::vector<RigidHost> rigid;
+  bool rigid_on = false;
+  DBuf rb, rbtab, rbstate, rbstep;
+  DBuf rig_list;                // nodes with a rigid-body DOF
+  std::vector<int> rig_host;
+  long long rig_nodes = 0;
+  cudaStream_t stream2 = nullptr;  // the rigid-body branch of a step
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   DBuf slot_off, slots, node_inst, nbc, fnsbuf;
   DBuf dX, u, v, a, vh, mass, minv, fi;
   DBuf gpF, gpJ, gpS;
@@ -244,6 +262,9 @@ struct ftgpu_model {
     for (cudaEvent_t e : prof_ev) cudaEventDestroy(e);
     if (h_clock) cudaFreeHost(h_clock);
     if (h_err) cudaFreeHost(h_err);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (stream2) cudaStreamDestroy(stream2);
     if (stream) cudaStreamDestroy(stream);
   }
 };
@@ -342,6 +363,12 @@ NodeArgs node_args(ftgpu_model *m, int mode, int parity) {
     if (m->fns[i].kind == kBckRot) A.rot_ids[A.nrot++] = (int)i;
   A.stepsc = m->stepsc.as<StepScalars>();
   A.rottrig = m->rottrig.as<double>();
+  if (m->rigid_on) {
+    A.rb = m->rb.as<RigidBody>();
+    A.rbtab = m->rbtab.as<double>();
+    A.rbstate = m->rbstate.as<RigidState>();
+    A.rbstep = m->rbstep.as<RigidStep>();
+  }
   if (m->energy_on) {
     A.du = m->du.p;
     A.fprev = m->fprev.p;
@@ -351,25 +378,57 @@ NodeArgs node_args(ftgpu_model *m, int mode, int parity) {
   return A;
 }
 
+template <class R, bool EN>
+void node_step_launch(long long nb, int th, cudaStream_t st, const NodeArgs &A) {
+  if (A.node_list)
+    k_node_step<R, EN, true><<<(unsigned)nb, th, 0, st>>>(A);
+  else
+    k_node_step<R, EN, false><<<(unsigned)nb, th, 0, st>>>(A);
+}
+
 int launch_node(ftgpu_model *m, int mode, int parity) {
   NodeArgs A = node_args(m, mode, parity);
   const int th = m->node_threads;
-  const long long nb = (m->nNodes + th - 1) / th;
+  long long nb = (m->nNodes + th - 1) / th;
   const bool step = mode == kNodeFused || mode == kNodeFinish;
-  if (step) k_step_scalars<<<(unsigned)((m->ninst + 127) / 128), 128, 0, m->stream>>>(A);
   const bool en = step && m->energy_on;
-  if (is_fp64(m)) {
-    if (en)
-      k_node_step<double, true><<<(unsigned)nb, th, 0, m->stream>>>(A);
-    else if (step)
-      k_node_step<double, false><<<(unsigned)nb, th, 0, m->stream>>>(A);
+  const bool f64 = is_fp64(m);
+  auto node_step = [&](long long blocks, cudaStream_t st, const NodeArgs &B) {
+    if (f64)
+      en ? node_step_launch<double, true>(blocks, th, st, B)
+         : node_step_launch<double, false>(blocks, th, st, B);
     else
-      k_node<double><<<(unsigned)nb, th, 0, m->stream>>>(A);
+      en ? node_step_launch<float, true>(blocks, th, st, B)
+         : node_step_launch<float, false>(blocks, th, st, B);
+  };
+  if (step)
+    k_step_scalars<<<(unsigned)((m->ninst + 127) / 128), 128, 0, m->stream>>>(A);
+  if (step && m->rigid_on && m->rig_nodes > 0) {
+    // fork: the rigid bodies' integrator and then their driven nodes on the
+    // second stream, every other node on the first; join before what follows
+    const long long nbr = (m->rig_nodes + th - 1) / th;
+    NodeArgs B = A;
+    B.node_list = m->rig_list.as<int>();
+    B.nlist = m->rig_nodes;
+    B.epart_off = nb;
+    A.skip_rigid = 1;
+    CK(cudaEventRecord(m->ev_fork, m->stream));
+    CK(cudaStreamWaitEvent(m->stream2, m->ev_fork, 0));
+    k_rigid_step<<<(unsigned)m->ninst, 32, 0, m->stream2>>>(B);
+    node_step(nbr, m->stream2, B);
+    node_step(nb, m->stream, A);
+    CK(cudaEventRecord(m->ev_join, m->stream2));
+    CK(cudaStreamWaitEvent(m->stream, m->ev_join, 0));
+    nb += nbr;
+  } else if (step) {
+    if (m->rigid_on)  // records without driven nodes: the state still advances
+      k_rigid_step<<<(unsigned)m->ninst, 32, 0, m->stream>>>(A);
+    node_step(nb, m->stream, A);
   } else {
-    if (en)
-      k_node_step<float, true><<<(unsigned)nb, th, 0, m->stream>>>(A);
-    else if (step)
-      k_node_step<float, false><<<(unsigned)nb, th, 0, m->stream>>>(A);
+    if (mode == kNodeBegin && m->rigid_on)
+      k_rigid_begin<<<(unsigned)m->ninst, 32, 0, m->stream>>>(A);
+    if (f64)
+      k_node<double><<<(unsigned)nb, th, 0, m->stream>>>(A);
     else
       k_node<float><<<(unsigned)nb, th, 0, m->stream>>>(A);
   }
@@ -383,6 +442,7 @@ int launch_groups_t(ftgpu_model *m, int parity, int use_clock, double dt_direct,
   const int PE = max_patch(m);
   for (size_t gi = 0; gi < m->ps.groups.size(); ++gi) {
     const PatchGroup &g = m->ps.groups[gi];
+    if (gp == 0 && gi < m->group_idle.size() && m->group_idle[gi]) continue;
     ElemArgs<R> A = elem_args<R>(m, g, (int)gi);
     A.parity = parity;
     A.use_clock = use_clock;
@@ -539,7 +599,7 @@ int check_err(ftgpu_model *m) {
 
 // Per-element part word: part | (1 << 31) when every node of the element has
 // all three DOFs constrained (skipped by StableTimeStep.cpp:13-19).
-int upload_epid(ftgpu_model *m) {
+int upload_epid(ftgpu_model *m, bool zero_idle) {
   std::vector<int> w(m->nE);
   for (int ge = 0; ge < m->nE; ++ge) {
     const int e = m->ps.elem_order[ge];
@@ -555,6 +615,23 @@ int upload_epid(ftgpu_model *m) {
       }
     }
     w[ge] = m->pid[e] | (active ? 0 : (int)0x80000000u);
+  }
+  m->group_idle.assign(m->ps.groups.size(), 0);
+  for (size_t gi = 0; gi < m->ps.groups.size(); ++gi) {
+    const PatchGroup &g = m->ps.groups[gi];
+    if (g.mat != 0 || g.npatch == 0) continue;
+    bool idle = true;
+    for (int ge = g.elem_begin; ge < g.elem_begin + g.nelem && idle; ++ge)
+      idle = (w[ge] & (int)0x80000000u) != 0;
+    m->group_idle[gi] = idle ? 1 : 0;
+    if (idle && zero_idle) {  // its slots may hold forces of an earlier BC table
+      const size_t rb = is_fp64(m) ? sizeof(double) : sizeof(float);
+      const long long s0 = m->ps.patch_node_off[g.patch_begin];
+      const long long s1 = m->ps.patch_node_off[g.patch_begin + g.npatch];
+      for (int d = 0; d < 3; ++d)
+        CK(cudaMemsetAsync((char *)m->sF.p + (d * m->S + s0) * rb, 0, (s1 - s0) * rb,
+                           m->stream));
+    }
   }
   return m->epid.upload(w.data(), w.size());
 }
@@ -643,7 +720,7 @@ int setup_t(ftgpu_model *m) {
   CKI(m->lconn.upload(ps.lconn.data(), ps.lconn.size()));
   CKI(m->slot_off.upload(ps.node_slot_off.data(), N + 1));
   CKI(m->slots.upload(ps.node_slots.data(), ps.node_slots.size()));
-  CKI(upload_epid(m));
+  CKI(upload_epid(m, false));  // the force slots are allocated zeroed below
   CKI(upload_materials<R>(m));
   // reference coordinates per slot: absolute in FP64 mode, relative to the
   // patch's first node in mixed mode (keeps FP32 digits for element geometry)
@@ -1078,11 +1155,11 @@ int ftgpu_set_bc(ftgpu_model *m, const int *dof_fn, int nfn, const ftgpu_bc_fn *
     m->fns[i].kind = fns[i].kind;
     m->fns[i].pad = 0;
     for (int k = 0; k < 8; ++k) m->fns[i].p[k] = fns[i].p[k];
-    if (fns[i].kind < 0 || fns[i].kind > 3) return fail(FTGPU_ERR_INPUT, "set_bc: kind");
+    if (fns[i].kind < 0 || fns[i].kind > 4) return fail(FTGPU_ERR_INPUT, "set_bc: kind");
   }
   if (m->setup_done) {
     CKI(upload_bc(m));
-    CKI(upload_epid(m));
+    CKI(upload_epid(m, true));
     drop_graphs(m);
   }
   return FTGPU_OK;
@@ -1236,6 +1313,50 @@ int ftgpu_set_state(ftgpu_model *m, const double *u, const double *v, const doub
   return FTGPU_OK;
 }
 
+// Rigid bodies at the start of the loop: every rigid-body DOF must belong
+// to an instance with acceleration records; state zero (ex5.cpp:886-890),
+// table cursors at 0 and the node maps of the zero state (u = v = a = 0).
+int reset_rigid(ftgpu_model *m) {
+  std::vector<int> rig;
+  for (size_t i = 0; i < m->dof_fn.size(); ++i) {
+    const int f = m->dof_fn[i];
+    if (f < 0 || m->fns[f].kind != kBckRigid) continue;
+    const int node = (int)(i / 3);
+    if (rig.empty() || rig.back() != node) rig.push_back(node);
+    int inst = 0;
+    if (m->inst_set)
+      inst = (int)(std::upper_bound(m->node_off.begin(), m->node_off.end(), node) -
+                   m->node_off.begin()) - 1;
+    if (!m->rigid_on || inst >= (int)m->rigid.size() || !m->rigid[inst].on)
+      return fail(FTGPU_ERR_INPUT, "rigid-body DOF in an instance without acceleration records");
+  }
+  if (!m->rigid_on) return 0;
+  if (rig != m->rig_host) {  // a new driven-node list: the captured branch changes
+    drop_graphs(m);
+    m->rig_host = rig;
+    m->rig_nodes = (long long)rig.size();
+    if (!rig.empty()) CKI(m->rig_list.upload(rig.data(), rig.size()));
+  }
+  if (!m->stream2) {
+    CK(cudaStreamCreateWithFlags(&m->stream2, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&m->ev_fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&m->ev_join, cudaEventDisableTiming));
+  }
+  std::vector<RigidState> st(m->ninst);
+  std::vector<RigidStep> sp(m->ninst);
+  for (int i = 0; i < m->ninst; ++i) {
+    memset(&st[i], 0, sizeof(RigidState));
+    memset(&sp[i], 0, sizeof(RigidStep));
+    for (int j = 0; j < 3; ++j) sp[i].c[j] = m->rigid[i].c[j];
+  }
+  CK(cudaMemcpyAsync(m->rbstate.p, st.data(), st.size() * sizeof(RigidState),
+                     cudaMemcpyHostToDevice, m->stream));
+  CK(cudaMemcpyAsync(m->rbstep.p, sp.data(), sp.size() * sizeof(RigidStep),
+                     cudaMemcpyHostToDevice, m->stream));
+  CK(cudaStreamSynchronize(m->stream));  // the host vectors go out of scope
+  return 0;
+}
+
 int ftgpu_init_explicit(ftgpu_model *m, double reduction, double failure_dt, double tmax) {
   if (!m || !m->setup_done) return fail(FTGPU_ERR_STATE, "init_explicit before setup");
   CK(cudaSetDevice(m->device));
@@ -1248,6 +1369,7 @@ int ftgpu_init_explicit(ftgpu_model *m, double reduction, double failure_dt, dou
   CK(cudaMemcpyAsync(m->instp.p, m->inst.data(), m->ninst * sizeof(InstParams),
                      cudaMemcpyHostToDevice, m->stream));
   CK(cudaMemsetAsync(m->err.p, 0, sizeof(int), m->stream));
+  CKI(reset_rigid(m));
   NodeArgs A = node_args(m, kNodeBegin, 0);
   k_apply_bc<<<(unsigned)((m->nNodes + 255) / 256), 256, 0, m->stream>>>(A, m->t0);
   CK(cudaGetLastError());
@@ -1333,7 +1455,8 @@ int ftgpu_get_instance_clock(ftgpu_model *m, double *time, double *dt, long long
 int ftgpu_launches_per_step(ftgpu_model *m) {
   if (!m || !m->setup_done) return 0;
   int g = 0;
-  for (auto &x : m->ps.groups) g += x.npatch > 0;
+  for (size_t gi = 0; gi < m->ps.groups.size(); ++gi)
+    g += m->ps.groups[gi].npatch > 0 && !(gi < m->group_idle.size() && m->group_idle[gi]);
   // element groups, k_step_scalars, k_node_step; a surrogate adds the
   // feature pass and the inference kernel of each material-7 group
   if (m->surr)
@@ -1487,7 +1610,8 @@ int ftgpu_set_energy(ftgpu_model *m, int enable) {
   if (enable && !m->energy_on) {
     // du and f_prev in the element precision (FP32 in mixed mode)
     const size_t n3b = 3 * (size_t)m->nNodes * (is_fp64(m) ? sizeof(double) : sizeof(float));
-    const size_t maxblocks = ((size_t)m->nNodes + 63) / 64;  // smallest node block: 64
+    // smallest node block: 64; the rigid-body branch adds at most as many
+    const size_t maxblocks = 2 * (((size_t)m->nNodes + 63) / 64);
     CKI(m->du.alloc(n3b));
     CKI(m->fprev.alloc(n3b));
     CKI(m->epart.alloc(3 * maxblocks * sizeof(double)));
@@ -1499,6 +1623,80 @@ int ftgpu_set_energy(ftgpu_model *m, int enable) {
   m->energy_on = enable != 0;
   drop_graphs(m);
   m->init_done = false;  // the loop must start again from init_explicit
+  return FTGPU_OK;
+}
+
+int ftgpu_set_rigid_body(ftgpu_model *m, int inst, const int *npts, const double *const *times,
+                         const double *const *values, const double *centre) {
+  if (!m || !m->setup_done) return fail(FTGPU_ERR_STATE, "set_rigid_body before setup");
+  if (inst < 0 || inst >= m->ninst) return fail(FTGPU_ERR_INPUT, "set_rigid_body: instance");
+  CK(cudaSetDevice(m->device));
+  CK(cudaStreamSynchronize(m->stream));
+  if ((int)m->rigid.size() != m->ninst) m->rigid.assign(m->ninst, ftgpu_model::RigidHost());
+  ftgpu_model::RigidHost r;
+  if (npts) {
+    if (!times || !values) return fail(FTGPU_ERR_INPUT, "set_rigid_body: tables");
+    for (int k = 0; k < 6; ++k) {
+      const int n = npts[k];
+      if (n < 1 || !times[k] || !values[k])
+        return fail(FTGPU_ERR_INPUT, "set_rigid_body: every channel needs >= 1 sample");
+      for (int j = 0; j < n; ++j) {
+        if (!std::isfinite(times[k][j]) || !std::isfinite(values[k][j]))
+          return fail(FTGPU_ERR_INPUT, "set_rigid_body: non-finite sample");
+        if (j > 0 && times[k][j] < times[k][j - 1])
+          return fail(FTGPU_ERR_INPUT, "set_rigid_body: sample times must not decrease");
+      }
+      r.tab[k].assign(times[k], times[k] + n);
+      r.tab[k].insert(r.tab[k].end(), values[k], values[k] + n);
+    }
+    if (centre)
+      for (int j = 0; j < 3; ++j) r.c[j] = centre[j];
+    r.on = true;
+  }
+  m->rigid[inst] = r;
+  m->rigid_on = false;
+  for (auto &x : m->rigid) m->rigid_on = m->rigid_on || x.on;
+  if (m->rigid_on) {
+    std::vector<RigidBody> rb(m->ninst);
+    std::vector<double> tab;
+    for (int i = 0; i < m->ninst; ++i) {
+      memset(&rb[i], 0, sizeof(RigidBody));
+      rb[i].on = m->rigid[i].on ? 1 : 0;
+      for (int k = 0; k < 6 && rb[i].on; ++k) {
+        const std::vector<double> &t = m->rigid[i].tab[k];
+        const int n = (int)t.size() / 2;
+        rb[i].off[k] = (int)tab.size();
+        rb[i].cnt[k] = n;
+        tab.insert(tab.end(), t.begin(), t.end());
+        for (int j = 0; j < n; ++j)  // segment slopes (a zero-length segment is never used)
+          tab.push_back(j + 1 < n && t[j + 1] > t[j] ? (t[n + j + 1] - t[n + j]) / (t[j + 1] - t[j])
+                                                     : 0.0);
+      }
+    }
+    if (tab.empty()) tab.push_back(0.0);
+    CKI(m->rb.upload(rb.data(), rb.size()));
+    CKI(m->rbtab.upload(tab.data(), tab.size()));
+    CKI(m->rbstate.alloc(m->ninst * sizeof(RigidState)));
+    CKI(m->rbstep.alloc(m->ninst * sizeof(RigidStep)));
+  }
+  drop_graphs(m);
+  m->init_done = false;  // the loop must start again from init_explicit
+  return FTGPU_OK;
+}
+
+int ftgpu_get_rigid_body(ftgpu_model *m, int inst, double *y, double *yd) {
+  if (!m || !m->rigid_on) return fail(FTGPU_ERR_STATE, "no rigid body");
+  if (inst < 0 || inst >= m->ninst || !m->rigid[inst].on)
+    return fail(FTGPU_ERR_INPUT, "get_rigid_body: instance without acceleration records");
+  CK(cudaSetDevice(m->device));
+  RigidState st;
+  CK(cudaMemcpyAsync(&st, m->rbstate.as<RigidState>() + inst, sizeof(st), cudaMemcpyDeviceToHost,
+                     m->stream));
+  CK(cudaStreamSynchronize(m->stream));
+  for (int j = 0; j < 12; ++j) {
+    if (y) y[j] = st.y[j];
+    if (yd) yd[j] = st.yd[j];
+  }
   return FTGPU_OK;
 }
 

@@ -47,7 +47,7 @@ constexpr unsigned long long kDtHugeBits = 0x4415af1d78b58c40ull;
 constexpr int kMaxRotFns = 8;
 
 enum { kBcFree = -1, kBcHold = -2 };
-enum { kBckFixed = 0, kBckRamp = 1, kBckSine = 2, kBckRot = 3 };
+enum { kBckFixed = 0, kBckRamp = 1, kBckSine = 2, kBckRot = 3, kBckRigid = 4 };
 enum { kErrInverted = 1, kErrDt = 2, kErrIndex = 4, kErrWait = 8 };
 
 template <class Real>
@@ -103,6 +103,36 @@ struct EnergyState {
   long long steps, violations;
 };
 
+// Rigid body of an instance driven by sampled accelerations (the brain
+// drivers' ApplyAccBoundaryConditions, examples/ex5/ex5.cpp:339-392):
+// channels 0-2 angular acceleration x, y, z, 3-5 linear acceleration x, y, z,
+// each a table of cnt[k] times, cnt[k] values and cnt[k] segment slopes
+// (the last unused) at off[k] of the table array.
+struct RigidBody {
+  int off[6], cnt[6];
+  int on, pad;
+};
+
+// Integrator state (ex5.cpp:100-105): y = [omega, r, v_cm, x_cm] (r: rotation
+// generator, R = exp(r) as a quaternion), yd = dy/dt at the last step's end
+// (first same as last), cur[k] = a table index at or below every later
+// lookup of channel k.
+struct RigidState {
+  double y[12], yd[12];
+  int cur[6];
+  int pad[2];
+};
+
+// The motion of every driven node at the current time, as three affine maps
+// of the position relative to the centre c (X' = X - c):
+//   u = Mm X' + disp,  v = WM X' + vel,  a = AM X' + ca,
+// Mm = R - I, WM = [omega]x R, AM = ([omega]x^2 + [alpha]x) R,
+// ca = 2 omega x v_cm + a_cm.
+struct RigidStep {
+  double Mm[9], WM[9], AM[9];
+  double disp[3], vel[3], ca[3], c[3];
+};
+
 // Per-instance scalars of one end-of-step launch (k_step_scalars)
 struct StepScalars {
   double t_np1, t_np2, ndt;
@@ -144,6 +174,18 @@ struct NodeArgs {
   void *fprev;                // [3][N] internal force of the previous step (Real)
   double *epart;              // [node blocks][3] partial sums: kinetic, internal, external
   EnergyState *energy;
+  // rigid bodies driven by sampled accelerations (null when none)
+  const RigidBody *rb;        // [ninst]
+  const double *rbtab;        // tables of every instance
+  RigidState *rbstate;        // [ninst]
+  RigidStep *rbstep;          // [ninst]
+  // k_node_step over a subset: node_list (nlist entries) or every node but
+  // those with a rigid-body DOF (skip_rigid); its energy partials start at
+  // block epart_off
+  const int *node_list;
+  long long nlist;
+  int skip_rigid;
+  long long epart_off;
 };
 
 enum { kNodeBegin = 0, kNodeFused = 1, kNodeFinish = 2, kNodeInit = 3, kNodeGather = 4,

@@ -80,6 +80,233 @@ __device__ __forceinline__ void bc_value(const BcFn &b, int d, double t, const d
   }
 }
 
+// ---- rigid body driven by sampled accelerations (ex5.cpp:339-392) ----
+
+// interpolateLinear (src/math/math.cpp:99-119) of the table (x, y) of n
+// points: 0 below the table, the last value above it, y[0] at x[0], else the
+// segment of the first x[i] >= value (i >= 1), evaluated with the segment
+// slopes g precomputed on the host (the reference divides per lookup; the
+// results differ in the last bit).  The search starts at i = cur + 1: every
+// x[1..cur] lies below every value looked up from now on (times only grow),
+// so the segment is the reference's.  seg = the segment found, -1 for the
+// three end cases.
+__device__ __forceinline__ double rb_interp(const double *x, const double *y, const double *g,
+                                            int n, int cur, double value, int &seg) {
+  seg = -1;
+  if (value < x[0]) return 0.0;
+  if (value > x[n - 1]) return y[n - 1];
+  if (value == x[0]) return y[0];
+  int i = cur + 1 < 1 ? 1 : cur + 1;
+  while (i < n - 1 && !(value <= x[i])) ++i;
+  seg = i - 1;
+  return fma(g[seg], value - x[seg], y[seg]);
+}
+
+// |r| cot|r| = 1 - s P(s) and (1 - |r| cot|r|) / |r|^2 = P(s), s = |r|^2, from
+// the Maclaurin series x cot x = 1 - sum_{n>=1} 2^{2n} |B_{2n}| x^{2n} / (2n)!
+// (B: Bernoulli numbers), twelve terms: for s < 1/4 the first omitted term is
+// below 1e-19.  Estrin's scheme (four dependent steps instead of Horner's
+// eleven: the step is a latency-bound FP64 chain), no division.
+__device__ __forceinline__ double xcotx_p(double s) {
+  const double s2 = s * s, s4 = s2 * s2, s8 = s4 * s4;
+  const double p0 = fma(1.0 / 45.0, s, 1.0 / 3.0);
+  const double p1 = fma(1.0 / 4725.0, s, 2.0 / 945.0);
+  const double p2 = fma(1382.0 / 638512875.0, s, 2.0 / 93555.0);
+  const double p3 = fma(3617.0 / 162820783125.0, s, 4.0 / 18243225.0);
+  const double p4 = fma(349222.0 / 1531329465290625.0, s, 87734.0 / 38979295480125.0);
+  const double p5 = fma(472728182.0 / 201919571963756521875.0, s, 310732.0 / 13447856940643125.0);
+  const double q0 = fma(p1, s2, p0), q1 = fma(p3, s2, p2), q2 = fma(p5, s2, p4);
+  return fma(q2, s8, fma(q1, s4, q0));
+}
+
+// Rate of the rotation generator (ex5.cpp:1001-1018; M. Boyle, "The
+// integration of angular velocity", 2017): component c of
+// (omega x r + |r| cot|r| omega + (1 - |r| cot|r|) (rhat . omega) rhat) / 2,
+// omega / 2 for |r| < 1e-10.  Every lane evaluates the same branch.
+__device__ __forceinline__ double rb_rdot(int c, double w0, double w1, double w2, double r0,
+                                          double r1, double r2) {
+  const double wc = c == 0 ? w0 : (c == 1 ? w1 : w2);
+  const double s = r0 * r0 + r1 * r1 + r2 * r2;
+  if (s < 1e-20) return 0.5 * wc;
+  double rc, g;
+  if (s < 0.25) {
+    g = xcotx_p(s);
+    rc = fma(-s, g, 1.0);
+  } else {
+    const double rm = sqrt(s);
+    rc = rm / tan(rm);
+    g = (1.0 - rc) / s;
+  }
+  const double cr = c == 0 ? w1 * r2 - w2 * r1 : (c == 1 ? -w0 * r2 + w2 * r0 : w0 * r1 - w1 * r0);
+  const double rcmp = c == 0 ? r0 : (c == 1 ? r1 : r2);
+  const double rw = r0 * w0 + r1 * w1 + r2 * w2;
+  return 0.5 * (cr + rc * wc + g * rw * rcmp);
+}
+
+// Component j (lane j < 12) of computeDerivatives (ex5.cpp:976-1020) at the
+// stage state held one component per lane, with the accelerations al[3],
+// ac[3] sampled at the stage time.  All 32 lanes take part in the shuffles.
+__device__ __forceinline__ double rb_deriv_lane(int j, double xj, const double *acc) {
+  const unsigned full = 0xffffffffu;
+  const double w0 = __shfl_sync(full, xj, 0), w1 = __shfl_sync(full, xj, 1),
+               w2 = __shfl_sync(full, xj, 2), r0 = __shfl_sync(full, xj, 3),
+               r1 = __shfl_sync(full, xj, 4), r2 = __shfl_sync(full, xj, 5);
+  const double vel = __shfl_sync(full, xj, j >= 9 && j < 12 ? j - 3 : 0);
+  if (j < 3) return acc[j];
+  if (j < 6) return rb_rdot(j - 3, w0, w1, w2, r0, r1, r2);
+  if (j < 9) return acc[j - 3];
+  return vel;
+}
+
+// One integrator step of instance i's rigid body from t over h, by one warp:
+// the explicit Runge-Kutta pair of Dormand and Prince (J. Comput. Appl. Math.
+// 6 (1980) 19-26), fifth-order solution, first stage from the stored
+// derivative and the derivative at t + h stored for the next step -- what
+// boost::numeric::odeint::runge_kutta_dopri5::do_step(sys, y, yd, t, h) does
+// at ex5.cpp:344.  FP64 issue is slow on this GPU and one instance's step is
+// a chain of dependent operations, so it is spread over the warp: lanes 0-29
+// look up the six channels at the five new stage times (the accelerations
+// depend on time only), then lane j < 12 carries state component j through
+// the stages, and lanes 0-11 write the node maps of the new state
+// (ex5.cpp:345-371 as matrices).
+__device__ void rigid_advance(const NodeArgs &A, int i, double t, double h,
+                              double (*sacc)[6]) {
+  const RigidBody &rb = A.rb[i];
+  if (!rb.on) return;
+  RigidState *st = A.rbstate + i;
+  const int lane = threadIdx.x & 31;
+  {
+    const int k = lane / 5, s = lane - 5 * (lane / 5);
+    int seg = -1;
+    if (lane < 30) {
+      const double cs = s == 0 ? 1.0 / 5 : (s == 1 ? 3.0 / 10 : (s == 2 ? 4.0 / 5 : 8.0 / 9));
+      const double tv = s == 4 ? t + h : t + h * cs;
+      const int n = rb.cnt[k];
+      const double *x = A.rbtab + rb.off[k];
+      sacc[s][k] = rb_interp(x, x + n, x + 2 * n, n, st->cur[k], tv, seg);
+    }
+    __syncwarp();
+    if (lane < 30 && s == 0 && seg >= 0) st->cur[k] = seg;  // stage 2: the earliest time
+    __syncwarp();
+  }
+  constexpr double a21 = 1.0 / 5, a31 = 3.0 / 40, a32 = 9.0 / 40, a41 = 44.0 / 45,
+                   a42 = -56.0 / 15, a43 = 32.0 / 9, a51 = 19372.0 / 6561,
+                   a52 = -25360.0 / 2187, a53 = 64448.0 / 6561, a54 = -212.0 / 729,
+                   a61 = 9017.0 / 3168, a62 = -355.0 / 33, a63 = 46732.0 / 5247,
+                   a64 = 49.0 / 176, a65 = -5103.0 / 18656;
+  constexpr double b1 = 35.0 / 384, b3 = 500.0 / 1113, b4 = 125.0 / 192,
+                   b5 = -2187.0 / 6784, b6 = 11.0 / 84;
+  const int j = lane < 12 ? lane : 0;
+  const double y = st->y[j], k1 = st->yd[j];
+  double x = y + (h * a21) * k1;
+  const double k2 = rb_deriv_lane(j, x, sacc[0]);
+  x = y + (h * a31) * k1 + (h * a32) * k2;
+  const double k3 = rb_deriv_lane(j, x, sacc[1]);
+  x = y + (h * a41) * k1 + (h * a42) * k2 + (h * a43) * k3;
+  const double k4 = rb_deriv_lane(j, x, sacc[2]);
+  x = y + (h * a51) * k1 + (h * a52) * k2 + (h * a53) * k3 + (h * a54) * k4;
+  const double k5 = rb_deriv_lane(j, x, sacc[3]);
+  x = y + (h * a61) * k1 + (h * a62) * k2 + (h * a63) * k3 + (h * a64) * k4 + (h * a65) * k5;
+  const double k6 = rb_deriv_lane(j, x, sacc[4]);
+  const double yn = y + (h * b1) * k1 + (h * b3) * k3 + (h * b4) * k4 + (h * b5) * k5 +
+                    (h * b6) * k6;
+  const double ydn = rb_deriv_lane(j, yn, sacc[4]);
+  if (lane < 12) {
+    st->y[j] = yn;
+    st->yd[j] = ydn;
+  }
+  // the new state on every lane
+  const unsigned full = 0xffffffffu;
+  double Y[12], L[3];
+#pragma unroll
+  for (int c = 0; c < 12; ++c) Y[c] = __shfl_sync(full, yn, c);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) L[c] = __shfl_sync(full, ydn, c);
+  const double acm = __shfl_sync(full, ydn, lane >= 9 && lane < 12 ? lane - 3 : 6);
+  // R = exp([0, r]) (quaternionExp, math.cpp:122-133): cos|r| and sin|r| / |r|
+  // by their Maclaurin series for |r| < 1/2 (nine terms each, the first
+  // omitted one below 1e-18), the library functions beyond; V -> R V R^-1 as
+  // the matrix of q / |q| (|q|^2 = 1 to rounding, so 1 / |q|^2 = 2 - |q|^2)
+  const double s = Y[3] * Y[3] + Y[4] * Y[4] + Y[5] * Y[5];
+  double qw = 1.0, d2 = 1.0;
+  if (s != 0.0) {
+    if (s < 0.25) {
+      double cw = 1.0 / 20922789888000.0, sw = 1.0 / 355687428096000.0;
+      cw = fma(cw, -s, 1.0 / 87178291200.0);
+      sw = fma(sw, -s, 1.0 / 1307674368000.0);
+      cw = fma(cw, -s, 1.0 / 479001600.0);
+      sw = fma(sw, -s, 1.0 / 6227020800.0);
+      cw = fma(cw, -s, 1.0 / 3628800.0);
+      sw = fma(sw, -s, 1.0 / 39916800.0);
+      cw = fma(cw, -s, 1.0 / 40320.0);
+      sw = fma(sw, -s, 1.0 / 362880.0);
+      cw = fma(cw, -s, 1.0 / 720.0);
+      sw = fma(sw, -s, 1.0 / 5040.0);
+      cw = fma(cw, -s, 1.0 / 24.0);
+      sw = fma(sw, -s, 1.0 / 120.0);
+      cw = fma(cw, -s, 1.0 / 2.0);
+      sw = fma(sw, -s, 1.0 / 6.0);
+      qw = fma(cw, -s, 1.0);
+      d2 = fma(sw, -s, 1.0);
+    } else {
+      const double vm = sqrt(s);
+      double sn;
+      sincos(vm, &sn, &qw);
+      d2 = sn / vm;
+    }
+  }
+  const double qx = d2 * Y[3], qy = d2 * Y[4], qz = d2 * Y[5];
+  const double nq = qw * qw + qx * qx + qy * qy + qz * qz;
+  const double s2 = 2.0 * (2.0 - nq);
+  double M[9], R[9];
+  M[0] = -s2 * (qy * qy + qz * qz);
+  M[1] = s2 * (qx * qy - qw * qz);
+  M[2] = s2 * (qx * qz + qw * qy);
+  M[3] = s2 * (qx * qy + qw * qz);
+  M[4] = -s2 * (qx * qx + qz * qz);
+  M[5] = s2 * (qy * qz - qw * qx);
+  M[6] = s2 * (qx * qz - qw * qy);
+  M[7] = s2 * (qy * qz + qw * qx);
+  M[8] = -s2 * (qx * qx + qy * qy);
+#pragma unroll
+  for (int c = 0; c < 9; ++c) R[c] = M[c] + ((c & 3) == 0 ? 1.0 : 0.0);
+  RigidStep *S = A.rbstep + i;
+  const double w0 = Y[0], w1 = Y[1], w2 = Y[2];
+  if (lane < 9) {  // entry (r, c) of Mm, [omega]x R and ([omega]x^2 + [alpha]x) R
+    const int r = lane / 3, c = lane - 3 * (lane / 3);
+    const double W[9] = {0.0, -w2, w1, w2, 0.0, -w0, -w1, w0, 0.0};
+    const double Al[9] = {0.0, -L[2], L[1], L[2], 0.0, -L[0], -L[1], L[0], 0.0};
+    double WW[3];  // row r of [omega]x^2 + [alpha]x
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      WW[k] = W[3 * r] * W[k] + W[3 * r + 1] * W[3 + k] + W[3 * r + 2] * W[6 + k] + Al[3 * r + k];
+    S->Mm[lane] = M[lane];
+    S->WM[lane] = W[3 * r] * R[c] + W[3 * r + 1] * R[3 + c] + W[3 * r + 2] * R[6 + c];
+    S->AM[lane] = WW[0] * R[c] + WW[1] * R[3 + c] + WW[2] * R[6 + c];
+  } else if (lane < 12) {  // component c of x_cm, v_cm and 2 omega x v_cm + a_cm
+    const int c = lane - 9;
+    const double v0 = Y[6], v1 = Y[7], v2 = Y[8];
+    const double ov = c == 0 ? w1 * v2 - w2 * v1 : (c == 1 ? -w0 * v2 + w2 * v0 : w0 * v1 - w1 * v0);
+    S->disp[c] = Y[9 + c];
+    S->vel[c] = Y[6 + c];
+    S->ca[c] = 2.0 * ov + acm;
+  }
+}
+
+// Displacement, velocity and acceleration of node n under its instance's
+// rigid-body motion (ex5.cpp:361-370 through the maps of RigidStep).
+__device__ __forceinline__ void rigid_node(const RigidStep *S, const double *X, long long N,
+                                           long long n, double (&u)[3], double (&v)[3],
+                                           double (&a)[3]) {
+  const double x0 = X[n] - S->c[0], x1 = X[N + n] - S->c[1], x2 = X[2 * N + n] - S->c[2];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    u[r] = S->Mm[3 * r] * x0 + S->Mm[3 * r + 1] * x1 + S->Mm[3 * r + 2] * x2 + S->disp[r];
+    v[r] = S->WM[3 * r] * x0 + S->WM[3 * r + 1] * x1 + S->WM[3 * r + 2] * x2 + S->vel[r];
+    a[r] = S->AM[3 * r] * x0 + S->AM[3 * r + 1] * x1 + S->AM[3 * r + 2] * x2 + S->ca[r];
+  }
+}
+
 // Time bookkeeping of one step, as the driver does it on the host
 // (ex9.cpp:107-113,172): t_{n+1} = t_n + dt, t_half = (t_{n+1} + t_n) / 2, the
 // next dt = ExplicitTimeStepReduction * StableTimeStep(), and the stop tests.
@@ -141,6 +368,17 @@ __global__ void __launch_bounds__(512) k_node(const NodeArgs A) {
     if (ck.done) return;
     const double t_n = ck.time, dt = ck.dt, t_np1 = t_n + dt, t_half = 0.5 * (t_np1 + t_n);
     double un[3];
+    // rigid-body DOFs: the motion at t_{n+1} (k_rigid_begin advanced it)
+    double ru[3] = {0.0, 0.0, 0.0}, rv[3] = {0.0, 0.0, 0.0}, ra[3] = {0.0, 0.0, 0.0};
+    if (A.rbstep) {
+      bool rig = false;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const int fn = A.nbc[d * N + n];
+        if (fn >= 0 && A.fns[fn].kind == kBckRigid) rig = true;
+      }
+      if (rig) rigid_node(A.rbstep + inst, A.X, N, n, ru, rv, ra);
+    }
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       const int fn = A.nbc[d * N + n];
@@ -151,6 +389,15 @@ __global__ void __launch_bounds__(512) k_node(const NodeArgs A) {
         u = u + dt * vh;
         A.vh[d * N + n] = vh;
         A.u[d * N + n] = u;
+      } else if (fn >= 0 && A.fns[fn].kind == kBckRigid) {
+        // v_half of a constrained DOF is unused: it keeps a_n + a_{n+1}, the
+        // inertia term of the DOF's reaction in the energy balance
+        const double aold = A.a[d * N + n];
+        u = ru[d];
+        A.u[d * N + n] = u;
+        A.v[d * N + n] = rv[d];
+        A.a[d * N + n] = ra[d];
+        A.vh[d * N + n] = aold + ra[d];
       } else if (fn >= 0) {
         double vb;
         bc_value(A.fns[fn], d, t_np1, A.X, N, n, u, vb);
@@ -207,17 +454,129 @@ __global__ void k_step_scalars(const NodeArgs A) {
     }
 }
 
+// The rigid bodies' step to t_{n+2} for the next step (ex5.cpp:344 with
+// Time = t_{n+2}, dt = the new dt), one warp per instance, after
+// k_step_scalars.  It runs on a second stream beside k_node_step over the
+// nodes without rigid-body DOFs: the integrator is a latency-bound FP64
+// chain, the free-node update is bandwidth-bound, and only the driven nodes
+// (k_node_step over their list, after this kernel) need its result.
+__global__ void __launch_bounds__(32) k_rigid_step(const NodeArgs A) {
+  __shared__ double sacc[5][6];
+  const int i = blockIdx.x;
+  const Clock ck = A.clock[A.parity * A.ninst + i];
+  const StepScalars sc = A.stepsc[i];
+  if (sc.advance && !ck.done) rigid_advance(A, i, sc.t_np2 - sc.ndt, sc.ndt, sacc);
+}
+
+// Before a kNodeBegin launch: advance each running instance's rigid body to
+// t_{n+1} = t_n + dt (ex5.cpp:344 with Time = t_{n+1}).  One warp per instance.
+__global__ void __launch_bounds__(32) k_rigid_begin(const NodeArgs A) {
+  __shared__ double sacc[5][6];
+  const int i = blockIdx.x;
+  const Clock ck = A.clock[A.parity * A.ninst + i];
+  if (ck.done) return;
+  const double t_np1 = ck.time + ck.dt;
+  rigid_advance(A, i, t_np1 - ck.dt, ck.dt, sacc);
+}
+
+// The constrained DOFs of node n in k_node_step: their kinetic-energy and
+// reaction-work terms (EN) and, when the step advances, the boundary
+// functions at t_{n+2} (a rigid rotation or the instance's rigid body
+// evaluated once for the node's three DOFs).  Out of line: only boundary
+// nodes take it, and the free-node path keeps its registers.  The reaction
+// is fi_prev + fi + m (a + a_prev) (CheckEnergy.cpp:39-42); a + a_prev is
+// kept in v_half for a rigid-body DOF and is 0 for the other constrained
+// DOFs (a = 0 there).
+template <class R, bool EN>
+__device__ __forceinline__ void node_step_bc_body(const NodeArgs &A, long long n, int inst,
+                                                  const StepScalars &sc, const int *nbc,
+                                                  const double *fsum, const R *du_,
+                                                  const R *fp_, const double *vb_,
+                                                  const double *vh0, double mass, double *un,
+                                                  R &eke, R &ewe) {
+  const long long N = A.N;
+  const bool advance = sc.advance;
+  double ur[3] = {0.0, 0.0, 0.0}, vr[3] = {0.0, 0.0, 0.0}, ar[3] = {0.0, 0.0, 0.0};
+  bool rigd[3] = {false, false, false}, rig = false;
+  int rot_fn = -1;
+  for (int d = 0; d < 3; ++d) {
+    const int fn = nbc[d];
+    if (fn < 0) continue;
+    const int kind = A.fns[fn].kind;
+    rigd[d] = kind == kBckRigid && A.rbstep;
+    rig = rig || rigd[d];
+    if (kind == kBckRot && rot_fn < 0) rot_fn = fn;
+  }
+  double aold[3] = {0.0, 0.0, 0.0};
+  if (advance && rig) {  // rigid body at t_{n+2} (k_step_scalars_rigid advanced it)
+    for (int d = 0; d < 3; ++d)
+      if (rigd[d]) aold[d] = A.a[d * N + n];
+    rigid_node(A.rbstep + inst, A.X, N, n, ur, vr, ar);
+  }
+  if (advance && rot_fn >= 0) {
+    const BcFn &b = A.fns[rot_fn];
+    double c, s, om;
+    if (b.pad >= 0 && b.pad < A.nrot) {
+      const double *r = A.rottrig + 3 * ((long long)inst * kMaxRotFns + b.pad);
+      c = r[0];
+      s = r[1];
+      om = r[2];
+    } else {
+      rot_trig(b, sc.t_np2, c, s, om);
+    }
+    rot_apply(b, c, s, om, A.X, N, n, ur, vr);
+  }
+  for (int d = 0; d < 3; ++d) {
+    const int fn = nbc[d];
+    if (fn == kBcFree) continue;
+    if (EN) {
+      const R fi = R(fsum[d]);
+      const R vb = R(vb_[d]);
+      eke += R(mass) * vb * vb;
+      ewe += rigd[d] ? du_[d] * (fp_[d] + fi + R(mass * vh0[d])) : du_[d] * (fp_[d] + fi);
+    }
+    if (fn >= 0 && advance) {
+      double u, vb, ab = 0.0;
+      if (rigd[d]) {
+        u = ur[d];
+        vb = vr[d];
+        ab = ar[d];
+        A.vh[d * N + n] = aold[d] + ab;
+      } else if (fn == rot_fn) {
+        u = ur[d];
+        vb = vr[d];
+      } else {
+        bc_value(A.fns[fn], d, sc.t_np2, A.X, N, n, u, vb);
+      }
+      A.u[d * N + n] = u;
+      A.v[d * N + n] = vb;
+      A.a[d * N + n] = ab;
+      un[d] = u;
+    }
+  }
+}
+
+// Out-of-line copy for the all-node launch, whose free-node path keeps its
+// registers; the driven-node launch inlines the body.
+template <class R, bool EN>
+__device__ __noinline__ void node_step_bc(const NodeArgs &A, long long n, int inst,
+                                          const StepScalars &sc, const int *nbc,
+                                          const double *fsum, const R *du_, const R *fp_,
+                                          const double *vb_, const double *vh0, double mass,
+                                          double *un, R &eke, R &ewe) {
+  node_step_bc_body<R, EN>(A, n, inst, sc, nbc, fsum, du_, fp_, vb_, vh0, mass, un, eke, ewe);
+}
+
 // End of step n (mode kNodeFused also starts step n+1; kNodeFinish stops
 // there), with the step scalars k_step_scalars left for the node's instance.
 // At most 64 registers: the kernel waits on memory, so resident warps matter.
 // One node of k_node_step.  EN: also this node's share of the energy balance
 // (CheckEnergy.cpp:18-55 with fe = 0): kinetic energy m v_{n+1}^2, internal
 // work du (f_prev + f) and, for constrained DOFs, the work of the reaction
-// du (f_prev + f + m (a + a_prev)) with a = a_prev = 0 on constrained DOFs.
-// The terms are formed in the element precision R (FP32 in mixed mode, where
-// du and f are FP32 already: FP64 issue is slow on this GPU), FP64 in FP64
-// mode.
-template <class R, bool EN>
+// (node_step_bc).  The terms are formed in the element precision R (FP32 in
+// mixed mode, where du and f are FP32 already: FP64 issue is slow on this
+// GPU), FP64 in FP64 mode.
+template <class R, bool EN, bool BCI = false>
 __device__ __forceinline__ void node_step(const NodeArgs &A, long long n, R &eke, R &ewi,
                                           R &ewe) {
   const long long N = A.N, S = A.S;
@@ -232,6 +591,12 @@ __device__ __forceinline__ void node_step(const NodeArgs &A, long long n, R &eke
     nbc[d] = A.nbc[d * N + n];
     u0[d] = A.u[d * N + n];
     vh0[d] = A.vh[d * N + n];
+  }
+  const bool anybc = nbc[0] != kBcFree || nbc[1] != kBcFree || nbc[2] != kBcFree;
+  if (anybc && A.skip_rigid) {  // handled by the rigid-body branch of the step
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      if (nbc[d] >= 0 && A.fns[nbc[d]].kind == kBckRigid) return;
   }
   // 1/m (mixed mode; FP64 mode divides by m as the reference does)
   const double minv = sizeof(R) == 8 ? 0.0 : A.minv[n];
@@ -275,37 +640,12 @@ __device__ __forceinline__ void node_step(const NodeArgs &A, long long n, R &eke
   const bool advance = sc.advance;
   constexpr bool kF64 = sizeof(R) == 8;
   const double fsum[3] = {double(fs0), double(fs1), double(fs2)};
-  double un[3];
-  // a rigid rotation drives all its DOFs at once: evaluate it once per node
-  double ur[3] = {0.0, 0.0, 0.0}, vr[3] = {0.0, 0.0, 0.0};
-  int rot_fn = -1;
-  if (advance) {
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      const int fn = nbc[d];
-      if (fn >= 0 && rot_fn < 0 && A.fns[fn].kind == kBckRot) rot_fn = fn;
-    }
-    if (rot_fn >= 0) {
-      const BcFn &b = A.fns[rot_fn];
-      double c, s, om;
-      if (b.pad >= 0 && b.pad < A.nrot) {
-        const double *r = A.rottrig + 3 * ((long long)inst * kMaxRotFns + b.pad);
-        c = r[0];
-        s = r[1];
-        om = r[2];
-      } else {
-        rot_trig(b, sc.t_np2, c, s, om);
-      }
-      rot_apply(b, c, s, om, A.X, N, n, ur, vr);
-    }
-  }
+  double un[3] = {u0[0], u0[1], u0[2]};
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const int fn = nbc[d];
-    double u = u0[d];
     if (EN) {
       const R fi = R(fsum[d]);  // exact: a sum in the element precision
-      const R w = du_[d] * (fp_[d] + fi);
       if (fn == kBcFree) {
         R v1;
         if (kF64) {
@@ -314,12 +654,8 @@ __device__ __forceinline__ void node_step(const NodeArgs &A, long long n, R &eke
           v1 = R(vh0[d]) + R(sc.c1) * (-fi * R(minv));
         }
         eke += R(mass) * v1 * v1;
-      } else {
-        const R vb = R(vb_[d]);
-        eke += R(mass) * vb * vb;
-        ewe += w;
       }
-      ewi += w;
+      ewi += du_[d] * (fp_[d] + fi);
       fp[d * N + n] = fi;
     }
     if (fn == kBcFree) {
@@ -333,26 +669,20 @@ __device__ __forceinline__ void node_step(const NodeArgs &A, long long n, R &eke
         } else {  // one update with the combined coefficient t_half' - t_half
           vh2 = vh + sc.c12 * acc;
         }
-        u = u + sc.ndt * vh2;
+        un[d] = u0[d] + sc.ndt * vh2;
         A.vh[d * N + n] = vh2;
-        A.u[d * N + n] = u;
+        A.u[d * N + n] = un[d];
       } else {
         A.v[d * N + n] = vh + sc.c1 * acc;
         A.a[d * N + n] = acc;
       }
-    } else if (fn >= 0 && advance) {
-      double vb;
-      if (fn == rot_fn) {
-        u = ur[d];
-        vb = vr[d];
-      } else {
-        bc_value(A.fns[fn], d, sc.t_np2, A.X, N, n, u, vb);
-      }
-      A.u[d * N + n] = u;
-      A.v[d * N + n] = vb;
-      A.a[d * N + n] = 0.0;
     }
-    un[d] = u;
+  }
+  if (anybc) {
+    if (BCI)
+      node_step_bc_body<R, EN>(A, n, inst, sc, nbc, fsum, du_, fp_, vb_, vh0, mass, un, eke, ewe);
+    else
+      node_step_bc<R, EN>(A, n, inst, sc, nbc, fsum, du_, fp_, vb_, vh0, mass, un, eke, ewe);
   }
   if (EN && advance) {
 #pragma unroll
@@ -379,15 +709,22 @@ __device__ __forceinline__ void node_step(const NodeArgs &A, long long n, R &eke
   }
 }
 
-template <class R, bool EN>
-__global__ void __launch_bounds__(512, EN ? 1 : 2) k_node_step(const NodeArgs A) {
-  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+// LIST: over A.node_list (the driven nodes of the rigid-body branch, whose
+// boundary path is inlined), else over every node.
+template <class R, bool EN, bool LIST = false>
+__global__ void __launch_bounds__(512, EN || LIST ? 1 : 2) k_node_step(const NodeArgs A) {
+  long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  bool on = n < A.N;
+  if (LIST) {
+    on = n < A.nlist;
+    n = on ? A.node_list[n] : 0;
+  }
   R eke = 0, ewi = 0, ewe = 0;
   if (!EN) {
-    if (n < A.N) node_step<R, false>(A, n, eke, ewi, ewe);
+    if (on) node_step<R, false, LIST>(A, n, eke, ewi, ewe);
     return;
   }
-  if (n < A.N) node_step<R, true>(A, n, eke, ewi, ewe);
+  if (on) node_step<R, true, LIST>(A, n, eke, ewi, ewe);
   // block partials in a fixed order: warp butterfly in R, then the warps in
   // order in FP64
 #pragma unroll
@@ -407,7 +744,7 @@ __global__ void __launch_bounds__(512, EN ? 1 : 2) k_node_step(const NodeArgs A)
   if (threadIdx.x < 3) {
     double s = 0.0;
     for (int k = 0; k < (int)(blockDim.x + 31) / 32; ++k) s += part[k][threadIdx.x];
-    A.epart[3 * (long long)blockIdx.x + threadIdx.x] = s;
+    A.epart[3 * (A.epart_off + blockIdx.x) + threadIdx.x] = s;
   }
 }
 
@@ -470,15 +807,24 @@ __global__ void k_apply_bc(const NodeArgs A, double t) {
   const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= A.N) return;
   const long long N = A.N;
+  const int inst = A.node_inst ? A.node_inst[n] : 0;
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const int fn = A.nbc[d * N + n];
     if (fn < 0) continue;
-    double u, v;
-    bc_value(A.fns[fn], d, t, A.X, N, n, u, v);
+    double u, v, a = 0.0;
+    if (A.fns[fn].kind == kBckRigid) {  // the rigid body's current state
+      double ru[3], rv[3], ra[3];
+      rigid_node(A.rbstep + inst, A.X, N, n, ru, rv, ra);
+      u = ru[d];
+      v = rv[d];
+      a = ra[d];
+    } else {
+      bc_value(A.fns[fn], d, t, A.X, N, n, u, v);
+    }
     A.u[d * N + n] = u;
     A.v[d * N + n] = v;
-    A.a[d * N + n] = 0.0;
+    A.a[d * N + n] = a;
   }
 }
 

@@ -17,7 +17,7 @@ import numpy as np
 
 C3D8, C3D4 = 0, 1
 BC_FREE, BC_HOLD = -1, -2
-BCK_FIXED, BCK_RAMP, BCK_SINE, BCK_ROT = 0, 1, 2, 3
+BCK_FIXED, BCK_RAMP, BCK_SINE, BCK_ROT, BCK_RIGID = 0, 1, 2, 3, 4
 
 
 def hex_block(nx, ny, nz, lx, ly, lz, jitter=0.0, seed=0, origin=(0.0, 0.0, 0.0)):
@@ -156,6 +156,14 @@ class Loads:
             self.dof_fn[3 * np.asarray(nodes) + d] = f
         return f
 
+    def rigid(self, nodes):
+        """All DOFs of ``nodes`` follow their instance's rigid body (acceleration
+        records given to Model.set_rigid_body)."""
+        f = self.add_fn(BCK_RIGID, [])
+        for d in range(3):
+            self.dof_fn[3 * np.asarray(nodes) + d] = f
+        return f
+
     def hold(self, nodes, dofs=(0, 1, 2)):
         for d in dofs:
             self.dof_fn[3 * np.asarray(nodes) + d] = BC_HOLD
@@ -236,6 +244,64 @@ def head_case(a=0.09, b=0.07, c=0.06, h=None, target_elements=2_000_000, shell=0
     loads.rotation(boundary_nodes_tet(mesh["connectivity"]), axis, [0.0, 0.0, 0.0], alpha_peak,
                    pulse)
     return mesh, mats, loads
+
+
+def rigid_nodes(mesh, mats):
+    """Nodes of the elements whose part has material 0 (rigid), sorted and
+    unique: the node set the brain drivers give the rigid-body motion
+    (examples/ex5/ex5.cpp:809-840)."""
+    mid = np.asarray(mats["materialID"])
+    pid = np.asarray(mesh["pid"])
+    eptr = np.asarray(mesh["eptr"])
+    conn = np.asarray(mesh["connectivity"])
+    rig = np.where(mid[pid] == 0)[0]
+    if len(rig) == 0:
+        return np.zeros(0, np.int64)
+    idx = np.concatenate([np.arange(eptr[e], eptr[e + 1]) for e in rig])
+    return np.unique(conn[idx])
+
+
+def pulse_records(seed=0, peak_ang=6.0e3, peak_lin=400.0, duration=0.01, t_end=0.03,
+                  rate=1.0e4):
+    """Seeded synthetic acceleration records in the form of the brain
+    drivers' sensor input (six channels of (time s, value)): a half-sine
+    angular acceleration of peak ``peak_ang`` rad/s^2 about a random axis plus
+    a smaller off-axis half-sine of shifted timing, and a half-sine linear
+    acceleration of peak ``peak_lin`` m/s^2 along a random direction, sampled
+    at ``rate`` Hz up to ``t_end``."""
+    rng = np.random.default_rng(seed)
+    t = np.arange(0.0, t_end + 0.5 / rate, 1.0 / rate)
+
+    def half_sine(t0, T):
+        x = (t - t0) / T
+        return np.where((x >= 0) & (x <= 1), np.sin(np.pi * np.clip(x, 0, 1)), 0.0)
+
+    ax = rng.normal(size=3)
+    ax /= np.linalg.norm(ax)
+    ax2 = rng.normal(size=3)
+    ax2 -= ax2 @ ax * ax
+    ax2 /= np.linalg.norm(ax2)
+    dl = rng.normal(size=3)
+    dl /= np.linalg.norm(dl)
+    ang = (peak_ang * np.outer(half_sine(0.0, duration), ax) +
+           0.3 * peak_ang * np.outer(half_sine(0.3 * duration, 0.8 * duration), ax2))
+    lin = peak_lin * np.outer(half_sine(0.0, 0.8 * duration), dl)
+    return [(t.copy(), ang[:, k].copy()) for k in range(3)] + \
+           [(t.copy(), lin[:, k].copy()) for k in range(3)]
+
+
+def head_impact_case(target_elements=2_000_000, seed=0, shell=0.005, **kw):
+    """head_case with the outer shell rigid (material 0) as the brain drivers
+    model the skull: the shell's nodes follow the rigid-body motion of the
+    acceleration records (pulse_records); returns mesh, materials, loads and
+    the six records."""
+    mesh, mats, _ = head_case(target_elements=target_elements, seed=seed, shell=shell, **kw)
+    mid = np.asarray(mats["materialID"]).copy()
+    mid[0] = 0  # part 0 is the shell
+    mats = dict(materialID=mid.astype(np.int32), properties=mats["properties"])
+    loads = Loads(len(mesh["coordinates"]))
+    loads.rigid(rigid_nodes(mesh, mats))
+    return mesh, mats, loads, pulse_records(seed=seed + 3)
 
 
 def ensemble_case(n_instances=256, e_min=4_000, e_max=250_000, seed=0, h=1.0e-3, jitter=0.1):

@@ -63,6 +63,10 @@ extern "C" {
 #define FTGPU_BCK_SINE 2  /* u = p0 sin(p1 t), v = p0 p1 cos(p1 t)                 */
 #define FTGPU_BCK_ROT 3   /* rigid rotation about unit axis p0..2 through p3..5 with
                              angular acceleration p6 sin(pi t / p7) for t <= p7     */
+#define FTGPU_BCK_RIGID 4 /* rigid-body motion of the node's instance from its
+                             acceleration records (ftgpu_set_rigid_body): u, v
+                             and a of the node as ApplyAccBoundaryConditions
+                             sets them (examples/ex5/ex5.cpp:339-392)            */
 
 typedef struct ftgpu_bc_fn {
   int kind;
@@ -243,6 +247,27 @@ int ftgpu_set_energy(ftgpu_model *m, int enable);
  * of steps where it exceeded 1 % (the reference's "Energy Violation" warning) */
 int ftgpu_get_energy(ftgpu_model *m, double *internal_work, double *external_work,
                      double *kinetic_energy, double *max_violation, long long *violations);
+
+/* ---- rigid-body motion from sampled accelerations (the brain drivers' skull
+ * boundary condition: InitBoundaryCondition's tables, ex5.cpp:574-720, the
+ * odeint Dormand-Prince 5(4) integrator state, ex5.cpp:100-105 and 886-890,
+ * computeDerivatives, ex5.cpp:976-1020, and ApplyAccBoundaryConditions,
+ * ex5.cpp:339-392, which this replaces) ----
+ * Channels 0-2: angular acceleration about x, y, z (rad/s^2); 3-5: linear
+ * acceleration along x, y, z (m/s^2); channel k has npts[k] >= 1 samples
+ * times[k][j] (s, non-decreasing), values[k][j], read as interpolateLinear
+ * (math.cpp:99-119) does.  Positions rotate about centre (NULL = the origin,
+ * where ex5 has moved the sensor point by TransformMesh).  Every DOF of the
+ * instance whose function has kind FTGPU_BCK_RIGID follows the motion.  Each
+ * step integrates the 12-state ODE once from Time - dt over dt, starting from
+ * zero state and zero derivative at ftgpu_init_explicit.  After ftgpu_setup,
+ * before ftgpu_init_explicit; npts = NULL removes the instance's records. */
+int ftgpu_set_rigid_body(ftgpu_model *m, int inst, const int *npts, const double *const *times,
+                         const double *const *values, const double *centre);
+/* integrator state of an instance: y = [omega(3), r(3), v_cm(3), x_cm(3)]
+ * (the reference's yInt) and yd = its derivative at the current time
+ * (ydotInt); either may be NULL */
+int ftgpu_get_rigid_body(ftgpu_model *m, int inst, double *y, double *yd);
 
 /* ---- learned constitutive surrogate for material 7 (no counterpart in the
  * reference; it replaces the isochoric part of HGOIsotropicViscoelastic's

@@ -726,6 +726,147 @@ static void or_rot_angle(const double *p, double t, double *theta, double *omega
 /* Driver boundary conditions in the style of examples/ex9/ex9.cpp:187-248:
  * constrained DOFs get the prescribed displacement/velocity and zero
  * acceleration at time t; HOLD DOFs are constrained but left untouched. */
+/* interpolateLinear, src/math/math.cpp:99-119: 0 below the table (the
+ * reference logs an error), the last value above it, y[0] at x[0], else the
+ * segment of the first x[i] >= value. */
+double or_interp_linear(int n, const double *x, const double *y, double value) {
+  if (value < x[0]) return 0.0;
+  if (value > x[n - 1]) return y[n - 1];
+  if (value == x[0]) return y[0];
+  int index = 0;
+  for (int i = 1; i < n; ++i)
+    if (value <= x[i]) {
+      index = i - 1;
+      break;
+    }
+  return y[index] + (y[index + 1] - y[index]) * (value - x[index]) / (x[index + 1] - x[index]);
+}
+
+/* crossProduct / dotProduct3D, src/math/math.cpp:50-60 */
+static void or_cross(const double *a, const double *b, double *r) {
+  r[0] = a[1] * b[2] - a[2] * b[1];
+  r[1] = -a[0] * b[2] + a[2] * b[0];
+  r[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+/* computeDerivatives, examples/ex5/ex5.cpp:976-1020: sampled angular and
+ * linear accelerations, the centre-of-mass velocity, and the rate of the
+ * rotation generator r from the angular velocity (M. Boyle, "The integration
+ * of angular velocity", 2017): rdot = omega / 2 for |r| < 1e-10, else
+ * (omega x r + |r| cot|r| omega + (1 - |r| cot|r|) (rhat . omega) rhat) / 2. */
+static void or_rigid_deriv(const or_rigid *rb, const double *y, double t, double *yd) {
+  for (int k = 0; k < 3; ++k) {
+    yd[k] = or_interp_linear(rb->n[k], rb->t[k], rb->v[k], t);
+    yd[6 + k] = or_interp_linear(rb->n[3 + k], rb->t[3 + k], rb->v[3 + k], t);
+    yd[9 + k] = y[6 + k];
+  }
+  double r[3] = {y[3], y[4], y[5]};
+  double *rdot = yd + 3;
+  double rm = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+  if (rm < 1e-10) {
+    for (int k = 0; k < 3; ++k) rdot[k] = 0.5 * y[k];
+  } else {
+    double rc = rm / tan(rm), om[3] = {y[0], y[1], y[2]};
+    or_cross(om, r, rdot);
+    for (int k = 0; k < 3; ++k) r[k] = r[k] / rm;
+    double rw = r[0] * om[0] + r[1] * om[1] + r[2] * om[2];
+    for (int k = 0; k < 3; ++k) rdot[k] = 0.5 * (rdot[k] + rc * y[k] + (1.0 - rc) * rw * r[k]);
+  }
+}
+
+/* One step of the explicit Runge-Kutta pair of Dormand and Prince (J. Comput.
+ * Appl. Math. 6 (1980) 19-26), fifth-order solution, first stage taken from
+ * yd (first same as last) and yd left at f(y(t + h), t + h): what
+ * runge_kutta_dopri5<boost::array<double,12>>::do_step(sys, y, yd, t, h) does
+ * at ex5.cpp:344 (Boost.Odeint is not part of the reference tree; this is the
+ * published tableau).  Sums are formed as y + (h a_i1) k1 + (h a_i2) k2 + ... */
+void or_rigid_step(or_rigid *rb, double t, double h) {
+  static const double c2 = 1.0 / 5, c3 = 3.0 / 10, c4 = 4.0 / 5, c5 = 8.0 / 9;
+  static const double a21 = 1.0 / 5, a31 = 3.0 / 40, a32 = 9.0 / 40, a41 = 44.0 / 45,
+                      a42 = -56.0 / 15, a43 = 32.0 / 9, a51 = 19372.0 / 6561,
+                      a52 = -25360.0 / 2187, a53 = 64448.0 / 6561, a54 = -212.0 / 729,
+                      a61 = 9017.0 / 3168, a62 = -355.0 / 33, a63 = 46732.0 / 5247,
+                      a64 = 49.0 / 176, a65 = -5103.0 / 18656;
+  static const double b1 = 35.0 / 384, b3 = 500.0 / 1113, b4 = 125.0 / 192,
+                      b5 = -2187.0 / 6784, b6 = 11.0 / 84;
+  double k2[12], k3[12], k4[12], k5[12], k6[12], x[12];
+  const double *y = rb->y, *k1 = rb->yd;
+  for (int i = 0; i < 12; ++i) x[i] = y[i] + (h * a21) * k1[i];
+  or_rigid_deriv(rb, x, t + h * c2, k2);
+  for (int i = 0; i < 12; ++i) x[i] = y[i] + (h * a31) * k1[i] + (h * a32) * k2[i];
+  or_rigid_deriv(rb, x, t + h * c3, k3);
+  for (int i = 0; i < 12; ++i)
+    x[i] = y[i] + (h * a41) * k1[i] + (h * a42) * k2[i] + (h * a43) * k3[i];
+  or_rigid_deriv(rb, x, t + h * c4, k4);
+  for (int i = 0; i < 12; ++i)
+    x[i] = y[i] + (h * a51) * k1[i] + (h * a52) * k2[i] + (h * a53) * k3[i] + (h * a54) * k4[i];
+  or_rigid_deriv(rb, x, t + h * c5, k5);
+  for (int i = 0; i < 12; ++i)
+    x[i] = y[i] + (h * a61) * k1[i] + (h * a62) * k2[i] + (h * a63) * k3[i] +
+           (h * a64) * k4[i] + (h * a65) * k5[i];
+  or_rigid_deriv(rb, x, t + h, k6);
+  for (int i = 0; i < 12; ++i)
+    x[i] = y[i] + (h * b1) * k1[i] + (h * b3) * k3[i] + (h * b4) * k4[i] + (h * b5) * k5[i] +
+           (h * b6) * k6[i];
+  memcpy(rb->y, x, sizeof(x));
+  or_rigid_deriv(rb, rb->y, t + h, rb->yd);
+}
+
+/* quaternionMultiply, src/math/math.cpp:135-140 */
+static void or_qmul(const double *p, const double *q, double *r) {
+  r[0] = p[0] * q[0] - p[1] * q[1] - p[2] * q[2] - p[3] * q[3];
+  r[1] = p[0] * q[1] + p[1] * q[0] + p[2] * q[3] - p[3] * q[2];
+  r[2] = p[0] * q[2] - p[1] * q[3] + p[2] * q[0] + p[3] * q[1];
+  r[3] = p[0] * q[3] + p[1] * q[2] - p[2] * q[1] + p[3] * q[0];
+}
+
+/* ApplyAccBoundaryConditions for one node, ex5.cpp:345-371: R = exp([0, r])
+ * (quaternionExp, math.cpp:122-133), Vp = R V R^-1 (quaternionInverse /
+ * quaternionRotate, math.cpp:142-158), then
+ *   u = Vp - X + x_cm,  v = omega x Vp + v_cm,
+ *   a = 2 omega x v_cm + omega x (omega x Vp) + a_cm + alpha x Vp. */
+void or_rigid_point(const or_rigid *rb, const double *X, double *u, double *v, double *a) {
+  const double *y = rb->y, *yd = rb->yd;
+  double R[4], Ri[4], V[4], RV[4], Vp[4];
+  double vm = y[3] * y[3] + y[4] * y[4] + y[5] * y[5];
+  if (vm == 0) {
+    R[0] = 1.0;
+    R[1] = R[2] = R[3] = 0.0;
+  } else {
+    vm = sqrt(vm);
+    const double d1 = exp(0.0), d2 = d1 * sin(vm) / vm;
+    R[0] = d1 * cos(vm);
+    R[1] = d2 * y[3];
+    R[2] = d2 * y[4];
+    R[3] = d2 * y[5];
+  }
+  const double nr = R[0] * R[0] + R[1] * R[1] + R[2] * R[2] + R[3] * R[3];
+  Ri[0] = R[0] / nr;
+  Ri[1] = -R[1] / nr;
+  Ri[2] = -R[2] / nr;
+  Ri[3] = -R[3] / nr;
+  double loc[3];
+  for (int j = 0; j < 3; ++j) loc[j] = X[j] - rb->c[j];
+  V[0] = 0.0;
+  V[1] = loc[0];
+  V[2] = loc[1];
+  V[3] = loc[2];
+  or_qmul(R, V, RV);
+  or_qmul(RV, Ri, Vp);
+  const double om[3] = {y[0], y[1], y[2]}, al[3] = {yd[0], yd[1], yd[2]},
+               vel[3] = {y[6], y[7], y[8]};
+  double oR[3], ooR[3], oV[3], aR[3];
+  or_cross(om, Vp + 1, oR);
+  or_cross(om, oR, ooR);
+  or_cross(om, vel, oV);
+  or_cross(al, Vp + 1, aR);
+  for (int j = 0; j < 3; ++j) {
+    u[j] = Vp[j + 1] - loc[j] + y[9 + j];
+    v[j] = oR[j] + y[6 + j];
+    a[j] = 2.0 * oV[j] + ooR[j] + yd[6 + j] + aR[j];
+  }
+}
+
 void or_apply_bc(const or_model *m, const int *dof_fn, const or_bc_fn *fns, double t,
                  double *u, double *v, double *a) {
   for (int n = 0; n < m->nNodes; ++n)
@@ -734,6 +875,14 @@ void or_apply_bc(const or_model *m, const int *dof_fn, const or_bc_fn *fns, doub
       if (f < 0) continue;
       const or_bc_fn *b = fns + f;
       int i = 3 * n + d;
+      if (b->kind == OR_BCK_RIGID) {
+        double ur[3] = {0, 0, 0}, vr[3] = {0, 0, 0}, ar[3] = {0, 0, 0};
+        if (m->rigid) or_rigid_point(m->rigid, m->coordinates + 3 * n, ur, vr, ar);
+        u[i] = ur[d];
+        v[i] = vr[d];
+        a[i] = ar[d];
+        continue;
+      }
       if (b->kind == OR_BCK_FIXED) {
         u[i] = b->p[0];
         v[i] = 0.0;
@@ -923,6 +1072,10 @@ int or_explicit_run(or_model *m, const int *dof_fn, const or_bc_fn *fns, int nfn
     fi_prev = (double *)calloc(nDOF, sizeof(double));
   }
   for (int i = 0; i < nDOF; ++i) boundary[i] = dof_fn[i] != OR_BC_FREE;
+  if (m->rigid) { /* ex5.cpp:886-890 */
+    memset(m->rigid->y, 0, sizeof(m->rigid->y));
+    memset(m->rigid->yd, 0, sizeof(m->rigid->yd));
+  }
   double Time = t0;
   *n_out = 0;
   *steps_done = 0;
@@ -947,6 +1100,7 @@ int or_explicit_run(or_model *m, const int *dof_fn, const or_bc_fn *fns, int nfn
     }
     for (int i = 0; i < nDOF; ++i)
       if (!boundary[i]) u[i] = u[i] + dt_nphalf * vh[i];
+    if (m->rigid) or_rigid_step(m->rigid, Time - dt, dt); /* ex5.cpp:344 */
     or_apply_bc(m, dof_fn, fns, Time, u, v, a);
     if (or_get_force(m, u, dt, fi)) { rc = -1; break; }
     for (int i = 0; i < nDOF; ++i)

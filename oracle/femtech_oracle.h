@@ -36,6 +36,7 @@ extern "C" {
 #define OR_BCK_SINE 2  /* u = p0 * sin(p1 t), v = p0 p1 cos(p1 t)           */
 #define OR_BCK_ROT 3   /* rigid rotation: axis p0..2, centre p3..5,
                           half-sine angular acceleration peak p6 over p7 s  */
+#define OR_BCK_RIGID 4 /* rigid-body motion of or_model.rigid (u, v and a)  */
 
 typedef struct or_bc_fn {
   int kind;
@@ -60,6 +61,22 @@ typedef struct or_injury {
   double mps95, mps95_time, mpsxsr95, mpsxsr95_time;
   int mps95_count, mpsxsr95_count;
 } or_injury;
+
+/* Rigid-body motion driven by sampled accelerations, as the brain drivers
+ * apply it to the nodes of material-0 parts (examples/ex5/ex5.cpp:339-392,
+ * ApplyAccBoundaryConditions).  Channels 0-2: angular acceleration about x,
+ * y, z; 3-5: linear acceleration along x, y, z; each a table of n[k]
+ * (time, value) pairs with non-decreasing times.  The integrator state of
+ * ex5.cpp:100-105: y = [omega(3), r(3), v_cm(3), x_cm(3)] with r the rotation
+ * generator (R = exp of the pure quaternion r), yd = dy/dt at the last step's
+ * end time (zero at the start, ex5.cpp:886-890).  Positions rotate about
+ * centre c (the reference rotates about the origin of the shifted mesh). */
+typedef struct or_rigid {
+  int n[6];
+  const double *t[6], *v[6];
+  double c[3];
+  double y[12], yd[12];
+} or_rigid;
 
 typedef struct or_model {
   /* inputs, reference layout; owned by the caller */
@@ -89,6 +106,9 @@ typedef struct or_model {
   /* optional: injury criteria updated after every step of
    * or_explicit_run (NULL = not computed) */
   or_injury *injury;
+  /* optional: the rigid body of OR_BCK_RIGID functions (NULL = none);
+   * or_explicit_run zeroes its state and advances it by one step per step */
+  or_rigid *rigid;
 } or_model;
 
 int or_setup(or_model *m);
@@ -111,6 +131,13 @@ double or_percentile95(const double *data, int n);
 void or_injury_step(const or_model *m, or_injury *s, double time, double dt);
 void or_apply_bc(const or_model *m, const int *dof_fn, const or_bc_fn *fns,
                  double t, double *u, double *v, double *a);
+/* interpolateLinear (src/math/math.cpp:99-119) */
+double or_interp_linear(int n, const double *x, const double *y, double value);
+/* one integrator step of ex5.cpp:344 from t over h (Dormand-Prince 5(4)) */
+void or_rigid_step(or_rigid *rb, double t, double h);
+/* displacement, velocity and acceleration of a point at reference position
+ * X under the current state (ex5.cpp:345-371) */
+void or_rigid_point(const or_rigid *rb, const double *X, double *u, double *v, double *a);
 void or_set_threads(or_model *m, int n);
 int or_max_threads(void);
 

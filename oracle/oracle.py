@@ -21,7 +21,7 @@ LIB = os.path.join(HERE, "liboracle.so")
 REFLIB = os.path.join(HERE, "_ref", "libfemtech_ref.so")
 
 BC_FREE, BC_HOLD = -1, -2
-BCK_FIXED, BCK_RAMP, BCK_SINE, BCK_ROT = 0, 1, 2, 3
+BCK_FIXED, BCK_RAMP, BCK_SINE, BCK_ROT, BCK_RIGID = 0, 1, 2, 3, 4
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
@@ -75,6 +75,63 @@ def _injury_result(st, arrs):
     return out
 
 
+class _Rigid(C.Structure):
+    _fields_ = [("n", C.c_int * 6), ("t", C.c_void_p * 6), ("v", C.c_void_p * 6),
+                ("c", C.c_double * 3), ("y", C.c_double * 12), ("yd", C.c_double * 12)]
+
+
+class RigidBody:
+    """Acceleration records of a rigid body for the oracle: channels = six
+    (times, values) pairs, angular x, y, z then linear x, y, z."""
+
+    def __init__(self, channels, centre=(0.0, 0.0, 0.0)):
+        self.tabs = [(np.ascontiguousarray(t, np.float64), np.ascontiguousarray(v, np.float64))
+                     for t, v in channels]
+        assert len(self.tabs) == 6
+        self.st = _Rigid()
+        for k, (t, v) in enumerate(self.tabs):
+            assert len(t) == len(v) and len(t) >= 1
+            self.st.n[k] = len(t)
+            self.st.t[k] = t.ctypes.data
+            self.st.v[k] = v.ctypes.data
+        for j in range(3):
+            self.st.c[j] = float(centre[j])
+
+    @property
+    def y(self):
+        return np.array(self.st.y[:])
+
+    @property
+    def yd(self):
+        return np.array(self.st.yd[:])
+
+    def set_state(self, y, yd):
+        for i in range(12):
+            self.st.y[i] = float(y[i])
+            self.st.yd[i] = float(yd[i])
+
+    def step(self, t, h):
+        Oracle.lib().or_rigid_step(C.byref(self.st), C.c_double(t), C.c_double(h))
+
+    def point(self, X):
+        """(u, v, a) of the points X (n x 3) under the current state."""
+        X = np.ascontiguousarray(X, np.float64).reshape(-1, 3)
+        out = np.zeros((3, len(X), 3))
+        L = Oracle.lib()
+        for i in range(len(X)):
+            u, v, a = np.zeros(3), np.zeros(3), np.zeros(3)
+            L.or_rigid_point(C.byref(self.st), X[i].copy(), u, v, a)
+            out[0, i], out[1, i], out[2, i] = u, v, a
+        return out
+
+
+def interp_linear(x, y, value):
+    """The oracle's interpolateLinear (math.cpp:99-119)."""
+    x = np.ascontiguousarray(x, np.float64)
+    y = np.ascontiguousarray(y, np.float64)
+    return Oracle.lib().or_interp_linear(len(x), x, y, C.c_double(value))
+
+
 class _Model(C.Structure):
     _fields_ = [
         ("nNodes", C.c_int), ("nelements", C.c_int), ("nPID", C.c_int),
@@ -90,6 +147,7 @@ class _Model(C.Structure):
         ("nthreads", C.c_int),
         ("energy", C.c_void_p), ("energy_cap", C.c_int),
         ("injury", C.c_void_p),
+        ("rigid", C.c_void_p),
     ]
 
 
@@ -145,6 +203,10 @@ class Oracle:
             L.or_percentile95.restype = C.c_double
             L.or_set_threads.argtypes = [M, C.c_int]
             L.or_max_threads.restype = C.c_int
+            L.or_interp_linear.argtypes = [C.c_int, _dp, _dp, C.c_double]
+            L.or_interp_linear.restype = C.c_double
+            L.or_rigid_step.argtypes = [C.c_void_p, C.c_double, C.c_double]
+            L.or_rigid_point.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
             cls._lib = L
         return cls._lib
 
@@ -226,16 +288,18 @@ class Oracle:
 
     def explicit_run(self, dof_fn, fns, tmax, reduction, max_steps, out_every, t0=0.0,
                      failure_dt=0.0, u=None, v=None, a=None, max_out=None, energy=False,
-                     injury_ids=None):
+                     injury_ids=None, rigid=None):
         """The ex9 loop; energy=True adds per step (Wint, Wext, WKE) of
         CheckEnergy (cumulative works, kinetic energy) as result['energy'];
         injury_ids adds the injury criteria of ex5 over those elements as
-        result['injury']."""
+        result['injury']; rigid (a RigidBody) drives the BCK_RIGID functions
+        (its final state is left in it)."""
         n = 3 * self.nNodes
         inj = None
         if injury_ids is not None:
             inj = _injury_struct(injury_ids)
             self.m.injury = C.addressof(inj[0])
+        self.m.rigid = None if rigid is None else C.addressof(rigid.st)
         ebuf = np.zeros(3 * max(max_steps, 1)) if energy else None
         self.m.energy = None if ebuf is None else ebuf.ctypes.data
         self.m.energy_cap = max_steps if energy else 0
@@ -256,6 +320,7 @@ class Oracle:
         self.m.energy = None
         self.m.energy_cap = 0
         self.m.injury = None
+        self.m.rigid = None
         k = nout.value
         res = dict(rc=rc, u=u, v=v, a=a, u_out=uo[: k * n].reshape(k, n), t_out=to[:k],
                    steps=steps.value, time=tt.value, dt=dd.value)
@@ -322,6 +387,9 @@ class RefBuild:
             L.ref_element_strain.argtypes = [_dp, _dp, _dp, _dp]
             L.ref_percentile95.argtypes = [_dp, C.c_int, C.POINTER(C.c_double),
                                            C.POINTER(C.c_double)]
+            L.ref_interp_linear.argtypes = [C.c_int, _dp, _dp, C.c_double]
+            L.ref_interp_linear.restype = C.c_double
+            L.ref_rigid_point.argtypes = [_dp, _dp, _dp, _dp, _dp, _dp]
             L.ref_explicit_run.argtypes = [_ip, C.c_void_p, C.c_int, C.c_double, C.c_double,
                                            C.c_double, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp,
                                            C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
@@ -368,6 +436,27 @@ class RefBuild:
         return fi
 
     @classmethod
+    def interp_linear(cls, x, y, value):
+        """The reference's interpolateLinear (math.cpp:99-119)."""
+        x = np.ascontiguousarray(x, np.float64).copy()
+        y = np.ascontiguousarray(y, np.float64).copy()
+        return cls.lib().ref_interp_linear(len(x), x, y, float(value))
+
+    @classmethod
+    def rigid_point(cls, y, yd, X):
+        """(u, v, a) of the points X (n x 3) by ex5's per-node rigid-body
+        kinematics on the reference's quaternion helpers."""
+        y = np.ascontiguousarray(y, np.float64)
+        yd = np.ascontiguousarray(yd, np.float64)
+        X = np.ascontiguousarray(X, np.float64).reshape(-1, 3)
+        out = np.zeros((3, len(X), 3))
+        for i in range(len(X)):
+            u, v, a = np.zeros(3), np.zeros(3), np.zeros(3)
+            cls.lib().ref_rigid_point(y, yd, X[i].copy(), u, v, a)
+            out[0, i], out[1, i], out[2, i] = u, v, a
+        return out
+
+    @classmethod
     def percentile95(cls, data):
         """The reference's compute95thPercentileValueBruteForce and
         compute95thPercentileValue (one rank) of the values."""
@@ -397,6 +486,7 @@ class RefBuild:
         logs them (works accumulate over the process: one energy run per process)."""
         n = 3 * self.nNodes
         u, v, a = np.zeros(n), np.zeros(n), np.zeros(n)
+        self.m.rigid = None if rigid is None else C.addressof(rigid.st)
         ebuf = np.zeros(3 * max(max_steps, 1)) if energy else None
         self.lib().ref_set_energy_out(None if ebuf is None else ebuf.ctypes.data,
                                       max_steps if energy else 0)

@@ -329,6 +329,49 @@ int ref_percentile95(double *data, int n, double *brute, double *parallel) {
   }
 }
 
+/* interpolateLinear (math.cpp:99-119) */
+double ref_interp_linear(int n, double *x, double *y, double value) {
+  return interpolateLinear(n, x, y, value);
+}
+
+/* The per-node body of ApplyAccBoundaryConditions (examples/ex5/ex5.cpp:
+ * 345-371) on the reference's own quaternion and vector helpers (math.cpp):
+ * the driver itself needs Boost.Odeint, which the reference tree does not
+ * carry, so its loop body is restated here over the reference's functions.
+ * y, yd: the integrator state yInt / ydotInt; X: the node position. */
+void ref_rigid_point(const double *y, const double *yd, const double *X, double *u, double *v,
+                     double *a) {
+  double r[4], R[4], Rinv[4], V[4], Vp[4];
+  double omegaR[3], omega[3], omegaOmegaR[3], omegaVel[3], vel[3];
+  double alpha[3], alphaR[3], locV[3];
+  r[0] = 0.0;
+  r[1] = y[3];
+  r[2] = y[4];
+  r[3] = y[5];
+  quaternionExp(r, R);
+  quaternionInverse(R, Rinv);
+  for (int j = 0; j < 3; ++j) {
+    omega[j] = y[j];
+    alpha[j] = yd[j];
+    vel[j] = y[6 + j];
+    locV[j] = X[j];
+  }
+  V[0] = 0.0;
+  V[1] = locV[0];
+  V[2] = locV[1];
+  V[3] = locV[2];
+  quaternionRotate(V, R, Rinv, Vp);
+  crossProduct(omega, &(Vp[1]), omegaR);
+  crossProduct(omega, omegaR, omegaOmegaR);
+  crossProduct(omega, vel, omegaVel);
+  crossProduct(alpha, &(Vp[1]), alphaR);
+  for (int j = 0; j < 3; ++j) {
+    u[j] = Vp[j + 1] - locV[j] + y[9 + j];
+    v[j] = omegaR[j] + y[6 + j];
+    a[j] = 2.0 * omegaVel[j] + omegaOmegaR[j] + yd[6 + j] + alphaR[j];
+  }
+}
+
 /* Energy output of the next ref_explicit_run: per step the cumulative internal
  * and external work and the kinetic energy that the reference's own
  * CheckEnergy() logs (ex9.cpp:154-156 calls it after every step).  Its works

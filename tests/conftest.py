@@ -24,4 +24,5 @@ def oracle_lib():
 @pytest.fixture(scope="session")
 def golden():
     import numpy as np
-    return {k: np.load(os.path.join(GOLDEN, k + ".npz")) for k in ("ref_force", "ref_ex9", "ref_cube")}
+    return {k: np.load(os.path.join(GOLDEN, k + ".npz")) for k in ("ref_force", "ref_ex9", "ref_cube",
+                                                                 "ref_rigid")}

@@ -25,6 +25,13 @@ Fixtures:
                   work, external work and kinetic energy of the reference's
                   CheckEnergy (the only energy run of the process, so its
                   works start from zero).
+  ref_rigid.npz   the rigid-body helpers of the brain drivers on the
+                  reference's math.cpp: interpolateLinear on tables with
+                  duplicate and uneven times (queries below, at, between and
+                  above the samples), and the per-node kinematics of
+                  ApplyAccBoundaryConditions (ex5.cpp:345-371, restated in the
+                  shim over the reference's quaternion helpers) for seeded
+                  integrator states, the zero rotation included.
 """
 import os
 import sys
@@ -104,6 +111,35 @@ def percentile_cases():
     return out
 
 
+def rigid_cases():
+    rng = np.random.default_rng(339)
+    out = {}
+    tables = [(np.array([0.0, 1e-3, 1e-3, 2.5e-3, 4e-3, 7e-3, 1e-2]),
+               np.array([0.0, 3.0, 5.0, -2.0, 4.5, 4.5, 1.0])),
+              (np.array([2e-3]), np.array([7.0])),
+              (np.array([0.0, 5e-3]), np.array([-1.0, 2.0]))]
+    for i, (x, y) in enumerate(tables):
+        q = np.concatenate([[x[0] - 1e-3, x[0], x[-1], x[-1] + 1e-3], x,
+                            0.5 * (x[1:] + x[:-1]), rng.uniform(x[0], x[-1], 20)])
+        out["interp_x_%d" % i] = x
+        out["interp_y_%d" % i] = y
+        out["interp_q_%d" % i] = q
+        out["interp_ref_%d" % i] = np.array([orc.RefBuild.interp_linear(x, y, v) for v in q])
+    ys, yds = [], []
+    for k in range(24):
+        y = rng.normal(size=12) * np.array([50, 50, 50, 0, 0, 0, 2, 2, 2, 0.01, 0.01, 0.01])
+        mag = [0.0, 1e-12, 0.3, 1.5][k % 4]
+        r = rng.normal(size=3)
+        y[3:6] = mag * r / np.linalg.norm(r)
+        ys.append(y)
+        yds.append(rng.normal(size=12) * 1e3)
+    X = rng.uniform(-0.1, 0.1, (10, 3))
+    res = [orc.RefBuild.rigid_point(y, yd, X) for y, yd in zip(ys, yds)]
+    out.update(rigid_y=np.array(ys), rigid_yd=np.array(yds), rigid_X=X,
+               rigid_uva=np.array(res))
+    return out
+
+
 def abaqus_last_row(path):
     rows = []
     with open(path) as f:
@@ -169,7 +205,8 @@ def main():
                         **percentile_cases())
     np.savez_compressed(os.path.join(HERE, "ref_ex9.npz"), **ex9_case())
     np.savez_compressed(os.path.join(HERE, "ref_cube.npz"), **cube_case())
-    for f in ("ref_force.npz", "ref_ex9.npz", "ref_cube.npz"):
+    np.savez_compressed(os.path.join(HERE, "ref_rigid.npz"), **rigid_cases())
+    for f in ("ref_force.npz", "ref_ex9.npz", "ref_cube.npz", "ref_rigid.npz"):
         print(f, os.path.getsize(os.path.join(HERE, f)))
 
 
