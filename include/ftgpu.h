@@ -41,6 +41,7 @@ extern "C" {
 /* ---- element types (ElementType strings "C3D8"/"C3D4" of the reference) ---- */
 #define FTGPU_C3D8 0
 #define FTGPU_C3D4 1
+#define FTGPU_T3D2 2 /* truss: read by ftgpu_read_mesh, not taken by ftgpu_set_mesh */
 
 /* ---- material IDs (StressUpdate.cpp:7-27, plus two new laws) ----
  * 0 rigid, 1 compressible Neo-Hookean [rho,mu,lambda], 2 St.Venant-Kirchhoff
@@ -81,6 +82,30 @@ int ftgpu_create(ftgpu_model **out, int device, int precision);
 int ftgpu_destroy(ftgpu_model *m);
 const char *ftgpu_status_string(int status);
 const char *ftgpu_last_error(void);
+
+/* ---- mesh input (host only, no device needed) ----
+ * Reads an Abaqus .inp or LS-DYNA .k file (by extension) into the arrays a
+ * single-rank FemTech run holds after ReadInputFile + PartitionMesh
+ * (ReadInputFile.cpp:26-77, ReadAbaqus.cpp:26-246, ReadLsDyna.cpp:48-319,
+ * PartitionMesh.cpp:485-535): nodes used by elements, numbered by ascending
+ * node ID (global_node_id, 1-based); elements in file order with their IDs;
+ * pid = element set index in order of first appearance (.inp) or part ID - 1
+ * (.k); nPID distinct parts, nPIDglobal = largest pid + 1.  etype: FTGPU_C3D8,
+ * FTGPU_C3D4, FTGPU_T3D2 or -1 (other Abaqus types; LS-DYNA node counts
+ * classified as the reference does).  missing_nodes: used nodes that no node
+ * line defined (their coordinates are 0, as in the reference). */
+typedef struct ftgpu_mesh {
+  int nNodes, nelements, ndim, nPID, nPIDglobal;
+  long long missing_nodes;
+  double *coordinates; /* ndim * nNodes */
+  int *eptr;           /* nelements + 1 */
+  int *connectivity;   /* eptr[nelements], local node indices */
+  int *etype, *pid, *global_eid; /* nelements */
+  int *global_node_id; /* nNodes */
+} ftgpu_mesh;
+int ftgpu_read_mesh(const char *path, ftgpu_mesh **out);
+void ftgpu_free_mesh(ftgpu_mesh *mesh);
+const char *ftgpu_read_mesh_error(void);
 
 /* Mesh in the reference's arrays (ReadInputFile + PartitionMesh leave these in
  * coordinates, eptr, connectivity, ElementType, pid: GlobalVariables.h:34-48).

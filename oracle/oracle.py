@@ -151,6 +151,13 @@ class _Model(C.Structure):
     ]
 
 
+def reference_tree():
+    """The reference checkout the checker is built from (FEMTECH_REFERENCE,
+    default as in build()), or None where it does not exist."""
+    ref = os.environ.get("FEMTECH_REFERENCE", "/root/reference")
+    return ref if os.path.isdir(os.path.join(ref, "src")) else None
+
+
 def build(quiet=True):
     """Compile liboracle.so (always) and the reference build (if the tree exists)."""
     out = subprocess.run(["make", "-C", HERE, "liboracle.so"], capture_output=True, text=True)
@@ -387,6 +394,8 @@ class RefBuild:
             L.ref_element_strain.argtypes = [_dp, _dp, _dp, _dp]
             L.ref_percentile95.argtypes = [_dp, C.c_int, C.POINTER(C.c_double),
                                            C.POINTER(C.c_double)]
+            L.ref_read_mesh.argtypes = [C.c_char_p, C.POINTER(C.c_int)]
+            L.ref_mesh_arrays.argtypes = [C.c_void_p] * 7
             L.ref_interp_linear.argtypes = [C.c_int, _dp, _dp, C.c_double]
             L.ref_interp_linear.restype = C.c_double
             L.ref_rigid_point.argtypes = [_dp, _dp, _dp, _dp, _dp, _dp]
@@ -434,6 +443,28 @@ class RefBuild:
         if rc:
             raise RuntimeError("ref_get_force failed %d" % rc)
         return fi
+
+    @classmethod
+    def read_mesh(cls, path):
+        """The reference's ReadInputFile (ReadAbaqus / ReadLsDyna) on one rank
+        plus the single-rank renumbering of PartitionMesh: the arrays of
+        femtech_gb300.meshio.read_mesh."""
+        L = cls.lib()
+        sz = (C.c_int * 5)()
+        rc = L.ref_read_mesh(str(path).encode(), sz)
+        if rc:
+            raise RuntimeError("reference reader failed %d" % rc)
+        nN, nE, nd, npg, nc = list(sz)
+        X = np.zeros(max(nN * nd, 1))
+        ep = np.zeros(nE + 1, np.int32)
+        conn = np.zeros(max(nc, 1), np.int32)
+        et, pid, eid = (np.zeros(max(nE, 1), np.int32) for _ in range(3))
+        gid = np.zeros(max(nN, 1), np.int32)
+        L.ref_mesh_arrays(X.ctypes.data, ep.ctypes.data, conn.ctypes.data, et.ctypes.data,
+                          pid.ctypes.data, eid.ctypes.data, gid.ctypes.data)
+        return dict(coordinates=X[: nN * nd].reshape(nN, nd), eptr=ep, connectivity=conn[:nc],
+                    etype=et[:nE], pid=pid[:nE], global_eid=eid[:nE], global_node_id=gid[:nN],
+                    nPIDglobal=npg)
 
     @classmethod
     def interp_linear(cls, x, y, value):

@@ -22,6 +22,8 @@
 #include "FemTech.h"
 #include "blas.h"
 
+#include <algorithm>
+#include <vector>
 #include <stdarg.h>
 #include <stdexcept>
 #include <string>
@@ -146,13 +148,9 @@ struct RefTerminate {
 void TerminateFemTech(int errorCode) { throw RefTerminate{errorCode}; }
 void FreeArrays() {}
 
-/* ---------------- globals defined outside the compiled hot-path files ---------------- */
-int nparts = 0, nelements = 0, nallelements = 0, nNodes = 0, ndim = 0, nDOF = 0;
-double *coordinates;
+/* ---------------- globals defined outside the compiled files ----------------
+ * (the mesh globals come with src/io/input/ReadInputFile.cpp:5-20) */
 double *mass, *stiffness, *rhs; /* src/fem/Assembly.cpp:3-4 */
-int *connectivity, *eptr, *pid, *global_eid;
-char **ElementType;
-int nPIDglobal = 0, nPID = 0;
 int *materialID;
 double *properties;
 int world_rank = 0, world_size = 1;
@@ -192,8 +190,81 @@ void StressUpdate(int e, int gp) {
   }
 }
 
+/* compare / unique of src/io/PartitionMesh.cpp:450-466 (that file needs
+ * ParMETIS and is not built): ascending int order; in-place removal of
+ * adjacent duplicates, returning the new length */
+int compare(const void *a, const void *b) { return (*(int *)a - *(int *)b); }
+int unique(int *arr, int n) {
+  if (n <= 0) return 0;
+  int j = 0;
+  for (int i = 0; i < n; ++i)
+    if (i == 0 || arr[i] != arr[j - 1]) arr[j++] = arr[i];
+  return j;
+}
+
 /* ---------------- extern "C" driver API ---------------- */
 extern "C" {
+
+/* ReadInputFile (the reference's ReadAbaqus / ReadLsDyna on one rank), then
+ * the single-rank node renumbering of updateConnectivityGlobalToLocal
+ * (PartitionMesh.cpp:485-535, restated: local node j = the j-th smallest node
+ * ID, coordinates of its first occurrence).  Sizes into sz[0..4] = nNodes,
+ * nelements, ndim, nPIDglobal, connectivity length; the arrays are read with
+ * ref_mesh_arrays. */
+static std::vector<int> g_gid;
+int ref_read_mesh(const char *path, int *sz) {
+  try {
+    nallelements = 0;
+    nelements = 0;
+    nNodes = 0;
+    ndim = 0;
+    ReadInputFile(path);
+  } catch (RefTerminate &t) {
+    return -t.code;
+  }
+  const int total = eptr[nelements];
+  std::vector<int> sorted(connectivity, connectivity + total);
+  std::sort(sorted.begin(), sorted.end());
+  sorted.erase(std::unique(sorted.begin(), sorted.end()), sorted.end());
+  const int nU = (int)sorted.size();
+  double *nc = (double *)malloc(sizeof(double) * ndim * (nU > 0 ? nU : 1));
+  for (int j = 0; j < nU; ++j)
+    for (int i = 0; i < total; ++i)
+      if (connectivity[i] == sorted[j]) {
+        memcpy(nc + ndim * j, coordinates + ndim * i, ndim * sizeof(double));
+        break;
+      }
+  for (int i = 0; i < total; ++i)
+    connectivity[i] = (int)(std::lower_bound(sorted.begin(), sorted.end(), connectivity[i]) -
+                            sorted.begin());
+  free(coordinates);
+  coordinates = nc;
+  nNodes = nU;
+  g_gid.assign(sorted.begin(), sorted.end());
+  for (int &g : g_gid) g += 1;
+  sz[0] = nNodes;
+  sz[1] = nelements;
+  sz[2] = ndim;
+  sz[3] = nPIDglobal;
+  sz[4] = total;
+  return 0;
+}
+
+/* the arrays of the last ref_read_mesh; etype: 0 "C3D8", 1 "C3D4", 2 "T3D2",
+ * -1 other */
+void ref_mesh_arrays(double *coords, int *ep, int *conn, int *etype, int *pidOut, int *eid,
+                     int *gid) {
+  memcpy(coords, coordinates, sizeof(double) * ndim * nNodes);
+  memcpy(ep, eptr, sizeof(int) * (nelements + 1));
+  memcpy(conn, connectivity, sizeof(int) * eptr[nelements]);
+  memcpy(pidOut, pid, sizeof(int) * nelements);
+  memcpy(eid, global_eid, sizeof(int) * nelements);
+  memcpy(gid, g_gid.data(), sizeof(int) * nNodes);
+  for (int e = 0; e < nelements; ++e) {
+    const char *t = ElementType[e];
+    etype[e] = strcmp(t, "C3D8") == 0 ? 0 : (strcmp(t, "C3D4") == 0 ? 1 : (strcmp(t, "T3D2") == 0 ? 2 : -1));
+  }
+}
 
 int ref_setup(int nN, int nE, const double *coords, const int *ep, const int *conn,
               const int *etype, const int *pidIn, int nP, const int *matID, const double *props,

@@ -26,3 +26,9 @@ def golden():
     import numpy as np
     return {k: np.load(os.path.join(GOLDEN, k + ".npz")) for k in ("ref_force", "ref_ex9", "ref_cube",
                                                                  "ref_rigid")}
+
+
+@pytest.fixture(scope="session")
+def golden_reader():
+    import numpy as np
+    return np.load(os.path.join(GOLDEN, "ref_reader.npz"))

@@ -25,6 +25,14 @@ Fixtures:
                   work, external work and kinetic energy of the reference's
                   CheckEnergy (the only energy run of the process, so its
                   works start from zero).
+  ref_reader.npz  the reference's mesh readers (ReadAbaqus / ReadLsDyna on one
+                  rank, then PartitionMesh's single-rank renumbering) on
+                  seeded mixed C3D8/C3D4 meshes written as .inp and .k, and on
+                  hand-written files with the formats' corner cases (comments,
+                  continued keyword lines, inherited element sets, node ID
+                  gaps and unused nodes, degenerate hexahedra, zero node slots,
+                  trusses, other element types, CRLF endings); the file texts
+                  are stored with the arrays.
   ref_rigid.npz   the rigid-body helpers of the brain drivers on the
                   reference's math.cpp: interpolateLinear on tables with
                   duplicate and uneven times (queries below, at, between and
@@ -108,6 +116,110 @@ def percentile_cases():
         assert a == b
         out["pct_data_%d" % i] = d
         out["pct_ref_%d" % i] = np.array(a)
+    return out
+
+
+READER_INP_QUIRKS = """** corner cases of the Abaqus reader
+*Heading
+ quirks
+*Node, nset=all
+      7,   0.,   0.,   0.
+      9,   1.,   0.,   0.
+     12,   1.,   1.,   0.
+     13,   0.,   1.,   0.
+     20,   0.,   0.,   1.
+     21,   1.,   0.,   1.
+     22,   1.,   1.,   1.
+     23,   0.,   1.,   1.
+     30,   0.5,  0.5,  2.
+     31,   9.,   9.,   9.
+     40,   2.,   0.,   0.
+*Element, type=C3D8,
+ elset=BLOCK
+ 101, 7, 9, 12, 13, 20, 21, 22, 23
+*ELEMENT, TYPE=C3D4
+ 102, 20, 21, 22, 30
+ 103, 20, 22, 23, 30
+*element, type=T3D2, elset=TRUSS
+ 104, 9, 40
+*Element, type=C3D8R, elset=BLOCK
+ 105, 7, 9, 12, 13, 20, 21, 22, 23
+*End Step
+"""
+
+READER_K_QUIRKS = """$ corner cases of the LS-DYNA reader
+*KEYWORD
+*NODE
+$#   nid               x               y               z      tc      rc
+       5             0.0             0.0             0.0       0       0
+       6             1.0             0.0             0.0       0       0
+       8             1.0             1.0             0.0       0       0
+       9             0.0             1.0             0.0       0       0
+      11             0.0             0.0             1.0       0       0
+      12             1.0             0.0             1.0       0       0
+      14             1.0             1.0             1.0       0       0
+      15             0.0             1.0             1.0       0       0
+      17             0.5             0.5             2.0       0       0
+      18             3.0             3.0             3.0       0       0
+*ELEMENT_SOLID
+$#   eid     pid      n1      n2      n3      n4      n5      n6      n7      n8
+      41       2       5       6       8       9      11      12      14      15
+      42       1      11      12      14      17      17      17      17      17
+      43       1      11      14      15      17       0       0       0       0
+*ELEMENT_SOLID
+$#   eid     pid      n1      n2      n3      n4      n5      n6      n7      n8
+      44       3      11      12      14      14      17      17      17      17
+*ELEMENT_BEAM
+$#   eid     pid      n1      n2
+      45       4       6      18
+*END
+"""
+
+
+def reader_cases():
+    """The reference's readers on written meshes and corner-case files."""
+    import tempfile
+    from femtech_gb300 import meshio
+    out = {}
+    rng = np.random.default_rng(7)
+    hexm = mg.hex_block(3, 2, 2, 0.03, 0.02, 0.02, jitter=0.1, seed=3)
+    tetm = mg.tet_ellipsoid(0.02, 0.015, 0.01, 0.006, jitter=0.1, seed=4)
+    nh = len(hexm["coordinates"])
+    mix = dict(coordinates=np.vstack([hexm["coordinates"], tetm["coordinates"] + [0.05, 0, 0]]),
+               eptr=np.concatenate([hexm["eptr"][:-1], hexm["eptr"][-1] + tetm["eptr"]]),
+               connectivity=np.concatenate([hexm["connectivity"], tetm["connectivity"] + nh]),
+               etype=np.concatenate([hexm["etype"], tetm["etype"]]),
+               pid=np.concatenate([np.zeros(len(hexm["etype"]), np.int32),
+                                   1 + (rng.random(len(tetm["etype"])) < 0.5).astype(np.int32)]))
+    order = np.argsort(mix["pid"], kind="stable")  # element sets in part order
+    nE = len(order)
+    ep, cn = [0], []
+    for e in order:
+        cn.extend(mix["connectivity"][mix["eptr"][e]:mix["eptr"][e + 1]])
+        ep.append(len(cn))
+    mix.update(eptr=np.array(ep, np.int32), connectivity=np.array(cn, np.int32),
+               etype=mix["etype"][order], pid=mix["pid"][order])
+    nN = len(mix["coordinates"])
+    mix["global_node_id"] = 10 + 3 * np.arange(nN)          # ID gaps
+    mix["global_eid"] = 1000 + 2 * np.arange(nE)
+    with tempfile.TemporaryDirectory() as d:
+        files = []
+        for ext, writer in ((".inp", meshio.write_inp), (".k", meshio.write_k)):
+            p = os.path.join(d, "mixed" + ext)
+            writer(p, mix)
+            files.append(("mixed" + ext, open(p).read()))
+        files.append(("quirks.inp", READER_INP_QUIRKS))
+        files.append(("quirks_crlf.inp", READER_INP_QUIRKS.replace("\n", "\r\n")))
+        files.append(("quirks.k", READER_K_QUIRKS))
+        for i, (name, text) in enumerate(files):
+            p = os.path.join(d, name)
+            with open(p, "w", newline="") as fh:
+                fh.write(text)
+            r = orc.RefBuild.read_mesh(p)
+            out["reader_name_%d" % i] = np.array(name)
+            out["reader_text_%d" % i] = np.array(text)
+            for k, v in r.items():
+                out["reader_%s_%d" % (k, i)] = np.asarray(v)
     return out
 
 
@@ -206,7 +318,8 @@ def main():
     np.savez_compressed(os.path.join(HERE, "ref_ex9.npz"), **ex9_case())
     np.savez_compressed(os.path.join(HERE, "ref_cube.npz"), **cube_case())
     np.savez_compressed(os.path.join(HERE, "ref_rigid.npz"), **rigid_cases())
-    for f in ("ref_force.npz", "ref_ex9.npz", "ref_cube.npz", "ref_rigid.npz"):
+    np.savez_compressed(os.path.join(HERE, "ref_reader.npz"), **reader_cases())
+    for f in ("ref_force.npz", "ref_ex9.npz", "ref_cube.npz", "ref_rigid.npz", "ref_reader.npz"):
         print(f, os.path.getsize(os.path.join(HERE, f)))
 
 
