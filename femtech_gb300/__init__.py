@@ -327,6 +327,18 @@ class Model:
         _check(L.ftgpu_get_rigid_body(self.h, int(inst), y, yd))
         return y, yd
 
+    def write_vtu(self, dir, name, step, cell_data=None):
+        """The reference's WriteVTU output of the current state (deformed
+        points, displacements, accelerations, boundary flags, parts, the
+        averaged strain computed on the device, extra int cell arrays)."""
+        from .meshio import _cell_args
+        L = lib()
+        L.ftgpu_write_vtu.argtypes = [C.c_void_p, C.c_char_p, C.c_char_p, C.c_int, C.c_int,
+                                      C.c_void_p, C.c_void_p]
+        nc, ptrs, cnames, keep = _cell_args(cell_data, self.nE)
+        _check(L.ftgpu_write_vtu(self.h, str(dir).encode(), name.encode(), int(step), nc,
+                                 C.cast(ptrs, C.c_void_p), C.cast(cnames, C.c_void_p)))
+
     def launches_per_step(self):
         return lib().ftgpu_launches_per_step(self.h)
 

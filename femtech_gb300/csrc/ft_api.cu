@@ -1503,6 +1503,23 @@ int ftgpu_element_strain(ftgpu_model *m, double *Eavg, double *ps_max, double *p
   return FTGPU_OK;
 }
 
+int ftgpu_write_vtu(ftgpu_model *m, const char *dir, const char *name, int step, int ncell,
+                    const int *const *cell_data, const char *const *cell_names) {
+  if (!m || !m->setup_done) return fail(FTGPU_ERR_STATE, "write_vtu before setup");
+  const size_t n3 = 3 * (size_t)m->nNodes;
+  std::vector<double> u(n3), a(n3), E(9 * (size_t)m->nE);
+  CKI(ftgpu_get_state(m, u.data(), nullptr, a.data(), nullptr, nullptr, nullptr));
+  CKI(ftgpu_element_strain(m, E.data(), nullptr, nullptr, nullptr));
+  std::vector<int> bnd(n3, 0);
+  for (size_t i = 0; i < m->dof_fn.size() && i < n3; ++i) bnd[i] = m->dof_fn[i] != FTGPU_BC_FREE;
+  const int r = ftgpu_write_vtu_arrays(dir, name, step, m->nNodes, m->nE, m->X.data(),
+                                       m->eptr.data(), m->conn.data(), m->etype.data(),
+                                       m->pid.data(), u.data(), a.data(), bnd.data(), E.data(),
+                                       ncell, cell_data, cell_names);
+  if (r) return fail(r, "write_vtu: cannot write the output files");
+  return FTGPU_OK;
+}
+
 static_assert(sizeof(ftgpu_injury) == sizeof(InjuryState), "injury record layout");
 
 int ftgpu_set_injury(ftgpu_model *m, int n, const int *element_ids) {

@@ -111,3 +111,50 @@ def write_k(path, mesh):
     out.append("*END")
     with open(path, "w") as fh:
         fh.write("\n".join(out) + "\n")
+
+
+def _cell_args(cell_data, nE):
+    names = list(cell_data or {})
+    arrs = [np.ascontiguousarray(cell_data[k], np.int32) for k in names]
+    if any(len(x) != nE for x in arrs):
+        raise ValueError("cell data needs one value per element")
+    ptrs = (C.c_void_p * max(1, len(arrs)))(*[x.ctypes.data for x in arrs])
+    cnames = (C.c_char_p * max(1, len(names)))(*[k.encode() for k in names])
+    return len(names), ptrs, cnames, arrs
+
+
+def write_vtu_arrays(dir, name, step, mesh, u, a, boundary, Eavg, cell_data=None):
+    """The reference's WriteVTU output (results/vtu/<name>.vtu.<step>.0000 and
+    results/<name>.<step>.pvtu under dir) from host arrays: u, a per DOF,
+    boundary 0/1 per DOF, Eavg 9 per element, cell_data name -> int array."""
+    L = lib()
+    L.ftgpu_write_vtu_arrays.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_int] + \
+        [C.c_void_p] * 9 + [C.c_int, C.c_void_p, C.c_void_p]
+    X = np.ascontiguousarray(mesh["coordinates"], np.float64).ravel()
+    ep = np.ascontiguousarray(mesh["eptr"], np.int32)
+    cn = np.ascontiguousarray(mesh["connectivity"], np.int32)
+    et = np.ascontiguousarray(mesh["etype"], np.int32)
+    pid = np.ascontiguousarray(mesh["pid"], np.int32)
+    u = np.ascontiguousarray(u, np.float64).ravel()
+    a = np.ascontiguousarray(a, np.float64).ravel()
+    b = np.ascontiguousarray(boundary, np.int32).ravel()
+    E = np.ascontiguousarray(Eavg, np.float64).ravel()
+    nc, ptrs, cnames, keep = _cell_args(cell_data, len(et))
+    rc = L.ftgpu_write_vtu_arrays(str(dir).encode(), name.encode(), int(step), len(X) // 3,
+                                  len(et), *[x.ctypes.data for x in (X, ep, cn, et, pid, u, a, b, E)],
+                                  nc, C.cast(ptrs, C.c_void_p), C.cast(cnames, C.c_void_p))
+    if rc != 0:
+        raise FtgpuError(rc, "write_vtu_arrays failed")
+
+
+def write_pvd(dir, name, step, step_times):
+    """<dir>/<name without extension>.pvd listing results/<name>.<j>.pvtu for
+    j = 0..step with their times (WritePVD)."""
+    L = lib()
+    L.ftgpu_write_pvd.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_void_p]
+    t = np.ascontiguousarray(step_times, np.float64)
+    if len(t) < step + 1:
+        raise ValueError("step + 1 times needed")
+    rc = L.ftgpu_write_pvd(str(dir).encode(), name.encode(), int(step), t.ctypes.data)
+    if rc != 0:
+        raise FtgpuError(rc, "write_pvd failed")

@@ -107,6 +107,30 @@ int ftgpu_read_mesh(const char *path, ftgpu_mesh **out);
 void ftgpu_free_mesh(ftgpu_mesh *mesh);
 const char *ftgpu_read_mesh_error(void);
 
+/* ---- output steps: the reference's ASCII VTU files (WriteVTU.cpp:3-263,
+ * WritePVD.cpp:6-36, one rank) ----
+ * ftgpu_write_vtu writes <dir>/results/vtu/<name>.vtu.<step>.0000 and
+ * <dir>/results/<name>.<step>.pvtu from the model's current state: deformed
+ * points, connectivity / offsets / VTK types, Displacements, Accelerations,
+ * Boundary (constrained DOFs), PartID, AvgStrain (CalculateStrain's Eavg,
+ * computed on the device), ProcID and ncell extra Int32 cell arrays (the
+ * brain drivers' injury outputs).  Text and layout are the reference's;
+ * displacements below 1e-20 in magnitude are written as 0 as the reference
+ * writes them (it also flushes them in its state; the device state is left
+ * as it is).  dir NULL or "" = the working directory.  ftgpu_write_pvd writes
+ * <dir>/<name without extension>.pvd listing steps 0..step with their times.
+ * ftgpu_write_vtu_arrays is the same writer on host arrays (reference layout,
+ * boundary as 0/1 per DOF, Eavg 9 per element); it needs no device. */
+int ftgpu_write_vtu(ftgpu_model *m, const char *dir, const char *name, int step, int ncell,
+                    const int *const *cell_data, const char *const *cell_names);
+int ftgpu_write_vtu_arrays(const char *dir, const char *name, int step, int nNodes,
+                           int nelements, const double *coordinates, const int *eptr,
+                           const int *connectivity, const int *etype, const int *pid,
+                           const double *u, const double *a, const int *boundary,
+                           const double *Eavg, int ncell, const int *const *cell_data,
+                           const char *const *cell_names);
+int ftgpu_write_pvd(const char *dir, const char *name, int step, const double *step_time);
+
 /* Mesh in the reference's arrays (ReadInputFile + PartitionMesh leave these in
  * coordinates, eptr, connectivity, ElementType, pid: GlobalVariables.h:34-48).
  * etype[e] is FTGPU_C3D8 or FTGPU_C3D4.  Arrays are copied. */

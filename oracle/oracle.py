@@ -394,6 +394,8 @@ class RefBuild:
             L.ref_element_strain.argtypes = [_dp, _dp, _dp, _dp]
             L.ref_percentile95.argtypes = [_dp, C.c_int, C.POINTER(C.c_double),
                                            C.POINTER(C.c_double)]
+            L.ref_write_vtu.argtypes = [C.c_char_p, C.c_char_p, C.c_int, _dp, _dp, _ip, _dp,
+                                        C.c_int, C.c_void_p, C.c_void_p, _dp]
             L.ref_read_mesh.argtypes = [C.c_char_p, C.POINTER(C.c_int)]
             L.ref_mesh_arrays.argtypes = [C.c_void_p] * 7
             L.ref_interp_linear.argtypes = [C.c_int, _dp, _dp, C.c_double]
@@ -443,6 +445,24 @@ class RefBuild:
         if rc:
             raise RuntimeError("ref_get_force failed %d" % rc)
         return fi
+
+    def write_vtu(self, dir, name, step, u, a, boundary, Eavg, cell_data, step_times):
+        """The reference's WriteVTU + WritePVD for this mesh and the given
+        state into dir (cell_data: dict name -> int array per element)."""
+        names = list(cell_data)
+        arrs = [np.ascontiguousarray(cell_data[k], np.int32) for k in names]
+        ptrs = (C.c_void_p * max(1, len(arrs)))(*[x.ctypes.data for x in arrs])
+        cnames = (C.c_char_p * max(1, len(names)))(*[k.encode() for k in names])
+        rc = self.lib().ref_write_vtu(str(dir).encode(), name.encode(), int(step),
+                                      np.ascontiguousarray(u, np.float64).ravel(),
+                                      np.ascontiguousarray(a, np.float64).ravel(),
+                                      np.ascontiguousarray(boundary, np.int32).ravel(),
+                                      np.ascontiguousarray(Eavg, np.float64).ravel(),
+                                      len(names), C.cast(ptrs, C.c_void_p),
+                                      C.cast(cnames, C.c_void_p),
+                                      np.ascontiguousarray(step_times, np.float64))
+        if rc:
+            raise RuntimeError("ref_write_vtu failed %d" % rc)
 
     @classmethod
     def read_mesh(cls, path):

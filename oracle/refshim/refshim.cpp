@@ -25,6 +25,8 @@
 #include <algorithm>
 #include <vector>
 #include <stdarg.h>
+#include <sys/stat.h>
+#include <unistd.h>
 #include <stdexcept>
 #include <string>
 
@@ -248,6 +250,30 @@ int ref_read_mesh(const char *path, int *sz) {
   sz[3] = nPIDglobal;
   sz[4] = total;
   return 0;
+}
+
+/* WriteVTU + WritePVD (src/io/output/WriteVTU.cpp, WritePVD.cpp) of the mesh
+ * of the last ref_setup with the given state, in directory dir (results/vtu
+ * is created first: the reference expects it); stepTimes has step + 1
+ * entries.  u is copied (the writer flushes tiny displacements in place). */
+int ref_write_vtu(const char *dir, const char *name, int step, const double *u, const double *a,
+                  const int *bnd, const double *E, int ncell, int **cell_data,
+                  const char **cell_names, const double *stepTimes) {
+  char cwd[4096];
+  if (!getcwd(cwd, sizeof(cwd))) return -1;
+  if (chdir(dir)) return -2;
+  mkdir("results", 0755);
+  mkdir("results/vtu", 0755);
+  memcpy(displacements, u, sizeof(double) * nDOF);
+  memcpy(accelerations, a, sizeof(double) * nDOF);
+  memcpy(boundary, bnd, sizeof(int) * nDOF);
+  memcpy(Eavg, E, sizeof(double) * 9 * nelements);
+  free(stepTime);
+  stepTime = (double *)malloc(sizeof(double) * (step + 1));
+  memcpy(stepTime, stepTimes, sizeof(double) * (step + 1));
+  WriteVTU(name, step, cell_data, ncell, cell_names);
+  WritePVD(name, step);
+  return chdir(cwd) ? -3 : 0;
 }
 
 /* the arrays of the last ref_read_mesh; etype: 0 "C3D8", 1 "C3D4", 2 "T3D2",

@@ -33,6 +33,11 @@ Fixtures:
                   gaps and unused nodes, degenerate hexahedra, zero node slots,
                   trusses, other element types, CRLF endings); the file texts
                   are stored with the arrays.
+  ref_vtu.npz     the reference's WriteVTU + WritePVD files (.vtu, .pvtu,
+                  .pvd texts) for a mixed C3D8/C3D4 mesh with a seeded state
+                  (displacements below 1e-20 included), boundary flags,
+                  averaged strains and two extra cell arrays, for an output
+                  name without and with an extension.
   ref_rigid.npz   the rigid-body helpers of the brain drivers on the
                   reference's math.cpp: interpolateLinear on tables with
                   duplicate and uneven times (queries below, at, between and
@@ -223,6 +228,52 @@ def reader_cases():
     return out
 
 
+def vtu_mesh():
+    """The mixed mesh of the VTU fixtures (also rebuilt by the tests)."""
+    hexm = mg.hex_block(2, 2, 1, 0.02, 0.02, 0.01, jitter=0.1, seed=5)
+    nh = len(hexm["coordinates"])
+    X = np.vstack([hexm["coordinates"], [[0.005, 0.005, 0.02], [0.015, 0.01, 0.02]]])
+    tets = np.array([[nh - 9, nh - 8, nh - 6, nh], [nh - 8, nh - 5, nh - 6, nh + 1]], np.int32)
+    conn = np.concatenate([hexm["connectivity"], tets.ravel()])
+    eptr = np.concatenate([hexm["eptr"], hexm["eptr"][-1] + 4 * np.arange(1, 3)]).astype(np.int32)
+    return dict(coordinates=X, eptr=eptr, connectivity=conn.astype(np.int32),
+                etype=np.array([0] * 4 + [1] * 2, np.int32),
+                pid=np.array([0, 0, 1, 1, 2, 2], np.int32))
+
+
+def vtu_state(mesh):
+    rng = np.random.default_rng(263)
+    n3, nE = 3 * len(mesh["coordinates"]), len(mesh["etype"])
+    u = rng.normal(0, 1e-3, n3)
+    u[::7] = rng.normal(0, 1e-22, len(u[::7]))  # below the writer's flush threshold
+    a = rng.normal(0, 10.0, n3)
+    b = (rng.random(n3) < 0.3).astype(np.int32)
+    E = rng.normal(0, 0.05, 9 * nE)
+    cells = {"MPS-95": (rng.random(nE) < 0.5).astype(np.int32),
+             "CSDM-15": rng.integers(0, 2, nE).astype(np.int32)}
+    return u, a, b, E, cells
+
+
+def vtu_cases():
+    import tempfile
+    mesh = vtu_mesh()
+    u, a, b, E, cells = vtu_state(mesh)
+    mats = mg.materials([(1, [1000.0, 3400.0, 2.0e6])] * 3)
+    r = orc.RefBuild(mesh, mats)
+    times = np.array([0.0, 1.25e-3, 2.5e-3, 3.75e-3])
+    out = {}
+    for i, name in enumerate(("head", "head.inp")):
+        with tempfile.TemporaryDirectory() as d:
+            r.write_vtu(d, name, 3, u, a, b, E, cells, times)
+            base = name.rsplit(".", 1)[0]
+            for key, rel in (("vtu", "results/vtu/%s.vtu.0003.0000" % name),
+                             ("pvtu", "results/%s.0003.pvtu" % name), ("pvd", base + ".pvd")):
+                out["vtu_%s_%d" % (key, i)] = np.array(open(os.path.join(d, rel)).read())
+        out["vtu_name_%d" % i] = np.array(name)
+    out["vtu_times"] = times
+    return out
+
+
 def rigid_cases():
     rng = np.random.default_rng(339)
     out = {}
@@ -319,7 +370,9 @@ def main():
     np.savez_compressed(os.path.join(HERE, "ref_cube.npz"), **cube_case())
     np.savez_compressed(os.path.join(HERE, "ref_rigid.npz"), **rigid_cases())
     np.savez_compressed(os.path.join(HERE, "ref_reader.npz"), **reader_cases())
-    for f in ("ref_force.npz", "ref_ex9.npz", "ref_cube.npz", "ref_rigid.npz", "ref_reader.npz"):
+    np.savez_compressed(os.path.join(HERE, "ref_vtu.npz"), **vtu_cases())
+    for f in ("ref_force.npz", "ref_ex9.npz", "ref_cube.npz", "ref_rigid.npz", "ref_reader.npz",
+              "ref_vtu.npz"):
         print(f, os.path.getsize(os.path.join(HERE, f)))
 
 
