@@ -442,9 +442,23 @@ int launch_groups_t(ftgpu_model *m, int parity, int use_clock, double dt_direct,
   const int PE = max_patch(m);
   for (size_t gi = 0; gi < m->ps.groups.size(); ++gi) {
     const PatchGroup &g = m->ps.groups[gi];
-    if (gp == 0 && gi < m->group_idle.size() && m->group_idle[gi]) continue;
+    if (gp != kLaunchGaussPoints && gi < m->group_idle.size() && m->group_idle[gi]) continue;
     ElemArgs<R> A = elem_args<R>(m, g, (int)gi);
     A.parity = parity;
+    // the injury criteria ride on the force pass of groups with listed elements
+    int mode = gp;
+    if (gp == kLaunchInjury) {
+      if (dt_only == kPassForce && m->injury_on && m->inj_group_n[gi] > 0) {
+        A.inj_cidx = m->inj_cidx.as<int>();
+        A.inj_upos = m->inj_upos_d.as<int>();
+        A.inj_flags = m->inj_flags.as<uint8_t>();
+        A.inj_ps_old = m->inj_ps_old.as<R>();
+        A.inj_psxsr = m->inj_psxsr.as<R>();
+        A.inj_part = m->inj_part.p;
+      } else {
+        mode = kLaunchPlain;
+      }
+    }
     A.use_clock = use_clock;
     A.dt_direct = dt_direct;
     const size_t smem = elem_smem_bytes_host<R>(g.etype, PE);
@@ -463,7 +477,7 @@ int launch_groups_t(ftgpu_model *m, int parity, int use_clock, double dt_direct,
       A.surr_x = nullptr;
       A.surr_y = m->surr_y.as<float>() + base * kMlpOut;
     }
-    int r = launch_elem<R>(g.etype, g.mat, gp, g.npatch, PE, smem, m->stream, A, dt_only);
+    int r = launch_elem<R>(g.etype, g.mat, mode, g.npatch, PE, smem, m->stream, A, dt_only);
     if (r) return r;
   }
   return 0;
@@ -900,24 +914,15 @@ InjuryArgs<R> injury_args(ftgpu_model *m, int parity) {
   return A;
 }
 
-// One step of the injury criteria, between the element pass and the nodal
-// update (the slots still hold this step's displacements): per group the
-// fused strain / principal-strain / update pass, the step's extremes (which
-// also clears the histograms), the radix passes of both selections, the
-// element lists and the running maxima.
+// One step of the injury criteria after the element pass (whose force
+// launches of groups with listed elements updated the per-element criteria
+// and left each block's extremes, launch mode kLaunchInjury): the step's
+// extremes (which also clears the histograms), the radix passes of both
+// selections, the element lists and the running maxima.  Partials of patches
+// without listed elements keep their sentinel values.
 template <class R>
 int launch_injury_t(ftgpu_model *m, int parity) {
   const InjuryArgs<R> J = injury_args<R>(m, parity);
-  const int PE = max_patch(m);
-  for (size_t gi = 0; gi < m->ps.groups.size(); ++gi) {
-    const PatchGroup &g = m->ps.groups[gi];
-    if (m->inj_group_n[gi] == 0) continue;  // its partials keep the sentinel values
-    const ElemArgs<R> A = elem_args<R>(m, g, (int)gi);
-    const size_t smem = elem_smem_bytes_host<R>(g.etype, PE);
-    const int r = launch_injury_pass(g.etype, g.npatch, PE, smem, m->stream, A, J);
-    if (r) return fail(FTGPU_ERR_CUDA, std::string("injury pass: ") +
-                                           cudaGetErrorString((cudaError_t)r));
-  }
   k_injury_reduce<R><<<(J.npart + kInjReduceSpan - 1) / kInjReduceSpan, 256, 0, m->stream>>>(J);
   const int hb = std::min((m->inj_n + kInjThreads - 1) / kInjThreads, 512);
   for (int pass = 0; pass < (int)sizeof(R); ++pass)
@@ -948,7 +953,7 @@ int capture_chunk(ftgpu_model *m, int K, bool prof) {
   int r = launch_node(m, kNodeBegin, 0);
   for (int k = 0; k < K && !r; ++k) {
     if (prof) r = (int)cudaEventRecordWithFlags(m->prof_ev[2 * k], m->stream, cudaEventRecordExternal);
-    if (!r) r = launch_groups(m, k & 1, 1, 0.0, 0, 0);
+    if (!r) r = launch_groups(m, k & 1, 1, 0.0, m->injury_on ? kLaunchInjury : kLaunchPlain, 0);
     if (prof && !r)
       r = (int)cudaEventRecordWithFlags(m->prof_ev[2 * k + 1], m->stream, cudaEventRecordExternal);
     if (!r && m->injury_on) r = launch_injury(m, k & 1);
@@ -1462,14 +1467,8 @@ int ftgpu_launches_per_step(ftgpu_model *m) {
   if (m->surr)
     for (auto &x : m->ps.groups) g += 2 * (x.npatch > 0 && x.mat == 7);
   int inj = 0;
-  if (m->injury_on) {  // injury pass per group, reduce, radix passes, list, final
-    int sg = 0;
-    for (auto &x : m->ps.groups) sg += x.npatch > 0;
-    sg = 0;
-    for (size_t gi = 0; gi < m->ps.groups.size(); ++gi)
-      sg += m->ps.groups[gi].npatch > 0 && m->inj_group_n[gi] > 0;
-    inj = sg + 1 + (is_fp64(m) ? 8 : 4) + 2;
-  }
+  if (m->injury_on)  // (element work rides on the force pass) reduce, radix passes, list, final
+    inj = 1 + (is_fp64(m) ? 8 : 4) + 2;
   return g + 2 + (m->energy_on ? 1 : 0) + inj;  // + k_energy_reduce
 }
 

@@ -89,6 +89,13 @@ struct ElemArgs {
   uint16_t *surr_x;
   const float *surr_y;
   SurrogateLaw law;
+  // per-step injury criteria fused into the force pass (launch mode 2):
+  // listed elements in group order and their state (null otherwise)
+  const int *inj_cidx;        // [E] compact index or -1
+  const int *inj_upos;        // [listed] position in the caller's list
+  uint8_t *inj_flags;         // [listed]
+  Real *inj_ps_old, *inj_psxsr;
+  void *inj_part;             // [patches] InjuryPart block extremes
 };
 
 enum { kPassForce = 0, kPassDt = 1, kPassSurrogateFeatures = 2 };

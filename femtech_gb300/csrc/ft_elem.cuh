@@ -482,11 +482,100 @@ __device__ __forceinline__ double dt_of<double>(double le, const MatP<double> &m
   return le / mp.ce;  // CalculateTimeStep.cpp:19
 }
 
-template <class R, int ET, int MAT, bool GP>
+template <class R, int ET>
+__device__ __forceinline__ void element_green_strain(const R (&x)[ET == 0 ? 8 : 4][3],
+                                                     const R (&u)[ET == 0 ? 8 : 4][3],
+                                                     R (&Es)[6]);
+
+// One listed element's injury update (the body of the reference's per-element
+// loop, ex5.cpp:1330-1383): principal strains of the averaged Green strain,
+// the sticky flags, the principal strain rate against the previous step, and
+// the thread's extremes.
+template <class R>
+__device__ __forceinline__ void injury_element(const ElemArgs<R> &A, int c, const R (&Es)[6],
+                                               R dt, R (&v)[4], int (&jj)[4], int (&cc)[4]) {
+  R mx, mn, sh;
+  principal_strains<R>(Es[0], Es[1], Es[2], Es[3], Es[4], Es[5], mx, mn, sh);
+  uint8_t f = A.inj_flags[c];
+  if (mx > R(0.15)) f |= kInjMps15;
+  if (mx > R(0.30)) f |= kInjMps30;
+  const R psr = (mx - A.inj_ps_old[c]) / dt;
+  const R psxsr = mx * psr;
+  if (psr > R(120)) f |= kInjPsr120;
+  if (psxsr > R(28)) f |= kInjPsxsr28;
+  A.inj_flags[c] = f;
+  A.inj_ps_old[c] = mx;
+  A.inj_psxsr[c] = psxsr;
+  v[0] = mx;
+  v[1] = mn;
+  v[2] = sh;
+  v[3] = psxsr;
+  const int up = A.inj_upos[c];
+  jj[0] = jj[1] = jj[2] = jj[3] = up;
+  cc[0] = cc[1] = cc[2] = cc[3] = c;
+}
+
+// The block's injury extremes into *out: a butterfly per warp, then the warps
+// in order by thread 0.  The order (value, then smallest list position) is
+// total over listed elements, so the result does not depend on the shape of
+// the reduction.  Values are compared in the element precision R (they are R
+// values; FP64 compares are slow on this GPU) and widened when written.
+// Every thread of the block calls it.
+template <int NT, class R>
+__device__ __forceinline__ void injury_block_extremes(R (&v)[4], int (&jj)[4], int (&cc)[4],
+                                                      InjuryPart *out) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const R ov = __shfl_xor_sync(0xffffffffu, v[k], o);
+      const int oj = __shfl_xor_sync(0xffffffffu, jj[k], o);
+      const int oc = __shfl_xor_sync(0xffffffffu, cc[k], o);
+      if (inj_better(k, ov, oj, v[k], jj[k])) {
+        v[k] = ov;
+        jj[k] = oj;
+        cc[k] = oc;
+      }
+    }
+  __shared__ R wv[NT / 32][4];
+  __shared__ int wj[NT / 32][4], wc[NT / 32][4];
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      wv[w][k] = v[k];
+      wj[w][k] = jj[k];
+      wc[w][k] = cc[k];
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  for (int x = 1; x < (int)(blockDim.x + 31) / 32; ++x)
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (inj_better(k, wv[x][k], wj[x][k], v[k], jj[k])) {
+        v[k] = wv[x][k];
+        jj[k] = wj[x][k];
+        cc[k] = wc[x][k];
+      }
+  InjuryPart q;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {  // no listed element: the reduction's sentinels
+    q.v[k] = cc[k] < 0 ? (k == 1 ? 1e300 : -1e300) : double(v[k]);
+    q.j[k] = jj[k];
+    q.c[k] = cc[k];
+  }
+  *out = q;
+}
+
+template <class R, int ET, int MAT, bool GP, bool INJ>
 // C3D8: at most 128 registers per thread (two 256-thread or four 128-thread
 // blocks per SM); only the rarely taken eigen-decomposition fallback of the
 // Ogden law needs more and spills there.  C3D4 (one Gauss point, latency
 // bound): at most 85, for three 256-thread or six 128-thread blocks per SM.
+// INJ: the force pass also updates the brain drivers' per-step injury
+// criteria of its listed elements (CalculateInjuryCriterions, ex5.cpp:
+// 1311-1430, on the F of this pass) and writes the block's extremes.
 __global__ void __launch_bounds__(kElemThreads, ET == 0 ? 2 : 3)
     k_elem(const ElemArgs<R> A, int pass) {
   constexpr int NC = ET == 0 ? 8 : 4;
@@ -516,6 +605,7 @@ __global__ void __launch_bounds__(kElemThreads, ET == 0 ? 2 : 3)
   R hin[NH];
 #pragma unroll
   for (int k = 0; k < NH; ++k) hin[k] = R(0);
+  const int ci = (INJ && act) ? A.inj_cidx[e] : -1;  // listed for the injury criteria
   if (act) {
     if (NC == 8) {
       cv = *reinterpret_cast<const uint4 *>(A.lconn + 8ll * el);
@@ -549,6 +639,10 @@ __global__ void __launch_bounds__(kElemThreads, ET == 0 ? 2 : 3)
   __syncthreads();
   double dte = r_inf<double>();
   int bad = 0;
+  // injury extremes of this thread's element: max / min principal strain,
+  // max shear, max MPS x rate, with list position and compact index
+  R iv[4] = {-r_inf<R>(), r_inf<R>(), -r_inf<R>(), -r_inf<R>()};
+  int ij[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff}, ic[4] = {-1, -1, -1, -1};
   if (act) {
     int lc[NC];
     lc[0] = cv.x & 0xffff; lc[1] = cv.x >> 16; lc[2] = cv.y & 0xffff; lc[3] = cv.y >> 16;
@@ -567,6 +661,8 @@ __global__ void __launch_bounds__(kElemThreads, ET == 0 ? 2 : 3)
         u[a][d] = shU[d * kMaxLocalNodes + l];
       }
     }
+    R Es[6];  // injury: the element's averaged Green strain (as k_elem_strain)
+    if (INJ && ci >= 0) element_green_strain<R, ET>(x, u, Es);
     const bool skip = pw < 0;
     const MatP<R> mp = A.mats[pw & 0x7fffffff];
     R pc[4];
@@ -591,9 +687,12 @@ __global__ void __launch_bounds__(kElemThreads, ET == 0 ? 2 : 3)
         for (int d = 0; d < 3; ++d) shF[(a * 3 + d) * PE + t] = f[a][d];
     }
     if (!skip) dte = dt_of<R>(le, mp);
+    if (INJ && ci >= 0) injury_element<R>(A, ci, Es, dt, iv, ij, ic);
   }
   if (bad) atomicOr(A.err, (bad & 1 ? kErrInverted : 0) | (bad & 2 ? kErrIndex : 0));
   if (pass == kPassSurrogateFeatures) return;  // features only (uniform per block)
+  if (INJ && pass == kPassForce)
+    injury_block_extremes<kElemThreads>(iv, ij, ic, reinterpret_cast<InjuryPart *>(A.inj_part) + p);
   // block minimum of the element time steps -> one FP64 atomicMin per block
   // (positive doubles order like their bit patterns)
 #pragma unroll
@@ -742,114 +841,6 @@ __global__ void __launch_bounds__(kElemThreads) k_elem_strain(const ElemArgs<R> 
   element_green_strain<R, ET>(x, u, Es);
 #pragma unroll
   for (int k = 0; k < 6; ++k) Eout[6 * (long long)e + k] = double(Es[k]);
-}
-
-// One step of the injury criteria for the listed elements of a group
-// (ex5.cpp:1311-1365): the element's averaged Green strain (as k_elem_strain),
-// its principal strains (CalculateStrain.cpp:38-74, in R), the sticky flags,
-// the principal strain rate against the previous step, and this block's
-// extremes (best value, then smallest list position) into part[p].
-template <class R, int ET>
-__global__ void __launch_bounds__(kElemThreads) k_elem_injury(const ElemArgs<R> A,
-                                                              const InjuryArgs<R> J) {
-  constexpr int NC = ET == 0 ? 8 : 4;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  R *shX = reinterpret_cast<R *>(smem_raw);
-  R *shU = shX + 3 * kMaxLocalNodes;
-  const int PE = blockDim.x;
-  const int t = threadIdx.x;
-  const int p = A.patch_begin + blockIdx.x;
-  const int e0 = A.patch_elem_off[p], ne = A.patch_elem_off[p + 1] - e0;
-  const int s0 = A.patch_node_off[p], ns = A.patch_node_off[p + 1] - s0;
-  const Clock ck = J.clock[J.parity];
-  for (int i = t; i < ns; i += PE) {
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      shX[d * kMaxLocalNodes + i] = A.sX[d * A.S + s0 + i];
-      shU[d * kMaxLocalNodes + i] = A.sU[d * A.S + s0 + i];
-    }
-  }
-  __syncthreads();
-  double v[4] = {-1e300, 1e300, -1e300, -1e300};
-  int jj[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff}, cc[4] = {-1, -1, -1, -1};
-  const int e = e0 + t;
-  const int c = (t < ne && !ck.done) ? J.cidx[e] : -1;
-  if (c >= 0) {
-    const long long el = e - A.elem_begin;
-    int lc[NC];
-    if (NC == 8) {
-      const uint4 w = *reinterpret_cast<const uint4 *>(A.lconn + 8ll * el);
-      lc[0] = w.x & 0xffff; lc[1] = w.x >> 16; lc[2] = w.y & 0xffff; lc[3] = w.y >> 16;
-      lc[4 % NC] = w.z & 0xffff; lc[5 % NC] = w.z >> 16; lc[6 % NC] = w.w & 0xffff; lc[7 % NC] = w.w >> 16;
-    } else {
-      const uint2 w = *reinterpret_cast<const uint2 *>(A.lconn + 4ll * el);
-      lc[0] = w.x & 0xffff; lc[1] = w.x >> 16; lc[2] = w.y & 0xffff; lc[3] = w.y >> 16;
-    }
-    R x[NC][3], u[NC][3];
-#pragma unroll
-    for (int a = 0; a < NC; ++a) {
-      const int l = lc[a] < ns ? lc[a] : 0;
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        x[a][d] = shX[d * kMaxLocalNodes + l];
-        u[a][d] = shU[d * kMaxLocalNodes + l];
-      }
-    }
-    R Es[6];
-    element_green_strain<R, ET>(x, u, Es);
-    R mx, mn, sh;
-    principal_strains<R>(Es[0], Es[1], Es[2], Es[3], Es[4], Es[5], mx, mn, sh);
-    uint8_t f = J.flags[c];
-    if (mx > R(0.15)) f |= kInjMps15;
-    if (mx > R(0.30)) f |= kInjMps30;
-    const R psr = (mx - J.ps_old[c]) / R(ck.dt);
-    const R psxsr = mx * psr;
-    if (psr > R(120)) f |= kInjPsr120;
-    if (psxsr > R(28)) f |= kInjPsxsr28;
-    J.flags[c] = f;
-    J.ps_old[c] = mx;
-    J.psxsr[c] = psxsr;
-    v[0] = double(mx);
-    v[1] = double(mn);
-    v[2] = double(sh);
-    v[3] = double(psxsr);
-    const int up = J.upos[c];
-    jj[0] = jj[1] = jj[2] = jj[3] = up;
-    cc[0] = cc[1] = cc[2] = cc[3] = c;
-  }
-  // block extremes (shared memory reuses the staging area)
-  __syncthreads();
-  double *sv = reinterpret_cast<double *>(smem_raw);  // [4][PE]
-  int *sj = reinterpret_cast<int *>(sv + 4 * PE);     // [4][PE]
-  int *sc = sj + 4 * PE;                              // [4][PE]
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    sv[k * PE + t] = v[k];
-    sj[k * PE + t] = jj[k];
-    sc[k * PE + t] = cc[k];
-  }
-  __syncthreads();
-  for (int h = PE > 1 ? 1 << (31 - __clz(PE - 1)) : 0; h > 0; h >>= 1) {
-    if (t < h && t + h < PE)
-#pragma unroll
-      for (int k = 0; k < 4; ++k)
-        if (inj_better(k, sv[k * PE + t + h], sj[k * PE + t + h], sv[k * PE + t], sj[k * PE + t])) {
-          sv[k * PE + t] = sv[k * PE + t + h];
-          sj[k * PE + t] = sj[k * PE + t + h];
-          sc[k * PE + t] = sc[k * PE + t + h];
-        }
-    __syncthreads();
-  }
-  if (t == 0) {
-    InjuryPart q;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      q.v[k] = sv[k * PE];
-      q.j[k] = sj[k * PE];
-      q.c[k] = sc[k * PE];
-    }
-    J.part[p] = q;
-  }
 }
 
 template <class R>

@@ -6,10 +6,12 @@ namespace ftgpu {
 
 template <int ET, int MAT>
 static int go(int gp, int nb, int th, size_t sm, cudaStream_t s, const ElemArgs<float> &A, int dto) {
-  if (gp)
-    k_elem<float, ET, MAT, true><<<nb, th, sm, s>>>(A, dto);
+  if (gp == kLaunchGaussPoints)
+    k_elem<float, ET, MAT, true, false><<<nb, th, sm, s>>>(A, dto);
+  else if (gp == kLaunchInjury)
+    k_elem<float, ET, MAT, false, true><<<nb, th, sm, s>>>(A, dto);
   else
-    k_elem<float, ET, MAT, false><<<nb, th, sm, s>>>(A, dto);
+    k_elem<float, ET, MAT, false, false><<<nb, th, sm, s>>>(A, dto);
   return (int)cudaGetLastError();
 }
 
@@ -27,16 +29,6 @@ static int by_mat(int mat, int gp, int nb, int th, size_t sm, cudaStream_t s,
     case 7: return go<ET, 7>(gp, nb, th, sm, s, A, dto);
     default: return (int)cudaErrorInvalidValue;
   }
-}
-
-int launch_injury_f32(int etype, int nblocks, int threads, size_t smem, cudaStream_t s,
-                      const ElemArgs<float> &A, const InjuryArgs<float> &J) {
-  if (nblocks <= 0) return 0;
-  if (etype == 0)
-    k_elem_injury<float, 0><<<nblocks, threads, smem, s>>>(A, J);
-  else
-    k_elem_injury<float, 1><<<nblocks, threads, smem, s>>>(A, J);
-  return (int)cudaGetLastError();
 }
 
 int launch_strain_f32(int etype, int nblocks, int threads, size_t smem, cudaStream_t s,

@@ -6,10 +6,12 @@ namespace ftgpu {
 
 template <int ET, int MAT>
 static int go(int gp, int nb, int th, size_t sm, cudaStream_t s, const ElemArgs<double> &A, int dto) {
-  if (gp)
-    k_elem<double, ET, MAT, true><<<nb, th, sm, s>>>(A, dto);
+  if (gp == kLaunchGaussPoints)
+    k_elem<double, ET, MAT, true, false><<<nb, th, sm, s>>>(A, dto);
+  else if (gp == kLaunchInjury)
+    k_elem<double, ET, MAT, false, true><<<nb, th, sm, s>>>(A, dto);
   else
-    k_elem<double, ET, MAT, false><<<nb, th, sm, s>>>(A, dto);
+    k_elem<double, ET, MAT, false, false><<<nb, th, sm, s>>>(A, dto);
   return (int)cudaGetLastError();
 }
 
@@ -27,16 +29,6 @@ static int by_mat(int mat, int gp, int nb, int th, size_t sm, cudaStream_t s,
     case 7: return go<ET, 7>(gp, nb, th, sm, s, A, dto);
     default: return (int)cudaErrorInvalidValue;
   }
-}
-
-int launch_injury_f64(int etype, int nblocks, int threads, size_t smem, cudaStream_t s,
-                      const ElemArgs<double> &A, const InjuryArgs<double> &J) {
-  if (nblocks <= 0) return 0;
-  if (etype == 0)
-    k_elem_injury<double, 0><<<nblocks, threads, smem, s>>>(A, J);
-  else
-    k_elem_injury<double, 1><<<nblocks, threads, smem, s>>>(A, J);
-  return (int)cudaGetLastError();
 }
 
 int launch_strain_f64(int etype, int nblocks, int threads, size_t smem, cudaStream_t s,

@@ -110,7 +110,8 @@ __device__ __forceinline__ double fkey_inv(uint64_t k) {
 
 // better (value, list index) of two candidates for extreme k (k = 1 is a
 // minimum): the better value, then the smaller list index
-__device__ __forceinline__ bool inj_better(int k, double bv, int bj, double av, int aj) {
+template <class V>
+__device__ __forceinline__ bool inj_better(int k, V bv, int bj, V av, int aj) {
   return (k == 1) ? (bv < av || (bv == av && bj < aj)) : (bv > av || (bv == av && bj < aj));
 }
 

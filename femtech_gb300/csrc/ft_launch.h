@@ -8,9 +8,14 @@
 
 namespace ftgpu {
 
+// Launch modes of the element kernel (argument gp of launch_elem_*)
+enum { kLaunchPlain = 0, kLaunchGaussPoints = 1, kLaunchInjury = 2 };
+
 // Launch the element kernel of (etype, material) over `nblocks` patches.
-// gp = 1 records per-Gauss-point F/detF/PK2; dt_only = 1 computes only the
-// stable-time-step contribution.  Returns a cudaError_t value.
+// gp = kLaunchGaussPoints records per-Gauss-point F/detF/PK2, kLaunchInjury
+// also updates the injury criteria of the listed elements (force pass);
+// dt_only = 1 computes only the stable-time-step contribution.  Returns a
+// cudaError_t value.
 int launch_elem_f32(int etype, int mat, int gp, int nblocks, int threads, size_t smem,
                     cudaStream_t s, const ElemArgs<float> &A, int dt_only);
 int launch_elem_f64(int etype, int mat, int gp, int nblocks, int threads, size_t smem,
@@ -34,20 +39,6 @@ template <>
 inline int launch_strain<double>(int etype, int nblocks, int threads, size_t smem,
                                  cudaStream_t s, const ElemArgs<double> &A, double *Eout) {
   return launch_strain_f64(etype, nblocks, threads, smem, s, A, Eout);
-}
-
-// Injury-criteria pass (k_elem_injury) of one group.  Returns a cudaError_t.
-int launch_injury_f32(int etype, int nblocks, int threads, size_t smem, cudaStream_t s,
-                      const ElemArgs<float> &A, const InjuryArgs<float> &J);
-int launch_injury_f64(int etype, int nblocks, int threads, size_t smem, cudaStream_t s,
-                      const ElemArgs<double> &A, const InjuryArgs<double> &J);
-inline int launch_injury_pass(int etype, int nblocks, int threads, size_t smem, cudaStream_t s,
-                              const ElemArgs<float> &A, const InjuryArgs<float> &J) {
-  return launch_injury_f32(etype, nblocks, threads, smem, s, A, J);
-}
-inline int launch_injury_pass(int etype, int nblocks, int threads, size_t smem, cudaStream_t s,
-                              const ElemArgs<double> &A, const InjuryArgs<double> &J) {
-  return launch_injury_f64(etype, nblocks, threads, smem, s, A, J);
 }
 
 // Dynamic shared memory of one element block: node X and u for
