@@ -639,12 +639,10 @@ int upload_epid(ftgpu_model *m, bool zero_idle) {
       idle = (w[ge] & (int)0x80000000u) != 0;
     m->group_idle[gi] = idle ? 1 : 0;
     if (idle && zero_idle) {  // its slots may hold forces of an earlier BC table
-      const size_t rb = is_fp64(m) ? sizeof(double) : sizeof(float);
+      const size_t rb = is_fp64(m) ? sizeof(Slot4<double>) : sizeof(Slot4<float>);
       const long long s0 = m->ps.patch_node_off[g.patch_begin];
       const long long s1 = m->ps.patch_node_off[g.patch_begin + g.npatch];
-      for (int d = 0; d < 3; ++d)
-        CK(cudaMemsetAsync((char *)m->sF.p + (d * m->S + s0) * rb, 0, (s1 - s0) * rb,
-                           m->stream));
+      CK(cudaMemsetAsync((char *)m->sF.p + s0 * rb, 0, (s1 - s0) * rb, m->stream));
     }
   }
   return m->epid.upload(w.data(), w.size());
@@ -750,10 +748,10 @@ int setup_t(ftgpu_model *m) {
     }
     CKI(m->sX.upload(sx.data(), sx.size()));
   }
-  CKI(m->sU.alloc(3 * S * sizeof(R)));
-  CK(cudaMemset(m->sU.p, 0, 3 * S * sizeof(R)));
-  CKI(m->sF.alloc(3 * S * sizeof(R)));
-  CK(cudaMemset(m->sF.p, 0, 3 * S * sizeof(R)));
+  CKI(m->sU.alloc(S * sizeof(Slot4<R>)));
+  CK(cudaMemset(m->sU.p, 0, S * sizeof(Slot4<R>)));
+  CKI(m->sF.alloc(S * sizeof(Slot4<R>)));
+  CK(cudaMemset(m->sF.p, 0, S * sizeof(Slot4<R>)));
   // fibres (material 7), group order, SoA
   bool any7 = false;
   for (auto &g : ps.groups) any7 |= g.mat == 7;

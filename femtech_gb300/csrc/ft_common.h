@@ -47,6 +47,15 @@ constexpr unsigned long long kDtHugeBits = 0x4415af1d78b58c40ull;
 constexpr int kMaxRotFns = 8;
 
 enum { kBcFree = -1, kBcHold = -2 };
+
+// One patch slot of the partial-force and displacement-replica arrays: x, y,
+// z and a pad, so that the node kernels' gathers and scatters (slots of a
+// node are spread over patches) move one 16-byte (FP32) or 32-byte (FP64)
+// record per slot instead of three scattered words.
+template <class R>
+struct alignas(4 * sizeof(R)) Slot4 {
+  R x, y, z, w;
+};
 enum { kBckFixed = 0, kBckRamp = 1, kBckSine = 2, kBckRot = 3, kBckRigid = 4 };
 enum { kErrInverted = 1, kErrDt = 2, kErrIndex = 4, kErrWait = 8 };
 
@@ -65,8 +74,8 @@ struct ElemArgs {
   const Real *fib;            // [3][E] unit fibre (material 7) or null
   // slots
   const Real *sX;             // [3][S] reference coordinates (patch-relative in mixed mode)
-  const Real *sU;             // [3][S] displacement replicas
-  Real *sF;                   // [3][S] patch-partial internal forces
+  const Real *sU;             // [S] Slot4: displacement replicas
+  Real *sF;                   // [S] Slot4: patch-partial internal forces
   // material state
   Real *hist;                 // [ncomp][NGP][nelem] of this group
   const MatP<Real> *mats;
@@ -161,8 +170,8 @@ struct NodeArgs {
   double *u, *v, *a, *vh;     // [3][N]
   const double *mass;         // [N] lumped mass (FP64)
   const double *minv;         // [N] 1 / mass
-  const void *sF;             // [3][S] partial forces (Real)
-  void *sU;                   // [3][S] displacement replicas (Real)
+  const void *sF;             // [S] Slot4<Real> partial forces
+  void *sU;                   // [S] Slot4<Real> displacement replicas
   Clock *clock;
   unsigned long long *dtmin;
   const InstParams *inst;

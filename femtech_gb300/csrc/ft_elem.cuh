@@ -627,11 +627,12 @@ __global__ void __launch_bounds__(kElemThreads, ET == 0 ? 2 : 3)
   }
   const Clock *ck = A.clock + A.parity * A.ninst + inst;
   for (int i = t; i < ns; i += PE) {
+    const Slot4<R> us = reinterpret_cast<const Slot4<R> *>(A.sU)[s0 + i];
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      shX[d * kMaxLocalNodes + i] = A.sX[d * A.S + s0 + i];
-      shU[d * kMaxLocalNodes + i] = A.sU[d * A.S + s0 + i];
-    }
+    for (int d = 0; d < 3; ++d) shX[d * kMaxLocalNodes + i] = A.sX[d * A.S + s0 + i];
+    shU[i] = us.x;
+    shU[kMaxLocalNodes + i] = us.y;
+    shU[2 * kMaxLocalNodes + i] = us.z;
   }
   // an instance past its end time: the whole block leaves (uniform per patch)
   if (A.use_clock && ck->done) return;
@@ -719,9 +720,7 @@ __global__ void __launch_bounds__(kElemThreads, ET == 0 ? 2 : 3)
       f1 += shF[(a * 3 + 1) * PE + el];
       f2 += shF[(a * 3 + 2) * PE + el];
     }
-    A.sF[s0 + i] = f0;
-    A.sF[A.S + s0 + i] = f1;
-    A.sF[2 * A.S + s0 + i] = f2;
+    reinterpret_cast<Slot4<R> *>(A.sF)[s0 + i] = Slot4<R>{f0, f1, f2, R(0)};
   }
 }
 
@@ -808,11 +807,12 @@ __global__ void __launch_bounds__(kElemThreads) k_elem_strain(const ElemArgs<R> 
   const int e0 = A.patch_elem_off[p], ne = A.patch_elem_off[p + 1] - e0;
   const int s0 = A.patch_node_off[p], ns = A.patch_node_off[p + 1] - s0;
   for (int i = t; i < ns; i += PE) {
+    const Slot4<R> us = reinterpret_cast<const Slot4<R> *>(A.sU)[s0 + i];
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      shX[d * kMaxLocalNodes + i] = A.sX[d * A.S + s0 + i];
-      shU[d * kMaxLocalNodes + i] = A.sU[d * A.S + s0 + i];
-    }
+    for (int d = 0; d < 3; ++d) shX[d * kMaxLocalNodes + i] = A.sX[d * A.S + s0 + i];
+    shU[i] = us.x;
+    shU[kMaxLocalNodes + i] = us.y;
+    shU[2 * kMaxLocalNodes + i] = us.z;
   }
   __syncthreads();
   if (t >= ne) return;

@@ -339,26 +339,27 @@ __global__ void __launch_bounds__(512) k_node(const NodeArgs A) {
   const int inst = A.node_inst ? A.node_inst[n] : 0;
   const InstParams &ip = A.inst[inst];
   const bool leader = (n == ip.node_begin);
-  const R *sF = reinterpret_cast<const R *>(A.sF);
-  R *sU = reinterpret_cast<R *>(A.sU);
+  const Slot4<R> *sF = reinterpret_cast<const Slot4<R> *>(A.sF);
+  Slot4<R> *sU = reinterpret_cast<Slot4<R> *>(A.sU);
   const int sb = A.slot_off[n], se = A.slot_off[n + 1];
-  const long long N = A.N, S = A.S;
+  const long long N = A.N;
 
   if (A.mode == kNodeScatterU) {  // replicate u into the patch slots
-    for (int k = sb; k < se; ++k) {
-      const int s = A.slots[k];
-#pragma unroll
-      for (int d = 0; d < 3; ++d) sU[d * S + s] = R(A.u[d * N + n]);
-    }
+    const Slot4<R> r{R(A.u[n]), R(A.u[N + n]), R(A.u[2 * N + n]), R(0)};
+    for (int k = sb; k < se; ++k) sU[A.slots[k]] = r;
     return;
   }
   if (A.mode == kNodeGather) {  // assembled internal force fi = sum of partials
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      double f = 0.0;
-      for (int k = sb; k < se; ++k) f += double(sF[d * S + A.slots[k]]);
-      A.fi_out[d * N + n] = f;
+    double f0 = 0.0, f1 = 0.0, f2 = 0.0;
+    for (int k = sb; k < se; ++k) {
+      const Slot4<R> q = sF[A.slots[k]];
+      f0 += double(q.x);
+      f1 += double(q.y);
+      f2 += double(q.z);
     }
+    A.fi_out[n] = f0;
+    A.fi_out[N + n] = f1;
+    A.fi_out[2 * N + n] = f2;
     return;
   }
 
@@ -408,25 +409,30 @@ __global__ void __launch_bounds__(512) k_node(const NodeArgs A) {
       if (A.du) reinterpret_cast<R *>(A.du)[d * N + n] = R(u - uold);  // energy: this step's du
       un[d] = u;
     }
-    for (int k = sb; k < se; ++k) {
-      const int s = A.slots[k];
-#pragma unroll
-      for (int d = 0; d < 3; ++d) sU[d * S + s] = R(un[d]);
-    }
+    const Slot4<R> r{R(un[0]), R(un[1]), R(un[2]), R(0)};
+    for (int k = sb; k < se; ++k) sU[A.slots[k]] = r;
     return;
   }
   if (A.mode == kNodeInit) {
-    // accelerations after the pre-loop GetForce (ex9.cpp:90-93)
+    // accelerations after the pre-loop GetForce (ex9.cpp:90-93): the partials
+    // summed in slot order, in R (the energy balance's f_prev, as
+    // k_node_step sums them) and in FP64
+    R fr[3] = {0, 0, 0};
+    double fd[3] = {0.0, 0.0, 0.0};
+    for (int k = sb; k < se; ++k) {
+      const Slot4<R> q = sF[A.slots[k]];
+      fr[0] += q.x;
+      fr[1] += q.y;
+      fr[2] += q.z;
+      fd[0] += double(q.x);
+      fd[1] += double(q.y);
+      fd[2] += double(q.z);
+    }
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      if (A.fprev) {  // energy balance: f of the pre-loop state, summed as k_node_step does
-        R fr = 0;
-        for (int k = sb; k < se; ++k) fr += sF[d * S + A.slots[k]];
-        reinterpret_cast<R *>(A.fprev)[d * N + n] = fr;
-      }
+      if (A.fprev) reinterpret_cast<R *>(A.fprev)[d * N + n] = fr[d];
       if (A.nbc[d * N + n] != kBcFree) continue;
-      double f = 0.0;
-      for (int k = sb; k < se; ++k) f += double(sF[d * S + A.slots[k]]);
+      const double f = fd[d];
       A.a[d * N + n] = A.fp64 ? -f / A.mass[n] : -f * A.minv[n];
     }
     if (leader) A.dtmin[A.parity * A.ninst + inst] = kDtHugeBits;
@@ -579,9 +585,9 @@ __device__ __noinline__ void node_step_bc(const NodeArgs &A, long long n, int in
 template <class R, bool EN, bool BCI = false>
 __device__ __forceinline__ void node_step(const NodeArgs &A, long long n, R &eke, R &ewi,
                                           R &ewe) {
-  const long long N = A.N, S = A.S;
-  const R *sF = reinterpret_cast<const R *>(A.sF);
-  R *sU = reinterpret_cast<R *>(A.sU);
+  const long long N = A.N;
+  const Slot4<R> *sF = reinterpret_cast<const Slot4<R> *>(A.sF);
+  Slot4<R> *sU = reinterpret_cast<Slot4<R> *>(A.sU);
   const int inst = A.node_inst ? A.node_inst[n] : 0;
   const int sb = A.slot_off[n], se = A.slot_off[n + 1];
   int nbc[3];
@@ -618,10 +624,10 @@ __device__ __forceinline__ void node_step(const NodeArgs &A, long long n, R &eke
   // sum of the patch partials in slot order (in the element precision)
   R fs0 = 0, fs1 = 0, fs2 = 0;
   for (int k = sb; k < se; ++k) {
-    const int s = A.slots[k];
-    fs0 += sF[s];
-    fs1 += sF[S + s];
-    fs2 += sF[2 * S + s];
+    const Slot4<R> q = sF[A.slots[k]];
+    fs0 += q.x;
+    fs1 += q.y;
+    fs2 += q.z;
   }
   const InstParams &ip = A.inst[inst];
   const bool leader = (n == ip.node_begin);
@@ -689,13 +695,8 @@ __device__ __forceinline__ void node_step(const NodeArgs &A, long long n, R &eke
     for (int d = 0; d < 3; ++d) du[d * N + n] = R(un[d] - u0[d]);
   }
   if (advance) {
-    const R r0 = R(un[0]), r1 = R(un[1]), r2 = R(un[2]);
-    for (int k = sb; k < se; ++k) {
-      const int s = A.slots[k];
-      sU[s] = r0;
-      sU[S + s] = r1;
-      sU[2 * S + s] = r2;
-    }
+    const Slot4<R> r{R(un[0]), R(un[1]), R(un[2]), R(0)};
+    for (int k = sb; k < se; ++k) sU[A.slots[k]] = r;
   }
   if (leader) {
     Clock c;
