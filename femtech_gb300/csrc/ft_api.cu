@@ -689,8 +689,30 @@ int upload_materials(ftgpu_model *m) {
         q.ser_a[k] = R(ba);
         q.ser_b[k] = R(bb);
       }
-      // FP32 path: series while |2E|_F < 0.04; FP64 mode keeps the eigen path
-      q.ser_thr2 = sizeof(R) == 4 ? R(0.04 * 0.04) : R(0);
+      // FP32 path: the series while |2E|_F < r, r the largest radius (at most
+      // 0.3) whose truncation bound sum_{k > n} (|b_a,k| + 2 |b_b,k|) r^k
+      // stays below 1e-7 r (FP32 rounding of the leading term); FP64 mode
+      // keeps the eigen path
+      auto tail = [&](double r) {
+        double ca = ba, cb = bb, rk = std::pow(r, kOgdenSeries), t = 0.0;
+        for (int k = kOgdenSeries; k < kOgdenSeries + 400; ++k) {
+          ca *= (a / 2.0 - 1.0 - k) / (k + 1.0);
+          cb *= (a / 2.0 - k) / (k + 1.0);
+          rk *= r;
+          t += (std::fabs(ca) + 2.0 * std::fabs(cb)) * rk;
+        }
+        return t;
+      };
+      double lo = 0.0, hi = 0.3;
+      if (tail(hi) <= 1e-7 * hi) {
+        lo = hi;
+      } else {
+        for (int it = 0; it < 60; ++it) {
+          const double mid = 0.5 * (lo + hi);
+          (tail(mid) <= 1e-7 * mid ? lo : hi) = mid;
+        }
+      }
+      q.ser_thr2 = sizeof(R) == 4 ? R(lo * lo) : R(0);
     }
     t[p] = q;
   }

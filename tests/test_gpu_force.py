@@ -111,3 +111,21 @@ def test_rigid_motion_gives_no_force():
         scale = MATS[mid][1] * 0.004 ** 2
         assert np.abs(fi).max() < 1e-9 * scale
         m.close()
+
+
+@pytest.mark.parametrize("alpha", [5.0, -5.0, 0.2])
+@pytest.mark.parametrize("g", [0.02, 0.06, 0.12, 0.2])
+def test_mixed_ogden_finite_strain_vs_oracle(oracle_lib, alpha, g):
+    """FP32 Ogden (series below its alpha-dependent bound, eigen-decomposition
+    above it) against the FP64 oracle on a finitely strained jittered block:
+    an affine stretch / shear of size g plus noise."""
+    mesh = mg.hex_block(6, 5, 4, 0.006, 0.005, 0.004, jitter=0.1, seed=7)
+    mats = mg.materials([(6, [1040.0, 1.5e3, 2.0e7, alpha])])
+    X = mesh["coordinates"]
+    rng = np.random.default_rng(int(100 * g) + int(abs(alpha) * 10))
+    G = g * rng.normal(size=(3, 3)) / 2
+    u = (X @ G.T + rng.normal(0, 1e-3 * g * 1e-3, X.shape)).ravel()
+    o = oracle_lib.Oracle(mesh, mats)
+    m = ft.Model(mesh, mats, precision=ft.MIXED)
+    assert rel(m.GetForce(u), o.get_force(u, 0.0)) < MIXED_TOL
+    m.close()
