@@ -58,12 +58,12 @@ NODE_BYTES_PER_NODE = 116.0
 # (small-strain series path), counted from the kernel source (ft_elem.cuh /
 # ft_materials.cuh), FMA = 2: per Gauss point Jacobian and displacement-
 # gradient columns 108, adj/det 32, D = H adj^T / det 63, J - 1 27, Ogden
-# series law 285 (2E 40, norm 11, M^2 30, invariants 21, five Cayley-Hamilton
-# steps of the I / M / M^2 coefficients 105, coefficients of S 15,
-# J^-alpha/3 5, S 21, volumetric 37), P = S + D S 54, P adj 45, moments 63
-# -> 677 per Gauss point, 5416 for 8; Hadamard transforms 150, face areas
-# 540, inverse transform 90.
-FLOP_PER_EL_OGDEN = 5416 + 150 + 540 + 90
+# series law 313 (2E 40, norm 11, M^2 30, invariants 21, seven Cayley-Hamilton
+# steps of the I / M / M^2 coefficients of the A and tr B series 126, exact
+# (I + M)^-1 7, coefficients of S 15, J^-alpha/3 5, S 21, volumetric 37),
+# P = S + D S 54, P adj 45, moments 63 -> 705 per Gauss point, 5640 for 8;
+# Hadamard transforms 150, face areas 540, inverse transform 90.
+FLOP_PER_EL_OGDEN = 5640 + 150 + 540 + 90
 
 
 def log(*a):
