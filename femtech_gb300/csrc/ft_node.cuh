@@ -711,9 +711,12 @@ __device__ __forceinline__ void node_step(const NodeArgs &A, long long n, R &eke
 }
 
 // LIST: over A.node_list (the driven nodes of the rigid-body branch, whose
-// boundary path is inlined), else over every node.
+// boundary path is inlined), else over every node.  At most 64 registers
+// (two 512-thread blocks per SM) also with the energy terms: their spills
+// cost less than half the resident warps (block node pass with the energy
+// balance 0.51 ms at 128 registers, 0.445 ms at 64).
 template <class R, bool EN, bool LIST = false>
-__global__ void __launch_bounds__(512, EN || LIST ? 1 : 2) k_node_step(const NodeArgs A) {
+__global__ void __launch_bounds__(512, LIST ? 1 : 2) k_node_step(const NodeArgs A) {
   long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   bool on = n < A.N;
   if (LIST) {
