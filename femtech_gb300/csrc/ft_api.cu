@@ -344,7 +344,7 @@ NodeArgs node_args(ftgpu_model *m, int mode, int parity) {
   A.a = m->a.as<double>();
   A.vh = m->vh.as<double>();
   A.mass = m->mass.as<double>();
-  A.minv = m->minv.as<double>();
+  A.minv = m->minv.as<float>();
   A.sF = m->sF.p;
   A.sU = m->sU.p;
   A.clock = m->clock.as<Clock>();
@@ -882,8 +882,8 @@ int setup_t(ftgpu_model *m) {
     CK(cudaMemcpyAsync(m->mass_host.data(), m->mass.p, N * sizeof(double), cudaMemcpyDeviceToHost,
                        m->stream));
     CK(cudaStreamSynchronize(m->stream));
-    std::vector<double> mi(N);
-    for (long long n = 0; n < N; ++n) mi[n] = 1.0 / m->mass_host[n];
+    std::vector<float> mi(N);
+    for (long long n = 0; n < N; ++n) mi[n] = (float)(1.0 / m->mass_host[n]);
     CKI(m->minv.upload(mi.data(), N));
   }
   if (m->h_clock) cudaFreeHost(m->h_clock);

@@ -169,7 +169,7 @@ struct NodeArgs {
   const double *X;            // [3][N] FP64 reference coordinates
   double *u, *v, *a, *vh;     // [3][N]
   const double *mass;         // [N] lumped mass (FP64)
-  const double *minv;         // [N] 1 / mass
+  const float *minv;          // [N] 1 / mass (mixed mode)
   const void *sF;             // [S] Slot4<Real> partial forces
   void *sU;                   // [S] Slot4<Real> displacement replicas
   Clock *clock;

@@ -604,8 +604,8 @@ __device__ __forceinline__ void node_step(const NodeArgs &A, long long n, R &eke
     for (int d = 0; d < 3; ++d)
       if (nbc[d] >= 0 && A.fns[nbc[d]].kind == kBckRigid) return;
   }
-  // 1/m (mixed mode; FP64 mode divides by m as the reference does)
-  const double minv = sizeof(R) == 8 ? 0.0 : A.minv[n];
+  // 1/m (mixed mode, FP32; FP64 mode divides by m as the reference does)
+  const float minv = sizeof(R) == 8 ? 0.f : A.minv[n];
   // energy inputs of all three DOFs, issued with the other loads and before
   // any store of this node (the stores could alias them and serialise loads)
   R *du = reinterpret_cast<R *>(A.du), *fp = reinterpret_cast<R *>(A.fprev);
@@ -646,18 +646,24 @@ __device__ __forceinline__ void node_step(const NodeArgs &A, long long n, R &eke
   const bool advance = sc.advance;
   constexpr bool kF64 = sizeof(R) == 8;
   const double fsum[3] = {double(fs0), double(fs1), double(fs2)};
+  const R fsr[3] = {fs0, fs1, fs2};
+  // mixed mode: a = f / m and the velocity increments c a in FP32 (f is an
+  // FP32 sum), accumulated into the FP64 state -- one FP64 add per DOF
+  // instead of a multiply and a fused multiply-add: FP64 issue is slow on
+  // this GPU
+  const float c1f = float(sc.c1), c12f = float(sc.c12);
   double un[3] = {u0[0], u0[1], u0[2]};
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const int fn = nbc[d];
     if (EN) {
-      const R fi = R(fsum[d]);  // exact: a sum in the element precision
+      const R fi = fsr[d];  // a sum in the element precision
       if (fn == kBcFree) {
         R v1;
         if (kF64) {
           v1 = R(vh0[d] + sc.c1 * (-fsum[d] / A.mass[n]));
         } else {
-          v1 = R(vh0[d]) + R(sc.c1) * (-fi * R(minv));
+          v1 = R(vh0[d]) + R(c1f) * (-fi * R(minv));
         }
         eke += R(mass) * v1 * v1;
       }
@@ -665,22 +671,30 @@ __device__ __forceinline__ void node_step(const NodeArgs &A, long long n, R &eke
       fp[d * N + n] = fi;
     }
     if (fn == kBcFree) {
-      const double acc = kF64 ? -fsum[d] / A.mass[n] : -fsum[d] * minv;
       const double vh = vh0[d];
-      if (advance) {
-        double vh2;
-        if (kF64) {  // the two half-step updates of ex9.cpp:147-152 and :116-123
+      if (kF64) {
+        const double acc = -fsum[d] / A.mass[n];
+        if (advance) {  // the two half-step updates of ex9.cpp:147-152 and :116-123
           const double vel = vh + sc.c1 * acc;
-          vh2 = vel + sc.c2 * acc;
-        } else {  // one update with the combined coefficient t_half' - t_half
-          vh2 = vh + sc.c12 * acc;
+          const double vh2 = vel + sc.c2 * acc;
+          un[d] = u0[d] + sc.ndt * vh2;
+          A.vh[d * N + n] = vh2;
+          A.u[d * N + n] = un[d];
+        } else {
+          A.v[d * N + n] = vh + sc.c1 * acc;
+          A.a[d * N + n] = acc;
         }
-        un[d] = u0[d] + sc.ndt * vh2;
-        A.vh[d * N + n] = vh2;
-        A.u[d * N + n] = un[d];
       } else {
-        A.v[d * N + n] = vh + sc.c1 * acc;
-        A.a[d * N + n] = acc;
+        const float acc = -float(fsr[d]) * minv;
+        if (advance) {  // one update with the combined coefficient t_half' - t_half
+          const double vh2 = vh + double(c12f * acc);
+          un[d] = u0[d] + sc.ndt * vh2;
+          A.vh[d * N + n] = vh2;
+          A.u[d * N + n] = un[d];
+        } else {
+          A.v[d * N + n] = vh + double(c1f * acc);
+          A.a[d * N + n] = double(acc);
+        }
       }
     }
   }
