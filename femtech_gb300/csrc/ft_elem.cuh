@@ -572,11 +572,13 @@ template <class R, int ET, int MAT, bool GP, bool INJ>
 // C3D8: at most 128 registers per thread (two 256-thread or four 128-thread
 // blocks per SM); only the rarely taken eigen-decomposition fallback of the
 // Ogden law needs more and spills there.  C3D4 (one Gauss point, latency
-// bound): at most 85, for three 256-thread or six 128-thread blocks per SM.
+// bound): at most 64, for four 256-thread or eight 128-thread blocks per SM
+// (head-like mesh: element pass 0.129 ms at 80 registers, 0.118 ms at 64,
+// 0.127 ms at 48; the GOH + Prony law spills some of its state at 64).
 // INJ: the force pass also updates the brain drivers' per-step injury
 // criteria of its listed elements (CalculateInjuryCriterions, ex5.cpp:
 // 1311-1430, on the F of this pass) and writes the block's extremes.
-__global__ void __launch_bounds__(kElemThreads, ET == 0 ? 2 : 3)
+__global__ void __launch_bounds__(kElemThreads, ET == 0 ? 2 : 4)
     k_elem(const ElemArgs<R> A, int pass) {
   constexpr int NC = ET == 0 ? 8 : 4;
   constexpr int NGP = ET == 0 ? 8 : 1;
