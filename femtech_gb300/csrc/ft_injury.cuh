@@ -212,41 +212,60 @@ __global__ void __launch_bounds__(256) k_injury_reduce(const InjuryArgs<R> A) {
 
 // Radix selection of the value of rank k = (int)(0.95 n) - 1 (rank 0 if
 // negative) of sel = 0: ps_old, 1: psxsr, 8 bits per pass from the most
-// significant byte.  Every pass first recovers the digits fixed so far by
-// scanning the histograms of the previous passes (the same in every block).
-template <class K>
-__device__ __forceinline__ void radix_prefix(const unsigned *hist, int pass, int n, K &prefix,
-                                             unsigned &krem) {
-  int k = (int)(n * 0.95) - 1;
-  if (k < 0) k = 0;
-  krem = (unsigned)k;
-  prefix = 0;
-  constexpr int KB = sizeof(K) * 8;
-  for (int q = 0; q < pass; ++q) {
-    const unsigned *h = hist + q * kRadixBins;
-    unsigned below = 0;
-    int d = 0;
-    for (; d < kRadixBins; ++d) {
-      if (below + h[d] > krem) break;
-      below += h[d];
-    }
-    krem -= below;
-    prefix |= (K)d << (KB - 8 * (q + 1));
-  }
-}
-
-// The digits fixed by the first `pass` histograms of a selection, computed by
-// one block: the histograms are staged in shared memory by all its threads,
-// then scanned by thread 0 (the result is in *prefix after the barrier).
+// significant byte.  Every pass first recovers the digits fixed so far from
+// the histograms of the previous passes (the same in every block).
+// The digits fixed by the first `pass` histograms of a selection, recovered
+// by every block (blockDim.x == kRadixBins: thread t owns bin t): per pass a
+// block-wide scan of the 256 counts finds the bin holding the remaining rank
+// (the first bin whose cumulative count exceeds it).  The result is in
+// *prefix after the final barrier; `stage` is unused scratch kept for the
+// callers' layout.
 template <class K>
 __device__ __forceinline__ void block_radix_prefix(const unsigned *hist, int pass, int n,
                                                    unsigned *stage, K *prefix) {
-  for (int i = threadIdx.x; i < pass * kRadixBins; i += blockDim.x) stage[i] = hist[i];
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned krem;
-    radix_prefix<K>(stage, pass, n, *prefix, krem);
+  (void)stage;
+  constexpr int KB = sizeof(K) * 8;
+  __shared__ unsigned wsum[kRadixBins / 32];
+  __shared__ unsigned s_krem, s_below;
+  __shared__ int s_d;
+  __shared__ K s_pref;
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  if (t == 0) {
+    int k = (int)(n * 0.95) - 1;
+    if (k < 0) k = 0;
+    s_krem = (unsigned)k;
+    s_pref = 0;
   }
+  for (int q = 0; q < pass; ++q) {
+    const unsigned c = hist[q * kRadixBins + t];
+    unsigned x = c;  // inclusive scan within the warp
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[w] = x;
+    if (t == 0) {
+      s_d = 0;
+      s_below = 0;
+    }
+    __syncthreads();
+    unsigned off = 0;
+#pragma unroll
+    for (int v = 0; v < kRadixBins / 32; ++v) off += v < w ? wsum[v] : 0u;
+    const unsigned incl = x + off, excl = incl - c, krem = s_krem;
+    if (excl <= krem && krem < incl) {
+      s_d = t;
+      s_below = excl;
+    }
+    __syncthreads();
+    if (t == 0) {
+      s_krem = krem - s_below;
+      s_pref |= (K)s_d << (KB - 8 * (q + 1));
+    }
+    __syncthreads();
+  }
+  if (t == 0) *prefix = s_pref;
   __syncthreads();
 }
 
