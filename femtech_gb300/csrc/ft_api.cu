@@ -235,10 +235,10 @@ struct ftgpu_model {
   std::vector<RigidHost> rigid;
   bool rigid_on = false;
   DBuf rb, rbtab, rbstate, rbstep;
-  DBuf rig_list;                // nodes with a rigid-body DOF
+  DBuf rig_list;                // driven nodes: a rigid-body or rigid-rotation DOF
   std::vector<int> rig_host;
   long long rig_nodes = 0;
-  cudaStream_t stream2 = nullptr;  // the rigid-body branch of a step
+  cudaStream_t stream2 = nullptr;  // the driven-node branch of a step
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   DBuf slot_off, slots, node_inst, nbc, fnsbuf;
   DBuf dX, u, v, a, vh, mass, minv, fi;
@@ -401,28 +401,36 @@ int launch_node(ftgpu_model *m, int mode, int parity) {
       en ? node_step_launch<float, true>(blocks, th, st, B)
          : node_step_launch<float, false>(blocks, th, st, B);
   };
-  if (step)
-    k_step_scalars<<<(unsigned)((m->ninst + 127) / 128), 128, 0, m->stream>>>(A);
-  if (step && m->rigid_on && m->rig_nodes > 0) {
-    // fork: the rigid bodies' integrator and then their driven nodes on the
-    // second stream, every other node on the first; join before what follows
+  const bool fork = step && m->rig_nodes > 0 && m->stream2;
+  if (step) {  // (with the fork, the rotation trigonometry moves to k_driven_step)
+    NodeArgs S = A;
+    if (fork) S.nrot = 0;
+    k_step_scalars<<<(unsigned)((m->ninst + 127) / 128), 128, 0, m->stream>>>(S);
+  }
+  if (fork) {
+    // fork: the driven nodes' motion (rigid bodies' integrator, rotation
+    // trigonometry) and then those nodes on the second stream, every other
+    // node on the first; join before what follows
     const long long nbr = (m->rig_nodes + th - 1) / th;
     NodeArgs B = A;
     B.node_list = m->rig_list.as<int>();
     B.nlist = m->rig_nodes;
     B.epart_off = nb;
-    A.skip_rigid = 1;
+    A.skip_driven = 1;
     CK(cudaEventRecord(m->ev_fork, m->stream));
     CK(cudaStreamWaitEvent(m->stream2, m->ev_fork, 0));
-    k_rigid_step<<<(unsigned)m->ninst, 32, 0, m->stream2>>>(B);
+    k_driven_step<<<(unsigned)m->ninst, 32, 0, m->stream2>>>(B);
     node_step(nbr, m->stream2, B);
     node_step(nb, m->stream, A);
     CK(cudaEventRecord(m->ev_join, m->stream2));
     CK(cudaStreamWaitEvent(m->stream, m->ev_join, 0));
     nb += nbr;
   } else if (step) {
-    if (m->rigid_on)  // records without driven nodes: the state still advances
-      k_rigid_step<<<(unsigned)m->ninst, 32, 0, m->stream>>>(A);
+    if (m->rigid_on) {  // records without driven nodes: the state still advances
+      NodeArgs S = A;
+      S.nrot = 0;
+      k_driven_step<<<(unsigned)m->ninst, 32, 0, m->stream>>>(S);
+    }
     node_step(nb, m->stream, A);
   } else {
     if (mode == kNodeBegin && m->rigid_on)
@@ -1338,16 +1346,18 @@ int ftgpu_set_state(ftgpu_model *m, const double *u, const double *v, const doub
   return FTGPU_OK;
 }
 
-// Rigid bodies at the start of the loop: every rigid-body DOF must belong
+// Driven nodes and rigid bodies at the start of the loop: the list of
+// nodes with rigid-body or rigid-rotation DOFs; every rigid-body DOF must belong
 // to an instance with acceleration records; state zero (ex5.cpp:886-890),
 // table cursors at 0 and the node maps of the zero state (u = v = a = 0).
 int reset_rigid(ftgpu_model *m) {
-  std::vector<int> rig;
+  std::vector<int> rig;  // driven nodes (rigid-body or rigid-rotation DOFs)
   for (size_t i = 0; i < m->dof_fn.size(); ++i) {
     const int f = m->dof_fn[i];
-    if (f < 0 || m->fns[f].kind != kBckRigid) continue;
+    if (f < 0 || (m->fns[f].kind != kBckRigid && m->fns[f].kind != kBckRot)) continue;
     const int node = (int)(i / 3);
     if (rig.empty() || rig.back() != node) rig.push_back(node);
+    if (m->fns[f].kind != kBckRigid) continue;
     int inst = 0;
     if (m->inst_set)
       inst = (int)(std::upper_bound(m->node_off.begin(), m->node_off.end(), node) -
@@ -1355,18 +1365,18 @@ int reset_rigid(ftgpu_model *m) {
     if (!m->rigid_on || inst >= (int)m->rigid.size() || !m->rigid[inst].on)
       return fail(FTGPU_ERR_INPUT, "rigid-body DOF in an instance without acceleration records");
   }
-  if (!m->rigid_on) return 0;
   if (rig != m->rig_host) {  // a new driven-node list: the captured branch changes
     drop_graphs(m);
     m->rig_host = rig;
     m->rig_nodes = (long long)rig.size();
     if (!rig.empty()) CKI(m->rig_list.upload(rig.data(), rig.size()));
   }
-  if (!m->stream2) {
+  if (!rig.empty() && !m->stream2) {
     CK(cudaStreamCreateWithFlags(&m->stream2, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&m->ev_fork, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&m->ev_join, cudaEventDisableTiming));
   }
+  if (!m->rigid_on) return 0;
   std::vector<RigidState> st(m->ninst);
   std::vector<RigidStep> sp(m->ninst);
   for (int i = 0; i < m->ninst; ++i) {

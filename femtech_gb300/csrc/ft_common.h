@@ -196,11 +196,11 @@ struct NodeArgs {
   RigidState *rbstate;        // [ninst]
   RigidStep *rbstep;          // [ninst]
   // k_node_step over a subset: node_list (nlist entries) or every node but
-  // those with a rigid-body DOF (skip_rigid); its energy partials start at
-  // block epart_off
+  // the driven ones -- a rigid-body or rigid-rotation DOF (skip_driven); its
+  // energy partials start at block epart_off
   const int *node_list;
   long long nlist;
-  int skip_rigid;
+  int skip_driven;
   long long epart_off;
 };
 

@@ -460,18 +460,26 @@ __global__ void k_step_scalars(const NodeArgs A) {
     }
 }
 
-// The rigid bodies' step to t_{n+2} for the next step (ex5.cpp:344 with
-// Time = t_{n+2}, dt = the new dt), one warp per instance, after
-// k_step_scalars.  It runs on a second stream beside k_node_step over the
-// nodes without rigid-body DOFs: the integrator is a latency-bound FP64
-// chain, the free-node update is bandwidth-bound, and only the driven nodes
-// (k_node_step over their list, after this kernel) need its result.
-__global__ void __launch_bounds__(32) k_rigid_step(const NodeArgs A) {
+// The driven nodes' motion at t_{n+2} for the next step, after
+// k_step_scalars, one warp per instance: the rigid body's integrator step
+// (ex5.cpp:344 with Time = t_{n+2}, dt = the new dt) and the trigonometry of
+// the rigid-rotation functions (lane k: function k).  It runs on a second
+// stream beside k_node_step over the nodes without such DOFs: the integrator
+// and sin/cos are latency-bound FP64 chains, the free-node update is
+// bandwidth-bound, and only the driven nodes (k_node_step over their list,
+// after this kernel) need the result.
+__global__ void __launch_bounds__(32) k_driven_step(const NodeArgs A) {
   __shared__ double sacc[5][6];
   const int i = blockIdx.x;
   const Clock ck = A.clock[A.parity * A.ninst + i];
   const StepScalars sc = A.stepsc[i];
-  if (sc.advance && !ck.done) rigid_advance(A, i, sc.t_np2 - sc.ndt, sc.ndt, sacc);
+  if (!sc.advance || ck.done) return;
+  const int k = threadIdx.x;
+  if (k < A.nrot) {
+    double *r = A.rottrig + 3 * ((long long)i * kMaxRotFns + k);
+    rot_trig(A.fns[A.rot_ids[k]], sc.t_np2, r[0], r[1], r[2]);
+  }
+  if (A.rb) rigid_advance(A, i, sc.t_np2 - sc.ndt, sc.ndt, sacc);
 }
 
 // Before a kNodeBegin launch: advance each running instance's rigid body to
@@ -514,7 +522,7 @@ __device__ __forceinline__ void node_step_bc_body(const NodeArgs &A, long long n
     if (kind == kBckRot && rot_fn < 0) rot_fn = fn;
   }
   double aold[3] = {0.0, 0.0, 0.0};
-  if (advance && rig) {  // rigid body at t_{n+2} (k_step_scalars_rigid advanced it)
+  if (advance && rig) {  // rigid body at t_{n+2} (k_driven_step advanced it)
     for (int d = 0; d < 3; ++d)
       if (rigd[d]) aold[d] = A.a[d * N + n];
     rigid_node(A.rbstep + inst, A.X, N, n, ur, vr, ar);
@@ -599,10 +607,11 @@ __device__ __forceinline__ void node_step(const NodeArgs &A, long long n, R &eke
     vh0[d] = A.vh[d * N + n];
   }
   const bool anybc = nbc[0] != kBcFree || nbc[1] != kBcFree || nbc[2] != kBcFree;
-  if (anybc && A.skip_rigid) {  // handled by the rigid-body branch of the step
+  if (anybc && A.skip_driven) {  // handled by the driven-node branch of the step
 #pragma unroll
     for (int d = 0; d < 3; ++d)
-      if (nbc[d] >= 0 && A.fns[nbc[d]].kind == kBckRigid) return;
+      if (nbc[d] >= 0 && (A.fns[nbc[d]].kind == kBckRigid || A.fns[nbc[d]].kind == kBckRot))
+        return;
   }
   // 1/m (mixed mode, FP32; FP64 mode divides by m as the reference does)
   const float minv = sizeof(R) == 8 ? 0.f : A.minv[n];
