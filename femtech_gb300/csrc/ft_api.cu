@@ -1351,6 +1351,9 @@ int ftgpu_set_state(ftgpu_model *m, const double *u, const double *v, const doub
 // to an instance with acceleration records; state zero (ex5.cpp:886-890),
 // table cursors at 0 and the node maps of the zero state (u = v = a = 0).
 int reset_rigid(ftgpu_model *m) {
+  if (m->rigid_on && (int)m->rigid.size() != m->ninst)
+    return fail(FTGPU_ERR_STATE, "the instance layout changed after set_rigid_body: set the "
+                                 "acceleration records again");
   std::vector<int> rig;  // driven nodes (rigid-body or rigid-rotation DOFs)
   for (size_t i = 0; i < m->dof_fn.size(); ++i) {
     const int f = m->dof_fn[i];

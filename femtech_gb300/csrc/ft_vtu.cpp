@@ -35,7 +35,7 @@ std::string format_rows(long long n, F fmt_row) {
       char line[1024];
       for (long long i = b; i < e; ++i) {
         const int k = fmt_row(i, line, sizeof(line));
-        s.append(line, k);
+        s.append(line, std::min<size_t>(k > 0 ? (size_t)k : 0, sizeof(line) - 1));
       }
     });
   for (auto &x : th) x.join();
