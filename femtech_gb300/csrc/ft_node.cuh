@@ -333,7 +333,7 @@ __device__ __forceinline__ StepScalars step_scalars(const Clock &ck, const InstP
 }
 
 template <class R>
-__global__ void __launch_bounds__(512) k_node(const NodeArgs A) {
+__global__ void __launch_bounds__(512, 2) k_node(const NodeArgs A) {
   const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= A.N) return;
   const int inst = A.node_inst ? A.node_inst[n] : 0;
