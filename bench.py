@@ -47,23 +47,26 @@ WORKLOAD = "ogden_hex8_block_200x200x100_jitter10_sine50Hz"
 
 # Algorithmic traffic model of one element-update (compulsory bytes at the
 # stated precisions; intermediate patch buffers are overhead, not counted):
-#   element pass: connectivity 8 x 4 B, per node X f32 12 B + u f32 12 B read
-#   and internal force f32 12 B written, x (nodes / elements)
+#   element pass: connectivity 8 x 4 B and the reference geometry of the 8
+#   Gauss points (A^-1 and det A, 80 x f32 = 320 B) per element, per node
+#   X f32 12 B + u f32 12 B read and internal force f32 12 B written,
+#   x (nodes / elements)
 #   nodal pass:   per node u f64 24 + v_half f64 24 + mass f64 8 read,
 #                 u 24 + v_half 24 written + force f32 12 read
-ELEM_BYTES_PER_EL = 32.0
+ELEM_BYTES_PER_EL = 32.0 + 320.0
 ELEM_BYTES_PER_NODE = 36.0
 NODE_BYTES_PER_NODE = 116.0
 # FP32 operations of one C3D8 Ogden element-update in this formulation
 # (small-strain series path), counted from the kernel source (ft_elem.cuh /
-# ft_materials.cuh), FMA = 2: per Gauss point Jacobian and displacement-
-# gradient columns 108, adj/det 32, D = H adj^T / det 63, J - 1 27, Ogden
-# series law 313 (2E 40, norm 11, M^2 30, invariants 21, seven Cayley-Hamilton
-# steps of the I / M / M^2 coefficients of the A and tr B series 126, exact
-# (I + M)^-1 7, coefficients of S 15, J^-alpha/3 5, S 21, volumetric 37),
-# P = S + D S 54, P adj 45, moments 63 -> 705 per Gauss point, 5640 for 8;
-# Hadamard transforms 150, face areas 540, inverse transform 90.
-FLOP_PER_EL_OGDEN = 5640 + 150 + 540 + 90
+# ft_materials.cuh), FMA = 2: per Gauss point displacement-gradient columns
+# 54, D = H A^-T 45, J - 1 27, Ogden series law 313 (2E 40, norm 11, M^2 30,
+# invariants 21, seven Cayley-Hamilton steps of the I / M / M^2 coefficients
+# of the A and tr B series 126, exact (I + M)^-1 7, coefficients of S 15,
+# J^-alpha/3 5, S 21, volumetric 37), det A S 6, P = S + D S 54, P A^-1 45,
+# moments 63 -> 607 per Gauss point, 4856 for 8; Hadamard transform of u 75,
+# face areas 540, inverse transform 90.  (A^-1 and det A of the reference
+# geometry are read from the set-up table, not recomputed.)
+FLOP_PER_EL_OGDEN = 4856 + 75 + 540 + 90
 
 
 def log(*a):

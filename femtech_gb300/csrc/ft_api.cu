@@ -213,6 +213,7 @@ struct ftgpu_model {
   DBuf patch_elem_off, patch_node_off, patch_inst, patch_ent_off, lptr, lent, lconn, epid, fib;
   DBuf sX, sU, sF, mats;
   std::vector<std::unique_ptr<DBuf>> hist;
+  std::vector<std::unique_ptr<DBuf>> geo;  // per C3D8 group: Gauss-point A^{-1}, det A
   DBuf clock, dtmin, err, instp;
   DBuf stepsc, rottrig;  // per-instance step scalars / rotation trigonometry
   DBuf stage;            // AoS staging of host <-> device state copies
@@ -304,6 +305,7 @@ ElemArgs<R> elem_args(ftgpu_model *m, const PatchGroup &g, int gi) {
   A.sU = m->sU.as<R>();
   A.sF = m->sF.as<R>();
   A.hist = m->hist[gi] ? m->hist[gi]->as<R>() : nullptr;
+  A.geo = gi < (int)m->geo.size() && m->geo[gi] ? m->geo[gi]->as<R>() : nullptr;
   A.mats = m->mats.as<MatP<R>>();
   A.clock = m->clock.as<Clock>();
   A.dtmin = m->dtmin.as<unsigned long long>();
@@ -852,6 +854,23 @@ int setup_t(ftgpu_model *m) {
   CKI(m->rottrig.alloc((size_t)m->ninst * kMaxRotFns * 3 * sizeof(double)));
   CKI(m->err.alloc(sizeof(int)));
   CK(cudaMemset(m->err.p, 0, sizeof(int)));
+  // FP32: reference geometry of every C3D8 Gauss point, once (the element
+  // passes read it instead of rebuilding A^{-1} from the slot coordinates)
+  m->geo.clear();
+  if constexpr (sizeof(R) == 4) {
+    for (size_t gi = 0; gi < ps.groups.size(); ++gi) {
+      const PatchGroup &g = ps.groups[gi];
+      if (g.etype != 0 || g.nelem == 0) {
+        m->geo.emplace_back(nullptr);
+        continue;
+      }
+      auto b = std::make_unique<DBuf>();
+      CKI(b->alloc((size_t)80 * g.nelem * sizeof(float)));
+      m->geo.push_back(std::move(b));
+      const ElemArgs<float> A = elem_args<float>(m, g, (int)gi);
+      CK((cudaError_t)launch_geo_f32(g.npatch, m->stream, A, m->geo.back()->as<float>()));
+    }
+  }
   CKI(fill_dtmin(m));
   // lumped mass on the device (FP64), replaces AssembleLumpedMass()
   {

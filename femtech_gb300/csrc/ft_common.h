@@ -78,6 +78,10 @@ struct ElemArgs {
   Real *sF;                   // [S] Slot4: patch-partial internal forces
   // material state
   Real *hist;                 // [ncomp][NGP][nelem] of this group
+  // C3D8 reference geometry of this group, written once at setup: per Gauss
+  // point the inverse Jacobian A^{-1} (row major) and det A as five pairs,
+  // [NGP][5][nelem] (null for C3D4 groups)
+  const Real *geo;
   const MatP<Real> *mats;
   // clock
   Clock *clock;               // [2][ninst]

@@ -56,6 +56,30 @@ __device__ __forceinline__ void hex_hadamard(const R (&x)[8][3], R (&h)[7][3]) {
   }
 }
 
+// 16-byte asynchronous global -> shared copy (both addresses 16-byte aligned)
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc) {
+  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(smem_dst));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
+template <class R> struct Pair;
+template <> struct Pair<float> { using T = float2; };
+template <> struct Pair<double> { using T = double2; };
+
+// Gauss point g of the 2x2x2 rule in the order of GaussQuadrature3D.cpp:17-58
+// (the literal 0.577350269189626 as there): xi > 0 for g in {1,2,5,6},
+// eta > 0 for {2,3,6,7}, zeta > 0 for g < 4.
+template <class R>
+__device__ __forceinline__ void hex_gauss_point(int g, R &xi, R &et, R &ze) {
+  const R G = R(0.577350269189626);
+  xi = ((g + 1) & 2) ? G : -G;
+  et = (g & 2) ? G : -G;
+  ze = g < 4 ? G : -G;
+}
+
 template <class R>
 __device__ __forceinline__ void adj3(const R (&A)[3][3], R (&J)[3][3], R &det) {
   J[0][0] = A[1][1] * A[2][2] - A[1][2] * A[2][1];
@@ -241,12 +265,18 @@ __device__ __forceinline__ R hex_face_area(const R (&xc)[8][3], int i1, int i2, 
   return area;
 }
 
-template <class R, int MAT, bool GP>
+// GEO: the Gauss points' A^{-1} and det A come from the setup-time table
+// (k_elem_geo; the reference likewise evaluates dN/dX and det J once, at
+// initialisation, ShapeFunctions.cpp:197-215) instead of being rebuilt from
+// the reference coordinates: `geo` is this element's column of the block's
+// shared-memory copy, value k of the 80-value record at geo[(k/4)*rs + k%4].
+template <class R, int MAT, bool GP, bool GEO>
 __device__ __forceinline__ void hex_element(const R (&x)[8][3], const R (&u)[8][3],
                                             const MatP<R> &mp, const R (&pc)[4],
                                             const R (&a0)[3], R *hist, long long hs,
                                             long long gs, int pass, R (&f)[8][3], R &le,
-                                            int &bad, const ElemArgs<R> &A, long long gpo) {
+                                            int &bad, const ElemArgs<R> &A, long long gpo,
+                                            const R *geo, int rs) {
   const bool dt_only = pass == kPassDt;
   // characteristic length on the current geometry first (volume / max face
   // area, CalculateCharacteristicLength_C3D8.cpp:6-29) so that the nodal
@@ -267,54 +297,64 @@ __device__ __forceinline__ void hex_element(const R (&x)[8][3], const R (&u)[8][
     amax = fmax(amax, hex_face_area(xc, 3, 2, 6, 7));
   }
   R hx[7][3], hu[7][3];
-  hex_hadamard(x, hx);
+  if (!GEO) hex_hadamard(x, hx);
   hex_hadamard(u, hu);
   R vol = 0;
   R m[7][3];
 #pragma unroll
   for (int i = 0; i < 7; ++i) m[i][0] = m[i][1] = m[i][2] = 0;
-  const R G = R(0.577350269189626);
-  // Gauss points in the order of GaussQuadrature3D.cpp:17-58 (literal as
-  // there): xi > 0 for g in {1,2,5,6}, eta > 0 for {2,3,6,7}, zeta > 0 for g < 4.
   // The loop is not unrolled: one Gauss point's code stays in the
   // instruction cache and its temporaries are the only ones live.
 #pragma unroll 1
   for (int g = 0; g < 8; ++g) {
-    const R xi = ((g + 1) & 2) ? G : -G, et = (g & 2) ? G : -G, ze = g < 4 ? G : -G;
+    R xi, et, ze;
+    hex_gauss_point(g, xi, et, ze);
     const R ez = et * ze, xz = xi * ze, xe = xi * et;
-    R Am[3][3], H[3][3];
+    R Q[3][3], detA;  // Q = A^{-1}, A[i][d] = dX_d / dxi_i
+    if (GEO) {
+      typedef typename Pair<R>::T P2;
+      const int k0 = 10 * g;  // even: every pair lies in one 4-value row
+#define FT_GEO_PAIR(k) (*reinterpret_cast<const P2 *>(geo + ((k) >> 2) * rs + ((k) & 3)))
+      const P2 q0 = FT_GEO_PAIR(k0), q1 = FT_GEO_PAIR(k0 + 2), q2 = FT_GEO_PAIR(k0 + 4),
+               q3 = FT_GEO_PAIR(k0 + 6), q4 = FT_GEO_PAIR(k0 + 8);
+#undef FT_GEO_PAIR
+      Q[0][0] = q0.x; Q[0][1] = q0.y; Q[0][2] = q1.x;
+      Q[1][0] = q1.y; Q[1][1] = q2.x; Q[1][2] = q2.y;
+      Q[2][0] = q3.x; Q[2][1] = q3.y; Q[2][2] = q4.x;
+      detA = q4.y;
+    } else {
+      R Am[3][3], Ad[3][3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        Am[0][d] = hx[0][d] + et * hx[3][d] + ze * hx[4][d] + ez * hx[6][d];
+        Am[1][d] = hx[1][d] + xi * hx[3][d] + ze * hx[5][d] + xz * hx[6][d];
+        Am[2][d] = hx[2][d] + xi * hx[4][d] + et * hx[5][d] + xe * hx[6][d];
+      }
+      adj3(Am, Ad, detA);
+      const R idet = 1 / detA;
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) Q[i][j] = idet * Ad[i][j];
+    }
+    R H[3][3];  // H[d][i] = du_d / dxi_i
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      Am[0][d] = hx[0][d] + et * hx[3][d] + ze * hx[4][d] + ez * hx[6][d];
-      Am[1][d] = hx[1][d] + xi * hx[3][d] + ze * hx[5][d] + xz * hx[6][d];
-      Am[2][d] = hx[2][d] + xi * hx[4][d] + et * hx[5][d] + xe * hx[6][d];
       H[d][0] = hu[0][d] + et * hu[3][d] + ze * hu[4][d] + ez * hu[6][d];
       H[d][1] = hu[1][d] + xi * hu[3][d] + ze * hu[5][d] + xz * hu[6][d];
       H[d][2] = hu[2][d] + xi * hu[4][d] + et * hu[5][d] + xe * hu[6][d];
     }
-    R Ad[3][3], detA;
-    adj3(Am, Ad, detA);
-    if (dt_only) {
-      // current Jacobian = reference Jacobian + displacement derivatives
-      R Ac[3][3], Adc[3][3], detc;
-#pragma unroll
-      for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int d = 0; d < 3; ++d) Ac[i][d] = Am[i][d] + H[d][i];
-      adj3(Ac, Adc, detc);
-      vol += detc;
-      continue;
-    }
-    const R idet = 1 / detA;
-    R D[3][3];  // D = H A^{-T} = H adj(A)^T / det A
+    R D[3][3];  // D = H A^{-T} = du/dX
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
       for (int j = 0; j < 3; ++j)
-        D[i][j] = idet * (H[i][0] * Ad[j][0] + H[i][1] * Ad[j][1] + H[i][2] * Ad[j][2]);
+        D[i][j] = H[i][0] * Q[j][0] + H[i][1] * Q[j][1] + H[i][2] * Q[j][2];
     const R Jm1 = jm1_of(D);
-    if (!(Jm1 > R(-1)) || !(detA != 0)) bad = 1;
+    // det(dx/dxi) = det A det F
     vol += (1 + Jm1) * detA;
+    if (dt_only) continue;
+    if (!(Jm1 > R(-1)) || !(detA != 0)) bad = 1;
     const long long sg = gpo - A.gpbase + g;  // Gauss point within the group
     if (MAT == 7 && pass == kPassSurrogateFeatures) {
       write_surrogate_features(D, a0, A.law, A.surr_x + sg * kMlpIn);
@@ -336,8 +376,10 @@ __device__ __forceinline__ void hex_element(const R (&x)[8][3], const R (&u)[8][
       A.gpS[6 * q + 4] = S.xz;
       A.gpS[6 * q + 5] = S.xy;
     }
-    // P = F S = S + D S ; Gm = P adj(A)  (w = 1; det A cancels A^{-1})
-    const R s[3][3] = {{S.xx, S.xy, S.xz}, {S.xy, S.yy, S.yz}, {S.xz, S.yz, S.zz}};
+    // w detJ B0^T S with w = 1: P = det A F S = det A (S + D S), Gm = P A^{-1}
+    const R sxx = detA * S.xx, syy = detA * S.yy, szz = detA * S.zz, syz = detA * S.yz,
+            sxz = detA * S.xz, sxy = detA * S.xy;
+    const R s[3][3] = {{sxx, sxy, sxz}, {sxy, syy, syz}, {sxz, syz, szz}};
     R P[3][3];
 #pragma unroll
     for (int i = 0; i < 3; ++i)
@@ -346,9 +388,9 @@ __device__ __forceinline__ void hex_element(const R (&x)[8][3], const R (&u)[8][
         P[i][j] = s[i][j] + D[i][0] * s[0][j] + D[i][1] * s[1][j] + D[i][2] * s[2][j];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-      R g0 = P[i][0] * Ad[0][0] + P[i][1] * Ad[1][0] + P[i][2] * Ad[2][0];
-      R g1 = P[i][0] * Ad[0][1] + P[i][1] * Ad[1][1] + P[i][2] * Ad[2][1];
-      R g2 = P[i][0] * Ad[0][2] + P[i][1] * Ad[1][2] + P[i][2] * Ad[2][2];
+      R g0 = P[i][0] * Q[0][0] + P[i][1] * Q[1][0] + P[i][2] * Q[2][0];
+      R g1 = P[i][0] * Q[0][1] + P[i][1] * Q[1][1] + P[i][2] * Q[2][1];
+      R g2 = P[i][0] * Q[0][2] + P[i][1] * Q[1][2] + P[i][2] * Q[2][2];
       m[0][i] += g0;
       m[1][i] += g1;
       m[2][i] += g2;
@@ -588,7 +630,11 @@ __global__ void __launch_bounds__(kElemThreads, ET == 0 ? 2 : 4)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   R *shX = reinterpret_cast<R *>(smem_raw);
   R *shU = shX + 3 * kMaxLocalNodes;
-  R *shF = shU + 3 * kMaxLocalNodes;  // [NC*3][blockDim]
+  // [NC*3][blockDim] corner forces; FP32 C3D8: first the elements' reference
+  // geometry, [20][blockDim] x 4 values, in the same space (a barrier
+  // separates the last geometry read from the first corner-force write)
+  R *shF = shU + 3 * kMaxLocalNodes;
+  constexpr bool GEO = ET == 0 && sizeof(R) == 4;
   const int PE = blockDim.x;
   const int t = threadIdx.x;
   const int p = A.patch_begin + blockIdx.x;
@@ -601,6 +647,14 @@ __global__ void __launch_bounds__(kElemThreads, ET == 0 ? 2 : 4)
   const int e = e0 + (act ? t : 0);
   const long long el = e - A.elem_begin;
   const long long gs = A.nelem, hs = (long long)NGP * A.nelem;
+  if (GEO && act) {
+    // 20 rows of 16 bytes, coalesced across the block, landing while the
+    // per-element loads and the slot staging below are in flight
+    const R *src = A.geo + 4 * el;
+    R *dst = shF + 4 * t;
+#pragma unroll 4
+    for (int r = 0; r < 20; ++r) cp_async16(dst + 4 * r * PE, src + 4 * r * gs);
+  }
   uint4 cv = make_uint4(0u, 0u, 0u, 0u);
   int pw = 0;
   R a0[3] = {R(1), R(0), R(0)};
@@ -636,6 +690,7 @@ __global__ void __launch_bounds__(kElemThreads, ET == 0 ? 2 : 4)
     shU[kMaxLocalNodes + i] = us.y;
     shU[2 * kMaxLocalNodes + i] = us.z;
   }
+  if (GEO) cp_async_wait_all();  // this thread's geometry rows
   // an instance past its end time: the whole block leaves (uniform per patch)
   if (A.use_clock && ck->done) return;
   const R dt = A.use_clock ? R(ck->dt) : R(A.dt_direct);
@@ -646,6 +701,7 @@ __global__ void __launch_bounds__(kElemThreads, ET == 0 ? 2 : 4)
   // max shear, max MPS x rate, with list position and compact index
   R iv[4] = {-r_inf<R>(), r_inf<R>(), -r_inf<R>(), -r_inf<R>()};
   int ij[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff}, ic[4] = {-1, -1, -1, -1};
+  R f[NC][3];
   if (act) {
     int lc[NC];
     lc[0] = cv.x & 0xffff; lc[1] = cv.x >> 16; lc[2] = cv.y & 0xffff; lc[3] = cv.y >> 16;
@@ -671,19 +727,19 @@ __global__ void __launch_bounds__(kElemThreads, ET == 0 ? 2 : 4)
     R pc[4];
     prony_consts<R, MAT>(mp, dt, pc);
     R *hist = A.hist ? A.hist + el : nullptr;
-    R f[NC][3];
     R le;
     const long long gpo = A.gpbase + el * NGP;
     if (ET == 0)
-      hex_element<R, MAT, GP>(reinterpret_cast<const R(&)[8][3]>(x),
-                              reinterpret_cast<const R(&)[8][3]>(u), mp, pc, a0, hist, hs, gs,
-                              pass, reinterpret_cast<R(&)[8][3]>(f), le, bad, A, gpo);
+      hex_element<R, MAT, GP, GEO>(
+          reinterpret_cast<const R(&)[8][3]>(x), reinterpret_cast<const R(&)[8][3]>(u), mp, pc,
+          a0, hist, hs, gs, pass, reinterpret_cast<R(&)[8][3]>(f), le, bad, A, gpo, shF + 4 * t,
+          4 * PE);
     else
       tet_element<R, MAT, GP>(reinterpret_cast<const R(&)[4][3]>(x),
                               reinterpret_cast<const R(&)[4][3]>(u), mp, pc, a0, hist, hs,
                               pass, reinterpret_cast<R(&)[4][3]>(f), le, bad, A, gpo,
                               NH > 1 ? hin : nullptr);
-    if (pass == kPassForce) {
+    if (!GEO && pass == kPassForce) {
 #pragma unroll
       for (int a = 0; a < NC; ++a)
 #pragma unroll
@@ -691,6 +747,15 @@ __global__ void __launch_bounds__(kElemThreads, ET == 0 ? 2 : 4)
     }
     if (!skip) dte = dt_of<R>(le, mp);
     if (INJ && ci >= 0) injury_element<R>(A, ci, Es, dt, iv, ij, ic);
+  }
+  if (GEO && pass == kPassForce) {
+    __syncthreads();  // every thread is done with its geometry rows
+    if (act) {
+#pragma unroll
+      for (int a = 0; a < NC; ++a)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) shF[(a * 3 + d) * PE + t] = f[a][d];
+    }
   }
   if (bad) atomicOr(A.err, (bad & 1 ? kErrInverted : 0) | (bad & 2 ? kErrIndex : 0));
   if (pass == kPassSurrogateFeatures) return;  // features only (uniform per block)
@@ -724,6 +789,64 @@ __global__ void __launch_bounds__(kElemThreads, ET == 0 ? 2 : 4)
     }
     reinterpret_cast<Slot4<R> *>(A.sF)[s0 + i] = Slot4<R>{f0, f1, f2, R(0)};
   }
+}
+
+// Setup pass of an FP32 C3D8 group: per Gauss point the inverse Jacobian of
+// the reference geometry and its determinant (ShapeFunction_C3D8.cpp:35-120,
+// evaluated once as in ShapeFunctions.cpp:197-215), computed in FP64 from the
+// slot coordinates.  Per element an 80-value record, value 10 g + k of Gauss
+// point g = (Q00 Q01 Q02 Q10 Q11 Q12 Q20 Q21 Q22 det A)[k], stored as 20 rows
+// of 4 values: value v at geo[4 (v/4 * nelem + element) + v%4].
+template <class R>
+__global__ void __launch_bounds__(kElemThreads) k_elem_geo(const ElemArgs<R> A, float *geo) {
+  static_assert(sizeof(R) == 4, "the geometry table serves the FP32 element kernels");
+  __shared__ double shX[3][kMaxLocalNodes];
+  const int p = A.patch_begin + blockIdx.x;
+  const int e0 = A.patch_elem_off[p], ne = A.patch_elem_off[p + 1] - e0;
+  const int s0 = A.patch_node_off[p], ns = A.patch_node_off[p + 1] - s0;
+  for (int i = threadIdx.x; i < ns && i < kMaxLocalNodes; i += blockDim.x)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) shX[d][i] = double(A.sX[d * A.S + s0 + i]);
+  __syncthreads();
+  const long long gs = A.nelem;
+  int bad = 0;
+  for (int t = threadIdx.x; t < ne; t += blockDim.x) {
+    const long long el = e0 + t - A.elem_begin;
+    double x[8][3];
+#pragma unroll
+    for (int a = 0; a < 8; ++a) {
+      int l = A.lconn[8 * el + a];
+      if (l >= ns || l >= kMaxLocalNodes) {
+        bad |= kErrIndex;
+        l = 0;
+      }
+#pragma unroll
+      for (int d = 0; d < 3; ++d) x[a][d] = shX[d][l];
+    }
+    double hx[7][3];
+    hex_hadamard(x, hx);
+    for (int g = 0; g < 8; ++g) {
+      double xi, et, ze;
+      hex_gauss_point(g, xi, et, ze);
+      const double ez = et * ze, xz = xi * ze, xe = xi * et;
+      double Am[3][3], Ad[3][3], det;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        Am[0][d] = hx[0][d] + et * hx[3][d] + ze * hx[4][d] + ez * hx[6][d];
+        Am[1][d] = hx[1][d] + xi * hx[3][d] + ze * hx[5][d] + xz * hx[6][d];
+        Am[2][d] = hx[2][d] + xi * hx[4][d] + et * hx[5][d] + xe * hx[6][d];
+      }
+      adj3(Am, Ad, det);
+      const double id = 1.0 / det;  // det = 0: non-finite entries, flagged by the force pass
+#pragma unroll
+      for (int k = 0; k < 10; ++k) {
+        const int v = 10 * g + k;
+        const double q = k < 9 ? Ad[k / 3][k % 3] * id : det;
+        geo[4 * ((v >> 2) * gs + el) + (v & 3)] = float(q);
+      }
+    }
+  }
+  if (bad) atomicOr(A.err, bad);
 }
 
 // Gauss-point average of the Green strain of one element (see k_elem_strain)

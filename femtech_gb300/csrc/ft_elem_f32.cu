@@ -6,6 +6,24 @@ namespace ftgpu {
 
 template <int ET, int MAT>
 static int go(int gp, int nb, int th, size_t sm, cudaStream_t s, const ElemArgs<float> &A, int dto) {
+  // C3D8 blocks of more than 128 elements need more than 48 KB of shared
+  // memory (the geometry records); allowed once per device, at the first
+  // launch there (set-up)
+  static bool opted[64] = {};
+  int dev = 0;
+  if (ET == 0 && (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64))
+    return (int)cudaErrorInvalidDevice;
+  if (ET == 0 && !opted[dev]) {
+    const int mx = (int)elem_smem_bytes_host<float>(0, kMaxPatchElems);
+    for (cudaError_t e : {cudaFuncSetAttribute(k_elem<float, ET, MAT, true, false>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, mx),
+                          cudaFuncSetAttribute(k_elem<float, ET, MAT, false, true>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, mx),
+                          cudaFuncSetAttribute(k_elem<float, ET, MAT, false, false>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, mx)})
+      if (e != cudaSuccess) return (int)e;
+    opted[dev] = true;
+  }
   if (gp == kLaunchGaussPoints)
     k_elem<float, ET, MAT, true, false><<<nb, th, sm, s>>>(A, dto);
   else if (gp == kLaunchInjury)
@@ -38,6 +56,12 @@ int launch_strain_f32(int etype, int nblocks, int threads, size_t smem, cudaStre
     k_elem_strain<float, 0><<<nblocks, threads, smem, s>>>(A, Eout);
   else
     k_elem_strain<float, 1><<<nblocks, threads, smem, s>>>(A, Eout);
+  return (int)cudaGetLastError();
+}
+
+int launch_geo_f32(int nblocks, cudaStream_t s, const ElemArgs<float> &A, float *geo) {
+  if (nblocks <= 0) return 0;
+  k_elem_geo<float><<<nblocks, 128, 0, s>>>(A, geo);
   return (int)cudaGetLastError();
 }
 

@@ -41,12 +41,19 @@ inline int launch_strain<double>(int etype, int nblocks, int threads, size_t sme
   return launch_strain_f64(etype, nblocks, threads, smem, s, A, Eout);
 }
 
+// Setup pass of an FP32 C3D8 group (k_elem_geo): the Gauss points' inverse
+// reference Jacobians and determinants into geo ([20][nelem] x 4 values).
+// Returns a cudaError_t value.
+int launch_geo_f32(int nblocks, cudaStream_t s, const ElemArgs<float> &A, float *geo);
+
 // Dynamic shared memory of one element block: node X and u for
-// kMaxLocalNodes slots plus NC*3 corner forces per element.
+// kMaxLocalNodes slots plus NC*3 corner forces per element, or for FP32
+// C3D8 the larger 80-value geometry record per element in the same space.
 template <class R>
 inline size_t elem_smem_bytes_host(int etype, int PE) {
   const int NC = etype == 0 ? 8 : 4;
-  return sizeof(R) * (6 * (size_t)kMaxLocalNodes + (size_t)NC * 3 * PE);
+  const size_t per_elem = (etype == 0 && sizeof(R) == 4) ? 80 : (size_t)NC * 3;
+  return sizeof(R) * (6 * (size_t)kMaxLocalNodes + per_elem * PE);
 }
 
 template <class R>

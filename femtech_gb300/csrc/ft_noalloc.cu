@@ -60,7 +60,8 @@ __global__ void k_noalloc_hex(int nelements, const double *X, const int *conn, c
   const double a0[3] = {1, 0, 0};
   double f[8][3], le;
   int bad = 0;
-  hex_element<double, MAT, false>(x, uu, mp, pc, a0, nullptr, 0, 0, false, f, le, bad, none, 0);
+  hex_element<double, MAT, false, false>(x, uu, mp, pc, a0, nullptr, 0, 0, false, f, le, bad,
+                                         none, 0, nullptr, 0);
   if (bad) atomicOr(bad_out, 1);
 #pragma unroll
   for (int a = 0; a < 8; ++a)
