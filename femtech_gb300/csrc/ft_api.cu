@@ -241,7 +241,7 @@ struct ftgpu_model {
   long long rig_nodes = 0;
   cudaStream_t stream2 = nullptr;  // the driven-node branch of a step
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-  DBuf slot_off, slots, node_inst, nbc, fnsbuf;
+  DBuf slot_off, slots, slot4, node_inst, nbc, fnsbuf;
   DBuf dX, u, v, a, vh, mass, minv, fi;
   DBuf gpF, gpJ, gpS;
   // graph of one chunk of steps (plain, and with timing events)
@@ -337,6 +337,7 @@ NodeArgs node_args(ftgpu_model *m, int mode, int parity) {
   memset(&A, 0, sizeof(A));
   A.slot_off = m->slot_off.as<int>();
   A.slots = m->slots.as<int>();
+  A.slot4 = m->slot4.as<int4>();
   A.node_inst = m->ninst > 1 ? m->node_inst.as<int>() : nullptr;
   A.nbc = m->nbc.as<int16_t>();
   A.fns = m->fnsbuf.as<BcFn>();
@@ -764,6 +765,17 @@ int setup_t(ftgpu_model *m) {
   CKI(m->lconn.upload(ps.lconn.data(), ps.lconn.size()));
   CKI(m->slot_off.upload(ps.node_slot_off.data(), N + 1));
   CKI(m->slots.upload(ps.node_slots.data(), ps.node_slots.size()));
+  {
+    std::vector<int> rec(4 * (size_t)N, -1);
+    for (long long n = 0; n < N; ++n) {
+      const int b = ps.node_slot_off[n], e = ps.node_slot_off[n + 1];
+      if (e - b > 4)
+        rec[4 * n] = kSlotCsr;
+      else
+        for (int k = b; k < e; ++k) rec[4 * n + (k - b)] = ps.node_slots[k];
+    }
+    CKI(m->slot4.upload(rec.data(), rec.size()));
+  }
   CKI(upload_epid(m, false));  // the force slots are allocated zeroed below
   CKI(upload_materials<R>(m));
   // reference coordinates per slot: absolute in FP64 mode, relative to the

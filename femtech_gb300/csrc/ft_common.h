@@ -59,6 +59,8 @@ struct alignas(4 * sizeof(R)) Slot4 {
 enum { kBckFixed = 0, kBckRamp = 1, kBckSine = 2, kBckRot = 3, kBckRigid = 4 };
 enum { kErrInverted = 1, kErrDt = 2, kErrIndex = 4, kErrWait = 8 };
 
+constexpr int kSlotCsr = -2;  // NodeArgs::slot4 marker: more than four slots
+
 template <class Real>
 struct ElemArgs {
   // patches
@@ -166,6 +168,9 @@ struct StepScalars {
 struct NodeArgs {
   const int *slot_off;        // [N+1]
   const int *slots;           // node -> slots
+  // [N] the node's first four slots in CSR order (-1: none), or x = kSlotCsr
+  // for a node with more than four (read through slot_off / slots)
+  const int4 *slot4;
   const int *node_inst;       // [N] or null (one instance)
   const int16_t *nbc;         // [3N] per-DOF function (-1 free, -2 hold, >= 0 fn)
   const uint8_t *nbcflag;     // [N] bit0 any constrained DOF

@@ -597,7 +597,11 @@ __device__ __forceinline__ void node_step(const NodeArgs &A, long long n, R &eke
   const Slot4<R> *sF = reinterpret_cast<const Slot4<R> *>(A.sF);
   Slot4<R> *sU = reinterpret_cast<Slot4<R> *>(A.sU);
   const int inst = A.node_inst ? A.node_inst[n] : 0;
-  const int sb = A.slot_off[n], se = A.slot_off[n + 1];
+  // the node's slots: one 16-byte record, so that the partial-force loads
+  // wait on one round trip instead of two (offsets, then slot ids)
+  const int4 sr = A.slot4[n];
+  const int ss[4] = {sr.x, sr.y, sr.z, sr.w};
+  const bool csr = sr.x == kSlotCsr;
   int nbc[3];
   double u0[3], vh0[3];
 #pragma unroll
@@ -632,11 +636,25 @@ __device__ __forceinline__ void node_step(const NodeArgs &A, long long n, R &eke
 
   // sum of the patch partials in slot order (in the element precision)
   R fs0 = 0, fs1 = 0, fs2 = 0;
-  for (int k = sb; k < se; ++k) {
-    const Slot4<R> q = sF[A.slots[k]];
-    fs0 += q.x;
-    fs1 += q.y;
-    fs2 += q.z;
+  if (!csr) {
+    Slot4<R> q[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (ss[j] >= 0) q[j] = sF[ss[j]];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (ss[j] >= 0) {
+        fs0 += q[j].x;
+        fs1 += q[j].y;
+        fs2 += q[j].z;
+      }
+  } else {
+    for (int k = A.slot_off[n]; k < A.slot_off[n + 1]; ++k) {
+      const Slot4<R> q = sF[A.slots[k]];
+      fs0 += q.x;
+      fs1 += q.y;
+      fs2 += q.z;
+    }
   }
   const InstParams &ip = A.inst[inst];
   const bool leader = (n == ip.node_begin);
@@ -719,7 +737,13 @@ __device__ __forceinline__ void node_step(const NodeArgs &A, long long n, R &eke
   }
   if (advance) {
     const Slot4<R> r{R(un[0]), R(un[1]), R(un[2]), R(0)};
-    for (int k = sb; k < se; ++k) sU[A.slots[k]] = r;
+    if (!csr) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (ss[j] >= 0) sU[ss[j]] = r;
+    } else {
+      for (int k = A.slot_off[n]; k < A.slot_off[n + 1]; ++k) sU[A.slots[k]] = r;
+    }
   }
   if (leader) {
     Clock c;
