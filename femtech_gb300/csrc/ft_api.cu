@@ -241,7 +241,7 @@ struct ftgpu_model {
   long long rig_nodes = 0;
   cudaStream_t stream2 = nullptr;  // the driven-node branch of a step
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-  DBuf slot_off, slots, slot4, node_inst, nbc, fnsbuf;
+  DBuf slot_off, slots, slot4, slot4b, node_inst, nbc, fnsbuf;
   DBuf dX, u, v, a, vh, mass, minv, fi;
   DBuf gpF, gpJ, gpS;
   // graph of one chunk of steps (plain, and with timing events)
@@ -338,6 +338,7 @@ NodeArgs node_args(ftgpu_model *m, int mode, int parity) {
   A.slot_off = m->slot_off.as<int>();
   A.slots = m->slots.as<int>();
   A.slot4 = m->slot4.as<int4>();
+  A.slot4b = m->slot4b.p ? m->slot4b.as<int4>() : nullptr;
   A.node_inst = m->ninst > 1 ? m->node_inst.as<int>() : nullptr;
   A.nbc = m->nbc.as<int16_t>();
   A.fns = m->fnsbuf.as<BcFn>();
@@ -766,15 +767,26 @@ int setup_t(ftgpu_model *m) {
   CKI(m->slot_off.upload(ps.node_slot_off.data(), N + 1));
   CKI(m->slots.upload(ps.node_slots.data(), ps.node_slots.size()));
   {
-    std::vector<int> rec(4 * (size_t)N, -1);
+    // slot records: four slots per node, eight (a second record array) when
+    // more than 5 % of the nodes have more than four (tetrahedral meshes)
+    long long over4 = 0;
+    for (long long n = 0; n < N; ++n) over4 += ps.node_slot_off[n + 1] - ps.node_slot_off[n] > 4;
+    const int W = over4 * 20 > N ? 8 : 4;
+    std::vector<int> rec(4 * (size_t)N, -1), rec2(W == 8 ? 4 * (size_t)N : 0, -1);
     for (long long n = 0; n < N; ++n) {
       const int b = ps.node_slot_off[n], e = ps.node_slot_off[n + 1];
-      if (e - b > 4)
+      if (e - b > W) {
         rec[4 * n] = kSlotCsr;
-      else
-        for (int k = b; k < e; ++k) rec[4 * n + (k - b)] = ps.node_slots[k];
+        continue;
+      }
+      for (int k = b; k < e; ++k) {
+        const int j = k - b;
+        (j < 4 ? rec[4 * n + j] : rec2[4 * n + j - 4]) = ps.node_slots[k];
+      }
     }
     CKI(m->slot4.upload(rec.data(), rec.size()));
+    m->slot4b.release();
+    if (W == 8) CKI(m->slot4b.upload(rec2.data(), rec2.size()));
   }
   CKI(upload_epid(m, false));  // the force slots are allocated zeroed below
   CKI(upload_materials<R>(m));

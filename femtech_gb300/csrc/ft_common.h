@@ -59,7 +59,7 @@ struct alignas(4 * sizeof(R)) Slot4 {
 enum { kBckFixed = 0, kBckRamp = 1, kBckSine = 2, kBckRot = 3, kBckRigid = 4 };
 enum { kErrInverted = 1, kErrDt = 2, kErrIndex = 4, kErrWait = 8 };
 
-constexpr int kSlotCsr = -2;  // NodeArgs::slot4 marker: more than four slots
+constexpr int kSlotCsr = -2;  // NodeArgs::slot4 marker: more slots than the records hold
 
 template <class Real>
 struct ElemArgs {
@@ -169,8 +169,11 @@ struct NodeArgs {
   const int *slot_off;        // [N+1]
   const int *slots;           // node -> slots
   // [N] the node's first four slots in CSR order (-1: none), or x = kSlotCsr
-  // for a node with more than four (read through slot_off / slots)
+  // for a node with more slots than the records hold (read through slot_off /
+  // slots); slot4b, when set (meshes where many nodes have more than four
+  // slots, e.g. tetrahedra), slots five to eight
   const int4 *slot4;
+  const int4 *slot4b;
   const int *node_inst;       // [N] or null (one instance)
   const int16_t *nbc;         // [3N] per-DOF function (-1 free, -2 hold, >= 0 fn)
   const uint8_t *nbcflag;     // [N] bit0 any constrained DOF

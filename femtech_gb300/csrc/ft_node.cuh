@@ -600,7 +600,9 @@ __device__ __forceinline__ void node_step(const NodeArgs &A, long long n, R &eke
   // the node's slots: one 16-byte record, so that the partial-force loads
   // wait on one round trip instead of two (offsets, then slot ids)
   const int4 sr = A.slot4[n];
-  const int ss[4] = {sr.x, sr.y, sr.z, sr.w};
+  int4 sr2 = make_int4(-1, -1, -1, -1);
+  if (A.slot4b) sr2 = A.slot4b[n];
+  const int ss[8] = {sr.x, sr.y, sr.z, sr.w, sr2.x, sr2.y, sr2.z, sr2.w};
   const bool csr = sr.x == kSlotCsr;
   int nbc[3];
   double u0[3], vh0[3];
@@ -648,6 +650,18 @@ __device__ __forceinline__ void node_step(const NodeArgs &A, long long n, R &eke
         fs1 += q[j].y;
         fs2 += q[j].z;
       }
+    if (A.slot4b) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (ss[4 + j] >= 0) q[j] = sF[ss[4 + j]];
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (ss[4 + j] >= 0) {
+          fs0 += q[j].x;
+          fs1 += q[j].y;
+          fs2 += q[j].z;
+        }
+    }
   } else {
     for (int k = A.slot_off[n]; k < A.slot_off[n + 1]; ++k) {
       const Slot4<R> q = sF[A.slots[k]];
@@ -739,7 +753,7 @@ __device__ __forceinline__ void node_step(const NodeArgs &A, long long n, R &eke
     const Slot4<R> r{R(un[0]), R(un[1]), R(un[2]), R(0)};
     if (!csr) {
 #pragma unroll
-      for (int j = 0; j < 4; ++j)
+      for (int j = 0; j < 8; ++j)
         if (ss[j] >= 0) sU[ss[j]] = r;
     } else {
       for (int k = A.slot_off[n]; k < A.slot_off[n + 1]; ++k) sU[A.slots[k]] = r;
