@@ -303,6 +303,9 @@ __device__ __forceinline__ void hex_element(const R (&x)[8][3], const R (&u)[8][
   R m[7][3];
 #pragma unroll
   for (int i = 0; i < 7; ++i) m[i][0] = m[i][1] = m[i][2] = 0;
+  // first pair of the current Gauss point in the geometry rows: value 10 g,
+  // at column 0 of a row for even g and column 2 for odd g
+  const R *gb = geo;
   // The loop is not unrolled: one Gauss point's code stays in the
   // instruction cache and its temporaries are the only ones live.
 #pragma unroll 1
@@ -313,11 +316,14 @@ __device__ __forceinline__ void hex_element(const R (&x)[8][3], const R (&u)[8][
     R Q[3][3], detA;  // Q = A^{-1}, A[i][d] = dX_d / dxi_i
     if (GEO) {
       typedef typename Pair<R>::T P2;
-      const int k0 = 10 * g;  // even: every pair lies in one 4-value row
-#define FT_GEO_PAIR(k) (*reinterpret_cast<const P2 *>(geo + ((k) >> 2) * rs + ((k) & 3)))
-      const P2 q0 = FT_GEO_PAIR(k0), q1 = FT_GEO_PAIR(k0 + 2), q2 = FT_GEO_PAIR(k0 + 4),
-               q3 = FT_GEO_PAIR(k0 + 6), q4 = FT_GEO_PAIR(k0 + 8);
-#undef FT_GEO_PAIR
+      // values 10g .. 10g+9 as five pairs (a pair never straddles a row)
+      const int o1 = (g & 1) ? rs - 2 : 2;
+      const P2 q0 = *reinterpret_cast<const P2 *>(gb),
+               q1 = *reinterpret_cast<const P2 *>(gb + o1),
+               q2 = *reinterpret_cast<const P2 *>(gb + rs),
+               q3 = *reinterpret_cast<const P2 *>(gb + rs + o1),
+               q4 = *reinterpret_cast<const P2 *>(gb + 2 * rs);
+      gb += (g & 1) ? 3 * rs - 2 : 2 * rs + 2;
       Q[0][0] = q0.x; Q[0][1] = q0.y; Q[0][2] = q1.x;
       Q[1][0] = q1.y; Q[1][1] = q2.x; Q[1][2] = q2.y;
       Q[2][0] = q3.x; Q[2][1] = q3.y; Q[2][2] = q4.x;

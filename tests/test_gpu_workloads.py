@@ -12,12 +12,27 @@ from helpers import rel
 pytestmark = pytest.mark.gpu
 
 
-def test_head_case_small_vs_oracle(oracle_lib):
-    mesh, mats, loads = mg.head_case(target_elements=12_000, seed=4)
-    o = oracle_lib.Oracle(mesh, mats, threads=4)
-    ref = o.explicit_run(loads.dof_fn, loads.fns, tmax=1.0, reduction=0.9, max_steps=300,
-                         out_every=100)
-    m = ft.Model(mesh, mats, precision=ft.MIXED, loads=loads)
+_HEAD = {}
+
+
+def _head_small(oracle_lib):
+    """The small head case and its FP64 oracle run (computed once per module)."""
+    if not _HEAD:
+        mesh, mats, loads = mg.head_case(target_elements=12_000, seed=4)
+        o = oracle_lib.Oracle(mesh, mats, threads=4)
+        ref = o.explicit_run(loads.dof_fn, loads.fns, tmax=1.0, reduction=0.9, max_steps=300,
+                             out_every=100)
+        _HEAD.update(mesh=mesh, mats=mats, loads=loads, ref=ref)
+    return _HEAD["mesh"], _HEAD["mats"], _HEAD["loads"], _HEAD["ref"]
+
+
+# patch size 0 (default 128): most nodes in one to eight patches (eight-slot
+# node records); 32: many nodes in more than eight (the CSR path of the
+# node step)
+@pytest.mark.parametrize("patch", [0, 32])
+def test_head_case_small_vs_oracle(oracle_lib, patch):
+    mesh, mats, loads, ref = _head_small(oracle_lib)
+    m = ft.Model(mesh, mats, precision=ft.MIXED, loads=loads, patch_size=patch)
     m.init_explicit(0.9, 0.0, 1.0)
     us = []
     for _ in range(3):
