@@ -442,7 +442,8 @@ def main():
                    + ("_injury_criteria" if args.injury else ""),
                    "elements": E, "nodes": N,
                    "material": wl["material"], "precision": "mixed",
-                   "l2": "inputs larger than L2 (%.2f GB resident)" % ((E * 48 + N * 140) / 1e9),
+                   "l2": "inputs larger than L2 (%.2f GB resident)" % (
+                       (E * (48 + (320 if "C3D8" in wl["kernel"] else 0)) + N * 140) / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "gpu_launches": launches,
         "clocks": clocks,
