@@ -247,6 +247,9 @@ struct ftgpu_model {
   // graph of one chunk of steps (plain, and with timing events)
   cudaGraphExec_t chunk_exec = nullptr;
   int chunk_steps = 0;
+  // shorter graphs of 2, 4, ..., 14 steps (index steps / 2) for the end of a
+  // run, so that a run of any length launches no steps past its limit
+  cudaGraphExec_t tail_exec[8] = {};
   cudaGraphExec_t prof_exec = nullptr;
   int prof_steps = 0;
   std::vector<cudaEvent_t> prof_ev;
@@ -259,6 +262,8 @@ struct ftgpu_model {
   std::vector<long long> surr_base;   // per group: first Gauss point in the buffers
   ~ftgpu_model() {
     if (chunk_exec) cudaGraphExecDestroy(chunk_exec);
+    for (cudaGraphExec_t &e : tail_exec)
+      if (e) cudaGraphExecDestroy(e);
     if (prof_exec) cudaGraphExecDestroy(prof_exec);
     for (cudaEvent_t e : prof_ev) cudaEventDestroy(e);
     if (h_clock) cudaFreeHost(h_clock);
@@ -277,6 +282,10 @@ bool is_fp64(const ftgpu_model *m) { return m->precision == FTGPU_FP64; }
 // Captured graphs bake in buffer pointers and BC tables: drop them whenever those change.
 void drop_graphs(ftgpu_model *m) {
   if (m->chunk_exec) cudaGraphExecDestroy(m->chunk_exec);
+  for (cudaGraphExec_t &e : m->tail_exec) {
+    if (e) cudaGraphExecDestroy(e);
+    e = nullptr;
+  }
   if (m->prof_exec) cudaGraphExecDestroy(m->prof_exec);
   m->chunk_exec = m->prof_exec = nullptr;
   m->chunk_steps = m->prof_steps = 0;
@@ -1008,9 +1017,16 @@ int launch_injury(ftgpu_model *m, int parity) {
   return is_fp64(m) ? launch_injury_t<double>(m, parity) : launch_injury_t<float>(m, parity);
 }
 
+// Steps per chunk graph (even: the clock slots alternate with the step
+// parity, so a graph of an even number of steps fits any starting step).
+constexpr int kChunkSteps = 16;
+
 int capture_chunk(ftgpu_model *m, int K, bool prof) {
-  cudaGraphExec_t &exec = prof ? m->prof_exec : m->chunk_exec;
-  int &steps = prof ? m->prof_steps : m->chunk_steps;
+  int tail_steps = 0;
+  const bool tail = !prof && K < kChunkSteps;  // even K from 2 to 14
+  cudaGraphExec_t &exec = tail ? m->tail_exec[K / 2] : prof ? m->prof_exec : m->chunk_exec;
+  int &steps = tail ? tail_steps : prof ? m->prof_steps : m->chunk_steps;
+  if (tail && exec) return 0;
   if (exec && steps == K) return 0;
   if (exec) cudaGraphExecDestroy(exec);
   exec = nullptr;
@@ -1063,7 +1079,7 @@ int run_impl(ftgpu_model *m, int max_steps, int *steps_done, bool prof, double *
   CK(cudaMemcpyAsync(m->clock.p, m->h_clock, sizeof(Clock) * ni, cudaMemcpyHostToDevice, m->stream));
   CK(cudaMemcpyAsync(m->instp.p, m->inst.data(), ni * sizeof(InstParams), cudaMemcpyHostToDevice,
                      m->stream));
-  const int K = 16;
+  const int K = kChunkSteps;
   CKI(capture_chunk(m, K, prof));
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (device_ms) {
@@ -1071,11 +1087,22 @@ int run_impl(ftgpu_model *m, int max_steps, int *steps_done, bool prof, double *
     CK(cudaEventCreate(&e1));
     CK(cudaEventRecord(e0, m->stream));
   }
-  const long long max_chunks = (max_steps + K - 1) / K + 1;
+  // every launch advances each running instance by its steps (or ends it)
+  const long long max_chunks = (max_steps + 1) / 2 + 2;
   int rc = FTGPU_OK;
   long long prev = start0;
+  long long left = max_steps;  // most steps any running instance still has
   for (long long c = 0; c < max_chunks; ++c) {
-    CK(cudaGraphLaunch(prof ? m->prof_exec : m->chunk_exec, m->stream));
+    cudaGraphExec_t g = prof ? m->prof_exec : m->chunk_exec;
+    if (!prof && left < K) {
+      // the end of the run: the shortest even graph that covers it
+      const int Kt = (int)std::max<long long>(2, (left + 1) & ~1ll);
+      if (Kt < K) {
+        CKI(capture_chunk(m, Kt, false));
+        g = m->tail_exec[Kt / 2];
+      }
+    }
+    CK(cudaGraphLaunch(g, m->stream));
     CK(cudaMemcpyAsync(m->h_clock, m->clock.p, sizeof(Clock) * ni, cudaMemcpyDeviceToHost,
                        m->stream));
     CK(cudaMemcpyAsync(m->h_err, m->err.p, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
@@ -1091,6 +1118,10 @@ int run_impl(ftgpu_model *m, int max_steps, int *steps_done, bool prof, double *
       }
     }
     prev = m->h_clock[0].step;
+    left = 0;
+    for (int i = 0; i < ni; ++i)
+      if (!m->h_clock[i].done)
+        left = std::max<long long>(left, m->inst[i].step_limit - m->h_clock[i].step);
     if (*m->h_err & kErrInverted) {
       rc = fail(FTGPU_ERR_INVERTED, "non-positive or non-finite Jacobian");
       break;
