@@ -18,10 +18,13 @@
 // order: no floating-point atomics anywhere, so runs are bitwise reproducible.
 //
 // C3D8 kinematics use the tensor-product structure of the trilinear element:
-// the 8 nodal vectors are Hadamard-transformed once, after which every
-// Jacobian column at a Gauss point costs 3 FMAs, and the B0^T S contraction is
-// accumulated as 7 moment vectors that one inverse transform turns into the 8
-// nodal forces.  Mathematically this is the reference's
+// the 8 nodal displacement vectors are Hadamard-transformed once, after which
+// every column of du/dxi at a Gauss point costs 3 FMAs, and the B0^T S
+// contraction is accumulated as 7 moment vectors that one inverse transform
+// turns into the 8 nodal forces.  The reference Jacobian's inverse and
+// determinant at each Gauss point come from a table written at set-up (FP32
+// kernels) or from the same transform of the reference coordinates (FP64).
+// Mathematically this is the reference's
 //   F = sum_a x_a (x) dN_a/dX,  f_a = sum_gp w detJ B0_a^T S.
 #pragma once
 
