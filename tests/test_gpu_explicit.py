@@ -72,15 +72,19 @@ def test_runs_are_bitwise_reproducible():
     assert np.array_equal(out[0], out[1])
 
 
-def test_chunked_equals_continuous():
+# runs of 5 steps; and lengths that end in every tail graph (2 to 14 steps,
+# odd lengths with one step past the limit) and in whole 16-step chunks
+@pytest.mark.parametrize("lengths", [[5] * 20, [1, 2, 3, 14, 15, 17, 16, 32]])
+def test_chunked_equals_continuous(lengths):
+    assert sum(lengths) == 100
     mesh, mats, loads = mg.cube_tension_case(n=6)
     a = ft.Model(mesh, mats, precision=ft.FP64, loads=loads)
     a.init_explicit(0.9, 0.0, 1.0)
     a.run(100)
     b = ft.Model(mesh, mats, precision=ft.FP64, loads=loads)
     b.init_explicit(0.9, 0.0, 1.0)
-    for _ in range(20):
-        b.run(5)
+    for k in lengths:
+        assert b.run(k) == k
     sa, sb = a.state(), b.state()
     assert sa["step"] == sb["step"] == 100
     assert np.array_equal(sa["u"], sb["u"]) and np.array_equal(sa["v"], sb["v"])
