@@ -1022,11 +1022,12 @@ int launch_injury(ftgpu_model *m, int parity) {
 constexpr int kChunkSteps = 16;
 
 int capture_chunk(ftgpu_model *m, int K, bool prof) {
-  int tail_steps = 0;
-  const bool tail = !prof && K < kChunkSteps;  // even K from 2 to 14
+  // a tail graph (even K from 2 to 14) is captured once and kept in its slot
+  const bool tail = !prof && K < kChunkSteps;
+  if (tail && (K < 2 || (K & 1))) return fail(FTGPU_ERR_INPUT, "tail graph of an odd step count");
+  int tail_steps = K;  // the slot of a tail graph fixes its step count
   cudaGraphExec_t &exec = tail ? m->tail_exec[K / 2] : prof ? m->prof_exec : m->chunk_exec;
   int &steps = tail ? tail_steps : prof ? m->prof_steps : m->chunk_steps;
-  if (tail && exec) return 0;
   if (exec && steps == K) return 0;
   if (exec) cudaGraphExecDestroy(exec);
   exec = nullptr;
