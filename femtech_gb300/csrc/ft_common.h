@@ -80,9 +80,10 @@ struct ElemArgs {
   Real *sF;                   // [S] Slot4: patch-partial internal forces
   // material state
   Real *hist;                 // [ncomp][NGP][nelem] of this group
-  // C3D8 reference geometry of this group, written once at setup: per Gauss
-  // point the inverse Jacobian A^{-1} (row major) and det A as five pairs,
-  // [NGP][5][nelem] (null for C3D4 groups)
+  // FP32 C3D8 groups: the reference geometry, written once at set-up -- per
+  // element 80 values (Gauss point g: A^{-1} row major, then det A, at
+  // 10 g .. 10 g + 9) in 20 rows of 4, value v at [4 (v/4 * nelem + e) + v%4]
+  // (null for C3D4 groups and in FP64 mode)
   const Real *geo;
   const MatP<Real> *mats;
   // clock
