@@ -442,8 +442,11 @@ def main():
                    + ("_injury_criteria" if args.injury else ""),
                    "elements": E, "nodes": N,
                    "material": wl["material"], "precision": "mixed",
-                   "l2": "inputs larger than L2 (%.2f GB resident)" % (
-                       (E * (48 + (320 if "C3D8" in wl["kernel"] else 0)) + N * 140) / 1e9),
+                   # device bytes from the set-up allocations: per C3D8 element 36 B
+                   # + the 320 B geometry table, per C3D4 element about 80 B (with
+                   # history and fibre), per node about 285 B with its slots
+                   "l2": "inputs larger than L2 (about %.2f GB resident)" % (
+                       (E * (356 if "C3D8" in wl["kernel"] else 80) + N * 285) / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "gpu_launches": launches,
         "clocks": clocks,
