@@ -208,7 +208,8 @@ int ftgpu_init_explicit(ftgpu_model *m, double reduction, double failure_dt, dou
 
 /* Advance every instance by up to max_steps central-difference steps
  * (ex9.cpp:107-175) or until Time >= tMax; the loop runs on the device as
- * CUDA-graph chunks.  *steps_done = steps taken by instance 0. */
+ * CUDA graphs of 16 steps and, at the end of the run, one of 2-14 steps.
+ * *steps_done = steps taken by instance 0. */
 int ftgpu_run(ftgpu_model *m, int max_steps, int *steps_done);
 
 /* ftgpu_run with CUDA events recorded on the model's stream around the whole
