@@ -537,7 +537,6 @@ class RefBuild:
         logs them (works accumulate over the process: one energy run per process)."""
         n = 3 * self.nNodes
         u, v, a = np.zeros(n), np.zeros(n), np.zeros(n)
-        self.m.rigid = None if rigid is None else C.addressof(rigid.st)
         ebuf = np.zeros(3 * max(max_steps, 1)) if energy else None
         self.lib().ref_set_energy_out(None if ebuf is None else ebuf.ctypes.data,
                                       max_steps if energy else 0)
