@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(128) k_gemm(const GemmArgs g) {
           : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
     }
   }
-  if (EPI == kEpiBiasSilu) {  // column pairs (c, c + 1) -> one BF16 pair (N is even)
+  if constexpr (EPI == kEpiBiasSilu) {  // column pairs (c, c + 1) -> one BF16 pair (N is even)
 #pragma unroll
     for (int j = 0; j < 4; ++j)
 #pragma unroll
@@ -180,24 +180,24 @@ __global__ void __launch_bounds__(128) k_gemm(const GemmArgs g) {
         g.Z[i * g.N + c + 1] = v1;
         *reinterpret_cast<uint32_t *>(g.H + i * g.N + c) = silu_bf16x2(v0, v1);
       }
-    return;
-  }
+  } else {
 #pragma unroll
-  for (int j = 0; j < 4; ++j)
+    for (int j = 0; j < 4; ++j)
 #pragma unroll
-    for (int h = 0; h < 4; ++h) {
-      const long long i = m0 + gq + (h >= 2 ? 8 : 0);
-      const int c = n0 + 8 * j + 2 * tq + (h & 1);
-      if (i >= g.M || c >= g.N) continue;
-      float v = acc[j][h];
-      if (EPI == kEpiStore) {
-        g.C[i * g.scm + (long long)c * g.scn] = v;
-      } else if (EPI == kEpiBias) {
-        g.C[i * g.scm + (long long)c * g.scn] = v + g.bias[c];
-      } else {  // kEpiSiluGrad
-        g.dZ[i * g.N + c] = __float2bfloat16_rn(v * dsilu(g.Zp[i * g.N + c]));
+      for (int h = 0; h < 4; ++h) {
+        const long long i = m0 + gq + (h >= 2 ? 8 : 0);
+        const int c = n0 + 8 * j + 2 * tq + (h & 1);
+        if (i >= g.M || c >= g.N) continue;
+        float v = acc[j][h];
+        if (EPI == kEpiStore) {
+          g.C[i * g.scm + (long long)c * g.scn] = v;
+        } else if (EPI == kEpiBias) {
+          g.C[i * g.scm + (long long)c * g.scn] = v + g.bias[c];
+        } else {  // kEpiSiluGrad
+          g.dZ[i * g.N + c] = __float2bfloat16_rn(v * dsilu(g.Zp[i * g.N + c]));
+        }
       }
-    }
+  }
 }
 
 // column sums of an [M][N] bf16 matrix (bias gradients), fixed-order tree
