@@ -17,8 +17,13 @@ Reported (one JSON line from rank 0):
   e2e         the same metric through the public C ABI with host buffers:
               initial state uploaded from host, displacements read back every
               100 steps, setup of the loop included
-  roofline    dominant kernel (element pass) against measured HBM bandwidth,
-              with its FP32-pipe use against the nominal FP32 rate
+  roofline    dominant kernel (element pass): the algorithmic bytes of one
+              element-update (32 B per element + 116 B per node) over its
+              time against the measured HBM bandwidth, its FP32 rate against
+              the measured FMA rate of this GPU, and which of the two roofs
+              binds
+  rel_disp_err_vs_fp64  mixed path against the FP64 path over the
+              configuration's 5000 steps on a 40x40x20 sub-block
   cpu_baseline the FP64 oracle (OpenMP port of the reference algorithm) on
               the host cores, on a bounded sub-block of the same workload
 
@@ -45,16 +50,20 @@ NX, NY, NZ = 200, 200, 100
 LX, LY, LZ = 0.2, 0.2, 0.1
 WORKLOAD = "ogden_hex8_block_200x200x100_jitter10_sine50Hz"
 
-# Algorithmic traffic model of one element-update (compulsory bytes at the
-# stated precisions; intermediate patch buffers are overhead, not counted):
-#   element pass: connectivity 8 x 4 B and the reference geometry of the 8
-#   Gauss points (A^-1 and det A, 80 x f32 = 320 B) per element, per node
-#   X f32 12 B + u f32 12 B read and internal force f32 12 B written,
-#   x (nodes / elements)
-#   nodal pass:   per node u f64 24 + v_half f64 24 + mass f64 8 read,
-#                 u 24 + v_half 24 written + force f32 12 read
-ELEM_BYTES_PER_EL = 32.0 + 320.0
-ELEM_BYTES_PER_NODE = 36.0
+# Algorithmic (compulsory) bytes of one element-update at the stated
+# precisions, whole step: per element the connectivity 8 x 4 B; per node
+# (x nodes / elements) X f32 12 B + u f64 24 B + v_half f64 24 B + mass f64
+# 8 B read and u, v_half (48 B) written = 116 B.  For the 4M block:
+# 32 + 116 x 4,080,501 / 4,000,000 = 150.3 B.  Everything else the kernels
+# move is overhead of this design, not algorithmic: the Gauss-point geometry
+# table of the FP32 C3D8 kernels (320 B per element), the patch-local slot
+# replicas of u and of the partial forces, the f32 force hand-off between the
+# passes.  The measured DRAM bytes of the element pass (profiles/) carry it.
+ALG_BYTES_PER_EL_C3D8 = 32.0
+ALG_BYTES_PER_NODE = 116.0
+# design overheads per element of the FP32 C3D8 path (for the line's notes)
+GEO_TABLE_BYTES_PER_EL = 320.0
+# nodal pass alone: u, v_half, mass f64 read, u, v_half written, force f32 read
 NODE_BYTES_PER_NODE = 116.0
 # FP32 operations of one C3D8 Ogden element-update in this formulation
 # (small-strain series path), counted from the kernel source (ft_elem.cuh /
@@ -229,7 +238,7 @@ def make_workload(name, size=None):
         E, N = len(mesh["etype"]), len(mesh["coordinates"])
         return dict(mesh=mesh, mats=mats, loads=loads, instances=None,
                     label=WORKLOAD if not size else "ogden_hex8_block_%dx%dx%d" % (nx, ny, nz),
-                    elem_bytes=E * ELEM_BYTES_PER_EL + N * ELEM_BYTES_PER_NODE,
+                    alg_bytes=E * ALG_BYTES_PER_EL_C3D8 + N * ALG_BYTES_PER_NODE,
                     flop=FLOP_PER_EL_OGDEN * E, kernel="k_elem<float,C3D8,Ogden>",
                     material="ogden mu=1.5e3 alpha=5 K=2e7 rho=1040")
     if name == "head":
@@ -239,10 +248,10 @@ def make_workload(name, size=None):
         inner = int((mesh["pid"] == 1).sum())
         # C3D4: connectivity 16 B + part 4 B per element; interior fibre 12 B and
         # Prony history (H, S0: 12 f32) read + written 96 B; nodes as above
-        eb = E * (16 + 4) + inner * (12 + 96) + N * ELEM_BYTES_PER_NODE
+        eb = E * (16 + 4) + inner * (12 + 96) + N * ALG_BYTES_PER_NODE
         return dict(mesh=mesh, mats=mats, loads=loads, instances=None,
                     label="head_tet4_ellipsoid_%dk_shell_NH_core_GOH_prony_rotation" % (E // 1000),
-                    elem_bytes=eb, flop=None, kernel="k_elem<float,C3D4,NH|GOH+Prony>",
+                    alg_bytes=eb, flop=None, kernel="k_elem<float,C3D4,NH|GOH+Prony>",
                     material="shell NH E=6GPa nu=0.3; core GOH mu=1kPa k1=5kPa k2=10 kappa=0.1 "
                              "lambda=2.19e8 + Prony g1=0.6 tau1=6ms")
     if name == "head-impact":
@@ -252,11 +261,11 @@ def make_workload(name, size=None):
         mesh, mats, loads, rec = mg.head_impact_case(target_elements=target)
         E, N = len(mesh["etype"]), len(mesh["coordinates"])
         inner = int((mesh["pid"] == 1).sum())
-        eb = E * (16 + 4) + inner * (12 + 96) + N * ELEM_BYTES_PER_NODE
+        eb = E * (16 + 4) + inner * (12 + 96) + N * ALG_BYTES_PER_NODE
         return dict(mesh=mesh, mats=mats, loads=loads, instances=None, rigid=rec,
                     label="head_tet4_ellipsoid_%dk_rigid_skull_GOH_prony_sampled_accelerations"
                           % (E // 1000),
-                    elem_bytes=eb, flop=None, kernel="k_elem<float,C3D4,GOH+Prony>",
+                    alg_bytes=eb, flop=None, kernel="k_elem<float,C3D4,GOH+Prony>",
                     material="shell rigid (material 0); core GOH mu=1kPa k1=5kPa k2=10 "
                              "kappa=0.1 lambda=2.19e8 + Prony g1=0.6 tau1=6ms; 6 records at 10 kHz")
     if name == "ensemble":
@@ -266,65 +275,74 @@ def make_workload(name, size=None):
         inst = dict(node_offset=off, tmax=np.full(n, 1e300), reduction=np.full(n, 0.9))
         return dict(mesh=mesh, mats=mats, loads=loads, instances=inst,
                     label="ensemble_%d_ogden_hex8_blocks_4k_250k" % n,
-                    elem_bytes=E * ELEM_BYTES_PER_EL + N * ELEM_BYTES_PER_NODE,
+                    alg_bytes=E * ALG_BYTES_PER_EL_C3D8 + N * ALG_BYTES_PER_NODE,
                     flop=FLOP_PER_EL_OGDEN * E, kernel="k_elem<float,C3D8,Ogden> (all instances)",
                     material="ogden per instance mu~U[0.5,5]kPa alpha~U[-5,8] K~U[2,50]MPa")
     raise SystemExit("unknown workload " + name)
 
 
-def surrogate_compare(args, dev):
+def surrogate_summary(dev, size=None, steps=1000, warmup=20, samples=10_000_000, epochs=3,
+                      trust_e2=0.04):
     """Head-like mesh: plain mixed path vs the learned surrogate for the GOH +
     Prony core, same steps, both against an FP64 run of the plain path (the
-    FP64 GPU path matches the CPU oracle to ~1e-13 in the parity tests)."""
+    FP64 GPU path matches the CPU oracle to ~1e-13 in the parity tests).
+    The network is trained on the GPU first (its time is reported, not timed
+    in the rates)."""
     import torch
     import femtech_gb300 as ft
     from femtech_gb300.surrogate import Surrogate
-    wl = make_workload("head", args.size)
+    wl = make_workload("head", size)
     mesh, mats, loads = wl["mesh"], wl["mats"], wl["loads"]
     E = len(mesh["etype"])
     props7 = list(mats["properties"].reshape(-1, 9)[1])
     t0 = time.perf_counter()
     s = Surrogate(props7, device=dev, seed=1)
-    s.generate(args.train_samples, seed=2)
-    loss = s.train(epochs=args.train_epochs, batch=8192, lr=2e-3)
+    s.generate(samples, seed=2)
+    loss = s.train(epochs=epochs, batch=8192, lr=2e-3)
     torch.cuda.synchronize(dev)
     t_train = time.perf_counter() - t0
     res = {}
-    total = args.warmup + args.steps
     for name in ("plain", "surrogate", "fp64"):
         m = ft.Model(mesh, mats, precision=ft.FP64 if name == "fp64" else ft.MIXED, device=dev,
                      loads=loads)
         if name == "surrogate":
-            m.set_surrogate(s, trust_e2=args.trust_e2)
+            m.set_surrogate(s, trust_e2=trust_e2)
         m.init_explicit(0.9, 0.0, 1e300)
-        m.run(args.warmup)
-        steps, ms = timed_run(m, args.steps)
-        res[name] = dict(steps=steps, ms=ms, u=m.state()["u"],
-                         value=E * steps / (ms / 1e3))
+        m.run(warmup)
+        k, ms = timed_run(m, steps)
+        res[name] = dict(steps=k, ms=ms, u=m.state()["u"], value=E * k / (ms / 1e3))
         m.close()
+    s.close()
     ref = res["fp64"]["u"]
 
     def rel(a):
         return float(np.linalg.norm(a - ref) / max(np.linalg.norm(ref), 1e-300))
 
+    return {"workload": wl["label"], "elements": E, "steps": steps, "warmup": warmup,
+            "value": res["surrogate"]["value"], "unit": "element-updates/s",
+            "ms_per_step": res["surrogate"]["ms"] / max(steps, 1),
+            "plain_value": res["plain"]["value"],
+            "speedup_vs_plain": res["surrogate"]["value"] / res["plain"]["value"],
+            "rel_disp_err_vs_fp64": rel(res["surrogate"]["u"]),
+            "plain_mixed_rel_disp_err_vs_fp64": rel(res["plain"]["u"]),
+            "fp64_value": res["fp64"]["value"], "trust_e2": trust_e2,
+            "train_samples": samples, "epochs": epochs, "final_batch_mse": loss,
+            "train_s": t_train}
+
+
+def surrogate_compare(args, dev):
+    r = surrogate_summary(dev, args.size, args.steps, args.warmup, args.train_samples,
+                          args.train_epochs, args.trust_e2)
     line = {
-        "metric": "element-updates/s", "value": res["surrogate"]["value"],
-        "unit": "element-updates/s", "n_gpus": 1, "steps": res["surrogate"]["steps"],
-        "warmup": args.warmup, "ms_per_step": res["surrogate"]["ms"] / max(args.steps, 1),
+        "metric": "element-updates/s", "value": r["value"], "unit": "element-updates/s",
+        "n_gpus": 1, "steps": r["steps"], "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "bf16 surrogate MLP (fp32 accumulate) / f32 element kernels / f64 nodal state",
         "data": "synthetic (seeded, generated in-run)",
-        "config": {"workload": wl["label"] + "_surrogate", "elements": E, "total_steps": total,
-                   "trust_e2": args.trust_e2},
-        "surrogate": {"train_samples": args.train_samples, "epochs": args.train_epochs,
-                      "final_batch_mse": loss, "train_s": t_train,
-                      "plain_value": res["plain"]["value"],
-                      "speedup_vs_plain": res["surrogate"]["value"] / res["plain"]["value"],
-                      "rel_disp_err_vs_fp64": rel(res["surrogate"]["u"]),
-                      "plain_mixed_rel_disp_err_vs_fp64": rel(res["plain"]["u"]),
-                      "fp64_value": res["fp64"]["value"]},
+        "config": {"workload": r["workload"] + "_surrogate", "elements": r["elements"],
+                   "total_steps": args.warmup + args.steps, "trust_e2": args.trust_e2},
+        "surrogate": r,
     }
-    s.close()
     print(json.dumps(line), flush=True)
 
 
@@ -337,6 +355,8 @@ def main():
     ap.add_argument("--workload", default="block",
                     choices=["block", "head", "head-impact", "ensemble"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the mixed-vs-FP64 displacement error of the block workload")
     ap.add_argument("--size", default=None,
                     help="block: nx,ny,nz; head: target elements; ensemble: instances")
     ap.add_argument("--injury", action="store_true",
@@ -346,6 +366,8 @@ def main():
                     help="track the energy balance (CheckEnergy) in the loop (single instance)")
     ap.add_argument("--surrogate", action="store_true",
                     help="head workload: plain vs learned surrogate vs FP64")
+    ap.add_argument("--no-surrogate", action="store_true",
+                    help="block workload: skip the surrogate arm (head-like mesh) of the line")
     ap.add_argument("--train-samples", type=int, default=10_000_000)
     ap.add_argument("--train-epochs", type=int, default=3)
     ap.add_argument("--trust-e2", type=float, default=0.04)
@@ -411,23 +433,44 @@ def main():
     elem_ms = em.value / max(sd.value, 1)
     node_ms = nm.value / max(sd.value, 1)
     hbm, peak_kind = peaks()
-    elem_bytes = wl["elem_bytes"]
+    alg_bytes = wl["alg_bytes"]  # one step = one launch of each pass
     node_bytes = N * NODE_BYTES_PER_NODE
     if elem_ms >= node_ms:
-        dom, dom_ms, dom_bytes = wl["kernel"] + " (one element pass)", elem_ms, elem_bytes
+        dom, dom_ms = wl["kernel"] + " (one element pass)", elem_ms
+        traffic = load_traffic(args.workload, E)
     else:
-        dom, dom_ms, dom_bytes = "k_node_step<float> fused update", node_ms, node_bytes
-    achieved = dom_bytes / (dom_ms / 1e3) / 1e9
-    traffic = load_traffic(args.workload, E) if dom_ms == elem_ms else None
-    sm_mhz = clocks.get("sm_mhz") or 2070.0
-    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+        dom, dom_ms, traffic = "k_node_step<float> fused update", node_ms, None
+    # the per-element-update algorithmic bytes over the dominant pass's time
+    achieved = alg_bytes / (dom_ms / 1e3) / 1e9
     fp32 = None
+    binding = "hbm"
     if wl["flop"]:
+        fp32_peak, fp32_src = fp32_peak_tflops(dev)
         fp32_ach = wl["flop"] / (elem_ms / 1e3) / 1e12
         fp32 = {"achieved": fp32_ach, "peak": fp32_peak, "unit": "TFLOP/s",
-                "frac": fp32_ach / fp32_peak,
-                "peak_source": "nominal 152 SM x 128 lanes x 2 x median SM clock",
+                "frac": fp32_ach / fp32_peak, "peak_source": fp32_src,
                 "flop_per_element": wl["flop"] / E}
+        # the roof that binds: the larger of the two lower bounds on time
+        t_hbm = alg_bytes / (hbm * 1e9)
+        t_fp32 = wl["flop"] / (fp32_peak * 1e12)
+        binding = "fp32" if t_fp32 > t_hbm else "hbm"
+        fp32["roof_ms"] = t_fp32 * 1e3
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
+                "unit": "GB/s", "frac": achieved / hbm, "peak_source": peak_kind,
+                "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes,
+                "algorithmic_bytes_per_element_update": alg_bytes / E,
+                "launch_ms": dom_ms, "hbm_roof_ms": alg_bytes / (hbm * 1e9) * 1e3,
+                "binding_roof": binding,
+                "elem_pass_ms": elem_ms, "node_pass_ms": node_ms,
+                "node_pass_algorithmic_gbs": node_bytes / (node_ms / 1e3) / 1e9,
+                "node_pass_frac": node_bytes / (node_ms / 1e3) / 1e9 / hbm,
+                "step_algorithmic_gbs": alg_bytes / (ms / max(steps, 1) / 1e3) / 1e9,
+                "fp32": fp32}
+    if traffic is not None and "C3D8" in wl["kernel"]:
+        roofline["traffic_note"] = (
+            "measured DRAM bytes of one element pass (ncu, scaled per element); they include "
+            "the %d B/element Gauss-point geometry table and the slot replicas, which are "
+            "overheads of this design, not algorithmic bytes" % GEO_TABLE_BYTES_PER_EL)
 
     # ---- end to end through the C ABI with host buffers ----
     e2e = end_to_end(ft, wl, dev, args.steps, E, N)
@@ -450,16 +493,18 @@ def main():
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "gpu_launches": launches,
         "clocks": clocks,
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
-                     "unit": "GB/s", "frac": achieved / hbm, "peak_source": peak_kind,
-                     "traffic": traffic, "algorithmic_bytes_per_launch": dom_bytes,
-                     "launch_ms": dom_ms, "elem_pass_ms": elem_ms, "node_pass_ms": node_ms,
-                     "node_pass_algorithmic_gbs": node_bytes / (node_ms / 1e3) / 1e9,
-                     "fp32": fp32},
+        "roofline": roofline,
         "e2e": e2e,
     }
+    if args.workload == "block" and not args.no_accuracy:
+        acc = accuracy_vs_fp64(dev)
+        line["rel_disp_err_vs_fp64"] = acc["rel_disp_err"]
+        line["accuracy"] = acc
     if rank == 0 and world == 1 and not args.no_cpu_baseline and args.workload == "block":
         line["cpu_baseline"] = cpu_reference_rate(os.cpu_count() or 1)
+    if rank == 0 and world == 1 and args.workload == "block" and not args.no_surrogate:
+        # the metric's second arm: the learned surrogate on the head-like mesh
+        line["surrogate"] = surrogate_summary(dev, steps=1000, warmup=20)
     if args.energy:
         line["energy"] = model.energy()
     if args.injury:
@@ -471,6 +516,52 @@ def main():
     model.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def fp32_peak_tflops(dev):
+    """Measured FP32 FMA rate of this GPU (the library's FMA-chain probe,
+    CUDA events, best of five launches)."""
+    import ctypes as C
+    import femtech_gb300 as ft
+    L = ft.lib()
+    L.ftgpu_fp32_fma_peak.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    tf, msb = C.c_double(), C.c_double()
+    ft._check(L.ftgpu_fp32_fma_peak(int(dev), C.byref(tf), C.byref(msb)))
+    return tf.value, "measured (ftgpu_fp32_fma_peak: FMA chains on every SM, CUDA events)"
+
+
+def accuracy_vs_fp64(dev, steps=5000, every=100):
+    """Relative nodal-displacement error of the mixed path against the FP64
+    path, max over outputs every `every` steps, on a 40x40x20 sub-block of the
+    block workload (same spacing, jitter, law and loads) for the
+    configuration's full 5000 steps.  The FP64 GPU path matches the CPU
+    oracle on this sub-block to <= 1e-5 over 2000 steps
+    (tests/test_gpu_scale_accuracy.py)."""
+    import femtech_gb300 as ft
+    sub = (40, 40, 20)
+    mesh, mats, loads = build_workload(sub[0], sub[1], sub[2], LX * sub[0] / NX,
+                                       LY * sub[1] / NY, LZ * sub[2] / NZ)
+    outs = {}
+    for name, prec in (("mixed", ft.MIXED), ("fp64", ft.FP64)):
+        m = ft.Model(mesh, mats, precision=prec, device=dev, loads=loads)
+        m.init_explicit(reduction=0.9, failure_dt=0.0, tmax=1e300)
+        us = []
+        for _ in range(steps // every):
+            m.run(every)
+            us.append(m.state()["u"])
+        if name == "mixed":
+            e9 = m.element_strain()[0]
+            two_e = 2.0 * np.linalg.norm(e9, axis=1)
+        outs[name] = us
+        m.close()
+    errs = [float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+            for a, b in zip(outs["mixed"], outs["fp64"])]
+    k = int(np.argmax(errs))
+    return {"rel_disp_err": max(errs), "at_step": (k + 1) * every, "final": errs[-1],
+            "case": "%dx%dx%d sub-block (%d C3D8, same spacing/jitter/law/loads), mixed vs FP64 "
+                    "on the GPU, %d steps, u every %d" % (sub + (len(mesh["etype"]), steps, every)),
+            "share_2E_above_0.04": float((two_e > 0.04).mean()),
+            "share_2E_above_0.2": float((two_e > 0.2).mean())}
 
 
 def timed_run(model, steps):

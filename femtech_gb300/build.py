@@ -18,7 +18,7 @@ LIB = os.path.join(HERE, "libftgpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["ft_elem_f32.cu", "ft_elem_f64.cu", "ft_api.cu", "ft_patches.cpp", "ft_noalloc.cu",
-           "ft_mlp.cu", "ft_meshio.cpp", "ft_vtu.cpp"]
+           "ft_mlp.cu", "ft_meshio.cpp", "ft_vtu.cpp", "ft_probe.cu"]
 
 
 def nvcc():

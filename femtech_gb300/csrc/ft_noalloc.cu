@@ -14,10 +14,12 @@
 // library holds that array until the process exits.  Host code cannot use
 // the array's name as a device address, so the first call on each device
 // looks the address up with cudaGetSymbolAddress (with that device current)
-// and passes it to the kernels; make that first call before any stream
-// capture.  All calls share the one array: two calls that overlap on the GPU
-// (different streams, or different host threads) race on it and must be
-// serialised by the caller.
+// and passes it to the kernels.  The address is cached per device index for
+// the life of that device's primary context: after cudaDeviceReset it is
+// stale.  Every call reads the error word back and waits for its stream, so
+// the call cannot be captured into a CUDA graph.  All calls share the one
+// array: two calls that overlap on the GPU (different streams, or different
+// host threads) race on it and must be serialised by the caller.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -29,7 +31,9 @@ namespace ftgpu {
 
 static __device__ __align__(256) double g_noalloc_corner_force[FTGPU_NOALLOC_MAX_ELEMENTS * 24];
 
-// The error word of the element pass also lives in static device memory.
+// The error word of the call also lives in static device memory: bit 0 = an
+// inverted or non-finite element, bit 1 = a node -> corner entry outside
+// [0, 8 * nelements).
 static __device__ int g_noalloc_bad;
 
 constexpr int kNoAllocMaxDevices = 64;
@@ -70,13 +74,21 @@ __global__ void k_noalloc_hex(int nelements, const double *X, const int *conn, c
 }
 
 // One thread per node: fi = sum of its corners, in the caller's CSR order.
-__global__ void k_noalloc_gather(int nNodes, const int *ptr, const int *ent, const double *corner,
-                                 double *fi) {
+// An entry outside this call's corners is skipped and flagged (bit 1), so a
+// bad map can neither read another call's leftovers nor run off the array.
+__global__ void k_noalloc_gather(int nNodes, int nelements, const int *ptr, const int *ent,
+                                 const double *corner, double *fi, int *bad_out) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= nNodes) return;
   double s0 = 0.0, s1 = 0.0, s2 = 0.0;
-  for (int k = ptr[n]; k < ptr[n + 1]; ++k) {
-    const long long c = 3ll * ent[k];
+  const int k1 = ptr[n + 1];
+  for (int k = ptr[n]; k < k1; ++k) {
+    const int c8 = ent[k];
+    if (c8 < 0 || c8 >= 8 * nelements) {
+      atomicOr(bad_out, 2);
+      continue;
+    }
+    const long long c = 3ll * c8;
     s0 += corner[c];
     s1 += corner[c + 1];
     s2 += corner[c + 2];
@@ -121,29 +133,36 @@ extern "C" int ftgpu_hex8_force_noalloc(int nNodes, int nelements, const double 
     scratch = g_noalloc_ptr[dev];
     bad = g_noalloc_bad_ptr[dev];
   }
+  // Parameters as the model's set-up builds them for FP64 mode; Ogden in
+  // FP64 always takes the eigen-decomposition (ser_thr2 = 0, no series).
   MatP<double> mp;
   memset(&mp, 0, sizeof(mp));
   for (int k = 0; k < 9; ++k) mp.p[k] = properties[k];
   mp.K = properties[2] + 2.0 * properties[1] / 3.0;
   mp.mat = materialID;
+  mp.ser_thr2 = 0.0;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (cudaMemsetAsync(bad, 0, sizeof(int), s) != cudaSuccess) return FTGPU_ERR_CUDA;
   const int th = 128, nb = (nelements + th - 1) / th;
+  // One case per law of StressUpdate.cpp:7-27 (plus Ogden); the two
+  // viscoelastic laws were rejected above.
   switch (materialID) {
     case 0: k_noalloc_hex<0><<<nb, th, 0, s>>>(nelements, coordinates, connectivity, u, mp, scratch, bad); break;
     case 1: k_noalloc_hex<1><<<nb, th, 0, s>>>(nelements, coordinates, connectivity, u, mp, scratch, bad); break;
     case 2: k_noalloc_hex<2><<<nb, th, 0, s>>>(nelements, coordinates, connectivity, u, mp, scratch, bad); break;
     case 3: k_noalloc_hex<3><<<nb, th, 0, s>>>(nelements, coordinates, connectivity, u, mp, scratch, bad); break;
     case 4: k_noalloc_hex<4><<<nb, th, 0, s>>>(nelements, coordinates, connectivity, u, mp, scratch, bad); break;
-    default: k_noalloc_hex<6><<<nb, th, 0, s>>>(nelements, coordinates, connectivity, u, mp, scratch, bad); break;
+    case 6: k_noalloc_hex<6><<<nb, th, 0, s>>>(nelements, coordinates, connectivity, u, mp, scratch, bad); break;
+    default: return FTGPU_ERR_MATERIAL;
   }
   if (cudaGetLastError() != cudaSuccess) return FTGPU_ERR_CUDA;
-  k_noalloc_gather<<<(nNodes + 255) / 256, 256, 0, s>>>(nNodes, node_elem_ptr, node_elem_ent,
-                                                        scratch, fi);
+  k_noalloc_gather<<<(nNodes + 255) / 256, 256, 0, s>>>(nNodes, nelements, node_elem_ptr,
+                                                        node_elem_ent, scratch, fi, bad);
   if (cudaGetLastError() != cudaSuccess) return FTGPU_ERR_CUDA;
   int hbad = 0;
   if (cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
       cudaStreamSynchronize(s) != cudaSuccess)
     return FTGPU_ERR_CUDA;
+  if (hbad & 2) return FTGPU_ERR_INPUT;
   return hbad ? FTGPU_ERR_INVERTED : FTGPU_OK;
 }

@@ -222,6 +222,12 @@ int ftgpu_run_timed(ftgpu_model *m, int max_steps, int *steps_done, double *devi
 int ftgpu_run_profiled(ftgpu_model *m, int max_steps, int *steps_done, double *elem_ms,
                        double *node_ms);
 
+/* Measured FP32 FMA throughput of `device` (TFLOP/s, FMA = 2 flops): 16
+ * independent FMA chains per thread on every SM, best of five launches timed
+ * with CUDA events.  The denominator of the element pass's FP32 fraction
+ * (no counterpart in the reference, which has no GPU code). */
+int ftgpu_fp32_fma_peak(int device, double *tflops, double *ms_best);
+
 /* Number of element patches (thread blocks of one element pass) and of node
  * slots (patch-local node replicas): the sizes the traffic model uses. */
 int ftgpu_layout_info(ftgpu_model *m, long long *npatch, long long *nslots, int *ngroups);
@@ -374,14 +380,18 @@ int ftgpu_set_surrogate(ftgpu_model *m, ftgpu_surrogate *s, double trust_e2);
  * internal force fi of one material on caller-owned DEVICE arrays in the
  * reference layout -- coordinates[3*nNodes], connectivity[8*nelements],
  * u[3*nNodes], and the node -> element-corner map node_elem_ptr[nNodes+1] /
- * node_elem_ent[8*nelements] (entries e*8+corner, summed in the given
- * order) -- written to fi[3*nNodes] (device).  properties: 9 host doubles.
- * Materials 0-4 and 6 (the viscoelastic laws need per-call state).  No
- * cudaMalloc/cudaFree: the corner-force scratch is a static device array
- * holding FTGPU_NOALLOC_MAX_ELEMENTS elements; larger meshes are rejected
- * with FTGPU_ERR_INPUT.  The first call on a device looks up that array's
- * address (make it before any stream capture).  All calls share the array,
- * so calls that overlap on the GPU race; the call waits for its stream. */
+ * node_elem_ent[8*nelements] (entries e*8+corner in [0, 8*nelements),
+ * summed in the given order; an entry outside that range returns
+ * FTGPU_ERR_INPUT) -- written to fi[3*nNodes] (device).  properties: 9 host
+ * doubles.  Materials 0, 1, 2, 3, 4 and 6 in FP64; 5 and 7 (they carry
+ * viscoelastic history between calls) return FTGPU_ERR_INPUT, any other ID
+ * FTGPU_ERR_MATERIAL.  No cudaMalloc/cudaFree: the corner-force scratch is a
+ * static device array holding FTGPU_NOALLOC_MAX_ELEMENTS elements; larger
+ * meshes are rejected with FTGPU_ERR_INPUT.  The first call on a device
+ * looks up that array's address, which stays valid for the life of the
+ * device's primary context.  The call reads its error word back and waits
+ * for its stream, so it cannot be captured into a CUDA graph.  All calls
+ * share the array, so calls that overlap on the GPU race. */
 #define FTGPU_NOALLOC_MAX_ELEMENTS 32768
 int ftgpu_hex8_force_noalloc(int nNodes, int nelements, const double *coordinates,
                              const int *connectivity, const int *node_elem_ptr,

@@ -152,10 +152,14 @@ class _Model(C.Structure):
 
 
 def reference_tree():
-    """The reference checkout the checker is built from (FEMTECH_REFERENCE,
-    default as in build()), or None where it does not exist."""
-    ref = os.environ.get("FEMTECH_REFERENCE", "/root/reference")
-    return ref if os.path.isdir(os.path.join(ref, "src")) else None
+    """The reference checkout the checker is built from ($FEMTECH_REFERENCE,
+    else the Makefile's default), or None where it does not exist."""
+    ref = os.environ.get("FEMTECH_REFERENCE")
+    if not ref:
+        out = subprocess.run(["make", "-s", "-C", HERE, "print-ref"], capture_output=True,
+                             text=True)
+        ref = out.stdout.strip() if out.returncode == 0 else ""
+    return ref if ref and os.path.isdir(os.path.join(ref, "src")) else None
 
 
 def build(quiet=True):
@@ -163,8 +167,8 @@ def build(quiet=True):
     out = subprocess.run(["make", "-C", HERE, "liboracle.so"], capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
-    ref = os.environ.get("FEMTECH_REFERENCE", "/root/reference")
-    if os.path.isdir(os.path.join(ref, "src")):
+    ref = reference_tree()
+    if ref:
         out = subprocess.run(["make", "-C", HERE, "-j8", "ref", "REF=" + ref],
                              capture_output=True, text=True)
         if out.returncode != 0:

@@ -1,7 +1,7 @@
 """Generate the golden fixtures in tests/golden/ from the reference itself.
 
-Run in a checkout where the reference tree exists (default /root/reference,
-override with FEMTECH_REFERENCE): it builds the reference's own hot-path
+Run in a checkout where the reference tree exists (the oracle Makefile's
+default, or FEMTECH_REFERENCE): it builds the reference's own hot-path
 sources into oracle/_ref/libfemtech_ref.so (oracle/Makefile) and records their
 outputs on small seeded inputs.  The fixtures are committed; tests never need
 the reference tree.
@@ -58,7 +58,9 @@ sys.path.insert(0, ROOT)
 from femtech_gb300 import meshgen as mg  # noqa: E402
 from oracle import oracle as orc  # noqa: E402
 
-REF = os.environ.get("FEMTECH_REFERENCE", "/root/reference")
+# the reference checkout (None where absent: the mesh builders below are
+# imported by tests that do not need it)
+REF = orc.reference_tree()
 
 MATS = {
     1: [1000.0, 3400.0, 2.0e6],
@@ -361,6 +363,8 @@ def cube_case():
 
 
 def main():
+    if REF is None:
+        raise SystemExit("no reference tree: set FEMTECH_REFERENCE to a FemTech checkout")
     orc.build()
     if not orc.RefBuild.available():
         raise SystemExit("reference build missing")

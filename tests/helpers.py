@@ -52,3 +52,21 @@ def random_fibers(E, seed=0):
 def rel(a, b):
     a, b = np.asarray(a), np.asarray(b)
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def run_to(m, tmax, reduction, out_every, max_steps=10**7):
+    """Run a model's device loop, pausing every out_every steps to record u;
+    returns (u at each full pause, their times, steps run, final state)."""
+    m.init_explicit(reduction=reduction, failure_dt=0.0, tmax=tmax)
+    us, ts = [], []
+    total = 0
+    while total < max_steps:
+        k = m.run(min(out_every, max_steps - total))
+        total += k
+        s = m.state()
+        if k == out_every:
+            us.append(s["u"])
+            ts.append(s["time"])
+        if k < out_every:
+            break
+    return np.array(us), np.array(ts), total, m.state()

@@ -9,26 +9,9 @@ import pytest
 
 import femtech_gb300 as ft
 from femtech_gb300 import meshgen as mg
-from helpers import MATS, ex9_mesh_loads, rel
+from helpers import MATS, ex9_mesh_loads, rel, run_to
 
 pytestmark = pytest.mark.gpu
-
-
-def run_to(m, tmax, reduction, out_every, max_steps=10**7):
-    """Run the device loop, pausing every out_every steps to record u."""
-    m.init_explicit(reduction=reduction, failure_dt=0.0, tmax=tmax)
-    us, ts = [], []
-    total = 0
-    while total < max_steps:
-        k = m.run(out_every)
-        total += k
-        s = m.state()
-        if k == out_every:
-            us.append(s["u"])
-            ts.append(s["time"])
-        if k < out_every:
-            break
-    return np.array(us), np.array(ts), total, m.state()
 
 
 @pytest.mark.parametrize("prec,tol", [(ft.FP64, 1e-5), (ft.MIXED, 1e-3)])
