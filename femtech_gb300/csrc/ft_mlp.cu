@@ -813,6 +813,8 @@ __global__ void __maxnreg__(128)
                  : "memory");
 }
 
+#include "ft_gemm_tc.cuh"
+
 }  // namespace ftgpu
 
 using namespace ftgpu;
@@ -835,12 +837,15 @@ struct ftgpu_surrogate {
        *dZ3 = nullptr;
   long long adam_t = 0;
   int *derr = nullptr;  // device error word of standalone inference calls
+  float *part = nullptr;  // split-K partial tiles of the weight gradients
+  long long part_cap = 0;
+  int tensor_cores = 1;   // training GEMMs: 1 tcgen05 (k_gemm_tc), 0 mma.sync (k_gemm)
   std::string err;
   ~ftgpu_surrogate() {
     for (void *p : {(void *)P, (void *)G, (void *)Mo, (void *)V, (void *)Wb, (void *)X, (void *)T,
                     (void *)Z1, (void *)Z2, (void *)Z3, (void *)Y, (void *)rowloss, (void *)loss,
                     (void *)H1, (void *)H2, (void *)H3, (void *)dY, (void *)dZ1, (void *)dZ2,
-                    (void *)dZ3, (void *)derr})
+                    (void *)dZ3, (void *)derr, (void *)part})
       if (p) cudaFree(p);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -879,15 +884,43 @@ int ensure_batch(ftgpu_surrogate *s, long long B) {
   r |= dalloc(&s->dZ1, B * kMlpHid) | dalloc(&s->dZ2, B * kMlpHid) | dalloc(&s->dZ3, B * kMlpHid);
   r |= dalloc(&s->Y, B * kMlpOut) | dalloc(&s->dY, B * kMlpOut) | dalloc(&s->rowloss, B);
   r |= dalloc(&s->loss, 1);
+  // split-K partial tiles of the weight gradients: K slices of 256 rows, tiles <= 128 x 128
+  const long long pc = ((B + 255) / 256) * 128 * 128;
+  if (pc > s->part_cap) {
+    r |= dalloc(&s->part, pc);
+    s->part_cap = pc;
+  }
   if (r) return FTGPU_ERR_ALLOC;
   s->cap = B;
   return 0;
 }
 
+// One training GEMM: on the tensor cores (k_gemm_tc: 128-row tiles, weight
+// gradients split over K in slices of 256 batch rows and summed in slice
+// order), or on the warp-level mma.sync kernel (the cross-check path).
 template <int EPI>
-int gemm(cudaStream_t st, const GemmArgs &g) {
-  dim3 grid((unsigned)((g.M + 63) / 64), (unsigned)((g.N + 31) / 32));
-  k_gemm<EPI><<<grid, 128, 0, st>>>(g);
+int gemm(ftgpu_surrogate *s, cudaStream_t st, const GemmArgs &g) {
+  if (!s->tensor_cores) {
+    dim3 grid((unsigned)((g.M + 63) / 64), (unsigned)((g.N + 31) / 32));
+    k_gemm<EPI><<<grid, 128, 0, st>>>(g);
+    return cudaGetLastError() == cudaSuccess ? 0 : FTGPU_ERR_CUDA;
+  }
+  const int Npad = (g.N + 15) / 16 * 16;
+  if (Npad > 128 || g.M <= 0 || g.K <= 0) return FTGPU_ERR_INPUT;
+  const int mt = (g.M + 127) / 128;
+  int slices = 1, kslice = g.K;
+  if (EPI == kEpiStore && mt == 1 && g.K > 512) {
+    kslice = 256;
+    slices = (g.K + kslice - 1) / kslice;
+    if ((long long)slices * g.M * g.N > s->part_cap) return FTGPU_ERR_INPUT;
+  }
+  k_gemm_tc<EPI><<<dim3((unsigned)mt, (unsigned)slices), tcg::kThreads, tcg::kSmem, st>>>(
+      g, Npad, kslice, slices > 1 ? s->part : nullptr, s->derr);
+  if (slices > 1) {
+    const long long n = (long long)g.M * g.N;
+    k_splitk_reduce<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(s->part, slices, g.M, g.N, g.C,
+                                                                g.scm, g.scn);
+  }
   return cudaGetLastError() == cudaSuccess ? 0 : FTGPU_ERR_CUDA;
 }
 
@@ -905,16 +938,16 @@ int forward(ftgpu_surrogate *s, const bf16 *X, long long B) {
   const float *P = s->P;
   GemmArgs g = ga((int)B, kMlpHid, kMlpIn, X, kMlpIn, 1, W + kOffW0, 1, kMlpIn);
   g.bias = P + kOffB0; g.Z = s->Z1; g.H = s->H1;
-  int r = gemm<kEpiBiasSilu>(s->stream, g);
+  int r = gemm<kEpiBiasSilu>(s, s->stream, g);
   g = ga((int)B, kMlpHid, kMlpHid, s->H1, kMlpHid, 1, W + kOffW1, 1, kMlpHid);
   g.bias = P + kOffB1; g.Z = s->Z2; g.H = s->H2;
-  r |= gemm<kEpiBiasSilu>(s->stream, g);
+  r |= gemm<kEpiBiasSilu>(s, s->stream, g);
   g = ga((int)B, kMlpHid, kMlpHid, s->H2, kMlpHid, 1, W + kOffW2, 1, kMlpHid);
   g.bias = P + kOffB2; g.Z = s->Z3; g.H = s->H3;
-  r |= gemm<kEpiBiasSilu>(s->stream, g);
+  r |= gemm<kEpiBiasSilu>(s, s->stream, g);
   g = ga((int)B, kMlpOut, kMlpHid, s->H3, kMlpHid, 1, W + kOffW3, 1, kMlpHid);
   g.bias = P + kOffB3; g.C = s->Y; g.scm = kMlpOut; g.scn = 1;
-  r |= gemm<kEpiBias>(s->stream, g);
+  r |= gemm<kEpiBias>(s, s->stream, g);
   return r;
 }
 
@@ -929,31 +962,31 @@ int backward(ftgpu_surrogate *s, const bf16 *X, const float *T, long long B) {
   // layer 3: dW3 = dY^T H3, db3, dZ3 = (dY W3) * silu'(Z3)
   GemmArgs g = ga(kMlpOut, kMlpHid, (int)B, s->dY, 1, kMlpOut, s->H3, kMlpHid, 1);
   g.C = G + kOffW3; g.scm = kMlpHid; g.scn = 1;
-  r |= gemm<kEpiStore>(st, g);
+  r |= gemm<kEpiStore>(s, st, g);
   k_colsum<<<kMlpOut, 256, 0, st>>>(s->dY, B, kMlpOut, G + kOffB3);
   g = ga((int)B, kMlpHid, kMlpOut, s->dY, kMlpOut, 1, W + kOffW3, kMlpHid, 1);
   g.Zp = s->Z3; g.dZ = s->dZ3;
-  r |= gemm<kEpiSiluGrad>(st, g);
+  r |= gemm<kEpiSiluGrad>(s, st, g);
   // layer 2
   g = ga(kMlpHid, kMlpHid, (int)B, s->dZ3, 1, kMlpHid, s->H2, kMlpHid, 1);
   g.C = G + kOffW2; g.scm = kMlpHid; g.scn = 1;
-  r |= gemm<kEpiStore>(st, g);
+  r |= gemm<kEpiStore>(s, st, g);
   k_colsum<<<kMlpHid, 256, 0, st>>>(s->dZ3, B, kMlpHid, G + kOffB2);
   g = ga((int)B, kMlpHid, kMlpHid, s->dZ3, kMlpHid, 1, W + kOffW2, kMlpHid, 1);
   g.Zp = s->Z2; g.dZ = s->dZ2;
-  r |= gemm<kEpiSiluGrad>(st, g);
+  r |= gemm<kEpiSiluGrad>(s, st, g);
   // layer 1
   g = ga(kMlpHid, kMlpHid, (int)B, s->dZ2, 1, kMlpHid, s->H1, kMlpHid, 1);
   g.C = G + kOffW1; g.scm = kMlpHid; g.scn = 1;
-  r |= gemm<kEpiStore>(st, g);
+  r |= gemm<kEpiStore>(s, st, g);
   k_colsum<<<kMlpHid, 256, 0, st>>>(s->dZ2, B, kMlpHid, G + kOffB1);
   g = ga((int)B, kMlpHid, kMlpHid, s->dZ2, kMlpHid, 1, W + kOffW1, kMlpHid, 1);
   g.Zp = s->Z1; g.dZ = s->dZ1;
-  r |= gemm<kEpiSiluGrad>(st, g);
+  r |= gemm<kEpiSiluGrad>(s, st, g);
   // layer 0
   g = ga(kMlpHid, kMlpIn, (int)B, s->dZ1, 1, kMlpHid, X, kMlpIn, 1);
   g.C = G + kOffW0; g.scm = kMlpIn; g.scn = 1;
-  r |= gemm<kEpiStore>(st, g);
+  r |= gemm<kEpiStore>(s, st, g);
   k_colsum<<<kMlpHid, 256, 0, st>>>(s->dZ1, B, kMlpHid, G + kOffB0);
   if (cudaGetLastError() != cudaSuccess) return FTGPU_ERR_CUDA;
   return r;
@@ -1125,6 +1158,7 @@ int ftgpu_surrogate_train(ftgpu_surrogate *s, int epochs, int batch, double lr,
   const long long nb = s->nsamples / batch;
   double last = 0.0;
   const long long total = nb * epochs;
+  SCK(cudaMemsetAsync(s->derr, 0, sizeof(int), s->stream));
   for (int ep = 0; ep < epochs; ++ep) {
     double acc = 0.0;
     for (long long b = 0; b < nb; ++b) {
@@ -1151,7 +1185,18 @@ int ftgpu_surrogate_train(ftgpu_surrogate *s, int epochs, int batch, double lr,
     last = acc;
   }
   SCK(cudaStreamSynchronize(s->stream));
+  int e = 0;
+  SCK(cudaMemcpy(&e, s->derr, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) return record_error(FTGPU_ERR_CUDA, "tensor-core training GEMM gave up waiting");
   if (final_loss) *final_loss = last;
+  return FTGPU_OK;
+}
+
+// training GEMMs on tcgen05 (tensor_cores = 1, the default) or on the
+// warp-level mma.sync kernel (0)
+int ftgpu_surrogate_gemm_path(ftgpu_surrogate *s, int tensor_cores) {
+  if (!s || (tensor_cores != 0 && tensor_cores != 1)) return FTGPU_ERR_INPUT;
+  s->tensor_cores = tensor_cores;
   return FTGPU_OK;
 }
 
@@ -1166,8 +1211,12 @@ int ftgpu_surrogate_forward(ftgpu_surrogate *s, long long n, const float *x, flo
   bf16 *dX = nullptr;
   if (dalloc(&dX, n * kMlpIn)) return FTGPU_ERR_ALLOC;
   SCK(cudaMemcpy(dX, xb.data(), n * kMlpIn * 2, cudaMemcpyHostToDevice));
+  SCK(cudaMemset(s->derr, 0, sizeof(int)));
   r = forward(s, dX, n);
   SCK(cudaStreamSynchronize(s->stream));
+  int e = 0;
+  SCK(cudaMemcpy(&e, s->derr, sizeof(int), cudaMemcpyDeviceToHost));
+  if (!r && e) r = record_error(FTGPU_ERR_CUDA, "tensor-core training GEMM gave up waiting");
   SCK(cudaMemcpy(y, s->Y, n * kMlpOut * 4, cudaMemcpyDeviceToHost));
   cudaFree(dX);
   return r;
@@ -1221,9 +1270,13 @@ int ftgpu_surrogate_gradient(ftgpu_surrogate *s, long long n, const float *x, co
   if (dalloc(&dX, n * kMlpIn) || dalloc(&dT, n * kMlpOut)) return FTGPU_ERR_ALLOC;
   SCK(cudaMemcpy(dX, xb.data(), n * kMlpIn * 2, cudaMemcpyHostToDevice));
   SCK(cudaMemcpy(dT, t, n * kMlpOut * 4, cudaMemcpyHostToDevice));
+  SCK(cudaMemset(s->derr, 0, sizeof(int)));
   r = forward(s, dX, n);
   r |= backward(s, dX, dT, n);
   SCK(cudaStreamSynchronize(s->stream));
+  int e = 0;
+  SCK(cudaMemcpy(&e, s->derr, sizeof(int), cudaMemcpyDeviceToHost));
+  if (!r && e) r = record_error(FTGPU_ERR_CUDA, "tensor-core training GEMM gave up waiting");
   float hl = 0.f;
   SCK(cudaMemcpy(&hl, s->loss, 4, cudaMemcpyDeviceToHost));
   if (loss) *loss = hl / (double(n) * kMlpUsedOut);

@@ -39,6 +39,7 @@ def _bind():
     L.ftgpu_surrogate_num_params.restype = C.c_int
     L.ftgpu_surrogate_predict.argtypes = [vp, C.c_longlong, vp, vp, vp]
     L.ftgpu_surrogate_output_scale.argtypes = [vp, C.POINTER(C.c_double)]
+    L.ftgpu_surrogate_gemm_path.argtypes = [vp, C.c_int]
     return L
 
 
@@ -131,6 +132,11 @@ class Surrogate:
         loss = C.c_double()
         _check(self.L.ftgpu_surrogate_train(self.h, int(epochs), int(batch), float(lr), C.byref(loss)))
         return loss.value
+
+    def gemm_path(self, tensor_cores=True):
+        """Training GEMMs on tcgen05 with TMEM accumulators (True, the
+        default) or on the warp-level mma.sync kernel (False, a cross-check)."""
+        _check(self.L.ftgpu_surrogate_gemm_path(self.h, 1 if tensor_cores else 0))
 
     def forward(self, x):
         x = np.ascontiguousarray(x, np.float32)

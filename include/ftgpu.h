@@ -353,6 +353,11 @@ int ftgpu_surrogate_forward(ftgpu_surrogate *s, long long n, const float *x, flo
 int ftgpu_surrogate_infer(ftgpu_surrogate *s, long long n, const float *x, float *y);
 /* the same through a warp-level mma.sync kernel (a cross-check of the above) */
 int ftgpu_surrogate_infer_mma(ftgpu_surrogate *s, long long n, const float *x, float *y);
+/* Training GEMMs (forward, dX and dW of ftgpu_surrogate_train / _forward /
+ * _gradient) on the tcgen05 tensor cores with TMEM accumulators
+ * (tensor_cores = 1, the default) or on a warp-level mma.sync kernel (0, kept
+ * as a cross-check).  No counterpart in the reference (no learned parts). */
+int ftgpu_surrogate_gemm_path(ftgpu_surrogate *s, int tensor_cores);
 /* MSE loss and its gradient w.r.t. the FP32 parameter vector for one batch */
 int ftgpu_surrogate_gradient(ftgpu_surrogate *s, long long n, const float *x, const float *t,
                              float *grad, double *loss);

@@ -129,6 +129,31 @@ def test_tensor_core_gradient_matches_fp64_checker():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("n", [100, 3001])
+def test_tcgen05_training_gemms_match_mma_sync(n):
+    """Forward, dX and dW on tcgen05 (TMEM accumulators, weight gradients
+    split over K) against the warp-level mma.sync kernels: a batch below one
+    128-row tile and a ragged one over 12 K slices."""
+    from femtech_gb300.surrogate import Surrogate
+    s = Surrogate(PROPS7, seed=3)
+    rng = np.random.default_rng(7)
+    s.params = rand_params(rng).astype(np.float32)
+    x, t = rand_batch(rng, n)
+    out = {}
+    for tc in (True, False):
+        s.gemm_path(tc)
+        g, loss = s.gradient(x, t)
+        out[tc] = (g, loss, s.forward(x))
+    s.close()
+    (g1, l1, y1), (g0, l0, y0) = out[True], out[False]
+    assert abs(l1 - l0) <= 1e-4 * l0
+    assert np.abs(y1 - y0).max() <= 2e-3 * np.abs(y0).max()
+    for k, (a, b) in mo.OFF.items():
+        err = np.linalg.norm(g1[a:b] - g0[a:b]) / max(np.linalg.norm(g0[a:b]), 1e-30)
+        assert err < 5e-3, (k, err)
+
+
+@pytest.mark.gpu
 def test_training_samples_follow_the_plain_law():
     from femtech_gb300 import surrogate as sg
     s = sg.Surrogate(PROPS7, seed=4)
