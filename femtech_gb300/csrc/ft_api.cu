@@ -216,7 +216,9 @@ struct ftgpu_model {
   std::vector<std::unique_ptr<DBuf>> geo;  // per C3D8 group: Gauss-point A^{-1}, det A
   DBuf clock, dtmin, err, instp;
   DBuf stepsc, rottrig;  // per-instance step scalars / rotation trigonometry
-  DBuf stage;            // AoS staging of host <-> device state copies
+  DBuf stage;            // AoS staging of host <-> device state copies (u, v, a)
+  cudaStream_t cstream[3] = {};   // copy streams of the three state arrays
+  cudaEvent_t cev[3] = {};
   // injury criteria of the brain drivers (single instance only)
   bool injury_on = false;
   int inj_n = 0;
@@ -238,10 +240,19 @@ struct ftgpu_model {
   DBuf rb, rbtab, rbstate, rbstep;
   DBuf rig_list;                // driven nodes: a rigid-body or rigid-rotation DOF
   std::vector<int> rig_host;
+  // from the boundary table (upload_bc): nodes with a rigid-body or
+  // rigid-rotation DOF, and the nodes with a rigid-body DOF
+  std::vector<int> drv_nodes, rigid_nodes;
   long long rig_nodes = 0;
   cudaStream_t stream2 = nullptr;  // the driven-node branch of a step
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   DBuf slot_off, slots, slot4, slot4b, node_inst, nbc, fnsbuf;
+  // mixed-precision node pass split: k_node_free over every node not marked
+  // kNodeRest in nkind, k_node_step over rest_list (the marked ones)
+  std::vector<int> slot4_host;
+  std::vector<int> fn_owner;  // instance owning each boundary function, -1 none / shared
+  DBuf nkind, fnval, rest_list;
+  long long rest_n = 0;
   DBuf dX, u, v, a, vh, mass, minv, fi;
   DBuf gpF, gpJ, gpS;
   // graph of one chunk of steps (plain, and with timing events)
@@ -271,6 +282,10 @@ struct ftgpu_model {
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
     if (stream2) cudaStreamDestroy(stream2);
+    for (int k = 0; k < 3; ++k) {
+      if (cev[k]) cudaEventDestroy(cev[k]);
+      if (cstream[k]) cudaStreamDestroy(cstream[k]);
+    }
     if (stream) cudaStreamDestroy(stream);
   }
 };
@@ -350,6 +365,9 @@ NodeArgs node_args(ftgpu_model *m, int mode, int parity) {
   A.slot4b = m->slot4b.p ? m->slot4b.as<int4>() : nullptr;
   A.node_inst = m->ninst > 1 ? m->node_inst.as<int>() : nullptr;
   A.nbc = m->nbc.as<int16_t>();
+  A.nkind = m->nkind.p ? m->nkind.as<uint8_t>() : nullptr;
+  A.fnval = m->nkind.p ? m->fnval.as<double2>() : nullptr;
+  A.nfns = (int)m->fns.size();
   A.fns = m->fnsbuf.as<BcFn>();
   A.X = m->dX.as<double>();
   A.u = m->u.as<double>();
@@ -418,7 +436,8 @@ int launch_node(ftgpu_model *m, int mode, int parity) {
   if (step) {  // (with the fork, the rotation trigonometry moves to k_driven_step)
     NodeArgs S = A;
     if (fork) S.nrot = 0;
-    k_step_scalars<<<(unsigned)((m->ninst + 127) / 128), 128, 0, m->stream>>>(S);
+    const long long nth = std::max<long long>(m->ninst, A.nkind ? (long long)m->fns.size() : 0);
+    k_step_scalars<<<(unsigned)((nth + 127) / 128), 128, 0, m->stream>>>(S);
   }
   if (fork) {
     // fork: the driven nodes' motion (rigid bodies' integrator, rotation
@@ -444,7 +463,18 @@ int launch_node(ftgpu_model *m, int mode, int parity) {
       S.nrot = 0;
       k_driven_step<<<(unsigned)m->ninst, 32, 0, m->stream>>>(S);
     }
-    node_step(nb, m->stream, A);
+    if (!f64 && !en && A.nkind) {
+      // free nodes on their lean kernel, the rest through k_node_step's list
+      k_node_free<<<(unsigned)nb, th, 0, m->stream>>>(A);
+      if (m->rest_n > 0) {
+        NodeArgs B = A;
+        B.node_list = m->rest_list.as<int>();
+        B.nlist = m->rest_n;
+        node_step((m->rest_n + th - 1) / th, m->stream, B);
+      }
+    } else {
+      node_step(nb, m->stream, A);
+    }
   } else {
     if (mode == kNodeBegin && m->rigid_on)
       k_rigid_begin<<<(unsigned)m->ninst, 32, 0, m->stream>>>(A);
@@ -539,6 +569,64 @@ int ensure_stage(ftgpu_model *m) {
   return m->stage.alloc(b);
 }
 
+// Staging for the three state arrays at once, with a copy stream each.
+int ensure_stage3(ftgpu_model *m) {
+  const size_t b = 9 * (size_t)m->nNodes * sizeof(double);
+  if (m->stage.bytes < b) CKI(m->stage.alloc(b));
+  for (int k = 0; k < 3; ++k) {
+    if (!m->cstream[k]) CK(cudaStreamCreateWithFlags(&m->cstream[k], cudaStreamNonBlocking));
+    if (!m->cev[k]) CK(cudaEventCreateWithFlags(&m->cev[k], cudaEventDisableTiming));
+  }
+  return 0;
+}
+
+// u, v, a between AoS host arrays and the SoA device state in one call: each
+// array has its own staging third and copy stream, so the three host <->
+// device copies run side by side and overlap the transposes (which run on
+// the model's stream).  Null host arrays: zero (upload) / not read (download).
+int upload_state3(ftgpu_model *m, const double *const h[3], DBuf *const d[3]) {
+  const long long N = m->nNodes;
+  CKI(ensure_stage3(m));
+  CK(cudaEventRecord(m->cev[0], m->stream));  // the state is free to overwrite
+  for (int k = 0; k < 3; ++k) {
+    if (!h[k]) continue;
+    double *st = m->stage.as<double>() + 3 * N * k;
+    CK(cudaStreamWaitEvent(m->cstream[k], m->cev[0], 0));
+    CK(cudaMemcpyAsync(st, h[k], 3 * N * sizeof(double), cudaMemcpyHostToDevice, m->cstream[k]));
+  }
+  for (int k = 0; k < 3; ++k) {
+    if (!h[k]) {
+      CK(cudaMemsetAsync(d[k]->p, 0, 3 * N * sizeof(double), m->stream));
+      continue;
+    }
+    CK(cudaEventRecord(m->cev[k], m->cstream[k]));
+    CK(cudaStreamWaitEvent(m->stream, m->cev[k], 0));
+    k_aos_to_soa<<<(unsigned)((N + 255) / 256), 256, 0, m->stream>>>(
+        m->stage.as<double>() + 3 * N * k, d[k]->as<double>(), N);
+    CK(cudaGetLastError());
+  }
+  CK(cudaStreamSynchronize(m->stream));
+  return 0;
+}
+
+int download_state3(ftgpu_model *m, DBuf *const d[3], double *const h[3]) {
+  const long long N = m->nNodes;
+  CKI(ensure_stage3(m));
+  for (int k = 0; k < 3; ++k) {
+    if (!h[k]) continue;
+    k_soa_to_aos<<<(unsigned)((N + 255) / 256), 256, 0, m->stream>>>(
+        d[k]->as<double>(), m->stage.as<double>() + 3 * N * k, N);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(m->cev[k], m->stream));
+    CK(cudaStreamWaitEvent(m->cstream[k], m->cev[k], 0));
+    CK(cudaMemcpyAsync(h[k], m->stage.as<double>() + 3 * N * k, 3 * N * sizeof(double),
+                       cudaMemcpyDeviceToHost, m->cstream[k]));
+  }
+  for (int k = 0; k < 3; ++k)
+    if (h[k]) CK(cudaStreamSynchronize(m->cstream[k]));
+  return 0;
+}
+
 // AoS [3N] host -> SoA [3][N] device (h == NULL: zero)
 int upload_aos(ftgpu_model *m, const double *h, DBuf &d) {
   const long long N = m->nNodes;
@@ -614,7 +702,7 @@ int strain_groups_t(ftgpu_model *m, double *E6) {
   for (size_t gi = 0; gi < m->ps.groups.size(); ++gi) {
     const PatchGroup &g = m->ps.groups[gi];
     const ElemArgs<R> A = elem_args<R>(m, g, (int)gi);
-    const size_t smem = elem_smem_bytes_host<R>(g.etype, PE);
+    const size_t smem = strain_smem_bytes_host<R>();
     const int r = launch_strain<R>(g.etype, g.npatch, PE, smem, m->stream, A, E6);
     if (r) return fail(FTGPU_ERR_CUDA, std::string("element strain pass: ") +
                                            cudaGetErrorString((cudaError_t)r));
@@ -669,6 +757,46 @@ int upload_epid(ftgpu_model *m, bool zero_idle) {
   return m->epid.upload(w.data(), w.size());
 }
 
+// The instance of every node (empty node_off: one instance).
+static int instance_of(const ftgpu_model *m, long long n) {
+  if (m->node_off.size() < 2) return 0;
+  return (int)(std::upper_bound(m->node_off.begin(), m->node_off.end(), (int)n) -
+               m->node_off.begin()) - 1;
+}
+
+// The split of the mixed-precision node pass: k_node_free takes every node
+// whose constrained DOFs (if any) follow a fixed / ramp / sine function owned
+// by one instance (its value at the new time is evaluated once per step by
+// k_step_scalars, which also advances the instances' clocks) or hold; a node
+// without slots and a node with a rigid-rotation or rigid-body DOF go to
+// k_node_step over rest_list.
+int upload_split(ftgpu_model *m) {
+  const long long N = m->nNodes;
+  m->nkind.release();
+  m->rest_list.release();
+  m->rest_n = 0;
+  if (is_fp64(m) || (long long)m->slot4_host.size() != 4 * N) return 0;
+  std::vector<uint8_t> kind(N, 0);
+  if (!m->dof_fn.empty())
+    for (long long n = 0; n < N; ++n)
+      for (int d = 0; d < 3; ++d) {
+        const int f = m->dof_fn[3 * n + d];
+        if (f == FTGPU_BC_FREE) continue;
+        kind[n] |= kNodeBcCached;
+        if (f >= 0 && (m->fns[f].kind > kBckSine || m->fn_owner[f] < 0)) kind[n] |= kNodeRest;
+      }
+  std::vector<int> list;
+  for (long long n = 0; n < N; ++n) {
+    if (m->slot4_host[4 * n] == -1) kind[n] |= kNodeRest;  // no slots
+    if (kind[n] & kNodeRest) list.push_back((int)n);
+  }
+  CKI(m->nkind.upload(kind.data(), kind.size()));
+  CKI(m->fnval.alloc(std::max<size_t>(m->fns.size(), 1) * sizeof(double2)));
+  m->rest_n = (long long)list.size();
+  if (!list.empty()) CKI(m->rest_list.upload(list.data(), list.size()));
+  return 0;
+}
+
 int upload_bc(ftgpu_model *m) {
   const long long N = m->nNodes;
   std::vector<int16_t> nb(3 * N, (int16_t)FTGPU_BC_FREE);
@@ -677,11 +805,50 @@ int upload_bc(ftgpu_model *m) {
       for (int d = 0; d < 3; ++d) nb[d * N + n] = (int16_t)m->dof_fn[3 * n + d];
   int r = m->nbc.upload(nb.data(), nb.size());
   if (r) return r;
+  // driven nodes (a rigid-body or rigid-rotation DOF), once per table
+  m->drv_nodes.clear();
+  m->rigid_nodes.clear();
+  if (!m->dof_fn.empty())
+    for (long long n = 0; n < N; ++n) {
+      bool drv = false, rgd = false;
+      for (int d = 0; d < 3; ++d) {
+        const int f = m->dof_fn[3 * n + d];
+        if (f < 0) continue;
+        drv |= m->fns[f].kind == kBckRigid || m->fns[f].kind == kBckRot;
+        rgd |= m->fns[f].kind == kBckRigid;
+      }
+      if (drv) m->drv_nodes.push_back((int)n);
+      if (rgd) m->rigid_nodes.push_back((int)n);
+    }
+  // the instance that owns each function (-1: unused or shared by several)
+  m->fn_owner.assign(m->fns.size(), -2);
+  if (!m->dof_fn.empty())
+    for (long long i = 0; i < 3 * N; ++i) {
+      const int fi = m->dof_fn[i];
+      if (fi < 0) continue;
+      const int o = instance_of(m, i / 3);
+      int &w = m->fn_owner[fi];
+      w = (w == -2 || w == o) ? o : -1;
+    }
+  for (int &w : m->fn_owner) w = w < 0 ? -1 : w;
+  // pad: a rigid rotation's trigonometry cache slot; a fixed / ramp / sine
+  // function's owning instance (its values are evaluated once per step)
   std::vector<BcFn> f = m->fns;
   int slot = 0;
-  for (auto &b : f) b.pad = (b.kind == kBckRot && slot < kMaxRotFns) ? slot++ : -1;
-  if (f.empty()) f.resize(1);
-  return m->fnsbuf.upload(f.data(), f.size());
+  for (size_t i = 0; i < f.size(); ++i) {
+    BcFn &b = f[i];
+    if (b.kind == kBckRot)
+      b.pad = slot < kMaxRotFns ? slot++ : -1;
+    else
+      b.pad = b.kind <= kBckSine ? m->fn_owner[i] : -1;
+  }
+  if (f.empty()) {
+    f.resize(1);
+    f[0].pad = -1;
+  }
+  r = m->fnsbuf.upload(f.data(), f.size());
+  if (r) return r;
+  return upload_split(m);
 }
 
 template <class R>
@@ -740,6 +907,8 @@ int upload_materials(ftgpu_model *m) {
   return m->mats.upload(t.data(), t.size());
 }
 
+int prepare_graphs(ftgpu_model *m);
+
 template <class R>
 int setup_t(ftgpu_model *m) {
   const long long N = m->nNodes;
@@ -794,6 +963,7 @@ int setup_t(ftgpu_model *m) {
       }
     }
     CKI(m->slot4.upload(rec.data(), rec.size()));
+    m->slot4_host = std::move(rec);
     m->slot4b.release();
     if (W == 8) CKI(m->slot4b.upload(rec2.data(), rec2.size()));
   }
@@ -879,6 +1049,7 @@ int setup_t(ftgpu_model *m) {
   }
   for (int i = 0; i < m->ninst; ++i) m->inst[i].node_begin = m->node_off[i];
   CKI(m->instp.upload(m->inst.data(), m->ninst));
+  CKI(upload_bc(m));  // function owners and the node-pass split need the instances
   std::vector<Clock> ck(2 * m->ninst);
   for (auto &c : ck) c = Clock{0.0, 0.0, 0, 0, 0};
   CKI(m->clock.upload(ck.data(), ck.size()));
@@ -953,7 +1124,7 @@ int setup_t(ftgpu_model *m) {
   m->setup_done = true;
   m->init_done = false;
   drop_graphs(m);
-  return 0;
+  return prepare_graphs(m);
 }
 
 int ensure_gp(ftgpu_model *m) {
@@ -1055,6 +1226,17 @@ int capture_chunk(ftgpu_model *m, int K, bool prof) {
   cudaGraphDestroy(g);
   if (ce != cudaSuccess) return fail(FTGPU_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(ce));
   steps = K;
+  return 0;
+}
+
+// Capture the loop's graphs (the 16-step chunk and the 2..14-step tails) at
+// set-up, so that the first run of a model does not pay for capture and
+// instantiation.  A later change of what a step launches (boundary
+// conditions, energy, injury criteria, surrogate, driven nodes) drops them
+// and the next run captures again.
+int prepare_graphs(ftgpu_model *m) {
+  CKI(capture_chunk(m, kChunkSteps, false));
+  for (int K = 2; K < kChunkSteps; K += 2) CKI(capture_chunk(m, K, false));
   return 0;
 }
 
@@ -1413,9 +1595,9 @@ int ftgpu_set_state(ftgpu_model *m, const double *u, const double *v, const doub
                     double time) {
   if (!m || !m->setup_done) return fail(FTGPU_ERR_STATE, "set_state before setup");
   CK(cudaSetDevice(m->device));
-  CKI(upload_aos(m, u, m->u));
-  CKI(upload_aos(m, v, m->v));
-  CKI(upload_aos(m, a, m->a));
+  const double *const hs[3] = {u, v, a};
+  DBuf *const ds[3] = {&m->u, &m->v, &m->a};
+  CKI(upload_state3(m, hs, ds));
   m->t0 = time;
   m->init_done = false;
   return FTGPU_OK;
@@ -1429,13 +1611,8 @@ int reset_rigid(ftgpu_model *m) {
   if (m->rigid_on && (int)m->rigid.size() != m->ninst)
     return fail(FTGPU_ERR_STATE, "the instance layout changed after set_rigid_body: set the "
                                  "acceleration records again");
-  std::vector<int> rig;  // driven nodes (rigid-body or rigid-rotation DOFs)
-  for (size_t i = 0; i < m->dof_fn.size(); ++i) {
-    const int f = m->dof_fn[i];
-    if (f < 0 || (m->fns[f].kind != kBckRigid && m->fns[f].kind != kBckRot)) continue;
-    const int node = (int)(i / 3);
-    if (rig.empty() || rig.back() != node) rig.push_back(node);
-    if (m->fns[f].kind != kBckRigid) continue;
+  const std::vector<int> &rig = m->drv_nodes;  // driven nodes (from upload_bc)
+  for (const int node : m->rigid_nodes) {
     int inst = 0;
     if (m->inst_set)
       inst = (int)(std::upper_bound(m->node_off.begin(), m->node_off.end(), node) -
@@ -1541,9 +1718,9 @@ int ftgpu_get_state(ftgpu_model *m, double *u, double *v, double *a, double *tim
                     long long *step) {
   if (!m || !m->setup_done) return fail(FTGPU_ERR_STATE, "get_state before setup");
   CK(cudaSetDevice(m->device));
-  CKI(download_aos(m, m->u, u));
-  CKI(download_aos(m, m->v, v));
-  CKI(download_aos(m, m->a, a));
+  DBuf *const ds[3] = {&m->u, &m->v, &m->a};
+  double *const hs[3] = {u, v, a};
+  CKI(download_state3(m, ds, hs));
   Clock c;
   CK(cudaMemcpy(&c, m->clock.p, sizeof(Clock), cudaMemcpyDeviceToHost));
   if (time) *time = c.time;
@@ -1577,7 +1754,10 @@ int ftgpu_launches_per_step(ftgpu_model *m) {
   int inj = 0;
   if (m->injury_on)  // (element work rides on the force pass) reduce, radix passes, list, final
     inj = 1 + (is_fp64(m) ? 8 : 4) + 2;
-  return g + 2 + (m->energy_on ? 1 : 0) + inj;  // + k_energy_reduce
+  // mixed precision without the energy balance or driven nodes: the node
+  // pass is k_node_free plus k_node_step over the rest list
+  const int split = (m->nkind.p && !m->energy_on && m->rig_nodes == 0 && m->rest_n > 0) ? 1 : 0;
+  return g + 2 + split + (m->energy_on ? 1 : 0) + inj;  // + k_energy_reduce
 }
 
 int ftgpu_element_strain(ftgpu_model *m, double *Eavg, double *ps_max, double *ps_min,

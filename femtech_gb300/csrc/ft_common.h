@@ -57,6 +57,7 @@ struct alignas(4 * sizeof(R)) Slot4 {
   R x, y, z, w;
 };
 enum { kBckFixed = 0, kBckRamp = 1, kBckSine = 2, kBckRot = 3, kBckRigid = 4 };
+enum { kNodeBcCached = 1, kNodeRest = 2 };
 enum { kErrInverted = 1, kErrDt = 2, kErrIndex = 4, kErrWait = 8 };
 
 constexpr int kSlotCsr = -2;  // NodeArgs::slot4 marker: more slots than the records hold
@@ -162,6 +163,7 @@ struct StepScalars {
   double c1;   // t_{n+1} - t_half         (full-step velocity)
   double c2;   // t_half' - t_{n+1}        (next half-step velocity)
   double c12;  // t_half' - t_half         (both at once)
+  float c1f, c12f;  // c1 and c12 rounded to FP32 (the mixed update's increments)
   int done;
   bool advance;
 };
@@ -177,7 +179,13 @@ struct NodeArgs {
   const int4 *slot4b;
   const int *node_inst;       // [N] or null (one instance)
   const int16_t *nbc;         // [3N] per-DOF function (-1 free, -2 hold, >= 0 fn)
-  const uint8_t *nbcflag;     // [N] bit0 any constrained DOF
+  // mixed-precision split of the node pass (null: no split): per node
+  // kNodeBcCached (its constrained DOFs follow node-independent functions,
+  // values in fnval, or hold) and kNodeRest (left to k_node_step over the
+  // rest list: a node without slots, a rigid-rotation or rigid-body DOF)
+  const uint8_t *nkind;
+  double2 *fnval;             // [nfns] u, v at t_{n+2} of a cached function
+  int nfns;
   const BcFn *fns;
   const double *X;            // [3][N] FP64 reference coordinates
   double *u, *v, *a, *vh;     // [3][N]

@@ -238,7 +238,52 @@ __device__ __forceinline__ R norm3(R x, R y, R z) {
 // areaHexahedronFace, src/math/Geometry.cpp:29-64 (signed tolerance test kept;
 // the 2x2 quadrature uses (q cD + c1) x (q' cD + c2) = c1 x c2 + q cD x c2 + q' c1 x cD).
 template <class R>
+__device__ __forceinline__ R hex_face_area(const R (&xc)[8][3], int i1, int i2, int i3, int i4);
+
+// FP32 form of the same rule: the edge vectors without their factor 1/4
+// (one 1/16 on the area instead; the parallelogram test against 4 tol), and
+// the four quadrature-point norms |n0 + a n1 + b n2|, a, b = +-1/sqrt 3, from
+// the six dot products of n0, n1, n2.  Mathematically equal; FP32 rounding
+// only.
+__device__ __forceinline__ float hex_face_area_f32(const float (&xc)[8][3], int i1, int i2, int i3,
+                                                   int i4) {
+  float cD[3], c1[3], c2[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float p1 = xc[i1][k], p2 = xc[i2][k], p3 = xc[i3][k], p4 = xc[i4][k];
+    const float a = p3 - p1, b = p2 - p4;
+    cD[k] = (p1 - p2) + (p3 - p4);
+    c1[k] = a + b;
+    c2[k] = a - b;
+  }
+  const float n0x = c1[1] * c2[2] - c1[2] * c2[1], n0y = c1[2] * c2[0] - c1[0] * c2[2],
+              n0z = c1[0] * c2[1] - c1[1] * c2[0];
+  const float tol4 = 4e-6f;
+  if (cD[0] < tol4 && cD[1] < tol4 && cD[2] < tol4)
+    return 0.25f * sqrtf(n0x * n0x + n0y * n0y + n0z * n0z);
+  const float n1x = cD[1] * c2[2] - cD[2] * c2[1], n1y = cD[2] * c2[0] - cD[0] * c2[2],
+              n1z = cD[0] * c2[1] - cD[1] * c2[0];
+  const float n2x = c1[1] * cD[2] - c1[2] * cD[1], n2y = c1[2] * cD[0] - c1[0] * cD[2],
+              n2z = c1[0] * cD[1] - c1[1] * cD[0];
+  const float d00 = n0x * n0x + n0y * n0y + n0z * n0z;
+  const float d11 = n1x * n1x + n1y * n1y + n1z * n1z;
+  const float d22 = n2x * n2x + n2y * n2y + n2z * n2z;
+  const float d01 = n0x * n1x + n0y * n1y + n0z * n1z;
+  const float d02 = n0x * n2x + n0y * n2y + n0z * n2z;
+  const float d12 = n1x * n2x + n1y * n2y + n1z * n2z;
+  const float t = 0.57735026918962576451f, t2 = 1.0f / 3.0f;
+  const float base = d00 + t2 * (d11 + d22);
+  const float a01 = 2.0f * t * d01, a02 = 2.0f * t * d02, a12 = 2.0f * t2 * d12;
+  const float pp = base + a01 + a02 + a12, mm = base - a01 - a02 + a12;
+  const float pm = base + a01 - a02 - a12, mp = base - a01 + a02 - a12;
+  return 0.0625f * (sqrtf(fmaxf(pp, 0.f)) + sqrtf(fmaxf(mm, 0.f)) + sqrtf(fmaxf(pm, 0.f)) +
+                    sqrtf(fmaxf(mp, 0.f)));
+}
+
+template <class R>
 __device__ __forceinline__ R hex_face_area(const R (&xc)[8][3], int i1, int i2, int i3, int i4) {
+  if constexpr (sizeof(R) == 4)
+    return hex_face_area_f32(reinterpret_cast<const float(&)[8][3]>(xc), i1, i2, i3, i4);
   R cD[3], c1[3], c2[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
@@ -522,11 +567,15 @@ __device__ __forceinline__ void tet_element(const R (&x)[4][3], const R (&u)[4][
   le = six_v / nmax;
 }
 
+// Element time step l/c in the element precision R.  FP32: l times the
+// FP32 reciprocal wave speed, an FP32 value -- the block minimum is taken in
+// FP32 and widened once (exact), so no per-element FP64 work; FP64: l / c as
+// CalculateTimeStep.cpp:19.
 template <class R>
-__device__ __forceinline__ double dt_of(R le, const MatP<R> &mp);
+__device__ __forceinline__ R dt_of(R le, const MatP<R> &mp);
 template <>
-__device__ __forceinline__ double dt_of<float>(float le, const MatP<float> &mp) {
-  return double(le * mp.inv_ce);
+__device__ __forceinline__ float dt_of<float>(float le, const MatP<float> &mp) {
+  return le * mp.inv_ce;
 }
 template <>
 __device__ __forceinline__ double dt_of<double>(double le, const MatP<double> &mp) {
@@ -637,12 +686,13 @@ __global__ void __launch_bounds__(kElemThreads, ET == 0 ? 2 : 4)
   // per-element data, before the slot staging
   constexpr int NH = (ET == 1 && (MAT == 5 || MAT == 7)) ? (MAT == 5 ? 18 : 12) : 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  R *shX = reinterpret_cast<R *>(smem_raw);
-  R *shU = shX + 3 * kMaxLocalNodes;
+  // staged slots as {x, y, z, pad} records: one vector load per corner
+  Slot4<R> *shX = reinterpret_cast<Slot4<R> *>(smem_raw);
+  Slot4<R> *shU = shX + kMaxLocalNodes;
   // [NC*3][blockDim] corner forces; FP32 C3D8: first the elements' reference
   // geometry, [20][blockDim] x 4 values, in the same space (a barrier
   // separates the last geometry read from the first corner-force write)
-  R *shF = shU + 3 * kMaxLocalNodes;
+  R *shF = reinterpret_cast<R *>(shU + kMaxLocalNodes);
   constexpr bool GEO = ET == 0 && sizeof(R) == 4;
   const int PE = blockDim.x;
   const int t = threadIdx.x;
@@ -692,19 +742,15 @@ __global__ void __launch_bounds__(kElemThreads, ET == 0 ? 2 : 4)
   }
   const Clock *ck = A.clock + A.parity * A.ninst + inst;
   for (int i = t; i < ns; i += PE) {
-    const Slot4<R> us = reinterpret_cast<const Slot4<R> *>(A.sU)[s0 + i];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) shX[d * kMaxLocalNodes + i] = A.sX[d * A.S + s0 + i];
-    shU[i] = us.x;
-    shU[kMaxLocalNodes + i] = us.y;
-    shU[2 * kMaxLocalNodes + i] = us.z;
+    shU[i] = reinterpret_cast<const Slot4<R> *>(A.sU)[s0 + i];
+    shX[i] = Slot4<R>{A.sX[s0 + i], A.sX[A.S + s0 + i], A.sX[2 * A.S + s0 + i], R(0)};
   }
   if (GEO) cp_async_wait_all();  // this thread's geometry rows
   // an instance past its end time: the whole block leaves (uniform per patch)
   if (A.use_clock && ck->done) return;
   const R dt = A.use_clock ? R(ck->dt) : R(A.dt_direct);
   __syncthreads();
-  double dte = r_inf<double>();
+  R dte = r_inf<R>();
   int bad = 0;
   // injury extremes of this thread's element: max / min principal strain,
   // max shear, max MPS x rate, with list position and compact index
@@ -723,11 +769,9 @@ __global__ void __launch_bounds__(kElemThreads, ET == 0 ? 2 : 4)
     for (int a = 0; a < NC; ++a) {
       int l = lc[a] < ns ? lc[a] : 0;
       if (lc[a] >= ns) bad |= 2;
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        x[a][d] = shX[d * kMaxLocalNodes + l];
-        u[a][d] = shU[d * kMaxLocalNodes + l];
-      }
+      const Slot4<R> xs = shX[l], us = shU[l];
+      x[a][0] = xs.x; x[a][1] = xs.y; x[a][2] = xs.z;
+      u[a][0] = us.x; u[a][1] = us.y; u[a][2] = us.z;
     }
     R Es[6];  // injury: the element's averaged Green strain (as k_elem_strain)
     if (INJ && ci >= 0) element_green_strain<R, ET>(x, u, Es);
@@ -770,17 +814,19 @@ __global__ void __launch_bounds__(kElemThreads, ET == 0 ? 2 : 4)
   if (pass == kPassSurrogateFeatures) return;  // features only (uniform per block)
   if (INJ && pass == kPassForce)
     injury_block_extremes<kElemThreads>(iv, ij, ic, reinterpret_cast<InjuryPart *>(A.inj_part) + p);
-  // block minimum of the element time steps -> one FP64 atomicMin per block
-  // (positive doubles order like their bit patterns)
+  // block minimum of the element time steps (in R; widening to FP64 is
+  // exact and monotone) -> one FP64 atomicMin per block (positive doubles
+  // order like their bit patterns)
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) dte = fmin(dte, __shfl_xor_sync(0xffffffffu, dte, o));
-  __shared__ double wmin[kElemThreads / 32];
+  __shared__ R wmin[kElemThreads / 32];
   if ((t & 31) == 0) wmin[t >> 5] = dte;
   __syncthreads();
   if (t == 0) {
-    double mn = wmin[0];
+    R mn = wmin[0];
     for (int w = 1; w < (PE + 31) / 32; ++w) mn = fmin(mn, wmin[w]);
-    atomicMin(A.dtmin + A.parity * A.ninst + inst, (unsigned long long)__double_as_longlong(mn));
+    atomicMin(A.dtmin + A.parity * A.ninst + inst,
+              (unsigned long long)__double_as_longlong(double(mn)));
   }
   if (pass != kPassForce) return;
   // in-block assembly: local node i sums its corners in (element, corner) order
@@ -933,20 +979,17 @@ template <class R, int ET>
 __global__ void __launch_bounds__(kElemThreads) k_elem_strain(const ElemArgs<R> A, double *Eout) {
   constexpr int NC = ET == 0 ? 8 : 4;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  R *shX = reinterpret_cast<R *>(smem_raw);
-  R *shU = shX + 3 * kMaxLocalNodes;
+  // staged slots as {x, y, z, pad} records: one vector load per corner
+  Slot4<R> *shX = reinterpret_cast<Slot4<R> *>(smem_raw);
+  Slot4<R> *shU = shX + kMaxLocalNodes;
   const int PE = blockDim.x;
   const int t = threadIdx.x;
   const int p = A.patch_begin + blockIdx.x;
   const int e0 = A.patch_elem_off[p], ne = A.patch_elem_off[p + 1] - e0;
   const int s0 = A.patch_node_off[p], ns = A.patch_node_off[p + 1] - s0;
   for (int i = t; i < ns; i += PE) {
-    const Slot4<R> us = reinterpret_cast<const Slot4<R> *>(A.sU)[s0 + i];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) shX[d * kMaxLocalNodes + i] = A.sX[d * A.S + s0 + i];
-    shU[i] = us.x;
-    shU[kMaxLocalNodes + i] = us.y;
-    shU[2 * kMaxLocalNodes + i] = us.z;
+    shU[i] = reinterpret_cast<const Slot4<R> *>(A.sU)[s0 + i];
+    shX[i] = Slot4<R>{A.sX[s0 + i], A.sX[A.S + s0 + i], A.sX[2 * A.S + s0 + i], R(0)};
   }
   __syncthreads();
   if (t >= ne) return;
@@ -965,11 +1008,9 @@ __global__ void __launch_bounds__(kElemThreads) k_elem_strain(const ElemArgs<R> 
 #pragma unroll
   for (int a = 0; a < NC; ++a) {
     const int l = lc[a] < ns ? lc[a] : 0;
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      x[a][d] = shX[d * kMaxLocalNodes + l];
-      u[a][d] = shU[d * kMaxLocalNodes + l];
-    }
+    const Slot4<R> xs = shX[l], us = shU[l];
+    x[a][0] = xs.x; x[a][1] = xs.y; x[a][2] = xs.z;
+    u[a][0] = us.x; u[a][1] = us.y; u[a][2] = us.z;
   }
   R Es[6];
   element_green_strain<R, ET>(x, u, Es);

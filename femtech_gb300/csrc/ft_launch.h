@@ -46,14 +46,21 @@ inline int launch_strain<double>(int etype, int nblocks, int threads, size_t sme
 // Returns a cudaError_t value.
 int launch_geo_f32(int nblocks, cudaStream_t s, const ElemArgs<float> &A, float *geo);
 
-// Dynamic shared memory of one element block: node X and u for
-// kMaxLocalNodes slots plus NC*3 corner forces per element, or for FP32
+// Dynamic shared memory of one element block: node X and u records (4
+// values each) for kMaxLocalNodes slots plus NC*3 corner forces per element, or for FP32
 // C3D8 the larger 80-value geometry record per element in the same space.
 template <class R>
 inline size_t elem_smem_bytes_host(int etype, int PE) {
   const int NC = etype == 0 ? 8 : 4;
   const size_t per_elem = (etype == 0 && sizeof(R) == 4) ? 80 : (size_t)NC * 3;
-  return sizeof(R) * (6 * (size_t)kMaxLocalNodes + per_elem * PE);
+  return sizeof(R) * (8 * (size_t)kMaxLocalNodes + per_elem * PE);
+}
+
+// Dynamic shared memory of one strain block (k_elem_strain): the slot
+// records only.
+template <class R>
+inline size_t strain_smem_bytes_host() {
+  return sizeof(R) * 8 * (size_t)kMaxLocalNodes;
 }
 
 template <class R>

@@ -353,11 +353,30 @@ __device__ __forceinline__ Sym6<R> sym_mul(const Sym6<R> &a, const Sym6<R> &b) {
   return r;
 }
 
+// ln(1 + x) and exp(y) for the small arguments of nearly incompressible
+// tissue (|J - 1| << 1): in FP32 the Taylor polynomials to degree 6 and 5
+// (truncation below 2^-40 relative for |x|, |y| < 1/32), else the library
+// functions; FP64 always the library functions.
+template <class R>
+__device__ __forceinline__ R log1p_small(R x) {
+  if (sizeof(R) == 4 && fabs(x) < R(0.03125))
+    return x * (R(1) + x * (R(-0.5) + x * (R(1.0 / 3.0) + x * (R(-0.25) +
+                x * (R(0.2) + x * R(-1.0 / 6.0))))));
+  return d_log1p(x);
+}
+template <class R>
+__device__ __forceinline__ R exp_small(R y) {
+  if (sizeof(R) == 4 && fabs(y) < R(0.03125))
+    return R(1) + y * (R(1) + y * (R(0.5) + y * (R(1.0 / 6.0) + y * (R(1.0 / 24.0) +
+                y * R(1.0 / 120.0)))));
+  return d_exp(y);
+}
+
 template <class R>
 __device__ __forceinline__ Sym6<R> mat_ogden(const MatP<R> &m, const R (&D)[3][3], R Jm1) {
   R mu = m.p[1], alpha = m.p[3];
   Sym6<R> e = two_E(D);
-  R lnJ = d_log1p(Jm1);
+  R lnJ = log1p_small(Jm1);
   Sym6<R> S;
   const R n2 = e.xx * e.xx + e.yy * e.yy + e.zz * e.zz +
                2 * (e.yz * e.yz + e.xz * e.xz + e.xy * e.xy);
@@ -399,7 +418,7 @@ __device__ __forceinline__ Sym6<R> mat_ogden(const MatP<R> &m, const R (&D)[3][3
     }
     const R iC3 = R(1) / (1 + I1 + I2 + I3);  // Ci = Ca I + Cb M + Cg M^2
     const R Ca = -I3 * iC3, Cb = -(1 + I1) * iC3, Cg = iC3;
-    const R c = 2 * mu / alpha * d_exp(-alpha * R(1.0 / 3.0) * lnJ);
+    const R c = 2 * mu / alpha * exp_small(-alpha * R(1.0 / 3.0) * lnJ);
     const R t = trB * R(1.0 / 3.0);
     const R ka = c * (Aa - Ca - t * (1 + Ca)), kb = c * (Ab - Cb - t * Cb),
             kg = c * (Ag - Cg - t * Cg);

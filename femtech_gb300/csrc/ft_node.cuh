@@ -329,7 +329,38 @@ __device__ __forceinline__ StepScalars step_scalars(const Clock &ck, const InstP
   s.c1 = s.t_np1 - t_half;
   s.c2 = t_half2 - s.t_np1;
   s.c12 = t_half2 - t_half;
+  s.c1f = float(s.c1);
+  s.c12f = float(s.c12);
   return s;
+}
+
+// FP32 <-> FP64 conversions of the mixed nodal update by integer bit
+// arithmetic.  This GPU converts between FP32 and FP64 on its FP64 pipe (two
+// lanes per SM and cycle); a handful of integer operations give the same
+// bits for every normal number, and the rare others (zero, subnormal,
+// overflow, inf, NaN) take the hardware conversion.
+// float -> double: exact (rebias the exponent by 1023 - 127 = 896, widen the
+// mantissa).
+__device__ __forceinline__ double f2d_bits(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned ex = b & 0x7f800000u;
+  if (ex == 0u || ex == 0x7f800000u) return (double)f;
+  const unsigned hi = (b & 0x80000000u) | (((b >> 3) & 0x0fffffffu) + (896u << 20));
+  return __hiloint2double((int)hi, (int)(b << 29));
+}
+// double -> float, round to nearest even: the top 9 bits of (hi:lo) << 3 hold
+// the low exponent bits, the next 23 the kept mantissa; the 29 bits shifted
+// out decide the rounding (a carry into the exponent is the correct result,
+// up to infinity at the top of the range); the exponent is rebiased modulo
+// 512, exact for results in the normal FP32 range.
+__device__ __forceinline__ float d2f_bits(double d) {
+  const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+  const unsigned e11 = (hi >> 20) & 0x7ffu;
+  if (e11 <= 896u || e11 >= 1151u) return __double2float_rn(d);
+  unsigned t = __funnelshift_l(lo, hi, 3);
+  const unsigned rem = lo << 3;
+  t += (rem > 0x80000000u || (rem == 0x80000000u && (t & 1u))) ? 1u : 0u;
+  return __uint_as_float(((t - (384u << 23)) & 0x7fffffffu) | (hi & 0x80000000u));
 }
 
 template <class R>
@@ -447,12 +478,43 @@ __global__ void __launch_bounds__(512, 2) k_node(const NodeArgs A) {
 // thread per instance, launched between the element pass and k_node_step, so
 // that the FP64 divisions and sin/cos run once per instance and step rather
 // than once per node block (FP64 issue is slow on this GPU).
+// With the node-pass split, thread i also evaluates boundary function i once
+// for the step when its value is the same for every node (fixed, ramp, sine)
+// and one instance owns it (BcFn::pad): u and v at that instance's t_{n+2},
+// the values node_step's bc_value would compute per DOF.
 __global__ void k_step_scalars(const NodeArgs A) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (A.fnval && i < A.nfns) {
+    const BcFn &b = A.fns[i];
+    if (b.kind <= kBckSine && b.pad >= 0) {
+      const int o = b.pad;
+      const Clock co = A.clock[A.parity * A.ninst + o];
+      const StepScalars so =
+          step_scalars(co, A.inst[o], A.dtmin[A.parity * A.ninst + o], A.mode);
+      if (so.advance && !co.done) {
+        double u, v;
+        bc_value(b, 0, so.t_np2, A.X, A.N, 0, u, v);
+        A.fnval[i] = make_double2(u, v);
+      }
+    }
+  }
   if (i >= A.ninst) return;
   const Clock ck = A.clock[A.parity * A.ninst + i];
   const StepScalars sc = step_scalars(ck, A.inst[i], A.dtmin[A.parity * A.ninst + i], A.mode);
   A.stepsc[i] = sc;
+  // the instance's clock for the next step and its fresh dt-minimum slot
+  // (the other parity: nothing reads them before the next element pass).
+  // The first node's thread of k_node_step writes the same values.
+  Clock nx = ck;
+  if (!ck.done) {
+    nx.time = sc.t_np1;
+    nx.dt = sc.ndt;
+    nx.step = ck.step + 1;
+    nx.done = sc.done;
+    nx.err = (sc.done & 4) ? kErrDt : 0;
+  }
+  A.clock[(A.parity ^ 1) * A.ninst + i] = nx;
+  A.dtmin[(A.parity ^ 1) * A.ninst + i] = kDtHugeBits;
   if (sc.advance && !ck.done)
     for (int k = 0; k < A.nrot; ++k) {
       double *r = A.rottrig + 3 * ((long long)i * kMaxRotFns + k);
@@ -692,7 +754,7 @@ __device__ __forceinline__ void node_step(const NodeArgs &A, long long n, R &eke
   // FP32 sum), accumulated into the FP64 state -- one FP64 add per DOF
   // instead of a multiply and a fused multiply-add: FP64 issue is slow on
   // this GPU
-  const float c1f = float(sc.c1), c12f = float(sc.c12);
+  const float c1f = sc.c1f, c12f = sc.c12f;
   double un[3] = {u0[0], u0[1], u0[2]};
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
@@ -768,6 +830,125 @@ __device__ __forceinline__ void node_step(const NodeArgs &A, long long n, R &eke
     c.err = (sc.done & 4) ? kErrDt : 0;
     *nxt = c;
     A.dtmin[(A.parity ^ 1) * A.ninst + inst] = kDtHugeBits;
+  }
+}
+
+// The mixed-precision step of every node that is not in the rest list, one
+// thread per node: gather the partials (slot records, or the node's slot list
+// when it has more), a = f / m in FP32, then for a free DOF either v_half' =
+// v_half + c12 a and u' = u + dt v_half' in FP64, or -- the step that ends a
+// run -- v = v_half + c1 a and a; a DOF under a cached boundary function
+// takes its u and v at t_{n+2} from fnval (a = 0), a held DOF keeps u; u'
+// goes back into the node's slots.  The operations and their order are
+// node_step's, so the bits are too; the FP32 <-> FP64 conversions are integer
+// arithmetic, and no per-node transcendental or clock work is on this path.
+__global__ void __launch_bounds__(512, 2) k_node_free(const NodeArgs A) {
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= A.N) return;
+  const int kind = A.nkind[n];
+  if (kind & kNodeRest) return;
+  const long long N = A.N;
+  const int4 sr = A.slot4[n];
+  int4 sr2 = make_int4(-1, -1, -1, -1);
+  if (A.slot4b) sr2 = A.slot4b[n];
+  const int inst = A.node_inst ? A.node_inst[n] : 0;
+  int fn[3] = {kBcFree, kBcFree, kBcFree};
+  if (kind & kNodeBcCached) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) fn[d] = A.nbc[d * N + n];
+  }
+  double u0[3], vh0[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    u0[d] = A.u[d * N + n];
+    vh0[d] = A.vh[d * N + n];
+  }
+  const float minv = A.minv[n];
+  const Slot4<float> *sF = reinterpret_cast<const Slot4<float> *>(A.sF);
+  const bool csr = sr.x == kSlotCsr;
+  const int s4[4] = {sr.x, sr.y, sr.z, sr.w};
+  const int s8[4] = {sr2.x, sr2.y, sr2.z, sr2.w};
+  float fs0 = 0.f, fs1 = 0.f, fs2 = 0.f;
+  if (!csr) {
+    Slot4<float> q[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (s4[j] >= 0) q[j] = sF[s4[j]];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (s4[j] >= 0) {
+        fs0 += q[j].x;
+        fs1 += q[j].y;
+        fs2 += q[j].z;
+      }
+    if (A.slot4b) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (s8[j] >= 0) q[j] = sF[s8[j]];
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (s8[j] >= 0) {
+          fs0 += q[j].x;
+          fs1 += q[j].y;
+          fs2 += q[j].z;
+        }
+    }
+  } else {
+    for (int k = A.slot_off[n]; k < A.slot_off[n + 1]; ++k) {
+      const Slot4<float> q = sF[A.slots[k]];
+      fs0 += q.x;
+      fs1 += q.y;
+      fs2 += q.z;
+    }
+  }
+  if (A.clock[A.parity * A.ninst + inst].done) return;  // past its end: nothing moves
+  const StepScalars &sc = A.stepsc[inst];
+  const float fs[3] = {fs0, fs1, fs2};
+  if (!sc.advance) {  // the run ends with this step: v and a of the free DOFs
+    const float c1f = sc.c1f;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      if (fn[d] != kBcFree) continue;
+      const float acc = -fs[d] * minv;
+      A.v[d * N + n] = vh0[d] + f2d_bits(c1f * acc);
+      A.a[d * N + n] = f2d_bits(acc);
+    }
+    return;
+  }
+  const float c12f = sc.c12f;
+  const double ndt = sc.ndt;
+  float r[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    double un = u0[d];
+    if (fn[d] == kBcFree) {
+      const float acc = -fs[d] * minv;
+      const double vh2 = vh0[d] + f2d_bits(c12f * acc);
+      un = u0[d] + ndt * vh2;
+      A.vh[d * N + n] = vh2;
+      A.u[d * N + n] = un;
+    } else if (fn[d] >= 0) {  // boundary function: u, v at t_{n+2}, a = 0
+      const double2 bv = A.fnval[fn[d]];
+      un = bv.x;
+      A.u[d * N + n] = bv.x;
+      A.v[d * N + n] = bv.y;
+      A.a[d * N + n] = 0.0;
+    }
+    r[d] = d2f_bits(un);
+  }
+  Slot4<float> *sU = reinterpret_cast<Slot4<float> *>(A.sU);
+  const Slot4<float> w{r[0], r[1], r[2], 0.f};
+  if (!csr) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (s4[j] >= 0) sU[s4[j]] = w;
+    if (A.slot4b) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (s8[j] >= 0) sU[s8[j]] = w;
+    }
+  } else {
+    for (int k = A.slot_off[n]; k < A.slot_off[n + 1]; ++k) sU[A.slots[k]] = w;
   }
 }
 
