@@ -453,7 +453,17 @@ int launch_node(ftgpu_model *m, int mode, int parity) {
     CK(cudaStreamWaitEvent(m->stream2, m->ev_fork, 0));
     k_driven_step<<<(unsigned)m->ninst, 32, 0, m->stream2>>>(B);
     node_step(nbr, m->stream2, B);
-    node_step(nb, m->stream, A);
+    if (!f64 && !en && A.nkind) {  // every other node: the split, as below
+      k_node_free<<<(unsigned)nb, th, 0, m->stream>>>(A);
+      if (m->rest_n > 0) {
+        NodeArgs C = A;
+        C.node_list = m->rest_list.as<int>();
+        C.nlist = m->rest_n;
+        node_step((m->rest_n + th - 1) / th, m->stream, C);
+      }
+    } else {
+      node_step(nb, m->stream, A);
+    }
     CK(cudaEventRecord(m->ev_join, m->stream2));
     CK(cudaStreamWaitEvent(m->stream, m->ev_join, 0));
     nb += nbr;
@@ -583,7 +593,10 @@ int ensure_stage3(ftgpu_model *m) {
 // u, v, a between AoS host arrays and the SoA device state in one call: each
 // array has its own staging third and copy stream, so the three host <->
 // device copies run side by side and overlap the transposes (which run on
-// the model's stream).  Null host arrays: zero (upload) / not read (download).
+// the model's stream).  (Kernels reading or writing page-locked host arrays
+// in place through their mapping measured slower: 1.8 / 5.4 ms against
+// 1.5 / 1.6 ms for the 4M-node block's three arrays.)  Null host arrays:
+// zero (upload) / not read (download).
 int upload_state3(ftgpu_model *m, const double *const h[3], DBuf *const d[3]) {
   const long long N = m->nNodes;
   CKI(ensure_stage3(m));
@@ -612,6 +625,7 @@ int upload_state3(ftgpu_model *m, const double *const h[3], DBuf *const d[3]) {
 int download_state3(ftgpu_model *m, DBuf *const d[3], double *const h[3]) {
   const long long N = m->nNodes;
   CKI(ensure_stage3(m));
+  bool staged[3] = {false, false, false};
   for (int k = 0; k < 3; ++k) {
     if (!h[k]) continue;
     k_soa_to_aos<<<(unsigned)((N + 255) / 256), 256, 0, m->stream>>>(
@@ -621,9 +635,11 @@ int download_state3(ftgpu_model *m, DBuf *const d[3], double *const h[3]) {
     CK(cudaStreamWaitEvent(m->cstream[k], m->cev[k], 0));
     CK(cudaMemcpyAsync(h[k], m->stage.as<double>() + 3 * N * k, 3 * N * sizeof(double),
                        cudaMemcpyDeviceToHost, m->cstream[k]));
+    staged[k] = true;
   }
+  CK(cudaStreamSynchronize(m->stream));
   for (int k = 0; k < 3; ++k)
-    if (h[k]) CK(cudaStreamSynchronize(m->cstream[k]));
+    if (staged[k]) CK(cudaStreamSynchronize(m->cstream[k]));
   return 0;
 }
 
@@ -785,10 +801,14 @@ int upload_split(ftgpu_model *m) {
         kind[n] |= kNodeBcCached;
         if (f >= 0 && (m->fns[f].kind > kBckSine || m->fn_owner[f] < 0)) kind[n] |= kNodeRest;
       }
+  // the rest list leaves out the driven nodes: the driven-node branch of
+  // the step (a second stream) updates them
+  std::vector<char> drv(N, 0);
+  for (const int n : m->drv_nodes) drv[n] = 1;
   std::vector<int> list;
   for (long long n = 0; n < N; ++n) {
     if (m->slot4_host[4 * n] == -1) kind[n] |= kNodeRest;  // no slots
-    if (kind[n] & kNodeRest) list.push_back((int)n);
+    if ((kind[n] & kNodeRest) && !drv[n]) list.push_back((int)n);
   }
   CKI(m->nkind.upload(kind.data(), kind.size()));
   CKI(m->fnval.alloc(std::max<size_t>(m->fns.size(), 1) * sizeof(double2)));
@@ -1754,10 +1774,13 @@ int ftgpu_launches_per_step(ftgpu_model *m) {
   int inj = 0;
   if (m->injury_on)  // (element work rides on the force pass) reduce, radix passes, list, final
     inj = 1 + (is_fp64(m) ? 8 : 4) + 2;
-  // mixed precision without the energy balance or driven nodes: the node
-  // pass is k_node_free plus k_node_step over the rest list
-  const int split = (m->nkind.p && !m->energy_on && m->rig_nodes == 0 && m->rest_n > 0) ? 1 : 0;
-  return g + 2 + split + (m->energy_on ? 1 : 0) + inj;  // + k_energy_reduce
+  // mixed precision without the energy balance: the node pass is
+  // k_node_free plus k_node_step over the rest list (when it has nodes)
+  const int split = (m->nkind.p && !m->energy_on && m->rest_n > 0) ? 1 : 0;
+  // driven nodes: k_driven_step and k_node_step over their list (second
+  // stream); acceleration records without driven nodes: k_driven_step alone
+  const int drv = m->rig_nodes > 0 ? 2 : (m->rigid_on ? 1 : 0);
+  return g + 2 + split + drv + (m->energy_on ? 1 : 0) + inj;  // + k_energy_reduce
 }
 
 int ftgpu_element_strain(ftgpu_model *m, double *Eavg, double *ps_max, double *ps_min,

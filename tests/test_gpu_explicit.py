@@ -159,3 +159,24 @@ def test_errors_are_status_codes():
     with pytest.raises(ft.FtgpuError) as ei:
         ft.Model(mesh, bad)
     assert ei.value.status == ft.ERR_MATERIAL
+
+
+def test_state_transfer_pinned_and_pageable_agree():
+    """set_state / get_state move the reference-layout arrays exactly, whether
+    the host arrays are page-locked (read and written in place by the
+    transpose kernels) or pageable (staged copies)."""
+    import torch
+    mesh, mats, loads = mg.cube_tension_case(n=5)
+    m = ft.Model(mesh, mats, precision=ft.MIXED, loads=loads)
+    n = 3 * len(mesh["coordinates"])
+    rng = np.random.default_rng(3)
+    u, v, a = (rng.normal(size=n) for _ in range(3))
+    pin = {k: torch.tensor(x).pin_memory().numpy() for k, x in zip("uva", (u, v, a))}
+    out = {k: torch.empty(n, dtype=torch.float64).pin_memory().numpy() for k in "uva"}
+    for src in (pin, dict(u=u, v=v, a=a)):
+        m.set_state(src["u"], src["v"], src["a"], 0.0)
+        s1 = m.state()  # pageable destination
+        s2 = m.state(out=out)  # page-locked destination
+        for k, x in zip("uva", (u, v, a)):
+            assert np.array_equal(s1[k], x) and np.array_equal(s2[k], x), k
+    m.close()
