@@ -355,6 +355,10 @@ def main():
     ap.add_argument("--workload", default="block",
                     choices=["block", "head", "head-impact", "ensemble"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="ensemble: default launch shapes instead of the autotuned ones")
+    ap.add_argument("--retune", action="store_true",
+                    help="ensemble: tune again even when the cache holds this shape bucket")
     ap.add_argument("--no-accuracy", action="store_true",
                     help="skip the mixed-vs-FP64 displacement error of the block workload")
     ap.add_argument("--size", default=None,
@@ -396,8 +400,24 @@ def main():
     mesh, mats, loads = wl["mesh"], wl["mats"], wl["loads"]
     E = len(mesh["etype"])
     N = len(mesh["coordinates"])
-    model = ft.Model(mesh, mats, precision=ft.MIXED, device=dev, loads=loads,
-                     instances=wl["instances"])
+    tuning = None
+    if args.workload == "ensemble" and not args.no_tune:
+        # the batched ensemble through the autotuner: its launch shapes are
+        # tuned on this model (cached per shape bucket) and reported
+        from femtech_gb300 import autotune as at
+        model = at.tuned_model(mesh, mats, loads, wl["instances"], precision=ft.MIXED, device=dev,
+                               retune=args.retune, steps=20)
+        ch = model.tuning
+        d_ms = ch["ms"].get("p128_t256_s1")
+        b_ms = min(ch["ms"].values())
+        tuning = {"patch": ch["patch"], "node_threads": ch["node_threads"],
+                  "split": ch.get("split", 1), "default_ms_per_step": d_ms,
+                  "tuned_ms_per_step": b_ms, "gain": (d_ms / b_ms) if d_ms else None,
+                  "candidates_ms_per_step": ch["ms"]}
+        wl["tuning"] = ch
+    else:
+        model = ft.Model(mesh, mats, precision=ft.MIXED, device=dev, loads=loads,
+                         instances=wl["instances"])
     log("setup %.1f s (%d elements, %d nodes)" % (time.perf_counter() - t0, E, N))
     if wl.get("rigid") is not None:
         model.set_rigid_body(wl["rigid"])
@@ -505,6 +525,8 @@ def main():
     if rank == 0 and world == 1 and args.workload == "block" and not args.no_surrogate:
         # the metric's second arm: the learned surrogate on the head-like mesh
         line["surrogate"] = surrogate_summary(dev, steps=1000, warmup=20)
+    if tuning is not None:
+        line["tuning"] = tuning
     if args.energy:
         line["energy"] = model.energy()
     if args.injury:
@@ -576,8 +598,14 @@ def end_to_end(ft, wl, dev, steps, E, N):
     """Public-API run with host buffers: upload the initial state from host
     memory, run the loop, read all displacements back every 100 steps."""
     import torch
+    ch = wl.get("tuning")
     model = ft.Model(wl["mesh"], wl["mats"], precision=ft.MIXED, device=dev, loads=wl["loads"],
-                     instances=wl["instances"])
+                     instances=wl["instances"], patch_size=ch["patch"] if ch else 0,
+                     setup=ch is None)
+    if ch:
+        from femtech_gb300 import autotune as at
+        at.apply_choice(model, ch["node_threads"], ch.get("split", 1))
+        model.setup()
     u0 = torch.zeros(3 * N, dtype=torch.float64).pin_memory().numpy()
     v0 = torch.zeros(3 * N, dtype=torch.float64).pin_memory().numpy()
     a0 = torch.zeros(3 * N, dtype=torch.float64).pin_memory().numpy()

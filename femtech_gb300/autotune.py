@@ -1,17 +1,22 @@
 """Autotuner for the engine's launch shapes.
 
-Two choices decide how a mesh maps onto the GPU and are tuned per *shape
+Three choices decide how a mesh maps onto the GPU and are tuned per *shape
 bucket* (element types, materials, precision, element count rounded to a power
 of two, instance count rounded likewise):
 
 * elements per patch = threads per block of the element kernel (64..256):
   larger patches replicate fewer nodes (less slot traffic) but occupy more
   shared memory and registers per block;
-* threads per block of the nodal kernel (128 / 256 / 512).
+* threads per block of the nodal kernels (128 / 256 / 512);
+* the nodal pass split (mixed precision): a lean kernel over the free and
+  function-driven nodes plus the general kernel over the rest, or the general
+  kernel over every node (meshes where most nodes carry rigid-rotation or
+  rigid-body drives gain nothing from the split).
 
-`tune()` times every candidate on the actual model for a few steps (device
-time with CUDA events, after warm-up), keeps the fastest and stores it in a
-JSON cache (``$FTGPU_TUNING_CACHE``, default ``~/.cache/femtech_gb300/tuning.json``).
+`tune()` times the candidates on the actual model for a few steps (device
+time with CUDA events, after warm-up) -- the patch size first, then the nodal
+block size, then the split -- keeps the fastest and stores it in a JSON cache
+(``$FTGPU_TUNING_CACHE``, default ``~/.cache/femtech_gb300/tuning.json``).
 `tuned_model()` builds a Model with the cached choice, tuning first on a miss.
 """
 import ctypes as C
@@ -23,6 +28,7 @@ import numpy as np
 
 PATCH_CANDIDATES = (64, 96, 128, 192, 256)
 NODE_CANDIDATES = (128, 256, 512)
+SPLIT_CANDIDATES = (1, 0)
 
 
 def cache_path():
@@ -60,13 +66,22 @@ def save_cache(cache, path=None):
     os.replace(tmp, path)
 
 
-def time_config(mesh, mats, loads, instances, precision, patch, node_threads, steps=20,
-                warmup=5, device=0):
+def apply_choice(m, node_threads, split):
+    """Set the nodal knobs of a Model (before or after setup)."""
+    import femtech_gb300 as ft
+    L = ft.lib()
+    L.ftgpu_set_node_split.argtypes = [C.c_void_p, C.c_int]
+    ft._check(L.ftgpu_set_node_threads(m.h, int(node_threads)))
+    ft._check(L.ftgpu_set_node_split(m.h, int(split)))
+
+
+def time_config(mesh, mats, loads, instances, precision, patch, node_threads, split=1,
+                steps=20, warmup=5, device=0):
     """Device milliseconds per step of one configuration."""
     import femtech_gb300 as ft
     m = ft.Model(mesh, mats, precision=precision, device=device, loads=loads,
                  patch_size=patch, instances=instances, setup=False)
-    ft._check(ft.lib().ftgpu_set_node_threads(m.h, int(node_threads)))
+    apply_choice(m, node_threads, split)
     m.setup()
     m.init_explicit(0.9, 0.0, 1e300)
     m.run(warmup)
@@ -77,22 +92,29 @@ def time_config(mesh, mats, loads, instances, precision, patch, node_threads, st
 
 
 def tune(mesh, mats, loads=None, instances=None, precision=1, steps=20, device=0,
-         patch_candidates=PATCH_CANDIDATES, node_candidates=NODE_CANDIDATES, timer=None,
-         cache=True):
-    """Time the candidates, return {'patch': p, 'node_threads': t, 'ms': {...}}."""
-    timer = timer or (lambda p, t: time_config(mesh, mats, loads, instances, precision, p, t,
-                                               steps=steps, device=device))
+         patch_candidates=PATCH_CANDIDATES, node_candidates=NODE_CANDIDATES,
+         split_candidates=SPLIT_CANDIDATES, timer=None, cache=True):
+    """Time the candidates, return {'patch': p, 'node_threads': t, 'split': s,
+    'ms': {config: ms per step}} (timer(p, t, s) -> ms, injectable for tests)."""
+    timer = timer or (lambda p, t, s: time_config(mesh, mats, loads, instances, precision, p,
+                                                  t, s, steps=steps, device=device))
     pcs = [p for p in patch_candidates if not (precision == 0 and p > 128)]
+    scs = [s for s in split_candidates if not (precision == 0 and s == 0)] or [1]
     res = {}
-    for p in pcs:  # patch size first, at the default nodal block
-        res["p%d_t256" % p] = timer(p, 256)
-    best_p = min(pcs, key=lambda p: res["p%d_t256" % p])
-    for t in node_candidates:
-        k = "p%d_t%d" % (best_p, t)
+
+    def run(p, t, s):
+        k = "p%d_t%d_s%d" % (p, t, s)
         if k not in res:
-            res[k] = timer(best_p, t)
-    best_t = min(node_candidates, key=lambda t: res["p%d_t%d" % (best_p, t)])
-    out = {"patch": best_p, "node_threads": best_t, "ms": res}
+            res[k] = timer(p, t, s)
+        return res[k]
+
+    s0 = scs[0]
+    for p in pcs:  # patch size first, at the default nodal block
+        run(p, 256, s0)
+    best_p = min(pcs, key=lambda p: run(p, 256, s0))
+    best_t = min(node_candidates, key=lambda t: run(best_p, t, s0))
+    best_s = min(scs, key=lambda s: run(best_p, best_t, s))
+    out = {"patch": best_p, "node_threads": best_t, "split": best_s, "ms": res}
     if cache:
         c = load_cache()
         c[bucket(mesh, mats, precision, instances)] = out
@@ -111,7 +133,7 @@ def tuned_model(mesh, mats, loads=None, instances=None, precision=1, device=0, r
         choice = tune(mesh, mats, loads, instances, precision, device=device, **kw)
     m = ft.Model(mesh, mats, precision=precision, device=device, loads=loads,
                  patch_size=choice["patch"], instances=instances, setup=False)
-    ft._check(ft.lib().ftgpu_set_node_threads(m.h, int(choice["node_threads"])))
+    apply_choice(m, choice["node_threads"], choice.get("split", 1))
     m.setup()
     m.tuning = choice
     return m

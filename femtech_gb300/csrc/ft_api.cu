@@ -250,6 +250,7 @@ struct ftgpu_model {
   // mixed-precision node pass split: k_node_free over every node not marked
   // kNodeRest in nkind, k_node_step over rest_list (the marked ones)
   std::vector<int> slot4_host;
+  int node_split = 1;         // ftgpu_set_node_split
   std::vector<int> fn_owner;  // instance owning each boundary function, -1 none / shared
   DBuf nkind, fnval, rest_list;
   long long rest_n = 0;
@@ -791,7 +792,7 @@ int upload_split(ftgpu_model *m) {
   m->nkind.release();
   m->rest_list.release();
   m->rest_n = 0;
-  if (is_fp64(m) || (long long)m->slot4_host.size() != 4 * N) return 0;
+  if (is_fp64(m) || !m->node_split || (long long)m->slot4_host.size() != 4 * N) return 0;
   std::vector<uint8_t> kind(N, 0);
   if (!m->dof_fn.empty())
     for (long long n = 0; n < N; ++n)
@@ -1527,6 +1528,18 @@ int ftgpu_set_node_threads(ftgpu_model *m, int threads) {
   if (threads < 64 || threads > 512 || threads % 32) return fail(FTGPU_ERR_INPUT, "node threads");
   m->node_threads = threads;
   drop_graphs(m);
+  return FTGPU_OK;
+}
+
+int ftgpu_set_node_split(ftgpu_model *m, int on) {
+  if (!m || (on != 0 && on != 1)) return fail(FTGPU_ERR_INPUT, "set_node_split");
+  if (m->node_split == on) return FTGPU_OK;
+  m->node_split = on;
+  if (m->setup_done) {
+    CK(cudaSetDevice(m->device));
+    CKI(upload_split(m));
+    drop_graphs(m);
+  }
   return FTGPU_OK;
 }
 

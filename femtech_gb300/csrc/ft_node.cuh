@@ -845,25 +845,27 @@ __device__ __forceinline__ void node_step(const NodeArgs &A, long long n, R &eke
 __global__ void __launch_bounds__(512, 2) k_node_free(const NodeArgs A) {
   const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= A.N) return;
-  const int kind = A.nkind[n];
-  if (kind & kNodeRest) return;
   const long long N = A.N;
-  const int4 sr = A.slot4[n];
+  // every load of the node up front (a rest node's are wasted, the others'
+  // latencies overlap): kind, slot records, state, 1/m
+  const int kind = __ldg(A.nkind + n);
+  const int4 sr = __ldg(A.slot4 + n);
   int4 sr2 = make_int4(-1, -1, -1, -1);
-  if (A.slot4b) sr2 = A.slot4b[n];
-  const int inst = A.node_inst ? A.node_inst[n] : 0;
-  int fn[3] = {kBcFree, kBcFree, kBcFree};
-  if (kind & kNodeBcCached) {
-#pragma unroll
-    for (int d = 0; d < 3; ++d) fn[d] = A.nbc[d * N + n];
-  }
+  if (A.slot4b) sr2 = __ldg(A.slot4b + n);
+  const int inst = A.node_inst ? __ldg(A.node_inst + n) : 0;
   double u0[3], vh0[3];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    u0[d] = A.u[d * N + n];
+    u0[d] = A.u[d * N + n];  // (read and written here: plain loads)
     vh0[d] = A.vh[d * N + n];
   }
-  const float minv = A.minv[n];
+  const float minv = __ldg(A.minv + n);
+  if (kind & kNodeRest) return;
+  int fn[3] = {kBcFree, kBcFree, kBcFree};
+  if (kind & kNodeBcCached) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) fn[d] = __ldg(A.nbc + d * N + n);
+  }
   const Slot4<float> *sF = reinterpret_cast<const Slot4<float> *>(A.sF);
   const bool csr = sr.x == kSlotCsr;
   const int s4[4] = {sr.x, sr.y, sr.z, sr.w};
@@ -873,7 +875,10 @@ __global__ void __launch_bounds__(512, 2) k_node_free(const NodeArgs A) {
     Slot4<float> q[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j)
-      if (s4[j] >= 0) q[j] = sF[s4[j]];
+      if (s4[j] >= 0) {
+        const float4 v = __ldg(reinterpret_cast<const float4 *>(sF + s4[j]));
+        q[j] = Slot4<float>{v.x, v.y, v.z, v.w};
+      }
 #pragma unroll
     for (int j = 0; j < 4; ++j)
       if (s4[j] >= 0) {

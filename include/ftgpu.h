@@ -165,6 +165,12 @@ int ftgpu_set_patch_size(ftgpu_model *m, int elements_per_patch);
  * default 256).  Exposed for the autotuner. */
 int ftgpu_set_node_threads(ftgpu_model *m, int threads);
 
+/* Mixed precision: the nodal pass as a lean kernel over the free and
+ * function-driven nodes plus the general kernel over the rest (1, the
+ * default), or the general kernel over every node (0).  Same results either
+ * way.  Exposed for the autotuner; no counterpart in the reference. */
+int ftgpu_set_node_split(ftgpu_model *m, int on);
+
 /* One-time setup on the device: element patches, reference shape-function
  * data and the lumped mass.  Replaces ShapeFunctions() (ShapeFunctions.cpp:32)
  * and AssembleLumpedMass() (Mass3D.cpp:127). */
