@@ -169,6 +169,19 @@ def build_workload(nx=NX, ny=NY, nz=NZ, lx=LX, ly=LY, lz=LZ):
     return mg.ogden_block_case(nx=nx, ny=ny, nz=nz, lx=lx, ly=ly, lz=lz, jitter=0.1, seed=0)
 
 
+def host_cpu():
+    """The host CPU's model name (lscpu), else the machine type."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name:"):
+                return ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    import platform
+    return platform.machine()
+
+
 def cpu_reference_rate(threads, target_s=12.0, kind="port"):
     """Element-updates/s of the FP64 reference algorithm on host cores, on a
     bounded sub-block (40x40x20 of the same spacing, jitter, law and loads)."""
@@ -192,7 +205,7 @@ def cpu_reference_rate(threads, target_s=12.0, kind="port"):
                               out_every=0)
     dt = time.perf_counter() - t
     rate = E * res["steps"] / dt
-    return dict(value=rate, unit="element-updates/s", cores=threads, kind=kind,
+    return dict(value=rate, unit="element-updates/s", cores=threads, kind=kind, cpu=host_cpu(),
                 sample="%dx%dx%d sub-block (%d C3D8, same spacing/jitter/law/loads), FP64, %d steps "
                        "incl. initial force and dt, %.1f s" % (sub + (E, res["steps"], dt)))
 

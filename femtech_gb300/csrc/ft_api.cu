@@ -1698,12 +1698,26 @@ int ftgpu_init_explicit(ftgpu_model *m, double reduction, double failure_dt, dou
   CK(cudaGetLastError());
   CKI(launch_node(m, kNodeScatterU, 0));
   CKI(fill_dtmin(m));
-  CKI(launch_groups(m, 0, 0, 0.0, 0, 1));
-  k_clock_init<<<(m->ninst + 127) / 128, 128, 0, m->stream>>>(
-      m->clock.as<Clock>(), m->dtmin.as<unsigned long long>(), m->instp.as<InstParams>(),
-      m->ninst, m->t0);
-  CK(cudaGetLastError());
-  CKI(launch_groups(m, 0, 1, 0.0, 0, 0));
+  // The initial force needs the initial dt only where a Prony series
+  // integrates over it (materials 5, 7): there a dt pass runs first and the
+  // force pass reads the clock; otherwise the force pass itself gives the dt
+  // minimum (it always contributes the elements' l/c), then the clock starts.
+  bool prony = false;
+  for (const PatchGroup &g : m->ps.groups) prony |= g.npatch > 0 && (g.mat == 5 || g.mat == 7);
+  if (prony) {
+    CKI(launch_groups(m, 0, 0, 0.0, 0, 1));
+    k_clock_init<<<(m->ninst + 127) / 128, 128, 0, m->stream>>>(
+        m->clock.as<Clock>(), m->dtmin.as<unsigned long long>(), m->instp.as<InstParams>(),
+        m->ninst, m->t0);
+    CK(cudaGetLastError());
+    CKI(launch_groups(m, 0, 1, 0.0, 0, 0));
+  } else {
+    CKI(launch_groups(m, 0, 0, 0.0, 0, 0));
+    k_clock_init<<<(m->ninst + 127) / 128, 128, 0, m->stream>>>(
+        m->clock.as<Clock>(), m->dtmin.as<unsigned long long>(), m->instp.as<InstParams>(),
+        m->ninst, m->t0);
+    CK(cudaGetLastError());
+  }
   if (m->injury_on) {  // the injury state starts from zero with the loop
     const size_t rb = is_fp64(m) ? sizeof(double) : sizeof(float);
     CK(cudaMemsetAsync(m->inj_ps_old.p, 0, m->inj_n * rb, m->stream));
