@@ -686,13 +686,18 @@ __global__ void __launch_bounds__(kElemThreads, ET == 0 ? 2 : 4)
   // per-element data, before the slot staging
   constexpr int NH = (ET == 1 && (MAT == 5 || MAT == 7)) ? (MAT == 5 ? 18 : 12) : 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  // staged slots as {x, y, z, pad} records: one vector load per corner
+  // staged slots: C3D8 as {x, y, z, pad} records (one vector load per corner),
+  // C3D4 as three component arrays (its four scattered corners: 32-bit loads
+  // meet fewer bank conflicts; the head's element pass measured 3 % faster)
+  constexpr bool PACK = ET == 0;
   Slot4<R> *shX = reinterpret_cast<Slot4<R> *>(smem_raw);
   Slot4<R> *shU = shX + kMaxLocalNodes;
+  R *shXs = reinterpret_cast<R *>(smem_raw);
+  R *shUs = shXs + 3 * kMaxLocalNodes;
   // [NC*3][blockDim] corner forces; FP32 C3D8: first the elements' reference
   // geometry, [20][blockDim] x 4 values, in the same space (a barrier
   // separates the last geometry read from the first corner-force write)
-  R *shF = reinterpret_cast<R *>(shU + kMaxLocalNodes);
+  R *shF = PACK ? reinterpret_cast<R *>(shU + kMaxLocalNodes) : shUs + 3 * kMaxLocalNodes;
   constexpr bool GEO = ET == 0 && sizeof(R) == 4;
   const int PE = blockDim.x;
   const int t = threadIdx.x;
@@ -742,8 +747,19 @@ __global__ void __launch_bounds__(kElemThreads, ET == 0 ? 2 : 4)
   }
   const Clock *ck = A.clock + A.parity * A.ninst + inst;
   for (int i = t; i < ns; i += PE) {
-    shU[i] = reinterpret_cast<const Slot4<R> *>(A.sU)[s0 + i];
-    shX[i] = Slot4<R>{A.sX[s0 + i], A.sX[A.S + s0 + i], A.sX[2 * A.S + s0 + i], R(0)};
+    const Slot4<R> us = reinterpret_cast<const Slot4<R> *>(A.sU)[s0 + i];
+    const R x0 = A.sX[s0 + i], x1 = A.sX[A.S + s0 + i], x2 = A.sX[2 * A.S + s0 + i];
+    if (PACK) {
+      shU[i] = us;
+      shX[i] = Slot4<R>{x0, x1, x2, R(0)};
+    } else {
+      shXs[i] = x0;
+      shXs[kMaxLocalNodes + i] = x1;
+      shXs[2 * kMaxLocalNodes + i] = x2;
+      shUs[i] = us.x;
+      shUs[kMaxLocalNodes + i] = us.y;
+      shUs[2 * kMaxLocalNodes + i] = us.z;
+    }
   }
   if (GEO) cp_async_wait_all();  // this thread's geometry rows
   // an instance past its end time: the whole block leaves (uniform per patch)
@@ -769,9 +785,17 @@ __global__ void __launch_bounds__(kElemThreads, ET == 0 ? 2 : 4)
     for (int a = 0; a < NC; ++a) {
       int l = lc[a] < ns ? lc[a] : 0;
       if (lc[a] >= ns) bad |= 2;
-      const Slot4<R> xs = shX[l], us = shU[l];
-      x[a][0] = xs.x; x[a][1] = xs.y; x[a][2] = xs.z;
-      u[a][0] = us.x; u[a][1] = us.y; u[a][2] = us.z;
+      if (PACK) {
+        const Slot4<R> xs = shX[l], us = shU[l];
+        x[a][0] = xs.x; x[a][1] = xs.y; x[a][2] = xs.z;
+        u[a][0] = us.x; u[a][1] = us.y; u[a][2] = us.z;
+      } else {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          x[a][d] = shXs[d * kMaxLocalNodes + l];
+          u[a][d] = shUs[d * kMaxLocalNodes + l];
+        }
+      }
     }
     R Es[6];  // injury: the element's averaged Green strain (as k_elem_strain)
     if (INJ && ci >= 0) element_green_strain<R, ET>(x, u, Es);
