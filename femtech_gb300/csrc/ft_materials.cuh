@@ -420,14 +420,18 @@ __device__ __forceinline__ Sym6<R> mat_ogden(const MatP<R> &m, const R (&D)[3][3
     const R Ca = -I3 * iC3, Cb = -(1 + I1) * iC3, Cg = iC3;
     const R c = 2 * mu / alpha * exp_small(-alpha * R(1.0 / 3.0) * lnJ);
     const R t = trB * R(1.0 / 3.0);
-    const R ka = c * (Aa - Ca - t * (1 + Ca)), kb = c * (Ab - Cb - t * Cb),
-            kg = c * (Ag - Cg - t * Cg);
+    // the volumetric part J p C^{-1} in the same basis: C^{-1} = I + Ci, and
+    // J p = K (J^2 - 1) / 2 (HGOIsotropic.cpp:47 form) -- no second inverse
+    const R Jp = R(0.5) * m.K * Jm1 * (2 + Jm1);
+    const R ka = c * (Aa - Ca - t * (1 + Ca)) + Jp * (1 + Ca),
+            kb = c * (Ab - Cb - t * Cb) + Jp * Cb, kg = c * (Ag - Cg - t * Cg) + Jp * Cg;
     S.xx = ka + kb * e.xx + kg * M2.xx;
     S.yy = ka + kb * e.yy + kg * M2.yy;
     S.zz = ka + kb * e.zz + kg * M2.zz;
     S.yz = kb * e.yz + kg * M2.yz;
     S.xz = kb * e.xz + kg * M2.xz;
     S.xy = kb * e.xy + kg * M2.xy;
+    return S;
   } else {
     R w[3], V[3][3];
     jacobi_sym3<R, sizeof(R) == 4 ? 4 : 6>(e, w, V);
