@@ -434,16 +434,21 @@ __global__ void __launch_bounds__(256) k_mlp_infer(const bf16 *__restrict__ X, l
 // input image, an activation image and TMEM columns [128 s, 128 s + 128); row r
 // of its tile is TMEM lane r.  Warps 4s .. 4s+3 are the slot's epilogue (warp
 // 4s + q reaches lanes 32 q .. 32 q + 31); warp 12 issues every MMA from one
-// thread.  Per layer the slot's epilogue stores the layer's bias into the
-// accumulator columns (tcgen05.st), makes its operands visible and arrives on
-// full[s]; the MMA thread waits on full[s], issues the layer (tcgen05.mma,
-// M = 128, K = 16 per instruction, BF16 x BF16 -> FP32 accumulating onto the
-// bias) and commits to done[s]; the epilogue waits on done[s], reads the
-// accumulator (tcgen05.ld), applies SiLU and writes the BF16 activations as
-// the next layer's A operand.  While one slot runs its epilogue the tensor
-// core serves the others.  W0..W2 and b0..b2 are staged times 1/2 (exact), so
-// an accumulator holds h = z / 2 and SiLU(z) = z sigmoid(z) = h + h tanh(h)
-// is evaluated on BF16 pairs: one MUFU tanh and one FMA per two values.
+// thread.  Per layer the slot's epilogue makes its operand visible and
+// arrives on full[s]; the MMA thread waits on full[s], issues the layer
+// (tcgen05.mma, M = 128, K = 16 per instruction, BF16 x BF16 -> FP32) and
+// commits to done[s]; the epilogue waits on done[s], reads the accumulator
+// (tcgen05.ld), applies SiLU and writes the BF16 activations as the next
+// layer's A operand.  While one slot runs its epilogue the tensor core serves
+// the others.  The biases ride in the MMAs: every activation image carries
+// two constant columns of ones (columns 128, 129 of a K = 144 image; input
+// columns 14, 15, unused features) against the bias split into a BF16 high
+// part and the BF16 rounding of the rest (b = hi + lo to 2^-16) in the weight
+// images -- one more K = 16 MMA per hidden layer (the tensor core is mostly
+// idle) instead of a 128-column TMEM store per row and layer.  W0..W2 and
+// b0..b2 are staged times 1/2 (exact), so an accumulator holds h = z / 2 and
+// SiLU(z) = z sigmoid(z) = h + h tanh(h) is evaluated on BF16 pairs: one
+// MUFU tanh and one FMA per two values.
 // Every wait is bounded; a wait that gives
 // up raises a shared abort flag that ends all roles, and the error word.
 //
@@ -456,14 +461,15 @@ namespace tc {
 constexpr int kSlots = 3;
 constexpr int kMmaWarp = 4 * kSlots;               // warp 12
 constexpr int kThreads = 32 * (kMmaWarp + 1);      // 416: at most 4 warps per SMSP
-constexpr uint32_t kW0 = 0;                        // [128 x 16]     4 KB
-constexpr uint32_t kW1 = kW0 + 128 * 16 * 2;       // [128 x 128]   32 KB
-constexpr uint32_t kW2 = kW1 + 128 * 128 * 2;      // [128 x 128]   32 KB
-constexpr uint32_t kW3 = kW2 + 128 * 128 * 2;      // [16 x 128]     4 KB (rows 8..15 zero)
-constexpr uint32_t kXs = kW3 + 16 * 128 * 2;       // per slot [128 x 16]    4 KB
-constexpr uint32_t kHs = kXs + kSlots * 4096;      // per slot [128 x 128]  32 KB
-constexpr uint32_t kBias = kHs + kSlots * 32768;   // FP32 b0/2 b1/2 b2/2 (128 each), b3 (16)
-constexpr uint32_t kBar = kBias + (3 * 128 + 16) * 4;  // full[], done[], TMEM base, abort
+constexpr int kKH = kMlpHid + 16;                  // hidden K plus the bias columns (144)
+constexpr uint32_t kSBOH = 16 * kKH;               // 8-row group stride of a K = 144 image
+constexpr uint32_t kW0 = 0;                        // [128 x 16]     4 KB (bias in columns 14, 15)
+constexpr uint32_t kW1 = kW0 + 128 * 16 * 2;       // [128 x 144]   36 KB
+constexpr uint32_t kW2 = kW1 + 128 * kKH * 2;      // [128 x 144]   36 KB
+constexpr uint32_t kW3 = kW2 + 128 * kKH * 2;      // [16 x 144]   4.5 KB (rows 8..15 zero)
+constexpr uint32_t kXs = kW3 + 16 * kKH * 2;       // per slot [128 x 16]    4 KB
+constexpr uint32_t kHs = kXs + kSlots * 4096;      // per slot [128 x 144]  36 KB
+constexpr uint32_t kBar = kHs + kSlots * 128 * kKH * 2;  // full[], done[], TMEM base, abort
 constexpr uint32_t kSmem = kBar + 72 + 128;        // + alignment slack of the base
 constexpr uint32_t kTmemCols = 512;               // 128 per slot, rounded to a power of 2
 constexpr int kWaitLimit = 1 << 21;                // try_wait rounds before giving up
@@ -569,56 +575,45 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
 }
 
-// the same value row (bias) into n = 32 or 16 consecutive columns of this
-// thread's lane; completion is awaited with tmem_st_wait before the MMA
-__device__ __forceinline__ void tmem_st_row32(uint32_t taddr, const float *row) {
-  const float4 *q = reinterpret_cast<const float4 *>(row);
-  float4 a[8];
-#pragma unroll
-  for (int i = 0; i < 8; ++i) a[i] = q[i];
-  asm volatile(
-      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
-      "%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};\n" ::"r"(
-          taddr),
-      "f"(a[0].x), "f"(a[0].y), "f"(a[0].z), "f"(a[0].w), "f"(a[1].x), "f"(a[1].y), "f"(a[1].z),
-      "f"(a[1].w), "f"(a[2].x), "f"(a[2].y), "f"(a[2].z), "f"(a[2].w), "f"(a[3].x), "f"(a[3].y),
-      "f"(a[3].z), "f"(a[3].w), "f"(a[4].x), "f"(a[4].y), "f"(a[4].z), "f"(a[4].w), "f"(a[5].x),
-      "f"(a[5].y), "f"(a[5].z), "f"(a[5].w), "f"(a[6].x), "f"(a[6].y), "f"(a[6].z), "f"(a[6].w),
-      "f"(a[7].x), "f"(a[7].y), "f"(a[7].z), "f"(a[7].w)
-      : "memory");
-}
-__device__ __forceinline__ void tmem_st_row16(uint32_t taddr, const float *row) {
-  const float4 *q = reinterpret_cast<const float4 *>(row);
-  float4 a[4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) a[i] = q[i];
-  asm volatile(
-      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
-      "%13,%14,%15,%16};\n" ::"r"(taddr),
-      "f"(a[0].x), "f"(a[0].y), "f"(a[0].z), "f"(a[0].w), "f"(a[1].x), "f"(a[1].y), "f"(a[1].z),
-      "f"(a[1].w), "f"(a[2].x), "f"(a[2].y), "f"(a[2].z), "f"(a[2].w), "f"(a[3].x), "f"(a[3].y),
-      "f"(a[3].z), "f"(a[3].w)
-      : "memory");
-}
-__device__ __forceinline__ void tmem_st_wait() {
-  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-}
-
-// rows [0, rows) x K columns of a row-major BF16 matrix (times `scale`, a
-// power of two) into the K-major core-matrix image, rows up to rows_pad zero;
-// consecutive threads write consecutive 16-byte chunks of the image
-__device__ __forceinline__ void stage_kmajor(unsigned char *img, const bf16 *src, int rows,
-                                             int rows_pad, int K, float scale) {
-  for (int d = threadIdx.x; d < rows_pad * (K / 8); d += blockDim.x) {
-    const int g = d / K, rem = d - g * K;  // 8-row group, chunk within the group
-    const int q = rem >> 3, r = 8 * g + (rem & 7);
+// A row-major BF16 weight matrix [rows x Ks] (times `scale`) into a K-major
+// core-matrix image with K = Ks + 16 whose columns Ks, Ks + 1 hold the bias
+// (times `scale`) as a BF16 high part and the BF16 rounding of the rest; rows
+// up to rows_pad zero.  For the K = 16 input layer (Ks = 16) the bias goes
+// into columns 14, 15 instead (bcol), replacing weights of unused features.
+__device__ __forceinline__ void stage_kmajor_bias(unsigned char *img, const bf16 *src,
+                                                  const float *b, int rows, int rows_pad, int Ks,
+                                                  int Ki, int bcol, float scale) {
+  // chunk d of the image (16 bytes) is row 8 g + rr, columns 8 q .. 8 q + 7,
+  // with d = (g * (Ki / 8) + q) * 8 + rr: consecutive threads write
+  // consecutive chunks, rows_pad * Ki / 8 chunks in all
+  const int per_group = Ki;  // chunks per 8-row group: (Ki / 8) * 8
+  for (int d = threadIdx.x; d < rows_pad * (Ki / 8); d += blockDim.x) {
+    const int g = d / per_group, rem = d - g * per_group;
+    const int q = rem >> 3, r = 8 * g + (rem & 7), k0 = 8 * q;
     uint4 v = make_uint4(0u, 0u, 0u, 0u);
     if (r < rows) {
-      v = *reinterpret_cast<const uint4 *>(src + (long long)r * K + 8 * q);
-      if (scale != 1.f) {
-        bf16 *e = reinterpret_cast<bf16 *>(&v);
+      bf16 *e = reinterpret_cast<bf16 *>(&v);
+      if (k0 + 8 <= Ks && (bcol >= k0 + 8 || bcol + 1 < k0)) {
+        v = *reinterpret_cast<const uint4 *>(src + (long long)r * Ks + k0);
+        if (scale != 1.f) {
 #pragma unroll
-        for (int j = 0; j < 8; ++j) e[j] = __float2bfloat16_rn(__bfloat162float(e[j]) * scale);
+          for (int j = 0; j < 8; ++j) e[j] = __float2bfloat16_rn(__bfloat162float(e[j]) * scale);
+        }
+      } else {
+        const float bs = b[r] * scale;
+        const bf16 hi = __float2bfloat16_rn(bs);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int k = k0 + j;
+          float w = 0.f;
+          if (k == bcol)
+            w = __bfloat162float(hi);
+          else if (k == bcol + 1)
+            w = bs - __bfloat162float(hi);
+          else if (k < Ks)
+            w = __bfloat162float(src[(long long)r * Ks + k]) * scale;
+          e[j] = __float2bfloat16_rn(w);
+        }
       }
     }
     *reinterpret_cast<uint4 *>(img + 16 * d) = v;
@@ -633,7 +628,7 @@ __device__ __forceinline__ void tc_silu_chunk(uint32_t taddr, unsigned char *hs,
   uint32_t pk[16];
 #pragma unroll
   for (int j = 0; j < 16; ++j) pk[j] = silu_h_bf16x2(v[2 * j], v[2 * j + 1]);
-  unsigned char *dst = hs + (r / 8) * 2048 + (r % 8) * 16 + (c0 / 8) * 128;
+  unsigned char *dst = hs + (r / 8) * tc::kSBOH + (r % 8) * 16 + (c0 / 8) * 128;
 #pragma unroll
   for (int i = 0; i < 4; ++i)
     *reinterpret_cast<uint4 *>(dst + i * 128) =
@@ -645,16 +640,16 @@ __device__ __forceinline__ void tc_issue_layer(int layer, uint32_t tmem_d, uint3
                                                uint32_t sH, uint32_t sW0, uint32_t sW1,
                                                uint32_t sW2, uint32_t sW3) {
   constexpr uint32_t id128 = umma_idesc_bf16(128, 128), id16 = umma_idesc_bf16(128, 16);
-  if (layer == 0) {
-    umma_bf16(tmem_d, umma_sdesc(sX, 128, 256), umma_sdesc(sW0, 128, 256), id128, 1u);
+  if (layer == 0) {  // the bias comes with the input's constant columns
+    umma_bf16(tmem_d, umma_sdesc(sX, 128, 256), umma_sdesc(sW0, 128, 256), id128, 0u);
     return;
   }
   const uint32_t sW = layer == 1 ? sW1 : (layer == 2 ? sW2 : sW3);
   const uint32_t id = layer == 3 ? id16 : id128;
 #pragma unroll
-  for (int kk = 0; kk < 8; ++kk)
-    umma_bf16(tmem_d, umma_sdesc(sH + 256 * kk, 128, 2048), umma_sdesc(sW + 256 * kk, 128, 2048),
-              id, 1u);
+  for (int kk = 0; kk < tc::kKH / 16; ++kk)  // 8 steps of weights, 1 of bias columns
+    umma_bf16(tmem_d, umma_sdesc(sH + 256 * kk, 128, tc::kSBOH),
+              umma_sdesc(sW + 256 * kk, 128, tc::kSBOH), id, kk > 0 ? 1u : 0u);
 }
 
 __global__ void __maxnreg__(128)
@@ -663,22 +658,27 @@ __global__ void __maxnreg__(128)
   extern __shared__ __align__(128) unsigned char tc_raw[];
   unsigned char *sm = tc_raw + ((128 - (smem_u32(tc_raw) & 127)) & 127);
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-  float *bias = reinterpret_cast<float *>(sm + tc::kBias);
   const uint32_t full0 = smem_u32(sm + tc::kBar), done0 = full0 + 8 * tc::kSlots;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(sm + tc::kBar + 64);
   volatile int *abort = reinterpret_cast<volatile int *>(sm + tc::kBar + 68);
 
-  // weights and biases, once per CTA (layers 0..2 times 1/2, see above)
-  stage_kmajor(sm + tc::kW0, Wg + kOffW0, kMlpHid, kMlpHid, kMlpIn, 0.5f);
-  stage_kmajor(sm + tc::kW1, Wg + kOffW1, kMlpHid, kMlpHid, kMlpHid, 0.5f);
-  stage_kmajor(sm + tc::kW2, Wg + kOffW2, kMlpHid, kMlpHid, kMlpHid, 0.5f);
-  stage_kmajor(sm + tc::kW3, Wg + kOffW3, kMlpOut, 16, kMlpHid, 1.f);
-  for (int i = t; i < kMlpHid; i += blockDim.x) {
-    bias[i] = 0.5f * P[kOffB0 + i];
-    bias[kMlpHid + i] = 0.5f * P[kOffB1 + i];
-    bias[2 * kMlpHid + i] = 0.5f * P[kOffB2 + i];
+  // weights with their biases, once per CTA (layers 0..2 times 1/2, see above)
+  stage_kmajor_bias(sm + tc::kW0, Wg + kOffW0, P + kOffB0, kMlpHid, kMlpHid, kMlpIn, kMlpIn,
+                    kMlpIn - 2, 0.5f);
+  stage_kmajor_bias(sm + tc::kW1, Wg + kOffW1, P + kOffB1, kMlpHid, kMlpHid, kMlpHid, tc::kKH,
+                    kMlpHid, 0.5f);
+  stage_kmajor_bias(sm + tc::kW2, Wg + kOffW2, P + kOffB2, kMlpHid, kMlpHid, kMlpHid, tc::kKH,
+                    kMlpHid, 0.5f);
+  stage_kmajor_bias(sm + tc::kW3, Wg + kOffW3, P + kOffB3, kMlpOut, 16, kMlpHid, tc::kKH,
+                    kMlpHid, 1.f);
+  // the constant columns of every slot's activation image: ones in columns
+  // 128, 129, zeros in 130..143 (the epilogues write columns 0..127 only)
+  for (int d = t; d < tc::kSlots * 128; d += blockDim.x) {
+    const int sl = d / 128, r = d - sl * 128;
+    unsigned char *row = sm + tc::kHs + sl * 128 * tc::kKH * 2 + (r / 8) * tc::kSBOH + (r % 8) * 16;
+    *reinterpret_cast<uint4 *>(row + 16 * 128) = make_uint4(0x3F803F80u, 0u, 0u, 0u);
+    *reinterpret_cast<uint4 *>(row + 17 * 128) = make_uint4(0u, 0u, 0u, 0u);
   }
-  if (t < 16) bias[3 * kMlpHid + t] = t < kMlpOut ? P[kOffB3 + t] : 0.f;
   if (t == 0) {
     for (int sl = 0; sl < tc::kSlots; ++sl) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 128;" ::"r"(full0 + 8 * sl) : "memory");
@@ -708,7 +708,7 @@ __global__ void __maxnreg__(128)
     const int s = warp >> 2, q = warp & 3, r = 32 * q + lane;
     const uint32_t tl = tbase + ((uint32_t)(32 * q) << 16) + 128u * s;
     const uint32_t full = full0 + 8 * s, done = done0 + 8 * s;
-    unsigned char *xs = sm + tc::kXs + 4096 * s, *hs = sm + tc::kHs + 32768 * s;
+    unsigned char *xs = sm + tc::kXs + 4096 * s, *hs = sm + tc::kHs + 128 * tc::kKH * 2 * s;
     const long long first = (long long)tc::kSlots * blockIdx.x + s;
     uint32_t j = 0;  // steps (layers) completed: the parity of the next wait
     uint4 xa = make_uint4(0u, 0u, 0u, 0u), xb = xa;
@@ -720,12 +720,10 @@ __global__ void __maxnreg__(128)
     bool ok = true;
     for (long long tile = first; tile < tiles && ok; tile += stride) {
       const long long row = tile * 128 + r;
-      // layer 0 operands: the input rows and b0 in the accumulator
+      // layer 0 operand: the input row with ones in the bias columns 14, 15
       unsigned char *xd = xs + (r / 8) * 256 + (r % 8) * 16;
       *reinterpret_cast<uint4 *>(xd) = xa;
-      *reinterpret_cast<uint4 *>(xd + 128) = xb;
-#pragma unroll
-      for (int c = 0; c < 4; ++c) tmem_st_row32(tl + 32 * c, bias + 32 * c);
+      *reinterpret_cast<uint4 *>(xd + 128) = make_uint4(xb.x, xb.y, xb.z, 0x3F803F80u);
       {  // the next tile's rows, loaded while this one runs
         const long long nrow = (tile + stride) * 128 + r;
         xa = make_uint4(0u, 0u, 0u, 0u);
@@ -736,7 +734,6 @@ __global__ void __maxnreg__(128)
           xb = src[1];
         }
       }
-      tmem_st_wait();
       fence_proxy_async_smem();
       tc_fence_before();
       mbar_arrive(full);
@@ -748,14 +745,7 @@ __global__ void __maxnreg__(128)
         if (!ok) break;
         if (l < 3) {
 #pragma unroll 1
-          for (int c = 0; c < 4; ++c) {
-            tc_silu_chunk(tl + 32 * c, hs, r, 32 * c);
-            if (l < 2)
-              tmem_st_row32(tl + 32 * c, bias + 128 * (l + 1) + 32 * c);
-            else if (c == 0)
-              tmem_st_row16(tl, bias + 3 * kMlpHid);
-          }
-          tmem_st_wait();
+          for (int c = 0; c < 4; ++c) tc_silu_chunk(tl + 32 * c, hs, r, 32 * c);
           fence_proxy_async_smem();
           tc_fence_before();
           mbar_arrive(full);
@@ -790,7 +780,8 @@ __global__ void __maxnreg__(128)
         if (!ok) break;
         tc_fence_after();
         tc_issue_layer((int)(js[sl] & 3u), tbase + 128u * sl,
-                       smem_u32(sm + tc::kXs + 4096 * sl), smem_u32(sm + tc::kHs + 32768 * sl),
+                       smem_u32(sm + tc::kXs + 4096 * sl),
+                       smem_u32(sm + tc::kHs + 128 * tc::kKH * 2 * sl),
                        sW0, sW1, sW2, sW3);
         umma_commit(done0 + 8 * sl);
         ++js[sl];
