@@ -68,14 +68,15 @@ NODE_BYTES_PER_NODE = 116.0
 # FP32 operations of one C3D8 Ogden element-update in this formulation
 # (small-strain series path), counted from the kernel source (ft_elem.cuh /
 # ft_materials.cuh), FMA = 2: per Gauss point displacement-gradient columns
-# 54, D = H A^-T 45, J - 1 27, Ogden series law 313 (2E 40, norm 11, M^2 30,
-# invariants 21, seven Cayley-Hamilton steps of the I / M / M^2 coefficients
-# of the A and tr B series 126, exact (I + M)^-1 7, coefficients of S 15,
-# J^-alpha/3 5, S 21, volumetric 37), det A S 6, P = S + D S 54, P A^-1 45,
-# moments 63 -> 607 per Gauss point, 4856 for 8; Hadamard transform of u 75,
-# face areas 540, inverse transform 90.  (A^-1 and det A of the reference
-# geometry are read from the set-up table, not recomputed.)
-FLOP_PER_EL_OGDEN = 4856 + 75 + 540 + 90
+# 54, D = H A^-T 45, J - 1 27, Ogden series law 291 (2E 40, norm 11, M^2 30,
+# invariants 21, eight Cayley-Hamilton steps of the I / M / M^2 coefficients
+# of the A series 88, tr B from A 16, exact (I + M)^-1 7, coefficients of S
+# 15, J^-alpha/3 5, S 21, volumetric 37), det A S 6, P = S + D S 54, P A^-1
+# 45, moments 63 -> 585 per Gauss point, 4680 for 8; Hadamard transform of u
+# 75, face areas 540, inverse transform 90.  (A^-1 and det A of the reference
+# geometry are read from the set-up table, not recomputed.)  ncu counts
+# 1858 FFMA + 795 FADD + 844 FMUL = 5355 per element on this path.
+FLOP_PER_EL_OGDEN = 4680 + 75 + 540 + 90
 
 
 def log(*a):

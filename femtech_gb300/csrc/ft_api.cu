@@ -889,26 +889,24 @@ int upload_materials(ftgpu_model *m) {
     q.inv_ce = R(1.0 / ce);
     q.mat = m->materialID[p];
     if (q.mat == 6) {
-      // binomial coefficients of (1+x)^(alpha/2-1) and (1+x)^(alpha/2), powers 1..n
+      // binomial coefficients of (1+x)^(alpha/2-1), powers 1..n
       const double a = pr[3];
-      double ba = 1.0, bb = 1.0;
+      double ba = 1.0;
       for (int k = 0; k < kOgdenSeries; ++k) {
         ba *= (a / 2.0 - 1.0 - k) / (k + 1.0);
-        bb *= (a / 2.0 - k) / (k + 1.0);
         q.ser_a[k] = R(ba);
-        q.ser_b[k] = R(bb);
       }
       // FP32 path: the series while |2E|_F < r, r the largest radius (at most
-      // 0.3) whose truncation bound sum_{k > n} (|b_a,k| + 2 |b_b,k|) r^k
-      // stays below 1e-7 r (FP32 rounding of the leading term); FP64 mode
-      // keeps the eigen path
+      // 0.3) whose truncation bound sum_{k > n} |b_a,k| (3 + 2 r) r^k stays
+      // below 1e-7 r (FP32 rounding of the leading term; the 1 + 2 (1 + r)
+      // weighs A itself and tr B = tr(A + M + M A)); FP64 mode keeps the
+      // eigen path
       auto tail = [&](double r) {
-        double ca = ba, cb = bb, rk = std::pow(r, kOgdenSeries), t = 0.0;
+        double ca = ba, rk = std::pow(r, kOgdenSeries), t = 0.0;
         for (int k = kOgdenSeries; k < kOgdenSeries + 400; ++k) {
           ca *= (a / 2.0 - 1.0 - k) / (k + 1.0);
-          cb *= (a / 2.0 - k) / (k + 1.0);
           rk *= r;
-          t += (std::fabs(ca) + 2.0 * std::fabs(cb)) * rk;
+          t += std::fabs(ca) * (3.0 + 2.0 * r) * rk;
         }
         return t;
       };

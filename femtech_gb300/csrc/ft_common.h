@@ -13,6 +13,13 @@ constexpr int kMaxPatchElems = 256;   // elements per patch (thread block) upper
 constexpr int kMaxLocalNodes = 320;   // local nodes per patch (shared memory bound)
 constexpr int kElemThreads = 256;     // upper bound of threads per element block
 
+// Shared memory of an element block's staged local CSR (the in-block
+// assembly's offsets and corner entries, 16-bit): kMaxLocalNodes + 1 offsets
+// padded to 8, then NC entries per element.
+__host__ __device__ constexpr size_t elem_csr_smem_bytes(int NC, int PE) {
+  return 2 * ((size_t)kMaxLocalNodes + 8) + 2 * (size_t)NC * PE;
+}
+
 // Per-instance clock, double-buffered by step parity.  Between steps it holds
 // the state the reference keeps in the globals Time and dt (ex9.cpp:9).
 struct Clock {

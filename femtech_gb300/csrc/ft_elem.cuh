@@ -64,6 +64,13 @@ __device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc) {
   const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(smem_dst));
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gsrc) : "memory");
 }
+// 4- or 8-byte asynchronous global -> shared copy (addresses aligned to n)
+template <int NB>
+__device__ __forceinline__ void cp_async_small(void *smem_dst, const void *gsrc) {
+  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(smem_dst));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(d), "l"(gsrc), "n"(NB)
+               : "memory");
+}
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
@@ -700,6 +707,9 @@ __global__ void __launch_bounds__(kElemThreads, ET == 0 ? 2 : 4)
   R *shF = PACK ? reinterpret_cast<R *>(shU + kMaxLocalNodes) : shUs + 3 * kMaxLocalNodes;
   constexpr bool GEO = ET == 0 && sizeof(R) == 4;
   const int PE = blockDim.x;
+  // the local CSR of the in-block assembly: offsets, then entries
+  uint16_t *shLp = reinterpret_cast<uint16_t *>(shF + (GEO ? 80 : NC * 3) * PE);
+  uint16_t *shLe = shLp + kMaxLocalNodes + 8;
   const int t = threadIdx.x;
   const int p = A.patch_begin + blockIdx.x;
   const int inst = A.patch_inst[p];
@@ -746,22 +756,39 @@ __global__ void __launch_bounds__(kElemThreads, ET == 0 ? 2 : 4)
     }
   }
   const Clock *ck = A.clock + A.parity * A.ninst + inst;
+  // the slot records go to shared memory by asynchronous copies, in flight
+  // together (and with the C3D8 geometry rows) until the one wait below; the
+  // padding word of a C3D8 coordinate record is never read
   for (int i = t; i < ns; i += PE) {
-    const Slot4<R> us = reinterpret_cast<const Slot4<R> *>(A.sU)[s0 + i];
-    const R x0 = A.sX[s0 + i], x1 = A.sX[A.S + s0 + i], x2 = A.sX[2 * A.S + s0 + i];
+    const R *us = A.sU + 4ll * (s0 + i);
     if (PACK) {
-      shU[i] = us;
-      shX[i] = Slot4<R>{x0, x1, x2, R(0)};
+#pragma unroll
+      for (int h = 0; h < (int)sizeof(Slot4<R>) / 16; ++h)
+        cp_async16(reinterpret_cast<char *>(shU + i) + 16 * h, us + h * (16 / sizeof(R)));
+      cp_async_small<sizeof(R)>(&shX[i].x, A.sX + s0 + i);
+      cp_async_small<sizeof(R)>(&shX[i].y, A.sX + A.S + s0 + i);
+      cp_async_small<sizeof(R)>(&shX[i].z, A.sX + 2 * A.S + s0 + i);
     } else {
-      shXs[i] = x0;
-      shXs[kMaxLocalNodes + i] = x1;
-      shXs[2 * kMaxLocalNodes + i] = x2;
-      shUs[i] = us.x;
-      shUs[kMaxLocalNodes + i] = us.y;
-      shUs[2 * kMaxLocalNodes + i] = us.z;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        cp_async_small<sizeof(R)>(shXs + d * kMaxLocalNodes + i, A.sX + d * A.S + s0 + i);
+        cp_async_small<sizeof(R)>(shUs + d * kMaxLocalNodes + i, us + d);
+      }
     }
   }
-  if (GEO) cp_async_wait_all();  // this thread's geometry rows
+  if (ET == 0 && pass == kPassForce) {
+    // C3D8: the assembly's local CSR travels with the slots (needed only at
+    // the end of the block, but its loads would then be a dependent chain;
+    // the latency-bound C3D4 blocks measured faster loading it at the end)
+    const int eo = A.patch_ent_off[p], en = A.patch_ent_off[p + 1] - eo;
+    if (((eo | en) & 7) == 0) {
+      for (int c = t; 8 * c < en; c += PE) cp_async16(shLe + 8 * c, A.lent + eo + 8 * c);
+    } else {
+      for (int c = t; c < en; c += PE) shLe[c] = A.lent[eo + c];
+    }
+    for (int i = t; i <= ns; i += PE) shLp[i] = A.lptr[s0 + p + i];
+  }
+  cp_async_wait_all();  // this thread's slot records (and geometry rows)
   // an instance past its end time: the whole block leaves (uniform per patch)
   if (A.use_clock && ck->done) return;
   const R dt = A.use_clock ? R(ck->dt) : R(A.dt_direct);
@@ -854,8 +881,8 @@ __global__ void __launch_bounds__(kElemThreads, ET == 0 ? 2 : 4)
   }
   if (pass != kPassForce) return;
   // in-block assembly: local node i sums its corners in (element, corner) order
-  const uint16_t *lp = A.lptr + s0 + p;
-  const uint16_t *le = A.lent + A.patch_ent_off[p];
+  const uint16_t *lp = ET == 0 ? shLp : A.lptr + s0 + p;
+  const uint16_t *le = ET == 0 ? shLe : A.lent + A.patch_ent_off[p];
   for (int i = t; i < ns; i += PE) {
     const int b = lp[i], en = lp[i + 1];
     R f0 = 0, f1 = 0, f2 = 0;

@@ -54,7 +54,8 @@ inline size_t elem_smem_bytes_host(int etype, int PE) {
   const int NC = etype == 0 ? 8 : 4;
   const size_t per_elem = (etype == 0 && sizeof(R) == 4) ? 80 : (size_t)NC * 3;
   const size_t slot_words = etype == 0 ? 8 : 6;  // packed records (C3D8) / component arrays
-  return sizeof(R) * (slot_words * (size_t)kMaxLocalNodes + per_elem * PE);
+  return sizeof(R) * (slot_words * (size_t)kMaxLocalNodes + per_elem * PE) +
+         (etype == 0 ? elem_csr_smem_bytes(NC, PE) : 0);
 }
 
 // Dynamic shared memory of one strain block (k_elem_strain): the slot

@@ -22,7 +22,7 @@ struct Sym6 {
   R xx, yy, zz, yz, xz, xy;
 };
 
-constexpr int kOgdenSeries = 8;  // terms of the small-strain Ogden series
+constexpr int kOgdenSeries = 9;  // terms of the small-strain Ogden series
 
 template <class R>
 struct MatP {  // per-part material parameters, precomputed on the host
@@ -32,12 +32,11 @@ struct MatP {  // per-part material parameters, precomputed on the host
   double ce;   // dilatational wave speed in FP64
   int mat;     // material ID
   int pad;
-  // Ogden: binomial coefficients binom(alpha/2 - 1, k) and binom(alpha/2, k),
-  // k = 1..kOgdenSeries, and the squared Frobenius bound on 2E below which
-  // the series is used (0 = always the eigen-decomposition; set on the host
-  // from the series' truncation bound for this alpha)
+  // Ogden: binomial coefficients binom(alpha/2 - 1, k), k = 1..kOgdenSeries,
+  // and the squared Frobenius bound on 2E below which the series is used
+  // (0 = always the eigen-decomposition; set on the host from the series'
+  // truncation bound for this alpha)
   R ser_a[kOgdenSeries];
-  R ser_b[kOgdenSeries];
   R ser_thr2;
 };
 
@@ -384,13 +383,15 @@ __device__ __forceinline__ Sym6<R> mat_ogden(const MatP<R> &m, const R (&D)[3][3
     // Small strain: with M = 2E = C - I the isochoric stress is
     //   S_iso = (2 mu/alpha) J^{-alpha/3} [C^{alpha/2-1} - tr(C^{alpha/2})/3 C^{-1}]
     //         = c [A - Ci - tr(B)/3 (I + Ci)],
-    // A = (I+M)^{alpha/2-1} - I and B = (I+M)^{alpha/2} - I binomial series
-    // in powers of M (exact to FP32 rounding below the host's bound on |M|_F,
-    // no eigenvectors, no cancellation of O(1) terms).  By Cayley-Hamilton
-    // every power is M^p = a I + b M + c M^2 with
+    // A = (I+M)^{alpha/2-1} - I, a binomial series in powers of M (exact to
+    // FP32 rounding below the host's bound on |M|_F, no eigenvectors, no
+    // cancellation of O(1) terms), and B = (I+M)^{alpha/2} - I = A + M + M A
+    // (exact: (I+M)^{alpha/2} = (I+M)(I+A)).  By Cayley-Hamilton every power
+    // is M^p = a I + b M + c M^2 with
     //   M^{p+1}: (a, b, c) <- (c I3, a - c I2, b + c I1),
-    // so the series reduce to scalar coefficients of I, M and M^2.  Ci =
-    // (I+M)^{-1} - I is exact by Cayley-Hamilton for C = I + M:
+    // so the series reduces to scalar coefficients of I, M and M^2, and
+    //   tr B = I1 + tr A + tr(M A),  tr M^3 = I1 tr M^2 - I2 I1 + 3 I3.
+    // Ci = (I+M)^{-1} - I is exact by Cayley-Hamilton for C = I + M:
     //   C^{-1} = (C^2 - I1(C) C + I2(C) I) / I3(C)
     //   => Ci = (-I3 I - (1 + I1) M + M^2) / (1 + I1 + I2 + I3)
     // (I1..I3: invariants of M; no cancellation).
@@ -403,7 +404,6 @@ __device__ __forceinline__ Sym6<R> mat_ogden(const MatP<R> &m, const R (&D)[3][3
     // power 1: (0, 1, 0)
     R pa = 0, pb = 1, pc = 0;
     R Aa = 0, Ab = m.ser_a[0], Ag = 0;  // A  = Aa I + Ab M + Ag M^2
-    R trB = m.ser_b[0] * I1;
 #pragma unroll
     for (int k = 1; k < kOgdenSeries; ++k) {
       const R na = pc * I3, nb = pa - pc * I2, nc = pb + pc * I1;
@@ -414,8 +414,9 @@ __device__ __forceinline__ Sym6<R> mat_ogden(const MatP<R> &m, const R (&D)[3][3
       Aa += sa * pa;
       Ab += sa * pb;
       Ag += sa * pc;
-      trB += m.ser_b[k] * (R(3) * pa + pb * I1 + pc * trM2);
     }
+    const R trM3 = I1 * (trM2 - I2) + R(3) * I3;
+    const R trB = I1 + (R(3) * Aa + Ab * I1 + Ag * trM2) + (Aa * I1 + Ab * trM2 + Ag * trM3);
     const R iC3 = R(1) / (1 + I1 + I2 + I3);  // Ci = Ca I + Cb M + Cg M^2
     const R Ca = -I3 * iC3, Cb = -(1 + I1) * iC3, Cg = iC3;
     const R c = 2 * mu / alpha * exp_small(-alpha * R(1.0 / 3.0) * lnJ);
