@@ -256,12 +256,16 @@ struct ftgpu_model {
   long long rest_n = 0;
   DBuf dX, u, v, a, vh, mass, minv, fi;
   DBuf gpF, gpJ, gpS;
-  // graph of one chunk of steps (plain, and with timing events)
-  cudaGraphExec_t chunk_exec = nullptr;
+  // graph of one chunk of steps (plain, and with timing events): the first
+  // chunk of a run opens with the half-step of ex9.cpp:109-138 from (u, v,
+  // a); the chunks after it continue from the half-step state the previous
+  // one left (cont_exec)
+  cudaGraphExec_t chunk_exec = nullptr, cont_exec = nullptr;
   int chunk_steps = 0;
   // shorter graphs of 2, 4, ..., 14 steps (index steps / 2) for the end of a
-  // run, so that a run of any length launches no steps past its limit
-  cudaGraphExec_t tail_exec[8] = {};
+  // run, so that a run of any length launches no steps past its limit: with
+  // the opening half-step (a run shorter than a chunk) and without it
+  cudaGraphExec_t tail_exec[8] = {}, tailc_exec[8] = {};
   cudaGraphExec_t prof_exec = nullptr;
   int prof_steps = 0;
   std::vector<cudaEvent_t> prof_ev;
@@ -274,7 +278,10 @@ struct ftgpu_model {
   std::vector<long long> surr_base;   // per group: first Gauss point in the buffers
   ~ftgpu_model() {
     if (chunk_exec) cudaGraphExecDestroy(chunk_exec);
+    if (cont_exec) cudaGraphExecDestroy(cont_exec);
     for (cudaGraphExec_t &e : tail_exec)
+      if (e) cudaGraphExecDestroy(e);
+    for (cudaGraphExec_t &e : tailc_exec)
       if (e) cudaGraphExecDestroy(e);
     if (prof_exec) cudaGraphExecDestroy(prof_exec);
     for (cudaEvent_t e : prof_ev) cudaEventDestroy(e);
@@ -298,12 +305,17 @@ bool is_fp64(const ftgpu_model *m) { return m->precision == FTGPU_FP64; }
 // Captured graphs bake in buffer pointers and BC tables: drop them whenever those change.
 void drop_graphs(ftgpu_model *m) {
   if (m->chunk_exec) cudaGraphExecDestroy(m->chunk_exec);
+  if (m->cont_exec) cudaGraphExecDestroy(m->cont_exec);
   for (cudaGraphExec_t &e : m->tail_exec) {
     if (e) cudaGraphExecDestroy(e);
     e = nullptr;
   }
+  for (cudaGraphExec_t &e : m->tailc_exec) {
+    if (e) cudaGraphExecDestroy(e);
+    e = nullptr;
+  }
   if (m->prof_exec) cudaGraphExecDestroy(m->prof_exec);
-  m->chunk_exec = m->prof_exec = nullptr;
+  m->chunk_exec = m->cont_exec = m->prof_exec = nullptr;
   m->chunk_steps = m->prof_steps = 0;
 }
 
@@ -1211,12 +1223,23 @@ int launch_injury(ftgpu_model *m, int parity) {
 // parity, so a graph of an even number of steps fits any starting step).
 constexpr int kChunkSteps = 16;
 
-int capture_chunk(ftgpu_model *m, int K, bool prof) {
+// A graph of K steps.  open: it starts with the half-step from (u, v, a)
+// (kNodeBegin); otherwise it continues from the half-step state that the
+// previous graph of the run left.  The steps are all fused (full step, then
+// the next half-step): the step that reaches the run's step limit, tmax or a
+// failed dt finishes instead (v and a at t_{n+1}, the state a run ends in),
+// so a run is a sequence of graphs without a finish / restart at their
+// seams.  prof: the timing graph (events around every pass), which opens
+// and finishes every chunk.
+int capture_chunk(ftgpu_model *m, int K, bool prof, bool open = true) {
   // a tail graph (even K from 2 to 14) is captured once and kept in its slot
   const bool tail = !prof && K < kChunkSteps;
   if (tail && (K < 2 || (K & 1))) return fail(FTGPU_ERR_INPUT, "tail graph of an odd step count");
+  if (prof) open = true;
   int tail_steps = K;  // the slot of a tail graph fixes its step count
-  cudaGraphExec_t &exec = tail ? m->tail_exec[K / 2] : prof ? m->prof_exec : m->chunk_exec;
+  cudaGraphExec_t &exec = tail ? (open ? m->tail_exec[K / 2] : m->tailc_exec[K / 2])
+                               : prof ? m->prof_exec : open ? m->chunk_exec : m->cont_exec;
+  // (the opening and continuing full chunks are both kChunkSteps long)
   int &steps = tail ? tail_steps : prof ? m->prof_steps : m->chunk_steps;
   if (exec && steps == K) return 0;
   if (exec) cudaGraphExecDestroy(exec);
@@ -1228,14 +1251,14 @@ int capture_chunk(ftgpu_model *m, int K, bool prof) {
   }
   cudaGraph_t g;
   CK(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
-  int r = launch_node(m, kNodeBegin, 0);
+  int r = open ? launch_node(m, kNodeBegin, 0) : 0;
   for (int k = 0; k < K && !r; ++k) {
     if (prof) r = (int)cudaEventRecordWithFlags(m->prof_ev[2 * k], m->stream, cudaEventRecordExternal);
     if (!r) r = launch_groups(m, k & 1, 1, 0.0, m->injury_on ? kLaunchInjury : kLaunchPlain, 0);
     if (prof && !r)
       r = (int)cudaEventRecordWithFlags(m->prof_ev[2 * k + 1], m->stream, cudaEventRecordExternal);
     if (!r && m->injury_on) r = launch_injury(m, k & 1);
-    if (!r) r = launch_node(m, k == K - 1 ? kNodeFinish : kNodeFused, k & 1);
+    if (!r) r = launch_node(m, prof && k == K - 1 ? kNodeFinish : kNodeFused, k & 1);
   }
   if (prof && !r) r = (int)cudaEventRecordWithFlags(m->prof_ev[2 * K], m->stream, cudaEventRecordExternal);
   cudaError_t ce = cudaStreamEndCapture(m->stream, &g);
@@ -1254,8 +1277,10 @@ int capture_chunk(ftgpu_model *m, int K, bool prof) {
 // conditions, energy, injury criteria, surrogate, driven nodes) drops them
 // and the next run captures again.
 int prepare_graphs(ftgpu_model *m) {
-  CKI(capture_chunk(m, kChunkSteps, false));
-  for (int K = 2; K < kChunkSteps; K += 2) CKI(capture_chunk(m, K, false));
+  for (bool open : {true, false}) {
+    CKI(capture_chunk(m, kChunkSteps, false, open));
+    for (int K = 2; K < kChunkSteps; K += 2) CKI(capture_chunk(m, K, false, open));
+  }
   return 0;
 }
 
@@ -1282,7 +1307,8 @@ int run_impl(ftgpu_model *m, int max_steps, int *steps_done, bool prof, double *
   CK(cudaMemcpyAsync(m->instp.p, m->inst.data(), ni * sizeof(InstParams), cudaMemcpyHostToDevice,
                      m->stream));
   const int K = kChunkSteps;
-  CKI(capture_chunk(m, K, prof));
+  CKI(capture_chunk(m, K, prof, true));
+  if (!prof) CKI(capture_chunk(m, K, false, false));
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (device_ms) {
     CK(cudaEventCreate(&e0));
@@ -1295,13 +1321,15 @@ int run_impl(ftgpu_model *m, int max_steps, int *steps_done, bool prof, double *
   long long prev = start0;
   long long left = max_steps;  // most steps any running instance still has
   for (long long c = 0; c < max_chunks; ++c) {
-    cudaGraphExec_t g = prof ? m->prof_exec : m->chunk_exec;
+    // the run's first graph opens with the half-step, the others continue
+    const bool open = c == 0;
+    cudaGraphExec_t g = prof ? m->prof_exec : open ? m->chunk_exec : m->cont_exec;
     if (!prof && left < K) {
       // the end of the run: the shortest even graph that covers it
       const int Kt = (int)std::max<long long>(2, (left + 1) & ~1ll);
       if (Kt < K) {
-        CKI(capture_chunk(m, Kt, false));
-        g = m->tail_exec[Kt / 2];
+        CKI(capture_chunk(m, Kt, false, open));
+        g = open ? m->tail_exec[Kt / 2] : m->tailc_exec[Kt / 2];
       }
     }
     CK(cudaGraphLaunch(g, m->stream));
