@@ -512,10 +512,28 @@ __device__ __forceinline__ void tet_element(const R (&x)[4][3], const R (&u)[4][
       D[i][j] = idet * (H[i][0] * Ad[j][0] + H[i][1] * Ad[j][1] + H[i][2] * Ad[j][2]);
   const R Jm1 = jm1_of(D);
   if (!(Jm1 > R(-1)) || !(detA != 0)) bad = 1;
+  // (the characteristic length first: the nodal values are dead during the law)
+  // min altitude (CalculateCharacteristicLength_C3D4.cpp:5-46): 6V / max |n_face|
+  R xc[4][3];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) xc[a][d] = x[a][d] + u[a][d];
+  R six_v = fabs((1 + Jm1) * detA);
+  constexpr int fc[4][3] = {{1, 2, 3}, {2, 3, 0}, {3, 0, 1}, {0, 1, 2}};
+  R nmax = 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int p1 = fc[k][0], p2 = fc[k][1], p3 = fc[k][2];
+    R v1x = xc[p2][0] - xc[p1][0], v1y = xc[p2][1] - xc[p1][1], v1z = xc[p2][2] - xc[p1][2];
+    R v2x = xc[p3][0] - xc[p1][0], v2y = xc[p3][1] - xc[p1][1], v2z = xc[p3][2] - xc[p1][2];
+    R n = norm3(v1y * v2z - v1z * v2y, v1z * v2x - v1x * v2z, v1x * v2y - v1y * v2x);
+    nmax = fmax(nmax, n);
+  }
+  le = six_v / nmax;
   const long long sg = gpo - A.gpbase;  // Gauss point within the group
   if (MAT == 7 && pass == kPassSurrogateFeatures) {
     write_surrogate_features(D, a0, A.law, A.surr_x + sg * kMlpIn);
-    le = R(1);
     return;
   }
   if (!dt_only) {
@@ -554,24 +572,6 @@ __device__ __forceinline__ void tet_element(const R (&x)[4][3], const R (&u)[4][
       f[3][i] = -(g0 + g1 + g2);
     }
   }
-  // min altitude (CalculateCharacteristicLength_C3D4.cpp:5-46): 6V / max |n_face|
-  R xc[4][3];
-#pragma unroll
-  for (int a = 0; a < 4; ++a)
-#pragma unroll
-    for (int d = 0; d < 3; ++d) xc[a][d] = x[a][d] + u[a][d];
-  R six_v = fabs((1 + Jm1) * detA);
-  constexpr int fc[4][3] = {{1, 2, 3}, {2, 3, 0}, {3, 0, 1}, {0, 1, 2}};
-  R nmax = 0;
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const int p1 = fc[k][0], p2 = fc[k][1], p3 = fc[k][2];
-    R v1x = xc[p2][0] - xc[p1][0], v1y = xc[p2][1] - xc[p1][1], v1z = xc[p2][2] - xc[p1][2];
-    R v2x = xc[p3][0] - xc[p1][0], v2y = xc[p3][1] - xc[p1][1], v2z = xc[p3][2] - xc[p1][2];
-    R n = norm3(v1y * v2z - v1z * v2y, v1z * v2x - v1x * v2z, v1x * v2y - v1y * v2x);
-    nmax = fmax(nmax, n);
-  }
-  le = six_v / nmax;
 }
 
 // Element time step l/c in the element precision R.  FP32: l times the

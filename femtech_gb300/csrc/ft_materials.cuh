@@ -225,14 +225,26 @@ __device__ __forceinline__ Sym6<R> hgo_iso_pk2(const R (&D)[3][3], R J, R Jm23,
 // ---- 4/5/7: HGO family (HGOIsotropic.cpp:21-115, HGOIsotropicViscoelastic.cpp:27-168) ----
 // Returns the isochoric PK2 part (which is also the reference's "Sdev") and the
 // volumetric part separately so the viscoelastic update can use S_iso.
+// J^{-2/3} - 1 from x = J - 1: in FP32 for |x| < 1/32 the binomial series
+// of (1 + x)^{-2/3} to degree 7 (truncation below 2^-40 relative), else
+// expm1(-2/3 log1p(x)); FP64 always the library functions.
+template <class R>
+__device__ __forceinline__ R jm23m1_of(R x) {
+  if (sizeof(R) == 4 && fabs(x) < R(0.03125)) {
+    // binom(-2/3, k): -2/3, 5/9, -40/81, 110/243, -308/729, 2618/6561, -7480/19683
+    return x * (R(-2.0 / 3.0) + x * (R(5.0 / 9.0) + x * (R(-40.0 / 81.0) +
+                x * (R(110.0 / 243.0) + x * (R(-308.0 / 729.0) + x * (R(2618.0 / 6561.0) +
+                x * R(-7480.0 / 19683.0)))))));
+  }
+  return d_expm1(R(-2.0 / 3.0) * d_log1p(x));
+}
 template <class R, bool FIBER>
 __device__ __forceinline__ void mat_hgo_parts(const MatP<R> &m, const R (&D)[3][3], R Jm1,
                                               const R (&a0)[3], Sym6<R> &Siso, Sym6<R> &Svol) {
   R mu = m.p[1], k1 = m.p[3], k2 = m.p[4];
   R kappa = FIBER ? m.p[7] : R(1.0 / 3.0);
   R J = 1 + Jm1;
-  R lnJ = d_log1p(Jm1);
-  R Jm23m1 = d_expm1(R(-2.0 / 3.0) * lnJ);
+  R Jm23m1 = jm23m1_of(Jm1);
   R Jm23 = 1 + Jm23m1;
   Sym6<R> eB = two_e_left(D);
   R I1m3 = 3 * Jm23m1 + Jm23 * (eB.xx + eB.yy + eB.zz);
