@@ -289,8 +289,9 @@ __device__ __forceinline__ float hex_face_area_f32(const float (&xc)[8][3], int 
 
 template <class R>
 __device__ __forceinline__ R hex_face_area(const R (&xc)[8][3], int i1, int i2, int i3, int i4) {
-  if constexpr (sizeof(R) == 4)
+  if constexpr (sizeof(R) == 4) {
     return hex_face_area_f32(reinterpret_cast<const float(&)[8][3]>(xc), i1, i2, i3, i4);
+  } else {
   R cD[3], c1[3], c2[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
@@ -318,6 +319,138 @@ __device__ __forceinline__ R hex_face_area(const R (&xc)[8][3], int i1, int i2, 
                     n0z + qj * n1z + qi * n2z);
     }
   return area;
+  }
+}
+
+// FP32 Gauss loop of the C3D8 element with packed FP32 arithmetic: every
+// 3x3 product of the kinematics and of B0^T S (du/dxi, D = H A^-T,
+// P = S + D S, P A^-1, the moments) carries rows 0 and 1 as one float2
+// (fma.rn.f32x2: two independent IEEE fma, half the issued instructions;
+// a scalar operand is broadcast at no cost) and row 2 as a scalar.  The
+// material law sees the same scalar D as the generic loop.
+__device__ __forceinline__ float2 bc2(float s) { return make_float2(s, s); }
+
+template <int MAT, bool GP>
+__device__ __forceinline__ void hex_gauss_loop_x2(const float (&hu)[7][3], const MatP<float> &mp,
+                                                  const float (&pc)[4], const float (&a0)[3],
+                                                  float *hist, long long hs, long long gs,
+                                                  int pass, float &vol, float (&m)[7][3],
+                                                  int &bad, const ElemArgs<float> &A,
+                                                  long long gpo, const float *gb, int rs) {
+  const bool dt_only = pass == kPassDt;
+  float2 hp[7];
+  float hz[7];
+#pragma unroll
+  for (int k = 0; k < 7; ++k) {
+    hp[k] = make_float2(hu[k][0], hu[k][1]);
+    hz[k] = hu[k][2];
+  }
+  float2 mc[7];
+  float mz[7];
+#pragma unroll
+  for (int k = 0; k < 7; ++k) {
+    mc[k] = make_float2(0.f, 0.f);
+    mz[k] = 0.f;
+  }
+#pragma unroll 1
+  for (int g = 0; g < 8; ++g) {
+    float xi, et, ze;
+    hex_gauss_point(g, xi, et, ze);
+    const float ez = et * ze, xz = xi * ze, xe = xi * et;
+    // A^{-1} (Q) and det A: values 10g .. 10g+9 as five pairs
+    const int o1 = (g & 1) ? rs - 2 : 2;
+    const float2 q0 = *reinterpret_cast<const float2 *>(gb),
+                 q1 = *reinterpret_cast<const float2 *>(gb + o1),
+                 q2 = *reinterpret_cast<const float2 *>(gb + rs),
+                 q3 = *reinterpret_cast<const float2 *>(gb + rs + o1),
+                 q4 = *reinterpret_cast<const float2 *>(gb + 2 * rs);
+    gb += (g & 1) ? 3 * rs - 2 : 2 * rs + 2;
+    const float Q[3][3] = {{q0.x, q0.y, q1.x}, {q1.y, q2.x, q2.y}, {q3.x, q3.y, q4.x}};
+    const float detA = q4.y;
+    // H[d][i] = du_d / dxi_i: column i, rows 0-1 paired, row 2 scalar
+    const float2 Hc0 = __ffma2_rn(bc2(ez), hp[6], __ffma2_rn(bc2(ze), hp[4], __ffma2_rn(bc2(et), hp[3], hp[0])));
+    const float2 Hc1 = __ffma2_rn(bc2(xz), hp[6], __ffma2_rn(bc2(ze), hp[5], __ffma2_rn(bc2(xi), hp[3], hp[1])));
+    const float2 Hc2 = __ffma2_rn(bc2(xe), hp[6], __ffma2_rn(bc2(et), hp[5], __ffma2_rn(bc2(xi), hp[4], hp[2])));
+    const float Hz0 = fmaf(ez, hz[6], fmaf(ze, hz[4], fmaf(et, hz[3], hz[0])));
+    const float Hz1 = fmaf(xz, hz[6], fmaf(ze, hz[5], fmaf(xi, hz[3], hz[1])));
+    const float Hz2 = fmaf(xe, hz[6], fmaf(et, hz[5], fmaf(xi, hz[4], hz[2])));
+    // D = H A^{-T} = du/dX, column j
+    float2 Dc[3];
+    float Dz[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      Dc[j] = __ffma2_rn(bc2(Q[j][2]), Hc2, __ffma2_rn(bc2(Q[j][1]), Hc1, __fmul2_rn(bc2(Q[j][0]), Hc0)));
+      Dz[j] = fmaf(Hz2, Q[j][2], fmaf(Hz1, Q[j][1], Hz0 * Q[j][0]));
+    }
+    const float D[3][3] = {{Dc[0].x, Dc[1].x, Dc[2].x}, {Dc[0].y, Dc[1].y, Dc[2].y},
+                           {Dz[0], Dz[1], Dz[2]}};
+    const float Jm1 = jm1_of(D);
+    vol += (1 + Jm1) * detA;  // det(dx/dxi) = det A det F
+    if (dt_only) continue;
+    if (!(Jm1 > -1.f) || !(detA != 0)) bad = 1;
+    const long long sg = gpo - A.gpbase + g;  // Gauss point within the group
+    if (MAT == 7 && pass == kPassSurrogateFeatures) {
+      write_surrogate_features(D, a0, A.law, A.surr_x + sg * kMlpIn);
+      continue;
+    }
+    const float *sy = (MAT == 7 && A.surr_y) ? A.surr_y + sg * kMlpOut : nullptr;
+    const Sym6<float> S = stress_at<float, MAT>(mp, D, Jm1, a0, hist + g * gs, hs, pc, sy, A.law);
+    if (GP) {
+      const long long q = gpo + g;
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) A.gpF[9 * q + i + 3 * j] = double((i == j ? 1.f : 0.f) + D[i][j]);
+      A.gpJ[q] = double(1 + Jm1);
+      A.gpS[6 * q + 0] = S.xx;
+      A.gpS[6 * q + 1] = S.yy;
+      A.gpS[6 * q + 2] = S.zz;
+      A.gpS[6 * q + 3] = S.yz;
+      A.gpS[6 * q + 4] = S.xz;
+      A.gpS[6 * q + 5] = S.xy;
+    }
+    // w det J B0^T S with w = 1: s = det A S, P = s + D s, G = P A^{-1};
+    // column j of s, rows 0-1 paired, and row 2
+    const float2 sc[3] = {__fmul2_rn(bc2(detA), make_float2(S.xx, S.xy)),
+                          __fmul2_rn(bc2(detA), make_float2(S.xy, S.yy)),
+                          __fmul2_rn(bc2(detA), make_float2(S.xz, S.yz))};
+    const float sz[3] = {sc[2].x, sc[2].y, detA * S.zz};
+    float2 Pc[3];
+    float Pz[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      // s[k][j] for k = 0, 1, 2: sc[j].x, sc[j].y, sz[j]
+      Pc[j] = __ffma2_rn(bc2(sz[j]), Dc[2], __ffma2_rn(bc2(sc[j].y), Dc[1], __ffma2_rn(bc2(sc[j].x), Dc[0], sc[j])));
+      Pz[j] = fmaf(Dz[2], sz[j], fmaf(Dz[1], sc[j].y, fmaf(Dz[0], sc[j].x, sz[j])));
+    }
+    float2 Gc[3];
+    float Gz[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      Gc[j] = __ffma2_rn(bc2(Q[2][j]), Pc[2], __ffma2_rn(bc2(Q[1][j]), Pc[1], __fmul2_rn(bc2(Q[0][j]), Pc[0])));
+      Gz[j] = fmaf(Pz[2], Q[2][j], fmaf(Pz[1], Q[1][j], Pz[0] * Q[0][j]));
+    }
+    mc[0] = __fadd2_rn(mc[0], Gc[0]);
+    mc[1] = __fadd2_rn(mc[1], Gc[1]);
+    mc[2] = __fadd2_rn(mc[2], Gc[2]);
+    mc[3] = __ffma2_rn(bc2(et), Gc[0], __ffma2_rn(bc2(xi), Gc[1], mc[3]));
+    mc[4] = __ffma2_rn(bc2(ze), Gc[0], __ffma2_rn(bc2(xi), Gc[2], mc[4]));
+    mc[5] = __ffma2_rn(bc2(ze), Gc[1], __ffma2_rn(bc2(et), Gc[2], mc[5]));
+    mc[6] = __ffma2_rn(bc2(ez), Gc[0], __ffma2_rn(bc2(xz), Gc[1], __ffma2_rn(bc2(xe), Gc[2], mc[6])));
+    mz[0] += Gz[0];
+    mz[1] += Gz[1];
+    mz[2] += Gz[2];
+    mz[3] = fmaf(et, Gz[0], fmaf(xi, Gz[1], mz[3]));
+    mz[4] = fmaf(ze, Gz[0], fmaf(xi, Gz[2], mz[4]));
+    mz[5] = fmaf(ze, Gz[1], fmaf(et, Gz[2], mz[5]));
+    mz[6] = fmaf(ez, Gz[0], fmaf(xz, Gz[1], fmaf(xe, Gz[2], mz[6])));
+  }
+#pragma unroll
+  for (int k = 0; k < 7; ++k) {
+    m[k][0] = mc[k].x;
+    m[k][1] = mc[k].y;
+    m[k][2] = mz[k];
+  }
 }
 
 // GEO: the Gauss points' A^{-1} and det A come from the setup-time table
@@ -361,6 +494,11 @@ __device__ __forceinline__ void hex_element(const R (&x)[8][3], const R (&u)[8][
   // first pair of the current Gauss point in the geometry rows: value 10 g,
   // at column 0 of a row for even g and column 2 for odd g
   const R *gb = geo;
+  if constexpr (GEO && sizeof(R) == 4) {
+    hex_gauss_loop_x2<MAT, GP>(reinterpret_cast<const float(&)[7][3]>(hu), mp, pc, a0, hist, hs,
+                               gs, pass, vol, reinterpret_cast<float(&)[7][3]>(m), bad, A, gpo,
+                               gb, rs);
+  } else {
   // The loop is not unrolled: one Gauss point's code stays in the
   // instruction cache and its temporaries are the only ones live.
 #pragma unroll 1
@@ -460,6 +598,7 @@ __device__ __forceinline__ void hex_element(const R (&x)[8][3], const R (&u)[8][
       m[5][i] += ze * g1 + et * g2;
       m[6][i] += ez * g0 + xz * g1 + xe * g2;
     }
+  }
   }
   if (pass == kPassForce) {
     // inverse transform: f_a = 1/8 sum_k sign_k(a) m_k
