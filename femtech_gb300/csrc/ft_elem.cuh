@@ -330,23 +330,104 @@ __device__ __forceinline__ R hex_face_area(const R (&xc)[8][3], int i1, int i2, 
 // material law sees the same scalar D as the generic loop.
 __device__ __forceinline__ float2 bc2(float s) { return make_float2(s, s); }
 
+// hex_hadamard with components x, y of every corner as one float2 and z as a
+// scalar (a - b as fma(b, -1, a): one rounding, as the scalar subtraction)
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, bc2(-1.f), a); }
+__device__ __forceinline__ void hex_hadamard_x2(const float2 (&p)[8], const float (&z)[8],
+                                                float2 (&hp)[7], float (&hz)[7]) {
+  const float2 q = bc2(0.125f);
+  {
+    const float2 d0 = sub2(p[1], p[0]), d1 = sub2(p[2], p[3]), d2 = sub2(p[5], p[4]),
+                 d3 = sub2(p[6], p[7]);
+    const float2 s0 = __fadd2_rn(p[1], p[0]), s1 = __fadd2_rn(p[2], p[3]),
+                 s2 = __fadd2_rn(p[5], p[4]), s3 = __fadd2_rn(p[6], p[7]);
+    hp[0] = __fmul2_rn(q, __fadd2_rn(__fadd2_rn(d0, d1), __fadd2_rn(d2, d3)));
+    hp[3] = __fmul2_rn(q, __fadd2_rn(sub2(d1, d0), sub2(d3, d2)));
+    hp[4] = __fmul2_rn(q, sub2(__fadd2_rn(d2, d3), __fadd2_rn(d0, d1)));
+    hp[6] = __fmul2_rn(q, __fadd2_rn(sub2(d0, d1), sub2(d3, d2)));
+    hp[1] = __fmul2_rn(q, __fadd2_rn(sub2(s1, s0), sub2(s3, s2)));
+    hp[2] = __fmul2_rn(q, sub2(__fadd2_rn(s2, s3), __fadd2_rn(s0, s1)));
+    hp[5] = __fmul2_rn(q, __fadd2_rn(sub2(s0, s1), sub2(s3, s2)));
+  }
+  {
+    const float d0 = z[1] - z[0], d1 = z[2] - z[3], d2 = z[5] - z[4], d3 = z[6] - z[7];
+    const float s0 = z[1] + z[0], s1 = z[2] + z[3], s2 = z[5] + z[4], s3 = z[6] + z[7];
+    hz[0] = 0.125f * ((d0 + d1) + (d2 + d3));
+    hz[3] = 0.125f * ((d1 - d0) + (d3 - d2));
+    hz[4] = 0.125f * ((d2 + d3) - (d0 + d1));
+    hz[6] = 0.125f * ((d0 - d1) + (d3 - d2));
+    hz[1] = 0.125f * ((s1 - s0) + (s3 - s2));
+    hz[2] = 0.125f * ((s2 + s3) - (s0 + s1));
+    hz[5] = 0.125f * ((s0 - s1) + (s3 - s2));
+  }
+}
+
+// The areas of two opposite faces at once (areaHexahedronFace,
+// Geometry.cpp:29-64), lane x the first face, lane y the second.  In terms of
+// the Hadamard coefficients h of the current corner coordinates a face's
+// bilinear vectors are c1 = h_a -+ h_b, c2, cD likewise (its two faces
+// differ in the sign of the third coordinate), so they form as pairs from
+// broadcast scalars.  Area: for a face with all cD components below 1e-6 (the
+// reference's signed test) 4 |c1 x c2|, else the 2x2 Gauss rule
+// sum |n0 + a n1 + b n2|, a, b = +-1/sqrt 3, from the six dot products of
+// n0 = c1 x c2, n1 = cD x c2, n2 = c1 x cD.
+__device__ __forceinline__ float face_pair_area_max(const float (&h)[7][3], int a1, int b1,
+                                                    int a2, int b2, int aD, int bD) {
+  const float2 pm = make_float2(-1.f, 1.f), m1 = bc2(-1.f);
+  float2 c1[3], c2[3], cD[3], nc2[3], ncD[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    c1[k] = __ffma2_rn(bc2(h[b1][k]), pm, bc2(h[a1][k]));
+    c2[k] = __ffma2_rn(bc2(h[b2][k]), pm, bc2(h[a2][k]));
+    cD[k] = __ffma2_rn(bc2(h[bD][k]), pm, bc2(h[aD][k]));
+    nc2[k] = __fmul2_rn(c2[k], m1);
+    ncD[k] = __fmul2_rn(cD[k], m1);
+  }
+  const float2 n0x = __ffma2_rn(c1[1], c2[2], __fmul2_rn(c1[2], nc2[1])),
+               n0y = __ffma2_rn(c1[2], c2[0], __fmul2_rn(c1[0], nc2[2])),
+               n0z = __ffma2_rn(c1[0], c2[1], __fmul2_rn(c1[1], nc2[0]));
+  const float2 n1x = __ffma2_rn(cD[1], c2[2], __fmul2_rn(cD[2], nc2[1])),
+               n1y = __ffma2_rn(cD[2], c2[0], __fmul2_rn(cD[0], nc2[2])),
+               n1z = __ffma2_rn(cD[0], c2[1], __fmul2_rn(cD[1], nc2[0]));
+  const float2 n2x = __ffma2_rn(c1[1], cD[2], __fmul2_rn(c1[2], ncD[1])),
+               n2y = __ffma2_rn(c1[2], cD[0], __fmul2_rn(c1[0], ncD[2])),
+               n2z = __ffma2_rn(c1[0], cD[1], __fmul2_rn(c1[1], ncD[0]));
+  auto dot = [](float2 ax, float2 ay, float2 az, float2 bx, float2 by, float2 bz) {
+    return __ffma2_rn(az, bz, __ffma2_rn(ay, by, __fmul2_rn(ax, bx)));
+  };
+  const float2 d00 = dot(n0x, n0y, n0z, n0x, n0y, n0z), d11 = dot(n1x, n1y, n1z, n1x, n1y, n1z),
+               d22 = dot(n2x, n2y, n2z, n2x, n2y, n2z), d01 = dot(n0x, n0y, n0z, n1x, n1y, n1z),
+               d02 = dot(n0x, n0y, n0z, n2x, n2y, n2z), d12 = dot(n1x, n1y, n1z, n2x, n2y, n2z);
+  const float t = 0.57735026918962576451f;
+  const float2 base = __ffma2_rn(bc2(1.0f / 3.0f), __fadd2_rn(d11, d22), d00);
+  const float2 a01 = __fmul2_rn(bc2(2.0f * t), d01), a02 = __fmul2_rn(bc2(2.0f * t), d02),
+               a12 = __fmul2_rn(bc2(2.0f / 3.0f), d12);
+  const float2 u1 = __fadd2_rn(base, a12), u2 = __ffma2_rn(a12, m1, base);
+  const float2 v1 = __fadd2_rn(a01, a02), v2 = __ffma2_rn(a02, m1, a01);
+  const float2 pp = __fadd2_rn(u1, v1), mm = __ffma2_rn(v1, m1, u1), pq = __fadd2_rn(u2, v2),
+               mq = __ffma2_rn(v2, m1, u2);
+  const float tol = 1e-6f;
+  const bool par_x = cD[0].x < tol && cD[1].x < tol && cD[2].x < tol;
+  const bool par_y = cD[0].y < tol && cD[1].y < tol && cD[2].y < tol;
+  const float ax = par_x ? 4.f * sqrtf(d00.x)
+                         : (sqrtf(fmaxf(pp.x, 0.f)) + sqrtf(fmaxf(mm.x, 0.f))) +
+                               (sqrtf(fmaxf(pq.x, 0.f)) + sqrtf(fmaxf(mq.x, 0.f)));
+  const float ay = par_y ? 4.f * sqrtf(d00.y)
+                         : (sqrtf(fmaxf(pp.y, 0.f)) + sqrtf(fmaxf(mm.y, 0.f))) +
+                               (sqrtf(fmaxf(pq.y, 0.f)) + sqrtf(fmaxf(mq.y, 0.f)));
+  return fmaxf(ax, ay);
+}
+
 template <int MAT, bool GP>
-__device__ __forceinline__ void hex_gauss_loop_x2(const float (&hu)[7][3], const MatP<float> &mp,
+__device__ __forceinline__ void hex_gauss_loop_x2(const float2 (&hp)[7], const float (&hz)[7],
+                                                  const MatP<float> &mp,
                                                   const float (&pc)[4], const float (&a0)[3],
                                                   float *hist, long long hs, long long gs,
-                                                  int pass, float &vol, float (&m)[7][3],
-                                                  int &bad, const ElemArgs<float> &A,
-                                                  long long gpo, const float *gb, int rs) {
+                                                  int pass, float &vol, float2 (&mc)[7],
+                                                  float (&mz)[7], int &bad,
+                                                  const ElemArgs<float> &A, long long gpo,
+                                                  const float *gb, int rs) {
   const bool dt_only = pass == kPassDt;
-  float2 hp[7];
-  float hz[7];
-#pragma unroll
-  for (int k = 0; k < 7; ++k) {
-    hp[k] = make_float2(hu[k][0], hu[k][1]);
-    hz[k] = hu[k][2];
-  }
-  float2 mc[7];
-  float mz[7];
 #pragma unroll
   for (int k = 0; k < 7; ++k) {
     mc[k] = make_float2(0.f, 0.f);
@@ -445,12 +526,34 @@ __device__ __forceinline__ void hex_gauss_loop_x2(const float (&hu)[7][3], const
     mz[5] = fmaf(ze, Gz[1], fmaf(et, Gz[2], mz[5]));
     mz[6] = fmaf(ez, Gz[0], fmaf(xz, Gz[1], fmaf(xe, Gz[2], mz[6])));
   }
-#pragma unroll
-  for (int k = 0; k < 7; ++k) {
-    m[k][0] = mc[k].x;
-    m[k][1] = mc[k].y;
-    m[k][2] = mz[k];
-  }
+}
+
+// Inverse transform of the moments: f_a = 1/8 sum_k sign_k(a) m_k (one
+// force component row; T = float2 for rows 0-1, float for row 2)
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float add2(float a, float b) { return a + b; }
+__device__ __forceinline__ float sub2(float a, float b) { return a - b; }
+__device__ __forceinline__ float2 neg2(float2 a) { return __fmul2_rn(a, bc2(-1.f)); }
+__device__ __forceinline__ float neg2(float a) { return -a; }
+__device__ __forceinline__ float2 mul2(float s, float2 a) { return __fmul2_rn(bc2(s), a); }
+__device__ __forceinline__ float mul2(float s, float a) { return s * a; }
+template <class T>
+__device__ __forceinline__ void hex_inverse_transform(const T (&m)[7], T (&f)[8]) {
+  const float q = 0.125f;
+  const T t1 = add2(m[0], m[6]), t2 = sub2(m[0], m[6]), t3 = add2(m[3], m[4]),
+          t4 = sub2(m[3], m[4]);
+  const T Pmm = sub2(t1, t3), Ppp = add2(t1, t3), Ppm = add2(t2, t4), Pmp = sub2(t2, t4);
+  const T r1 = add2(m[1], m[2]), r2 = sub2(m[1], m[2]);
+  const T Qmm = sub2(m[5], r1), Qpp = add2(m[5], r1), Qpm = sub2(r2, m[5]),
+          Qmp = sub2(neg2(r2), m[5]);
+  f[0] = mul2(q, sub2(Qmm, Pmm));
+  f[1] = mul2(q, add2(Qmm, Pmm));
+  f[2] = mul2(q, add2(Qpm, Ppm));
+  f[3] = mul2(q, sub2(Qpm, Ppm));
+  f[4] = mul2(q, sub2(Qmp, Pmp));
+  f[5] = mul2(q, add2(Qmp, Pmp));
+  f[6] = mul2(q, add2(Qpp, Ppp));
+  f[7] = mul2(q, sub2(Qpp, Ppp));
 }
 
 // GEO: the Gauss points' A^{-1} and det A come from the setup-time table
@@ -470,6 +573,63 @@ __device__ __forceinline__ void hex_element(const R (&x)[8][3], const R (&u)[8][
   // area, CalculateCharacteristicLength_C3D8.cpp:6-29) so that the nodal
   // values are dead before the Gauss loop; the 2x2x2 Gauss sum of
   // det(dx/dxi) below is the exact volume of the trilinear hexahedron.
+  R vol = 0;
+  R m[7][3];
+  const R *gb = geo;
+  if constexpr (GEO && sizeof(R) == 4) {
+    // FP32: corners as (x, y) pairs + z; the current geometry's Hadamard
+    // coefficients give the six face areas as three opposite-face pairs
+    float2 xp[8], up[8];
+    float xz[8], uz[8];
+#pragma unroll
+    for (int a = 0; a < 8; ++a) {
+      up[a] = make_float2(u[a][0], u[a][1]);
+      uz[a] = u[a][2];
+      xp[a] = __fadd2_rn(make_float2(x[a][0], x[a][1]), up[a]);
+      xz[a] = x[a][2] + u[a][2];
+    }
+    float hcx[7][3];
+    {
+      float2 hcp[7];
+      float hcz[7];
+      hex_hadamard_x2(xp, xz, hcp, hcz);
+#pragma unroll
+      for (int k = 0; k < 7; ++k) {
+        hcx[k][0] = hcp[k].x;
+        hcx[k][1] = hcp[k].y;
+        hcx[k][2] = hcz[k];
+      }
+    }
+    // (0123, 4567): c1 = h0 -+ h4, c2 = h1 -+ h5, cD = h3 -+ h6;
+    // (0374, 1265): h1 -+ h3, h2 -+ h4, h5 -+ h6; (0154, 3267): h0 -+ h3, h2 -+ h5, h4 -+ h6
+    float amax = face_pair_area_max(hcx, 0, 4, 1, 5, 3, 6);
+    amax = fmaxf(amax, face_pair_area_max(hcx, 1, 3, 2, 4, 5, 6));
+    amax = fmaxf(amax, face_pair_area_max(hcx, 0, 3, 2, 5, 4, 6));
+    float2 hp[7], mc[7];
+    float hz[7], mz[7];
+    hex_hadamard_x2(up, uz, hp, hz);
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+      mc[k] = make_float2(0.f, 0.f);
+      mz[k] = 0.f;
+    }
+    hex_gauss_loop_x2<MAT, GP>(hp, hz, mp, pc, a0, hist, hs, gs, pass, vol, mc, mz, bad, A, gpo,
+                               gb, rs);
+    le = vol / amax;
+    if (pass == kPassForce) {
+      float2 fp[8];
+      float fz[8];
+      hex_inverse_transform(mc, fp);
+      hex_inverse_transform(mz, fz);
+#pragma unroll
+      for (int a = 0; a < 8; ++a) {
+        f[a][0] = fp[a].x;
+        f[a][1] = fp[a].y;
+        f[a][2] = fz[a];
+      }
+    }
+    return;
+  } else {
   R amax;
   {
     R xc[8][3];
@@ -487,18 +647,10 @@ __device__ __forceinline__ void hex_element(const R (&x)[8][3], const R (&u)[8][
   R hx[7][3], hu[7][3];
   if (!GEO) hex_hadamard(x, hx);
   hex_hadamard(u, hu);
-  R vol = 0;
-  R m[7][3];
 #pragma unroll
   for (int i = 0; i < 7; ++i) m[i][0] = m[i][1] = m[i][2] = 0;
   // first pair of the current Gauss point in the geometry rows: value 10 g,
   // at column 0 of a row for even g and column 2 for odd g
-  const R *gb = geo;
-  if constexpr (GEO && sizeof(R) == 4) {
-    hex_gauss_loop_x2<MAT, GP>(reinterpret_cast<const float(&)[7][3]>(hu), mp, pc, a0, hist, hs,
-                               gs, pass, vol, reinterpret_cast<float(&)[7][3]>(m), bad, A, gpo,
-                               gb, rs);
-  } else {
   // The loop is not unrolled: one Gauss point's code stays in the
   // instruction cache and its temporaries are the only ones live.
 #pragma unroll 1
@@ -599,6 +751,7 @@ __device__ __forceinline__ void hex_element(const R (&x)[8][3], const R (&u)[8][
       m[6][i] += ez * g0 + xz * g1 + xe * g2;
     }
   }
+  le = vol / amax;
   }
   if (pass == kPassForce) {
     // inverse transform: f_a = 1/8 sum_k sign_k(a) m_k
@@ -620,7 +773,6 @@ __device__ __forceinline__ void hex_element(const R (&x)[8][3], const R (&u)[8][
       f[7][i] = q * (Qpp - Ppp);
     }
   }
-  le = vol / amax;
 }
 
 // C3D4: one Gauss point at (1/4,1/4,1/4), weight 1/6, |det J|
