@@ -422,7 +422,7 @@ def main():
         model = at.tuned_model(mesh, mats, loads, wl["instances"], precision=ft.MIXED, device=dev,
                                retune=args.retune, steps=20)
         ch = model.tuning
-        d_ms = ch["ms"].get("p128_t256_s1")
+        d_ms = ch["ms"].get("p128_t128_s1")
         b_ms = min(ch["ms"].values())
         tuning = {"patch": ch["patch"], "node_threads": ch["node_threads"],
                   "split": ch.get("split", 1), "default_ms_per_step": d_ms,

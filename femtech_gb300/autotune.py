@@ -110,8 +110,8 @@ def tune(mesh, mats, loads=None, instances=None, precision=1, steps=20, device=0
 
     s0 = scs[0]
     for p in pcs:  # patch size first, at the default nodal block
-        run(p, 256, s0)
-    best_p = min(pcs, key=lambda p: run(p, 256, s0))
+        run(p, 128, s0)
+    best_p = min(pcs, key=lambda p: run(p, 128, s0))
     best_t = min(node_candidates, key=lambda t: run(best_p, t, s0))
     best_s = min(scs, key=lambda s: run(best_p, best_t, s))
     out = {"patch": best_p, "node_threads": best_t, "split": best_s, "ms": res}

@@ -196,7 +196,7 @@ struct ftgpu_model {
   std::vector<InstParams> inst;
   bool inst_set = false;
   int patch_elems = 0;
-  int node_threads = 256;
+  int node_threads = 128;  // nodal block (4M block: 0.834 ms/step against 0.839 at 256)
   bool setup_done = false, init_done = false;
   PatchSet ps;
   // per group: material 0 (rigid, zero stress) with every node of every
@@ -1550,7 +1550,7 @@ int ftgpu_set_surrogate(ftgpu_model *m, ftgpu_surrogate *s, double trust_e2) {
 
 int ftgpu_set_node_threads(ftgpu_model *m, int threads) {
   if (!m) return fail(FTGPU_ERR_INPUT, "set_node_threads");
-  if (threads == 0) threads = 256;
+  if (threads == 0) threads = 128;
   if (threads < 64 || threads > 512 || threads % 32) return fail(FTGPU_ERR_INPUT, "node threads");
   m->node_threads = threads;
   drop_graphs(m);

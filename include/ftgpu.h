@@ -162,7 +162,7 @@ int ftgpu_set_instances(ftgpu_model *m, int ninst, const int *node_offset, const
 int ftgpu_set_patch_size(ftgpu_model *m, int elements_per_patch);
 
 /* Threads per block of the nodal kernels (64..512, multiple of 32; 0 =
- * default 256).  Exposed for the autotuner. */
+ * default 128).  Exposed for the autotuner. */
 int ftgpu_set_node_threads(ftgpu_model *m, int threads);
 
 /* Mixed precision: the nodal pass as a lean kernel over the free and
