@@ -244,54 +244,9 @@ __device__ __forceinline__ R norm3(R x, R y, R z) {
 
 // areaHexahedronFace, src/math/Geometry.cpp:29-64 (signed tolerance test kept;
 // the 2x2 quadrature uses (q cD + c1) x (q' cD + c2) = c1 x c2 + q cD x c2 + q' c1 x cD).
-template <class R>
-__device__ __forceinline__ R hex_face_area(const R (&xc)[8][3], int i1, int i2, int i3, int i4);
-
-// FP32 form of the same rule: the edge vectors without their factor 1/4
-// (one 1/16 on the area instead; the parallelogram test against 4 tol), and
-// the four quadrature-point norms |n0 + a n1 + b n2|, a, b = +-1/sqrt 3, from
-// the six dot products of n0, n1, n2.  Mathematically equal; FP32 rounding
-// only.
-__device__ __forceinline__ float hex_face_area_f32(const float (&xc)[8][3], int i1, int i2, int i3,
-                                                   int i4) {
-  float cD[3], c1[3], c2[3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    const float p1 = xc[i1][k], p2 = xc[i2][k], p3 = xc[i3][k], p4 = xc[i4][k];
-    const float a = p3 - p1, b = p2 - p4;
-    cD[k] = (p1 - p2) + (p3 - p4);
-    c1[k] = a + b;
-    c2[k] = a - b;
-  }
-  const float n0x = c1[1] * c2[2] - c1[2] * c2[1], n0y = c1[2] * c2[0] - c1[0] * c2[2],
-              n0z = c1[0] * c2[1] - c1[1] * c2[0];
-  const float tol4 = 4e-6f;
-  if (cD[0] < tol4 && cD[1] < tol4 && cD[2] < tol4)
-    return 0.25f * sqrtf(n0x * n0x + n0y * n0y + n0z * n0z);
-  const float n1x = cD[1] * c2[2] - cD[2] * c2[1], n1y = cD[2] * c2[0] - cD[0] * c2[2],
-              n1z = cD[0] * c2[1] - cD[1] * c2[0];
-  const float n2x = c1[1] * cD[2] - c1[2] * cD[1], n2y = c1[2] * cD[0] - c1[0] * cD[2],
-              n2z = c1[0] * cD[1] - c1[1] * cD[0];
-  const float d00 = n0x * n0x + n0y * n0y + n0z * n0z;
-  const float d11 = n1x * n1x + n1y * n1y + n1z * n1z;
-  const float d22 = n2x * n2x + n2y * n2y + n2z * n2z;
-  const float d01 = n0x * n1x + n0y * n1y + n0z * n1z;
-  const float d02 = n0x * n2x + n0y * n2y + n0z * n2z;
-  const float d12 = n1x * n2x + n1y * n2y + n1z * n2z;
-  const float t = 0.57735026918962576451f, t2 = 1.0f / 3.0f;
-  const float base = d00 + t2 * (d11 + d22);
-  const float a01 = 2.0f * t * d01, a02 = 2.0f * t * d02, a12 = 2.0f * t2 * d12;
-  const float pp = base + a01 + a02 + a12, mm = base - a01 - a02 + a12;
-  const float pm = base + a01 - a02 - a12, mp = base - a01 + a02 - a12;
-  return 0.0625f * (sqrtf(fmaxf(pp, 0.f)) + sqrtf(fmaxf(mm, 0.f)) + sqrtf(fmaxf(pm, 0.f)) +
-                    sqrtf(fmaxf(mp, 0.f)));
-}
-
+// (FP64 path; the FP32 C3D8 kernels take face_pair_area_max)
 template <class R>
 __device__ __forceinline__ R hex_face_area(const R (&xc)[8][3], int i1, int i2, int i3, int i4) {
-  if constexpr (sizeof(R) == 4) {
-    return hex_face_area_f32(reinterpret_cast<const float(&)[8][3]>(xc), i1, i2, i3, i4);
-  } else {
   R cD[3], c1[3], c2[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
@@ -319,7 +274,6 @@ __device__ __forceinline__ R hex_face_area(const R (&xc)[8][3], int i1, int i2, 
                     n0z + qj * n1z + qi * n2z);
     }
   return area;
-  }
 }
 
 // FP32 Gauss loop of the C3D8 element with packed FP32 arithmetic: every
