@@ -1720,9 +1720,12 @@ int ftgpu_init_explicit(ftgpu_model *m, double reduction, double failure_dt, dou
   CK(cudaMemsetAsync(m->err.p, 0, sizeof(int), m->stream));
   CKI(reset_rigid(m));
   NodeArgs A = node_args(m, kNodeBegin, 0);
-  k_apply_bc<<<(unsigned)((m->nNodes + 255) / 256), 256, 0, m->stream>>>(A, m->t0);
+  // the boundary values at t0, and u into the slots in the same pass
+  if (is_fp64(m))
+    k_apply_bc<double><<<(unsigned)((m->nNodes + 255) / 256), 256, 0, m->stream>>>(A, m->t0);
+  else
+    k_apply_bc<float><<<(unsigned)((m->nNodes + 255) / 256), 256, 0, m->stream>>>(A, m->t0);
   CK(cudaGetLastError());
-  CKI(launch_node(m, kNodeScatterU, 0));
   CKI(fill_dtmin(m));
   // The initial force needs the initial dt only where a Prony series
   // integrates over it (materials 5, 7): there a dt pass runs first and the
@@ -1756,10 +1759,10 @@ int ftgpu_init_explicit(ftgpu_model *m, double reduction, double failure_dt, dou
     CK(cudaMemsetAsync(m->estate.p, 0, sizeof(EnergyState), m->stream));
   }
   CKI(launch_node(m, kNodeInit, 0));
-  CKI(check_err(m));
+  // the clocks and the error word with one wait
   CK(cudaMemcpyAsync(m->h_clock, m->clock.p, sizeof(Clock) * m->ninst, cudaMemcpyDeviceToHost,
                      m->stream));
-  CK(cudaStreamSynchronize(m->stream));
+  CKI(check_err(m));
   for (int i = 0; i < m->ninst; ++i)
     if (m->h_clock[i].done & 4) return fail(FTGPU_ERR_DT, "initial dt below FailureTimeStep");
   m->init_done = true;

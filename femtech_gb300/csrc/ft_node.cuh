@@ -1054,14 +1054,19 @@ __global__ void k_clock_init(Clock *clock, unsigned long long *dtmin, const Inst
 }
 
 // Apply the boundary functions at time t (pre-loop BC call, ex9.cpp:84).
+// (and, R: the node's displacement replicated into its patch slots, as
+// k_node's ScatterU mode does, in the element precision)
+template <class R>
 __global__ void k_apply_bc(const NodeArgs A, double t) {
   const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= A.N) return;
   const long long N = A.N;
   const int inst = A.node_inst ? A.node_inst[n] : 0;
+  double un[3];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const int fn = A.nbc[d * N + n];
+    un[d] = A.u[d * N + n];
     if (fn < 0) continue;
     double u, v, a = 0.0;
     if (A.fns[fn].kind == kBckRigid) {  // the rigid body's current state
@@ -1076,7 +1081,11 @@ __global__ void k_apply_bc(const NodeArgs A, double t) {
     A.u[d * N + n] = u;
     A.v[d * N + n] = v;
     A.a[d * N + n] = a;
+    un[d] = u;
   }
+  const Slot4<R> r{R(un[0]), R(un[1]), R(un[2]), R(0)};
+  Slot4<R> *sU = reinterpret_cast<Slot4<R> *>(A.sU);
+  for (int k = A.slot_off[n]; k < A.slot_off[n + 1]; ++k) sU[A.slots[k]] = r;
 }
 
 }  // namespace ftgpu
