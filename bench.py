@@ -456,7 +456,9 @@ def main():
     clocks = sampler.stop()
     ms = reduce_max_sum([dev_ms], world, "cuda:%d" % dev)[0]
     value = E * steps * world / (ms / 1000.0)
-    launches = model.launches_per_step() * steps + math.ceil(steps / 16)
+    # every step's kernels, plus the run's opening half-step (k_node; and
+    # k_rigid_begin where acceleration records drive a rigid body)
+    launches = model.launches_per_step() * steps + (2 if wl.get("rigid") is not None else 1)
 
     # ---- per-kernel times (events around every pass) for the roofline ----
     kp = min(args.steps, 400)
