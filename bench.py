@@ -33,7 +33,6 @@ compiled in this checkout) on the same metric.
 """
 import argparse
 import json
-import math
 import os
 import subprocess
 import sys
