@@ -246,6 +246,12 @@ struct ftgpu_model {
   long long rig_nodes = 0;
   cudaStream_t stream2 = nullptr;  // the driven-node branch of a step
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // models with several element groups: every second group's pass runs on
+  // gstream beside the others (disjoint patches and slots; the dt minimum
+  // and the error word are atomics), so a small group's partial last wave
+  // fills with the next group's blocks
+  cudaStream_t gstream = nullptr;
+  cudaEvent_t ev_gfork = nullptr, ev_gjoin = nullptr;
   DBuf slot_off, slots, slot4, slot4b, node_inst, nbc, fnsbuf;
   // mixed-precision node pass split: k_node_free over every node not marked
   // kNodeRest in nkind, k_node_step over rest_list (the marked ones)
@@ -290,6 +296,9 @@ struct ftgpu_model {
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
     if (stream2) cudaStreamDestroy(stream2);
+    if (ev_gfork) cudaEventDestroy(ev_gfork);
+    if (ev_gjoin) cudaEventDestroy(ev_gjoin);
+    if (gstream) cudaStreamDestroy(gstream);
     for (int k = 0; k < 3; ++k) {
       if (cev[k]) cudaEventDestroy(cev[k]);
       if (cstream[k]) cudaStreamDestroy(cstream[k]);
@@ -514,9 +523,22 @@ template <class R>
 int launch_groups_t(ftgpu_model *m, int parity, int use_clock, double dt_direct, int gp,
                     int dt_only) {
   const int PE = max_patch(m);
+  auto active = [&](size_t gi) {
+    return m->ps.groups[gi].npatch > 0 &&
+           !(gp != kLaunchGaussPoints && gi < m->group_idle.size() && m->group_idle[gi]);
+  };
+  int nact = 0;
+  for (size_t gi = 0; gi < m->ps.groups.size(); ++gi) nact += active(gi) ? 1 : 0;
+  const bool split = nact > 1 && m->gstream;
+  if (split) {
+    CK(cudaEventRecord(m->ev_gfork, m->stream));
+    CK(cudaStreamWaitEvent(m->gstream, m->ev_gfork, 0));
+  }
+  int k = 0;  // active groups so far
   for (size_t gi = 0; gi < m->ps.groups.size(); ++gi) {
     const PatchGroup &g = m->ps.groups[gi];
-    if (gp != kLaunchGaussPoints && gi < m->group_idle.size() && m->group_idle[gi]) continue;
+    if (!active(gi)) continue;
+    cudaStream_t st = split && (k++ & 1) ? m->gstream : m->stream;
     ElemArgs<R> A = elem_args<R>(m, g, (int)gi);
     A.parity = parity;
     // the injury criteria ride on the force pass of groups with listed elements
@@ -542,17 +564,21 @@ int launch_groups_t(ftgpu_model *m, int parity, int use_clock, double dt_direct,
       const long long base = m->surr_base[gi];
       const long long ngp = (long long)g.nelem * (g.etype == 0 ? 8 : 1);
       A.surr_x = m->surr_x.as<uint16_t>() + base * kMlpIn;
-      int r = launch_elem<R>(g.etype, g.mat, 0, g.npatch, PE, smem, m->stream, A,
+      int r = launch_elem<R>(g.etype, g.mat, 0, g.npatch, PE, smem, st, A,
                              kPassSurrogateFeatures);
       if (r) return r;
       r = surrogate_infer(m->surr, A.surr_x, ngp, m->surr_y.as<float>() + base * kMlpOut,
-                          m->stream, m->err.as<int>());
+                          st, m->err.as<int>());
       if (r) return r;
       A.surr_x = nullptr;
       A.surr_y = m->surr_y.as<float>() + base * kMlpOut;
     }
-    int r = launch_elem<R>(g.etype, g.mat, mode, g.npatch, PE, smem, m->stream, A, dt_only);
+    int r = launch_elem<R>(g.etype, g.mat, mode, g.npatch, PE, smem, st, A, dt_only);
     if (r) return r;
+  }
+  if (split) {
+    CK(cudaEventRecord(m->ev_gjoin, m->gstream));
+    CK(cudaStreamWaitEvent(m->stream, m->ev_gjoin, 0));
   }
   return 0;
 }
@@ -1000,6 +1026,11 @@ int setup_t(ftgpu_model *m) {
   }
   CKI(upload_epid(m, false));  // the force slots are allocated zeroed below
   CKI(upload_materials<R>(m));
+  if (m->ps.groups.size() > 1 && !m->gstream) {  // element groups side by side
+    CK(cudaStreamCreateWithFlags(&m->gstream, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&m->ev_gfork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&m->ev_gjoin, cudaEventDisableTiming));
+  }
   // reference coordinates per slot: absolute in FP64 mode, relative to the
   // patch's first node in mixed mode (keeps FP32 digits for element geometry)
   {
