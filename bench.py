@@ -508,7 +508,12 @@ def main():
             "overheads of this design, not algorithmic bytes" % GEO_TABLE_BYTES_PER_EL)
 
     # ---- end to end through the C ABI with host buffers ----
+    if world > 1:
+        torch.distributed.barrier()
     e2e = end_to_end(ft, wl, dev, args.steps, E, N)
+    # whole job: every rank's element-updates over the slowest rank's time
+    el_max = reduce_max_sum([e2e.pop("_elapsed_s")], world, "cuda:%d" % dev)[0]
+    e2e["value"] = E * e2e.pop("_steps") * world / el_max
 
     line = {
         "metric": "element-updates/s", "value": value, "unit": "element-updates/s",
@@ -531,7 +536,7 @@ def main():
         "roofline": roofline,
         "e2e": e2e,
     }
-    if args.workload == "block" and not args.no_accuracy:
+    if rank == 0 and args.workload == "block" and not args.no_accuracy:
         acc = accuracy_vs_fp64(dev)
         line["rel_disp_err_vs_fp64"] = acc["rel_disp_err"]
         line["accuracy"] = acc
@@ -651,7 +656,8 @@ def end_to_end(ft, wl, dev, steps, E, N):
     return {"value": E * done / el, "unit": "element-updates/s",
             "h2d_bytes_per_step": h2d / max(done, 1), "d2h_bytes_per_step": d2h / max(done, 1),
             "what": "set_state from pinned host arrays + init_explicit + run, full u/v/a read "
-                    "back into pinned host arrays every %d steps" % every}
+                    "back into pinned host arrays every %d steps" % every,
+            "_elapsed_s": el, "_steps": done}
 
 
 def load_traffic(workload, E):
