@@ -86,6 +86,32 @@ def test_ogden_block_mixed_vs_oracle(oracle_lib):
     assert err < 1e-3
 
 
+@pytest.mark.parametrize("prec,tol", [(ft.FP64, 1e-7), (ft.MIXED, 1e-3)])
+def test_three_element_groups_side_by_side_vs_oracle(oracle_lib, prec, tol):
+    """Three parts (Neo-Hookean, HGO, Ogden layers) make three element groups,
+    whose passes run on alternating streams of the step graph: the loop still
+    matches the oracle and repeats bitwise."""
+    mesh, mats, loads = mg.ogden_block_case(nx=8, ny=8, nz=6, lx=0.008, ly=0.008, lz=0.006,
+                                            amp=1e-4, freq=200.0)
+    X = mesh["coordinates"]
+    conn = np.asarray(mesh["connectivity"]).reshape(-1, 8)
+    zc = X[conn, 2].mean(axis=1)
+    mesh["pid"] = np.digitize(zc, [0.002, 0.004]).astype(np.int32)
+    mats = mg.materials([(1, MATS[1]), (4, MATS[4]), (6, MATS[6])])
+    o = oracle_lib.Oracle(mesh, mats, threads=4)
+    ref = o.explicit_run(loads.dof_fn, loads.fns, tmax=1.0, reduction=0.9, max_steps=200,
+                         out_every=100)
+    out = []
+    for _ in range(2):
+        m = ft.Model(mesh, mats, precision=prec, loads=loads)
+        us, ts, steps, st = run_to(m, 1.0, 0.9, 100, max_steps=200)
+        assert steps == 200
+        assert max(rel(us[i], ref["u_out"][i]) for i in range(2)) < tol
+        out.append(us[-1])
+        m.close()
+    assert np.array_equal(out[0], out[1])
+
+
 def test_batched_instances_equal_separate_runs():
     cases = [mg.cube_tension_case(n=n, mu=mu) for n, mu in ((4, 3400.0), (5, 5000.0), (3, 2000.0))]
     Xs, conns, eptrs, pids, fns, dofs = [], [], [], [], [], []
